@@ -1,0 +1,154 @@
+"""ctypes binding of the C ABI in include/hibf_gb300.h (libhibf_gb300.so, built in-tree by hibf_gb300._build).
+
+There is no CPU fallback: ``lib()`` raises when the shared library is missing, and every entry point that needs a
+GPU returns HIBF_GPU_ERR_NO_DEVICE, which ``check`` turns into an exception.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libhibf_gb300.so"
+
+u64 = ctypes.c_uint64
+u64p = ctypes.POINTER(ctypes.c_uint64)
+vp = ctypes.c_void_p
+ci = ctypes.c_int
+
+OK = 0
+ERR_INVALID_ARG = 1
+ERR_LOGIC = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_NO_DEVICE = 4
+ERR_CUDA = 5
+ERR_OVERFLOW = 6
+ERR_TIMEOUT = 7
+ERR_ADMISSION = 8
+ERR_CYCLE = 9
+
+QUERY_MEMBERSHIP = 1
+QUERY_COUNT = 2
+
+BIN_MERGED = (1 << 64) - 1
+BIN_DELETED = (1 << 64) - 2
+
+
+class HibfGpuError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[status {status}] {msg}")
+        self.status = status
+
+
+class LogicError(HibfGpuError, ValueError):
+    """std::logic_error of the reference (invalid IBF construction arguments)."""
+
+
+class InvalidArgument(HibfGpuError, ValueError):
+    """std::invalid_argument of the reference."""
+
+
+# (name, restype, argtypes); restype None means the int status convention.
+_SIGS = [
+    ("hibf_gpu_last_error", ctypes.c_char_p, []),
+    ("hibf_gpu_abi_version", ci, []),
+    ("hibf_gpu_device_count", None, [ctypes.POINTER(ci)]),
+    ("hibf_gpu_ibf_create", None, [u64, u64, u64, ci, ctypes.POINTER(vp)]),
+    ("hibf_gpu_ibf_destroy", None, [vp]),
+    ("hibf_gpu_ibf_info", None, [vp, u64p]),
+    ("hibf_gpu_ibf_emplace", None, [vp, vp, u64, u64]),
+    ("hibf_gpu_ibf_emplace_binned", None, [vp, vp, vp, u64]),
+    ("hibf_gpu_ibf_emplace_d", None, [vp, vp, vp, u64, u64, vp]),
+    ("hibf_gpu_ibf_clear", None, [vp, u64]),
+    ("hibf_gpu_ibf_clear_range", None, [vp, vp, u64]),
+    ("hibf_gpu_ibf_try_increase_bin_number_to", None, [vp, u64, ctypes.POINTER(ci)]),
+    ("hibf_gpu_ibf_increase_bin_number_to", None, [vp, u64]),
+    ("hibf_gpu_ibf_bulk_contains", None, [vp, vp, u64, vp]),
+    ("hibf_gpu_ibf_bulk_contains_d", None, [vp, vp, u64, vp, vp]),
+    ("hibf_gpu_ibf_bulk_count", None, [vp, vp, u64, ci, vp]),
+    ("hibf_gpu_ibf_bulk_count_d", None, [vp, vp, u64, ci, vp, vp]),
+    ("hibf_gpu_ibf_membership_for", None, [vp, vp, u64, ctypes.c_uint16, vp, u64p]),
+    ("hibf_gpu_ibf_upload_words", None, [vp, vp, u64]),
+    ("hibf_gpu_ibf_download_words", None, [vp, vp, u64]),
+    ("hibf_gpu_ibf_download_occupancy", None, [vp, vp, u64]),
+    ("hibf_gpu_ibf_status", None, [vp]),
+    ("hibf_gpu_hibf_create", None, [u64, u64, vp, vp, vp, vp, vp, ctypes.POINTER(vp)]),
+    ("hibf_gpu_hibf_destroy", None, [vp]),
+    ("hibf_gpu_hibf_info", None, [vp, u64p]),
+    ("hibf_gpu_hibf_ibf_info", None, [vp, u64, u64p]),
+    ("hibf_gpu_hibf_emplace", None, [vp, u64, vp, u64, u64]),
+    ("hibf_gpu_hibf_emplace_d", None, [vp, u64, vp, vp, u64, u64, vp]),
+    ("hibf_gpu_hibf_upload_words", None, [vp, u64, vp, u64]),
+    ("hibf_gpu_hibf_download_words", None, [vp, u64, vp, u64]),
+    ("hibf_gpu_agent_create", None, [vp, ctypes.POINTER(vp)]),
+    ("hibf_gpu_agent_destroy", None, [vp]),
+    ("hibf_gpu_agent_set_stream", None, [vp, vp]),
+    ("hibf_gpu_agent_reserve", None, [vp, u64, u64, u64, u64]),
+    ("hibf_gpu_agent_membership_for", None, [vp, vp, u64, ctypes.c_uint16, ctypes.POINTER(u64p), u64p]),
+    ("hibf_gpu_agent_bulk_count", None, [vp, vp, u64, u64, ci, ctypes.POINTER(vp)]),
+    ("hibf_gpu_agent_query_batch", None,
+     [vp, ci, vp, vp, u64, vp, ci, ctypes.POINTER(u64p), ctypes.POINTER(u64p), ctypes.POINTER(vp)]),
+    ("hibf_gpu_agent_query_batch_d", None,
+     [vp, ci, vp, vp, u64, vp, ci, ctypes.POINTER(u64p), ctypes.POINTER(u64p), ctypes.POINTER(vp)]),
+    ("hibf_gpu_agent_query_plain_d", None, [vp, ci, vp, vp, u64, vp, ci]),
+    ("hibf_gpu_agent_fetch_results", None,
+     [vp, u64, ci, ci, ctypes.POINTER(u64p), ctypes.POINTER(u64p), ctypes.POINTER(vp)]),
+    ("hibf_gpu_agent_status", None, [vp]),
+    ("hibf_gpu_agent_last_work", None, [vp, u64p, u64p]),
+]
+
+_lib = None
+
+
+def declared_symbols() -> list[str]:
+    return [name for name, _, _ in _SIGS]
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libhibf_gb300.so (building it first when HIBF_GB300_AUTOBUILD=1)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        if os.environ.get("HIBF_GB300_AUTOBUILD") == "1":
+            from . import _build
+
+            _build.build()
+        else:
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m hibf_gb300._build` "
+                              "(the library has no CPU fallback)")
+    L = ctypes.CDLL(str(LIB_PATH))
+    for name, res, args in _SIGS:
+        f = getattr(L, name)
+        f.restype = ci if res is None else res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return (lib().hibf_gpu_last_error() or b"").decode(errors="replace")
+
+
+def check(status: int) -> None:
+    if status == OK:
+        return
+    msg = last_error()
+    if status == ERR_LOGIC:
+        raise LogicError(status, msg)
+    if status == ERR_INVALID_ARG:
+        raise InvalidArgument(status, msg)
+    if status == ERR_OUT_OF_MEMORY:
+        raise MemoryError(msg)
+    raise HibfGpuError(status, msg)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args))
+
+
+def device_count() -> int:
+    n = ci(0)
+    call("hibf_gpu_device_count", ctypes.byref(n))
+    return n.value

@@ -1,0 +1,208 @@
+// count.cuh -- the per-warp counting loop shared by IBF bulk_count and the HIBF query kernels.
+//
+// For every value: hash it h times, fetch the h rows, AND them, add the resulting bit vector to per-bin counters
+// (include/hibf/interleaved_bloom_filter.hpp:652-665 + counting_vector::operator+=, counting_vector.hpp:171-175).
+//
+// Work mapping.  A row of bin_words 64-bit words is read by LPV = next_pow2(bin_words) lanes (capped at 32), lane
+// j of a group reading word j, so a row is one coalesced access of ceil(bytes/32) sectors.  Each lane first hashes
+// a different value (32 values per warp per pass), then the groups take turns on those values, receiving the row
+// offsets by shuffle.  Each lane accumulates its word's 64 bins in K bit-sliced planes (planes_add4) and flushes
+// them through a warp transpose into 32-bit counters in shared memory before they can overflow (2^K - 1 masks).
+// Counts are exact; the caller reduces them modulo the counter width, which equals the reference's wraparound.
+#pragma once
+
+#include "device.cuh"
+
+namespace hibf_gb300
+{
+
+struct row_params
+{
+    uint64_t const * words;
+    uint64_t bin_size;
+    uint32_t row_words;
+    uint32_t bin_words;
+    uint32_t hash_shift;
+    uint32_t hash_funs;
+};
+
+template <int LPV, int K, bool ATOMIC>
+__device__ __forceinline__ void planes_flush_to(uint64_t (&P)[K], uint32_t * out, int lane)
+{
+    uint32_t lo[K], hi[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+    {
+        lo[k] = warp_transpose32(static_cast<uint32_t>(P[k]), lane);
+        hi[k] = warp_transpose32(static_cast<uint32_t>(P[k] >> 32), lane);
+        P[k] = 0;
+    }
+#pragma unroll
+    for (int j = 0; j < LPV; ++j)
+    {
+        uint32_t gm = 0;
+#pragma unroll
+        for (int g = 0; g < 32 / LPV; ++g)
+            gm |= 1u << (g * LPV + j);
+        uint32_t cl = 0, ch = 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+        {
+            cl += static_cast<uint32_t>(__popc(lo[k] & gm)) << k;
+            ch += static_cast<uint32_t>(__popc(hi[k] & gm)) << k;
+        }
+        if constexpr (ATOMIC)
+        {
+            if (cl)
+                atomicAdd(out + 64 * j + lane, cl);
+            if (ch)
+                atomicAdd(out + 64 * j + 32 + lane, ch);
+        }
+        else
+        {
+            out[64 * j + lane] += cl;
+            out[64 * j + 32 + lane] += ch;
+        }
+    }
+}
+
+// One warp counts vals[0, n) into counts[0, 64 * LPV).  ATOMIC: counters shared with other warps.
+template <int LPV, int K, bool ATOMIC>
+__device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const * __restrict__ vals, uint64_t n,
+                                           uint32_t * counts, int lane)
+{
+    constexpr int G = 32 / LPV;
+    constexpr int U = LPV >= 4 ? 1 : 4 / LPV;
+    constexpr int STEPS = U * LPV;
+    constexpr int BLOCK = 32 * U;
+    static_assert(STEPS % 4 == 0, "masks are consumed in groups of four");
+    int const g = lane / LPV;
+    int const j = lane % LPV;
+    bool const wj = static_cast<uint32_t>(j) < rp.bin_words;
+    uint32_t const h = rp.hash_funs;
+    uint64_t const * __restrict__ words = rp.words + j;
+
+    uint64_t P[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        P[k] = 0;
+    int acc = 0;
+
+    for (uint64_t base = 0; base < n; base += BLOCK)
+    {
+        uint64_t off[U][5];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+        {
+            uint64_t const idx = base + static_cast<uint64_t>(u * 32 + lane);
+            uint64_t const v = idx < n ? vals[idx] : 0u;
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+                off[u][i] = (static_cast<uint32_t>(i) < h)
+                              ? hash_row(v, c_hash_seeds[i], rp.hash_shift, rp.bin_size) * rp.row_words
+                              : 0u;
+        }
+#pragma unroll
+        for (int s = 0; s < STEPS; s += 4)
+        {
+            uint64_t w[4][5];
+            bool ok[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+            {
+                int const step = s + t;
+                int const u = step / LPV;
+                int const src = (step % LPV) * G + g;
+                ok[t] = wj && (base + static_cast<uint64_t>(u * 32 + src) < n);
+#pragma unroll
+                for (int i = 0; i < 5; ++i)
+                {
+                    uint64_t o = off[u][i];
+                    if constexpr (LPV > 1)
+                        o = __shfl_sync(kFullMask, o, src);
+                    w[t][i] = (ok[t] && static_cast<uint32_t>(i) < h) ? __ldg(words + o) : ~0ull;
+                }
+            }
+            uint64_t m[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+            {
+                uint64_t x = w[t][0] & w[t][1] & w[t][2] & w[t][3] & w[t][4];
+                m[t] = ok[t] ? x : 0u;
+            }
+            planes_add4<K>(P, m[0], m[1], m[2], m[3]);
+            acc += 4;
+            if (acc > (1 << K) - 1 - 4)
+            {
+                planes_flush_to<LPV, K, ATOMIC>(P, counts, lane);
+                acc = 0;
+            }
+        }
+    }
+    if (acc)
+        planes_flush_to<LPV, K, ATOMIC>(P, counts, lane);
+}
+
+// Rows wider than a warp (bin_words > 32): lanes stride over the words, set bits are added one by one.
+__device__ __forceinline__ void warp_count_wide(row_params const & rp, uint64_t const * __restrict__ vals, uint64_t n,
+                                                uint32_t * counts, int lane)
+{
+    for (uint64_t i = 0; i < n; ++i)
+    {
+        uint64_t const v = vals[i];
+        uint64_t off[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+            off[k] = (static_cast<uint32_t>(k) < rp.hash_funs)
+                       ? hash_row(v, c_hash_seeds[k], rp.hash_shift, rp.bin_size) * rp.row_words
+                       : 0u;
+        for (uint32_t wi = lane; wi < rp.bin_words; wi += 32)
+        {
+            uint64_t x = ~0ull;
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                if (static_cast<uint32_t>(k) < rp.hash_funs)
+                    x &= __ldg(rp.words + off[k] + wi);
+            while (x)
+            {
+                int const b = __ffsll(static_cast<long long>(x)) - 1;
+                x &= x - 1;
+                atomicAdd(counts + 64 * wi + b, 1u);
+            }
+        }
+    }
+}
+
+// Dispatch on the node's lanes-per-value (log2).  K = 7 planes: flush every 124 masks per lane.
+template <bool ATOMIC>
+__device__ __forceinline__ void warp_count_any(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
+                                               uint64_t n, uint32_t * counts, int lane)
+{
+    if (rp.bin_words > 32)
+    {
+        warp_count_wide(rp, vals, n, counts, lane);
+        return;
+    }
+    switch (lpv_log2)
+    {
+    case 0:
+        warp_count<1, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    case 1:
+        warp_count<2, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    case 2:
+        warp_count<4, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    case 3:
+        warp_count<8, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    case 4:
+        warp_count<16, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    default:
+        warp_count<32, 7, ATOMIC>(rp, vals, n, counts, lane);
+    }
+}
+
+} // namespace hibf_gb300

@@ -1,0 +1,1415 @@
+// hibf.cu -- hierarchical interleaved Bloom filter on the device: per-IBF bit stores and tables, the persistent
+// (query, IBF) work-queue kernel, the result compaction passes, agents and their C-ABI entry points.
+//
+// Reference interface: seqan::hibf::hierarchical_interleaved_bloom_filter
+// (include/hibf/hierarchical_interleaved_bloom_filter.hpp, src/hierarchical_interleaved_bloom_filter.cpp).
+//
+// Query semantics (membership_for_impl HIBF.hpp:322-355, bulk_count_impl HIBF.hpp:463-496): for a query and an IBF,
+// count every value per technical bin, then scan the bins in order with a running sum in the counter type:
+//   deleted  -> keep the sum;   merged -> descend if sum >= t, reset;   last bin of a user bin -> report if sum >= t,
+//   reset.  We precompute per bin: MERGED, DELETED, RUN_END (last bin of a user bin's run) and HEAD (first bin of a
+// summation segment, i.e. bin 0 or the bin after a MERGED / RUN_END bin), which turns the scan into a segmented
+// prefix sum, done 32 bins at a time by a warp.  Counter wraparound: exact sums reduced modulo 2^(8*width) before
+// the comparison equal the reference's wrapping value_t sums.
+//
+// Work queue: task = (query, depth, IBF).  Claim indices below n_queries are the implicit root tasks; children are
+// appended behind them.  A worker that claims an index whose task is not written yet waits (bounded by a time
+// limit) until it appears or the count of unfinished tasks drops to zero.  Children are added to that count
+// before their parent retires, so zero means no task is queued or running anywhere.
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.hpp"
+#include "count.cuh"
+#include "device.cuh"
+
+namespace hibf_gb300
+{
+
+void set_last_error(std::string msg);
+int sm_count();
+
+namespace
+{
+
+constexpr uint32_t F_MERGED = 1u;
+constexpr uint32_t F_DELETED = 2u;
+constexpr uint32_t F_RUN_END = 4u;
+constexpr uint32_t F_HEAD = 8u;
+
+constexpr unsigned long long kEmpty = ~0ull;
+constexpr uint32_t kNodeBits = 26;
+constexpr uint32_t kNodeMask = (1u << kNodeBits) - 1u;
+
+// control words
+enum : int
+{
+    C_HEAD = 0,
+    C_TAIL = 1,
+    C_PENDING = 2,
+    C_NREC = 3,
+    C_ERROR = 4,
+    C_NLARGE = 5,
+    C_WORDS = 8
+};
+// error bits
+constexpr unsigned long long E_OVERFLOW_REC = 1ull;
+constexpr unsigned long long E_OVERFLOW_TASK = 2ull;
+constexpr unsigned long long E_TIMEOUT = 4ull;
+constexpr unsigned long long E_CYCLE = 8ull;
+
+struct alignas(16) dev_node
+{
+    uint64_t const * words;
+    uint64_t bin_size;
+    uint32_t bins;
+    uint32_t bin_words;
+    uint32_t row_words;
+    uint32_t hash_shift;
+    uint32_t hash_funs;
+    uint32_t desc_offset;
+    uint32_t lpv_log2;
+    uint32_t pad;
+};
+
+struct query_params
+{
+    dev_node const * nodes;
+    uint2 const * descs; // .x = user bin or next IBF, .y = flags
+    uint64_t const * values;
+    uint64_t const * qoff;
+    uint64_t const * thr;
+    uint64_t count_mask;
+    uint64_t n_queries;
+    uint64_t q_base; // added to the query index in records and per-query counters (plain form)
+    uint32_t max_depth;
+    uint32_t counters_per_warp;
+    unsigned long long * tasks;
+    uint64_t task_cap;
+    unsigned long long * ctrl;
+    uint32_t * rec_q;
+    uint32_t * rec_ub;
+    unsigned long long * rec_cnt;
+    uint64_t rec_cap;
+    unsigned int * qcount;
+    unsigned long long * stats;
+    uint64_t wait_limit_ns;
+    int self_init; // single-block launch that resets its own control words first
+};
+
+__device__ __forceinline__ unsigned long long make_task(uint64_t q, uint32_t depth, uint32_t node)
+{
+    return (static_cast<unsigned long long>(q) << 32) | (static_cast<unsigned long long>(depth) << kNodeBits) | node;
+}
+
+__device__ unsigned long long wait_for_task(query_params const & p, unsigned long long slot)
+{
+    volatile unsigned long long * t = p.tasks + slot;
+    volatile unsigned long long * pending = p.ctrl + C_PENDING;
+    uint64_t start = 0;
+    for (uint32_t it = 0;; ++it)
+    {
+        unsigned long long v = *t;
+        if (v != kEmpty)
+            return v;
+        if (*pending == 0ull)
+        {
+            __threadfence();
+            return *t; // still empty: nothing is queued or running, the batch is done
+        }
+        if (it == 0)
+            start = globaltimer_ns();
+        else if ((it & 31u) == 0 && globaltimer_ns() - start > p.wait_limit_ns)
+        {
+            atomicOr(p.ctrl + C_ERROR, E_TIMEOUT);
+            return kEmpty;
+        }
+        __nanosleep(256);
+    }
+}
+
+__device__ void process_task(query_params const & p, unsigned long long task, uint32_t * counts, int lane,
+                             unsigned long long & n_tasks, unsigned long long & n_visits)
+{
+    uint64_t const q = task >> 32;
+    uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
+    uint32_t const k = static_cast<uint32_t>(task) & kNodeMask;
+    dev_node const nd = p.nodes[k];
+    uint64_t const b0 = p.qoff[q];
+    uint64_t const n = p.qoff[q + 1] - b0;
+    uint64_t const thr = p.thr[q];
+
+    uint32_t const ncount = nd.bin_words > 32 ? 64u * nd.bin_words : (64u << nd.lpv_log2);
+    for (uint32_t i = lane; i < ncount; i += 32)
+        counts[i] = 0;
+    __syncwarp();
+    row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
+    warp_count_any<false>(rp, nd.lpv_log2, p.values + b0, n, counts, lane);
+    __syncwarp();
+
+    uint2 const * d = p.descs + nd.desc_offset;
+    unsigned long long carry = 0;
+    unsigned const lt_mask = (1u << lane) - 1u;
+    uint64_t const gq = q + p.q_base;
+    for (uint32_t c = 0; c < nd.bins; c += 32)
+    {
+        uint32_t const b = c + lane;
+        bool const valid = b < nd.bins;
+        uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
+        unsigned long long x = valid ? counts[b] : 0ull;
+        bool f = valid && (ds.y & F_HEAD);
+        if (lane == 0 && !f)
+            x += carry;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
+            int const fy = __shfl_up_sync(kFullMask, static_cast<int>(f), o);
+            if (lane >= o)
+            {
+                if (!f)
+                    x += y;
+                f = f || fy;
+            }
+        }
+        uint64_t const sum = x & p.count_mask;
+        bool const pass = sum >= thr;
+        bool const emit_ub = valid && (ds.y & F_RUN_END) && pass;
+        bool const emit_child = valid && (ds.y & F_MERGED) && pass;
+
+        unsigned const rb = __ballot_sync(kFullMask, emit_ub);
+        if (rb)
+        {
+            unsigned const nr = __popc(rb);
+            unsigned long long base = 0;
+            if (lane == 0)
+            {
+                base = atomicAdd(p.ctrl + C_NREC, static_cast<unsigned long long>(nr));
+                atomicAdd(p.qcount + gq, nr);
+                if (base + nr > p.rec_cap)
+                    atomicOr(p.ctrl + C_ERROR, E_OVERFLOW_REC);
+            }
+            base = __shfl_sync(kFullMask, base, 0);
+            if (emit_ub)
+            {
+                unsigned long long const r = base + __popc(rb & lt_mask);
+                if (r < p.rec_cap)
+                {
+                    p.rec_q[r] = static_cast<uint32_t>(gq);
+                    p.rec_ub[r] = ds.x;
+                    p.rec_cnt[r] = sum;
+                }
+            }
+        }
+        unsigned const cb = __ballot_sync(kFullMask, emit_child);
+        if (cb)
+        {
+            unsigned const nc = __popc(cb);
+            if (depth + 1u > p.max_depth)
+            {
+                if (lane == 0)
+                    atomicOr(p.ctrl + C_ERROR, E_CYCLE);
+            }
+            else
+            {
+                unsigned long long base = 0;
+                if (lane == 0)
+                {
+                    atomicAdd(p.ctrl + C_PENDING, static_cast<unsigned long long>(nc));
+                    base = atomicAdd(p.ctrl + C_TAIL, static_cast<unsigned long long>(nc));
+                }
+                base = __shfl_sync(kFullMask, base, 0);
+                if (emit_child)
+                {
+                    unsigned long long const s = base + __popc(cb & lt_mask);
+                    if (s < p.task_cap)
+                    {
+                        atomicExch(p.tasks + s, make_task(q, depth + 1u, ds.x));
+                    }
+                    else
+                    {
+                        atomicOr(p.ctrl + C_ERROR, E_OVERFLOW_TASK);
+                        atomicAdd(p.ctrl + C_PENDING, ~0ull); // this child will never run
+                    }
+                    __threadfence();
+                }
+            }
+        }
+        unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
+        uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
+        carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
+    }
+    __syncwarp();
+    if (lane == 0)
+    {
+        __threadfence();
+        atomicAdd(p.ctrl + C_PENDING, ~0ull); // this task retires
+        ++n_tasks;
+        n_visits += n;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_query(query_params p)
+{
+    extern __shared__ uint32_t s_counts[];
+    int const lane = threadIdx.x & 31;
+    uint32_t * counts = s_counts + (threadIdx.x >> 5) * p.counters_per_warp;
+    if (p.self_init)
+    {
+        if (threadIdx.x == 0)
+        {
+            p.ctrl[C_HEAD] = 0;
+            p.ctrl[C_TAIL] = 0;
+            p.ctrl[C_PENDING] = p.n_queries;
+            __threadfence();
+        }
+        __syncthreads();
+    }
+    unsigned long long n_tasks = 0, n_visits = 0;
+    for (;;)
+    {
+        unsigned long long idx = 0;
+        if (lane == 0)
+            idx = atomicAdd(p.ctrl + C_HEAD, 1ull);
+        idx = __shfl_sync(kFullMask, idx, 0);
+        unsigned long long task;
+        if (idx < p.n_queries)
+        {
+            task = make_task(idx, 0u, 0u);
+        }
+        else
+        {
+            unsigned long long const slot = idx - p.n_queries;
+            if (slot >= p.task_cap)
+                break;
+            task = 0;
+            if (lane == 0)
+                task = wait_for_task(p, slot);
+            task = __shfl_sync(kFullMask, task, 0);
+            if (task == kEmpty)
+                break;
+        }
+        process_task(p, task, counts, lane, n_tasks, n_visits);
+    }
+    if (lane == 0 && n_tasks)
+    {
+        atomicAdd(p.stats + 0, n_tasks);
+        atomicAdd(p.stats + 1, n_visits);
+    }
+}
+
+__global__ void k_init_ctrl(unsigned long long * ctrl, unsigned long long * stats, uint64_t n_queries)
+{
+    if (threadIdx.x < C_WORDS)
+        ctrl[threadIdx.x] = threadIdx.x == C_PENDING ? n_queries : 0ull;
+    if (threadIdx.x < 2)
+        stats[threadIdx.x] = 0;
+}
+
+// ---- exclusive scan of the per-query result counts -> result offsets (n + 1 entries) ----
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ unsigned long long warp_incl_scan(unsigned long long x, int lane)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    return x;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_local(unsigned int const * __restrict__ in, uint64_t n,
+                                                          unsigned long long * __restrict__ out,
+                                                          unsigned long long * __restrict__ block_sums)
+{
+    __shared__ unsigned long long warp_sums[32];
+    uint64_t const i = blockIdx.x * static_cast<uint64_t>(kScanBlock) + threadIdx.x;
+    int const lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned long long const v = i < n ? in[i] : 0ull;
+    unsigned long long x = warp_incl_scan(v, lane);
+    if (lane == 31)
+        warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0)
+    {
+        unsigned long long s = warp_sums[lane];
+        s = warp_incl_scan(s, lane);
+        warp_sums[lane] = s;
+    }
+    __syncthreads();
+    if (w > 0)
+        x += warp_sums[w - 1];
+    if (i < n)
+        out[i] = x - v; // exclusive
+    if (threadIdx.x == kScanBlock - 1)
+        block_sums[blockIdx.x] = x;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_sums(unsigned long long * sums, uint64_t nb)
+{
+    __shared__ unsigned long long warp_sums[32];
+    __shared__ unsigned long long carry;
+    int const lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0)
+        carry = 0;
+    __syncthreads();
+    for (uint64_t base = 0; base < nb; base += kScanBlock)
+    {
+        uint64_t const i = base + threadIdx.x;
+        unsigned long long const v = i < nb ? sums[i] : 0ull;
+        unsigned long long x = warp_incl_scan(v, lane);
+        if (lane == 31)
+            warp_sums[w] = x;
+        __syncthreads();
+        if (w == 0)
+            warp_sums[lane] = warp_incl_scan(warp_sums[lane], lane);
+        __syncthreads();
+        if (w > 0)
+            x += warp_sums[w - 1];
+        unsigned long long const c = carry;
+        if (i < nb)
+            sums[i] = c + x - v; // exclusive
+        __syncthreads();
+        if (threadIdx.x == kScanBlock - 1)
+            carry = c + x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        sums[nb] = carry;
+}
+
+__global__ void k_scan_add(unsigned long long * out, uint64_t n, unsigned long long const * sums, uint64_t nb)
+{
+    uint64_t const i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    if (i < n)
+        out[i] += sums[i / kScanBlock];
+    if (i == 0)
+        out[n] = sums[nb];
+}
+
+// ---- scatter records into per-query segments ----
+__global__ void k_scatter(unsigned long long const * __restrict__ ctrl, uint32_t const * __restrict__ rec_q,
+                          uint32_t const * __restrict__ rec_ub, unsigned long long const * __restrict__ rec_cnt,
+                          uint64_t rec_cap, unsigned long long const * __restrict__ roff,
+                          unsigned int * __restrict__ cursor, uint64_t * __restrict__ out_ids,
+                          uint64_t * __restrict__ out_cnt)
+{
+    if (ctrl[C_ERROR] & (E_OVERFLOW_REC | E_OVERFLOW_TASK))
+        return; // offsets describe records that were not stored; the batch reports OVERFLOW
+    uint64_t n = ctrl[C_NREC];
+    if (n > rec_cap)
+        n = rec_cap;
+    for (uint64_t r = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; r < n;
+         r += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        uint32_t const q = rec_q[r];
+        uint64_t const pos = roff[q] + atomicAdd(cursor + q, 1u);
+        out_ids[pos] = rec_ub[r];
+        out_cnt[pos] = rec_cnt[r];
+    }
+}
+
+// ---- sort every query's segment by user bin id ----
+constexpr uint32_t kSmallSegment = 32;
+constexpr uint32_t kSmemSegment = 2048;
+
+__global__ void k_sort_small(unsigned long long const * __restrict__ roff, uint64_t nq, uint64_t * ids,
+                             uint64_t * cnt, uint32_t * large, unsigned long long * ctrl)
+{
+    if (ctrl[C_ERROR] & (E_OVERFLOW_REC | E_OVERFLOW_TASK))
+        return;
+    for (uint64_t q = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; q < nq;
+         q += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        uint64_t const b = roff[q], e = roff[q + 1];
+        uint64_t const len = e - b;
+        if (len <= 1)
+            continue;
+        if (len > kSmallSegment)
+        {
+            unsigned long long const slot = atomicAdd(ctrl + C_NLARGE, 1ull);
+            large[slot] = static_cast<uint32_t>(q);
+            continue;
+        }
+        for (uint64_t i = b + 1; i < e; ++i)
+        {
+            uint64_t const ki = ids[i], ci = cnt[i];
+            uint64_t jx = i;
+            while (jx > b && ids[jx - 1] > ki)
+            {
+                ids[jx] = ids[jx - 1];
+                cnt[jx] = cnt[jx - 1];
+                --jx;
+            }
+            ids[jx] = ki;
+            cnt[jx] = ci;
+        }
+    }
+}
+
+// Bitonic sort of one segment with only ascending comparators (the "flip" form: the first exchange of every merge
+// pairs i with its mirror in the block, the rest are half-cleaners).  Positions >= len are virtual +infinity and,
+// being the larger element of every comparator they take part in, never move, so any length works.  The segment is
+// staged in shared memory up to kSmemSegment elements and sorted in place in global memory beyond.
+__device__ __forceinline__ void cmp_asc(uint64_t * kid, uint64_t * kcn, uint64_t i, uint64_t l, uint64_t len)
+{
+    if (l >= len)
+        return;
+    if (kid[i] > kid[l])
+    {
+        uint64_t t = kid[i];
+        kid[i] = kid[l];
+        kid[l] = t;
+        t = kcn[i];
+        kcn[i] = kcn[l];
+        kcn[l] = t;
+    }
+}
+
+__global__ void k_sort_large(unsigned long long const * __restrict__ roff, uint32_t const * __restrict__ large,
+                             unsigned long long const * __restrict__ ctrl, uint64_t * ids, uint64_t * cnt)
+{
+    __shared__ uint64_t s_ids[kSmemSegment];
+    __shared__ uint64_t s_cnt[kSmemSegment];
+    if (ctrl[C_ERROR] & (E_OVERFLOW_REC | E_OVERFLOW_TASK))
+        return;
+    unsigned long long const nl = ctrl[C_NLARGE];
+    for (unsigned long long li = blockIdx.x; li < nl; li += gridDim.x)
+    {
+        uint32_t const q = large[li];
+        uint64_t const b = roff[q];
+        uint64_t const len = roff[q + 1] - b;
+        uint64_t P = 1;
+        while (P < len)
+            P <<= 1;
+        bool const in_smem = len <= kSmemSegment;
+        uint64_t * kid = in_smem ? s_ids : ids + b;
+        uint64_t * kcn = in_smem ? s_cnt : cnt + b;
+        if (in_smem)
+        {
+            for (uint64_t i = threadIdx.x; i < len; i += blockDim.x)
+            {
+                s_ids[i] = ids[b + i];
+                s_cnt[i] = cnt[b + i];
+            }
+        }
+        __syncthreads();
+        for (uint64_t k = 2; k <= P; k <<= 1)
+        {
+            for (uint64_t i = threadIdx.x; i < P; i += blockDim.x)
+            {
+                uint64_t const l = i ^ (k - 1);
+                if (l > i && i < len)
+                    cmp_asc(kid, kcn, i, l, len);
+            }
+            __syncthreads();
+            for (uint64_t jj = k >> 2; jj > 0; jj >>= 1)
+            {
+                for (uint64_t i = threadIdx.x; i < P; i += blockDim.x)
+                {
+                    uint64_t const l = i ^ jj;
+                    if (l > i && i < len)
+                        cmp_asc(kid, kcn, i, l, len);
+                }
+                __syncthreads();
+            }
+        }
+        if (in_smem)
+        {
+            for (uint64_t i = threadIdx.x; i < len; i += blockDim.x)
+            {
+                ids[b + i] = s_ids[i];
+                cnt[b + i] = s_cnt[i];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_narrow(unsigned long long const * __restrict__ roff, uint64_t nq, uint64_t const * __restrict__ in,
+                         int width, void * out, unsigned long long const * __restrict__ ctrl)
+{
+    if (ctrl[C_ERROR] & (E_OVERFLOW_REC | E_OVERFLOW_TASK))
+        return;
+    uint64_t const n = roff[nq];
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        uint64_t const v = in[i];
+        switch (width)
+        {
+        case 1:
+            static_cast<uint8_t *>(out)[i] = static_cast<uint8_t>(v);
+            break;
+        case 2:
+            static_cast<uint16_t *>(out)[i] = static_cast<uint16_t>(v);
+            break;
+        case 4:
+            static_cast<uint32_t *>(out)[i] = static_cast<uint32_t>(v);
+            break;
+        default:
+            static_cast<uint64_t *>(out)[i] = v;
+        }
+    }
+}
+
+// emplace into an IBF (same as the single-level kernel, repeated here to keep the translation units independent).
+__global__ void k_hibf_emplace(uint64_t * __restrict__ words, uint64_t bin_size, uint32_t row_words, uint32_t shift,
+                               uint32_t h, uint64_t const * __restrict__ values, uint64_t const * __restrict__ bins,
+                               uint64_t n, uint64_t bin, uint64_t n_bins)
+{
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        uint64_t const v = values[i];
+        uint64_t const b = bins ? bins[i] : bin;
+        if (b >= n_bins)
+            continue; // out-of-range device-supplied bin: skipped (never written outside the IBF's row)
+        unsigned long long const bit = 1ull << (b & 63u);
+        uint64_t const wofs = b >> 6;
+        for (uint32_t k = 0; k < h; ++k)
+        {
+            uint64_t const r = hash_row(v, c_hash_seeds[k], shift, bin_size);
+            atomicOr(reinterpret_cast<unsigned long long *>(words + r * row_words + wofs), bit);
+        }
+    }
+}
+
+unsigned grid_cap(uint64_t work, unsigned block, unsigned per_sm = 16)
+{
+    uint64_t const want = (work + block - 1) / block;
+    uint64_t const cap = static_cast<uint64_t>(sm_count()) * per_sm;
+    return static_cast<unsigned>(std::max<uint64_t>(1, std::min(want, cap)));
+}
+
+} // namespace
+} // namespace hibf_gb300
+
+using namespace hibf_gb300;
+
+struct hibf_gpu_hibf
+{
+    uint64_t n_user_bins{};
+    uint64_t n_ibfs{};
+    uint32_t max_depth{};
+    uint32_t counters_per_warp{};
+    uint64_t total_bytes{};
+    std::vector<dev_node> nodes;           // host copy
+    std::vector<std::unique_ptr<dbuf>> stores;
+    std::vector<uint64_t> bins, bin_size, hash_funs, bin_words, row_words;
+    dbuf d_nodes;
+    dbuf d_descs;
+    dbuf io;
+    cudaStream_t stream{};
+    std::mutex mu;
+};
+
+struct hibf_gpu_agent
+{
+    hibf_gpu_hibf * h{};
+    cudaStream_t own{};
+    cudaStream_t stream{};
+    int status{HIBF_GPU_OK};
+    uint64_t last_tasks{}, last_visits{};
+    uint64_t cap_queries{}, cap_tasks{}, cap_results{};
+    int max_blocks_per_sm{};
+    // device workspace
+    dbuf ctrl, stats, tasks, rec_q, rec_ub, rec_cnt, qcount, cursor, roff, bsum, out_ids, out_cnt, out_cntw, large;
+    // host-call staging
+    dbuf in_values, in_qoff, in_thr;
+    hbuf h_roff, h_ids, h_cnt, h_ctrl, h_stats;
+    std::vector<uint64_t> single_ids;
+    std::vector<uint8_t> dense;
+    std::vector<uint64_t> thr_tmp, qoff_tmp;
+};
+
+namespace
+{
+
+void ensure_capacity(hibf_gpu_agent * a, uint64_t nq, uint64_t tasks, uint64_t results)
+{
+    if (nq > a->cap_queries)
+    {
+        a->qcount.ensure(nq * 4);
+        a->cursor.ensure(nq * 4);
+        a->roff.ensure((nq + 1) * 8);
+        a->bsum.ensure(((nq + kScanBlock - 1) / kScanBlock + 1) * 8);
+        a->large.ensure(nq * 4);
+        a->cap_queries = nq;
+    }
+    if (tasks > a->cap_tasks)
+    {
+        a->tasks.ensure(tasks * 8);
+        a->cap_tasks = tasks;
+    }
+    if (results > a->cap_results)
+    {
+        a->rec_q.ensure(results * 4);
+        a->rec_ub.ensure(results * 4);
+        a->rec_cnt.ensure(results * 8);
+        a->out_ids.ensure(results * 8);
+        a->out_cnt.ensure(results * 8);
+        a->out_cntw.ensure(results * 8);
+        a->cap_results = results;
+    }
+}
+
+query_params base_params(hibf_gpu_agent * a, uint64_t const * d_values, uint64_t const * d_qoff,
+                         uint64_t const * d_thr, uint64_t nq, uint64_t count_mask)
+{
+    hibf_gpu_hibf * h = a->h;
+    query_params p{};
+    p.nodes = h->d_nodes.as<dev_node>();
+    p.descs = h->d_descs.as<uint2>();
+    p.values = d_values;
+    p.qoff = d_qoff;
+    p.thr = d_thr;
+    p.count_mask = count_mask;
+    p.n_queries = nq;
+    p.q_base = 0;
+    p.max_depth = h->max_depth;
+    p.counters_per_warp = h->counters_per_warp;
+    p.tasks = a->tasks.as<unsigned long long>();
+    p.task_cap = a->cap_tasks;
+    p.ctrl = a->ctrl.as<unsigned long long>();
+    p.rec_q = a->rec_q.as<uint32_t>();
+    p.rec_ub = a->rec_ub.as<uint32_t>();
+    p.rec_cnt = a->rec_cnt.as<unsigned long long>();
+    p.rec_cap = a->cap_results;
+    p.qcount = a->qcount.as<unsigned int>();
+    p.stats = a->stats.as<unsigned long long>();
+    p.wait_limit_ns = 10ull * 1000 * 1000 * 1000;
+    p.self_init = 0;
+    return p;
+}
+
+uint64_t mask_for(int mode, int width)
+{
+    int const w = mode == HIBF_GPU_QUERY_MEMBERSHIP ? 2 : width;
+    return w >= 8 ? ~0ull : ((1ull << (8 * w)) - 1u);
+}
+
+size_t query_smem(hibf_gpu_hibf const * h)
+{
+    return static_cast<size_t>(8) * h->counters_per_warp * sizeof(uint32_t);
+}
+
+void launch_postprocess(hibf_gpu_agent * a, uint64_t nq, int mode, int width)
+{
+    cudaStream_t s = a->stream;
+    uint64_t const nb = (nq + kScanBlock - 1) / kScanBlock;
+    if (nq)
+    {
+        k_scan_local<<<static_cast<unsigned>(nb), kScanBlock, 0, s>>>(
+            a->qcount.as<unsigned int>(), nq, a->roff.as<unsigned long long>(), a->bsum.as<unsigned long long>());
+        HG_CUDA(cudaGetLastError());
+    }
+    k_scan_sums<<<1, kScanBlock, 0, s>>>(a->bsum.as<unsigned long long>(), nb);
+    HG_CUDA(cudaGetLastError());
+    k_scan_add<<<static_cast<unsigned>(std::max<uint64_t>(1, (nq + 255) / 256)), 256, 0, s>>>(
+        a->roff.as<unsigned long long>(), nq, a->bsum.as<unsigned long long>(), nb);
+    HG_CUDA(cudaGetLastError());
+    HG_CUDA(cudaMemsetAsync(a->cursor.p, 0, std::max<uint64_t>(nq, 1) * 4, s));
+    k_scatter<<<grid_cap(a->cap_results, 256, 8), 256, 0, s>>>(
+        a->ctrl.as<unsigned long long>(), a->rec_q.as<uint32_t>(), a->rec_ub.as<uint32_t>(),
+        a->rec_cnt.as<unsigned long long>(), a->cap_results, a->roff.as<unsigned long long>(),
+        a->cursor.as<unsigned int>(), a->out_ids.as<uint64_t>(), a->out_cnt.as<uint64_t>());
+    HG_CUDA(cudaGetLastError());
+    k_sort_small<<<grid_cap(nq, 256, 8), 256, 0, s>>>(a->roff.as<unsigned long long>(), nq, a->out_ids.as<uint64_t>(),
+                                                     a->out_cnt.as<uint64_t>(), a->large.as<uint32_t>(),
+                                                     a->ctrl.as<unsigned long long>());
+    HG_CUDA(cudaGetLastError());
+    k_sort_large<<<static_cast<unsigned>(sm_count()), 256, 0, s>>>(
+        a->roff.as<unsigned long long>(), a->large.as<uint32_t>(), a->ctrl.as<unsigned long long>(),
+        a->out_ids.as<uint64_t>(), a->out_cnt.as<uint64_t>());
+    HG_CUDA(cudaGetLastError());
+    if (mode == HIBF_GPU_QUERY_COUNT && width != 8)
+    {
+        k_narrow<<<grid_cap(a->cap_results, 256, 8), 256, 0, s>>>(a->roff.as<unsigned long long>(), nq,
+                                                                 a->out_cnt.as<uint64_t>(), width, a->out_cntw.p,
+                                                                 a->ctrl.as<unsigned long long>());
+        HG_CUDA(cudaGetLastError());
+    }
+}
+
+// One persistent launch over all queries plus compaction.  Asynchronous.
+void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint64_t const * d_qoff,
+                  uint64_t const * d_thr, uint64_t nq, int width)
+{
+    hibf_gpu_hibf * h = a->h;
+    cudaStream_t s = a->stream;
+    k_init_ctrl<<<1, 32, 0, s>>>(a->ctrl.as<unsigned long long>(), a->stats.as<unsigned long long>(), nq);
+    HG_CUDA(cudaGetLastError());
+    HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, a->cap_tasks * 8, s));
+    HG_CUDA(cudaMemsetAsync(a->qcount.p, 0, std::max<uint64_t>(nq, 1) * 4, s));
+    if (nq)
+    {
+        query_params p = base_params(a, d_values, d_qoff, d_thr, nq, mask_for(mode, width));
+        uint64_t const full = static_cast<uint64_t>(sm_count()) * static_cast<uint64_t>(a->max_blocks_per_sm);
+        uint64_t const want = (nq + 7) / 8;
+        unsigned const grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min(full, want)));
+        k_query<<<grid, 256, query_smem(h), s>>>(p);
+        HG_CUDA(cudaGetLastError());
+    }
+    launch_postprocess(a, nq, mode, width);
+}
+
+// Plain form: one single-block launch per query (the block resets its own control words), then one compaction.
+void launch_plain(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint64_t const * h_qoff,
+                  uint64_t const * d_qoff, uint64_t const * d_thr, uint64_t nq, int width)
+{
+    hibf_gpu_hibf * h = a->h;
+    cudaStream_t s = a->stream;
+    k_init_ctrl<<<1, 32, 0, s>>>(a->ctrl.as<unsigned long long>(), a->stats.as<unsigned long long>(), 0);
+    HG_CUDA(cudaGetLastError());
+    HG_CUDA(cudaMemsetAsync(a->qcount.p, 0, std::max<uint64_t>(nq, 1) * 4, s));
+    uint64_t const mask = mask_for(mode, width);
+    for (uint64_t q = 0; q < nq; ++q)
+    {
+        (void)h_qoff;
+        query_params p = base_params(a, d_values, d_qoff + q, d_thr + q, 1, mask);
+        p.q_base = q;
+        p.self_init = 1;
+        HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u) * 8, s));
+        p.task_cap = std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u);
+        k_query<<<1, 256, query_smem(h), s>>>(p);
+        HG_CUDA(cudaGetLastError());
+    }
+    launch_postprocess(a, nq, mode, width);
+}
+
+int read_status(hibf_gpu_agent * a)
+{
+    HG_CUDA(cudaMemcpyAsync(a->h_ctrl.p, a->ctrl.p, C_WORDS * 8, cudaMemcpyDeviceToHost, a->stream));
+    HG_CUDA(cudaMemcpyAsync(a->h_stats.p, a->stats.p, 2 * 8, cudaMemcpyDeviceToHost, a->stream));
+    HG_CUDA(cudaStreamSynchronize(a->stream));
+    unsigned long long const * c = a->h_ctrl.as<unsigned long long>();
+    unsigned long long const * st = a->h_stats.as<unsigned long long>();
+    a->last_tasks = st[0];
+    a->last_visits = st[1];
+    unsigned long long const e = c[C_ERROR];
+    if (e & E_TIMEOUT)
+        return HIBF_GPU_ERR_TIMEOUT;
+    if (e & E_CYCLE)
+        return HIBF_GPU_ERR_CYCLE;
+    if (e & (E_OVERFLOW_REC | E_OVERFLOW_TASK))
+        return HIBF_GPU_ERR_OVERFLOW;
+    return HIBF_GPU_OK;
+}
+
+void check_mode(int mode, int width, uint64_t const * thr, uint64_t nq)
+{
+    if (mode != HIBF_GPU_QUERY_MEMBERSHIP && mode != HIBF_GPU_QUERY_COUNT)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "mode must be HIBF_GPU_QUERY_MEMBERSHIP or HIBF_GPU_QUERY_COUNT");
+    if (mode == HIBF_GPU_QUERY_COUNT && !(width == 1 || width == 2 || width == 4 || width == 8))
+        fail(HIBF_GPU_ERR_INVALID_ARG, "width must be 1, 2, 4 or 8");
+    if (thr)
+        for (uint64_t q = 0; q < nq; ++q)
+        {
+            if (mode == HIBF_GPU_QUERY_MEMBERSHIP && thr[q] > 0xFFFFu)
+                fail(HIBF_GPU_ERR_INVALID_ARG, "membership thresholds are uint16");
+            if (mode == HIBF_GPU_QUERY_COUNT && thr[q] == 0)
+                fail(HIBF_GPU_ERR_INVALID_ARG, "bulk_count thresholds must be > 0");
+        }
+}
+
+// Host-pointer batch with automatic growth on overflow.  Results land in the agent's pinned host buffers.
+void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t const * qoff, uint64_t nq,
+                uint64_t const * thr, int width, bool plain)
+{
+    check_mode(mode, width, thr, nq);
+    for (uint64_t q = 0; q < nq; ++q)
+        if (qoff[q + 1] < qoff[q])
+            fail(HIBF_GPU_ERR_INVALID_ARG, "query offsets must be non-decreasing");
+    uint64_t const nv = nq ? qoff[nq] : 0;
+    a->in_values.ensure(nv * 8);
+    a->in_qoff.ensure((nq + 1) * 8);
+    a->in_thr.ensure(std::max<uint64_t>(nq, 1) * 8);
+    if (nv)
+        HG_CUDA(cudaMemcpyAsync(a->in_values.p, values, nv * 8, cudaMemcpyHostToDevice, a->stream));
+    HG_CUDA(cudaMemcpyAsync(a->in_qoff.p, qoff, (nq + 1) * 8, cudaMemcpyHostToDevice, a->stream));
+    if (nq)
+        HG_CUDA(cudaMemcpyAsync(a->in_thr.p, thr, nq * 8, cudaMemcpyHostToDevice, a->stream));
+    uint64_t tasks = std::max<uint64_t>(a->cap_tasks, nq * 4 + 1024);
+    uint64_t results = std::max<uint64_t>(a->cap_results, nq * 4 + 1024);
+    for (int attempt = 0;; ++attempt)
+    {
+        ensure_capacity(a, std::max<uint64_t>(nq, 1), tasks, results);
+        if (plain)
+            launch_plain(a, mode, a->in_values.as<uint64_t>(), qoff, a->in_qoff.as<uint64_t>(),
+                         a->in_thr.as<uint64_t>(), nq, width);
+        else
+            launch_batch(a, mode, a->in_values.as<uint64_t>(), a->in_qoff.as<uint64_t>(), a->in_thr.as<uint64_t>(),
+                         nq, width);
+        int const st = read_status(a);
+        if (st == HIBF_GPU_OK)
+            break;
+        unsigned long long const * c = a->h_ctrl.as<unsigned long long>();
+        if (st != HIBF_GPU_ERR_OVERFLOW || attempt > 8)
+            fail(st, st == HIBF_GPU_ERR_TIMEOUT ? "device wait limit expired" :
+                     st == HIBF_GPU_ERR_CYCLE   ? "merged bins form a cycle (descent deeper than the hierarchy)" :
+                                                  "batch capacity exceeded");
+        if (c[C_ERROR] & E_OVERFLOW_TASK)
+            tasks *= 4;
+        if (c[C_ERROR] & E_OVERFLOW_REC)
+            results = std::max<uint64_t>(results * 4, c[C_NREC] + 1024);
+    }
+    a->h_roff.ensure((nq + 1) * 8);
+    HG_CUDA(cudaMemcpyAsync(a->h_roff.p, a->roff.p, (nq + 1) * 8, cudaMemcpyDeviceToHost, a->stream));
+    HG_CUDA(cudaStreamSynchronize(a->stream));
+    uint64_t const nr = a->h_roff.as<uint64_t>()[nq];
+    a->h_ids.ensure(nr * 8);
+    a->h_cnt.ensure(nr * 8);
+    if (nr)
+    {
+        HG_CUDA(cudaMemcpyAsync(a->h_ids.p, a->out_ids.p, nr * 8, cudaMemcpyDeviceToHost, a->stream));
+        if (mode == HIBF_GPU_QUERY_COUNT)
+            HG_CUDA(cudaMemcpyAsync(a->h_cnt.p, width == 8 ? a->out_cnt.p : a->out_cntw.p, nr * width,
+                                    cudaMemcpyDeviceToHost, a->stream));
+    }
+    HG_CUDA(cudaStreamSynchronize(a->stream));
+}
+
+} // namespace
+
+extern "C"
+{
+
+    int hibf_gpu_hibf_create(uint64_t n_user_bins, uint64_t n_ibfs, uint64_t const * bins,
+                             uint64_t const * bin_sizes, uint64_t const * hash_funs, uint64_t const * next_ibf_id,
+                             uint64_t const * user_bin_id, hibf_gpu_hibf ** out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!out || !bins || !bin_sizes || !hash_funs || !next_ibf_id || !user_bin_id)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *out = nullptr;
+                if (n_ibfs == 0 || n_ibfs > kNodeMask)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "number of IBFs must be in [1, 2^26)");
+                if (n_user_bins >= 0xFFFFFFFEull)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "number of user bins must be below 2^32 - 2");
+                std::vector<uint64_t> off(n_ibfs + 1, 0);
+                for (uint64_t k = 0; k < n_ibfs; ++k)
+                {
+                    if (bins[k] == 0)
+                        fail(HIBF_GPU_ERR_LOGIC, "The number of bins must be > 0.");
+                    if (hash_funs[k] == 0 || hash_funs[k] > 5)
+                        fail(HIBF_GPU_ERR_LOGIC, "The number of hash functions must be > 0 and <= 5.");
+                    if (bin_sizes[k] == 0)
+                        fail(HIBF_GPU_ERR_LOGIC, "The size of a bin must be > 0.");
+                    off[k + 1] = off[k] + bins[k];
+                }
+                if (off[n_ibfs] >= 0xFFFFFFFFull)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "too many technical bins in total");
+                // per-bin descriptors
+                std::vector<uint2> descs(off[n_ibfs]);
+                for (uint64_t k = 0; k < n_ibfs; ++k)
+                {
+                    for (uint64_t b = 0; b < bins[k]; ++b)
+                    {
+                        uint64_t const i = off[k] + b;
+                        uint64_t const ub = user_bin_id[i];
+                        uint32_t flags = 0;
+                        uint32_t id = 0;
+                        if (ub == HIBF_GPU_BIN_MERGED)
+                        {
+                            flags |= F_MERGED;
+                            if (next_ibf_id[i] >= n_ibfs)
+                                fail(HIBF_GPU_ERR_INVALID_ARG, "next_ibf_id out of range");
+                            id = static_cast<uint32_t>(next_ibf_id[i]);
+                        }
+                        else if (ub == HIBF_GPU_BIN_DELETED)
+                        {
+                            flags |= F_DELETED;
+                        }
+                        else
+                        {
+                            if (ub >= n_user_bins)
+                                fail(HIBF_GPU_ERR_INVALID_ARG, "user bin id out of range");
+                            id = static_cast<uint32_t>(ub);
+                            // last bin || end of split bin (HIBF.hpp:345)
+                            if (b + 1 == bins[k] || ub != user_bin_id[i + 1])
+                                flags |= F_RUN_END;
+                        }
+                        if (b == 0)
+                            flags |= F_HEAD;
+                        else
+                        {
+                            uint64_t const pu = user_bin_id[i - 1];
+                            bool const prev_merged = pu == HIBF_GPU_BIN_MERGED;
+                            bool const prev_end = pu != HIBF_GPU_BIN_MERGED && pu != HIBF_GPU_BIN_DELETED &&
+                                                  pu != ub;
+                            if (prev_merged || prev_end)
+                                flags |= F_HEAD;
+                        }
+                        descs[i] = make_uint2(id, flags);
+                    }
+                }
+                // depth of the hierarchy (longest merged-bin path from the root); a cycle makes it unbounded
+                std::vector<uint32_t> depth(n_ibfs, 0xFFFFFFFFu);
+                std::vector<uint64_t> stack{0};
+                depth[0] = 0;
+                uint32_t max_depth = 0;
+                uint64_t visited = 0;
+                while (!stack.empty())
+                {
+                    uint64_t const k = stack.back();
+                    stack.pop_back();
+                    if (++visited > n_ibfs)
+                        break;
+                    for (uint64_t b = 0; b < bins[k]; ++b)
+                    {
+                        uint64_t const i = off[k] + b;
+                        if (user_bin_id[i] != HIBF_GPU_BIN_MERGED)
+                            continue;
+                        uint64_t const c = next_ibf_id[i];
+                        if (depth[c] != 0xFFFFFFFFu)
+                            continue; // already reached (or a cycle); the device enforces the depth bound
+                        depth[c] = depth[k] + 1;
+                        max_depth = std::max(max_depth, depth[c]);
+                        stack.push_back(c);
+                    }
+                }
+                if (max_depth > 60)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "hierarchy deeper than 60 levels");
+                require_device();
+                auto h = new hibf_gpu_hibf{};
+                try
+                {
+                    h->n_user_bins = n_user_bins;
+                    h->n_ibfs = n_ibfs;
+                    h->max_depth = max_depth;
+                    HG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+                    uint32_t cpw = 64;
+                    for (uint64_t k = 0; k < n_ibfs; ++k)
+                    {
+                        uint64_t const bw = (bins[k] + 63u) / 64u;
+                        uint64_t const rw = padded_row_words(bw);
+                        h->bins.push_back(bins[k]);
+                        h->bin_size.push_back(bin_sizes[k]);
+                        h->hash_funs.push_back(hash_funs[k]);
+                        h->bin_words.push_back(bw);
+                        h->row_words.push_back(rw);
+                        auto st = std::make_unique<dbuf>();
+                        size_t const bytes = bin_sizes[k] * rw * 8;
+                        st->ensure(bytes);
+                        HG_CUDA(cudaMemsetAsync(st->p, 0, bytes, h->stream));
+                        h->total_bytes += bytes;
+                        dev_node nd{};
+                        nd.words = st->as<uint64_t>();
+                        nd.bin_size = bin_sizes[k];
+                        nd.bins = static_cast<uint32_t>(bins[k]);
+                        nd.bin_words = static_cast<uint32_t>(bw);
+                        nd.row_words = static_cast<uint32_t>(rw);
+                        nd.hash_shift = static_cast<uint32_t>(__builtin_clzll(bin_sizes[k]));
+                        nd.hash_funs = static_cast<uint32_t>(hash_funs[k]);
+                        nd.desc_offset = static_cast<uint32_t>(off[k]);
+                        nd.lpv_log2 = lanes_per_value_log2(bw);
+                        uint32_t const need = bw > 32 ? static_cast<uint32_t>(64 * bw) : (64u << nd.lpv_log2);
+                        cpw = std::max(cpw, need);
+                        h->nodes.push_back(nd);
+                        h->stores.push_back(std::move(st));
+                    }
+                    h->counters_per_warp = cpw;
+                    if (static_cast<size_t>(8) * cpw * 4 > 200 * 1024)
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "an IBF is too wide for the query kernel's shared counters");
+                    h->d_nodes.ensure(n_ibfs * sizeof(dev_node));
+                    HG_CUDA(cudaMemcpyAsync(h->d_nodes.p, h->nodes.data(), n_ibfs * sizeof(dev_node),
+                                            cudaMemcpyHostToDevice, h->stream));
+                    h->d_descs.ensure(descs.size() * sizeof(uint2));
+                    HG_CUDA(cudaMemcpyAsync(h->d_descs.p, descs.data(), descs.size() * sizeof(uint2),
+                                            cudaMemcpyHostToDevice, h->stream));
+                    HG_CUDA(cudaStreamSynchronize(h->stream));
+                    size_t const smem = query_smem(h);
+                    HG_CUDA(cudaFuncSetAttribute(k_query, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(std::max<size_t>(smem, 48 * 1024))));
+                }
+                catch (...)
+                {
+                    if (h->stream)
+                        cudaStreamDestroy(h->stream);
+                    delete h;
+                    throw;
+                }
+                *out = h;
+            });
+    }
+
+    int hibf_gpu_hibf_destroy(hibf_gpu_hibf * h)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h)
+                    return;
+                cudaStreamSynchronize(h->stream);
+                cudaStreamDestroy(h->stream);
+                delete h;
+            });
+    }
+
+    int hibf_gpu_hibf_info(hibf_gpu_hibf const * h, uint64_t out[4])
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                out[0] = h->n_user_bins;
+                out[1] = h->n_ibfs;
+                out[2] = h->max_depth;
+                out[3] = h->total_bytes;
+            });
+    }
+
+    int hibf_gpu_hibf_ibf_info(hibf_gpu_hibf const * h, uint64_t k, uint64_t out[5])
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || !out || k >= h->n_ibfs)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                out[0] = h->bins[k];
+                out[1] = h->bin_words[k] * 64;
+                out[2] = h->bin_size[k];
+                out[3] = h->hash_funs[k];
+                out[4] = h->row_words[k] * 8;
+            });
+    }
+
+    int hibf_gpu_hibf_emplace_d(hibf_gpu_hibf * h, uint64_t k, uint64_t const * d_values, uint64_t const * d_bins,
+                                uint64_t n, uint64_t bin, void * stream)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || k >= h->n_ibfs || (n && !d_values))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                if (!d_bins && bin >= h->bins[k])
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bin index out of range");
+                if (!n)
+                    return;
+                cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+                dev_node const & nd = h->nodes[k];
+                k_hibf_emplace<<<grid_cap(n, 256), 256, 0, s>>>(const_cast<uint64_t *>(nd.words), nd.bin_size,
+                                                                nd.row_words, nd.hash_shift, nd.hash_funs, d_values,
+                                                                d_bins, n, bin, h->bins[k]);
+                HG_CUDA(cudaGetLastError());
+            });
+    }
+
+    int hibf_gpu_hibf_emplace(hibf_gpu_hibf * h, uint64_t k, uint64_t const * values, uint64_t n, uint64_t bin)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || k >= h->n_ibfs || (n && !values))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                if (bin >= h->bins[k])
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bin index out of range");
+                if (!n)
+                    return;
+                std::lock_guard<std::mutex> lk(h->mu);
+                h->io.ensure(n * 8);
+                HG_CUDA(cudaMemcpyAsync(h->io.p, values, n * 8, cudaMemcpyHostToDevice, h->stream));
+                dev_node const & nd = h->nodes[k];
+                k_hibf_emplace<<<grid_cap(n, 256), 256, 0, h->stream>>>(
+                    const_cast<uint64_t *>(nd.words), nd.bin_size, nd.row_words, nd.hash_shift, nd.hash_funs,
+                    h->io.as<uint64_t>(), nullptr, n, bin, h->bins[k]);
+                HG_CUDA(cudaGetLastError());
+                HG_CUDA(cudaStreamSynchronize(h->stream));
+            });
+    }
+
+    int hibf_gpu_hibf_upload_words(hibf_gpu_hibf * h, uint64_t k, uint64_t const * words, uint64_t n_words)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || k >= h->n_ibfs || !words)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                if (n_words != h->bin_words[k] * h->bin_size[k])
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "word count does not match the IBF");
+                std::lock_guard<std::mutex> lk(h->mu);
+                HG_CUDA(cudaMemcpy2DAsync(h->stores[k]->p, h->row_words[k] * 8, words, h->bin_words[k] * 8,
+                                          h->bin_words[k] * 8, h->bin_size[k], cudaMemcpyHostToDevice, h->stream));
+                HG_CUDA(cudaStreamSynchronize(h->stream));
+            });
+    }
+
+    int hibf_gpu_hibf_download_words(hibf_gpu_hibf * h, uint64_t k, uint64_t * words, uint64_t n_words)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || k >= h->n_ibfs || !words)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                if (n_words != h->bin_words[k] * h->bin_size[k])
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "word count does not match the IBF");
+                std::lock_guard<std::mutex> lk(h->mu);
+                HG_CUDA(cudaDeviceSynchronize());
+                HG_CUDA(cudaMemcpy2DAsync(words, h->bin_words[k] * 8, h->stores[k]->p, h->row_words[k] * 8,
+                                          h->bin_words[k] * 8, h->bin_size[k], cudaMemcpyDeviceToHost, h->stream));
+                HG_CUDA(cudaStreamSynchronize(h->stream));
+            });
+    }
+
+    int hibf_gpu_agent_create(hibf_gpu_hibf * h, hibf_gpu_agent ** out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *out = nullptr;
+                auto a = new hibf_gpu_agent{};
+                try
+                {
+                    a->h = h;
+                    HG_CUDA(cudaStreamCreateWithFlags(&a->own, cudaStreamNonBlocking));
+                    a->stream = a->own;
+                    a->ctrl.ensure(C_WORDS * 8);
+                    a->stats.ensure(2 * 8);
+                    a->h_ctrl.ensure(C_WORDS * 8);
+                    a->h_stats.ensure(2 * 8);
+                    int nb = 0;
+                    HG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_query, 256, query_smem(h)));
+                    a->max_blocks_per_sm = std::max(1, nb);
+                    ensure_capacity(a, 1024, 4096, 4096);
+                }
+                catch (...)
+                {
+                    if (a->own)
+                        cudaStreamDestroy(a->own);
+                    delete a;
+                    throw;
+                }
+                *out = a;
+            });
+    }
+
+    int hibf_gpu_agent_destroy(hibf_gpu_agent * a)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a)
+                    return;
+                cudaStreamSynchronize(a->stream);
+                cudaStreamDestroy(a->own);
+                delete a;
+            });
+    }
+
+    int hibf_gpu_agent_set_stream(hibf_gpu_agent * a, void * stream)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                a->stream = stream ? static_cast<cudaStream_t>(stream) : a->own;
+            });
+    }
+
+    int hibf_gpu_agent_reserve(hibf_gpu_agent * a, uint64_t max_queries, uint64_t max_values, uint64_t max_tasks,
+                               uint64_t max_results)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                ensure_capacity(a, std::max<uint64_t>(max_queries, 1), std::max<uint64_t>(max_tasks, 1),
+                                std::max<uint64_t>(max_results, 1));
+                a->in_values.ensure(max_values * 8);
+                a->in_qoff.ensure((max_queries + 1) * 8);
+                a->in_thr.ensure(std::max<uint64_t>(max_queries, 1) * 8);
+            });
+    }
+
+    int hibf_gpu_agent_membership_for(hibf_gpu_agent * a, uint64_t const * values, uint64_t n, uint16_t threshold,
+                                      uint64_t const ** ids, uint64_t * n_ids)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || (n && !values) || !ids || !n_ids)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                uint64_t const qoff[2] = {0, n};
+                uint64_t const thr = threshold;
+                host_batch(a, HIBF_GPU_QUERY_MEMBERSHIP, values, qoff, 1, &thr, 2, true);
+                uint64_t const nr = a->h_roff.as<uint64_t>()[1];
+                a->single_ids.assign(a->h_ids.as<uint64_t>(), a->h_ids.as<uint64_t>() + nr);
+                *ids = a->single_ids.data();
+                *n_ids = nr;
+            });
+    }
+
+    int hibf_gpu_agent_bulk_count(hibf_gpu_agent * a, uint64_t const * values, uint64_t n, uint64_t threshold,
+                                  int width, void const ** counts)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || (n && !values) || !counts)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                uint64_t const qoff[2] = {0, n};
+                host_batch(a, HIBF_GPU_QUERY_COUNT, values, qoff, 1, &threshold, width, true);
+                uint64_t const nr = a->h_roff.as<uint64_t>()[1];
+                a->dense.assign(a->h->n_user_bins * static_cast<size_t>(width), 0);
+                uint8_t const * src = a->h_cnt.as<uint8_t>();
+                uint64_t const * ids = a->h_ids.as<uint64_t>();
+                for (uint64_t i = 0; i < nr; ++i)
+                    std::memcpy(a->dense.data() + ids[i] * width, src + i * width, width);
+                *counts = a->dense.data();
+            });
+    }
+
+    int hibf_gpu_agent_query_batch(hibf_gpu_agent * a, int mode, uint64_t const * values,
+                                   uint64_t const * query_offsets, uint64_t n_queries, uint64_t const * thresholds,
+                                   int width, uint64_t const ** result_offsets, uint64_t const ** result_ids,
+                                   void const ** result_counts)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !query_offsets || (n_queries && !thresholds) || !result_offsets || !result_ids)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (n_queries >= 0xFFFFFFFFull)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "at most 2^32 - 1 queries per batch");
+                if (n_queries && query_offsets[n_queries] && !values)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null values");
+                host_batch(a, mode, values, query_offsets, n_queries, thresholds, width, false);
+                *result_offsets = a->h_roff.as<uint64_t>();
+                *result_ids = a->h_ids.as<uint64_t>();
+                if (result_counts)
+                    *result_counts = mode == HIBF_GPU_QUERY_COUNT ? a->h_cnt.p : nullptr;
+            });
+    }
+
+    int hibf_gpu_agent_query_batch_d(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
+                                     uint64_t const * d_query_offsets, uint64_t n_queries,
+                                     uint64_t const * d_thresholds, int width, uint64_t const ** d_result_offsets,
+                                     uint64_t const ** d_result_ids, void const ** d_result_counts)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !d_query_offsets || (n_queries && (!d_thresholds || !d_values)))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (n_queries >= 0xFFFFFFFFull)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "at most 2^32 - 1 queries per batch");
+                check_mode(mode, width, nullptr, 0);
+                ensure_capacity(a, std::max<uint64_t>(n_queries, 1), std::max<uint64_t>(a->cap_tasks, 1024),
+                                std::max<uint64_t>(a->cap_results, 1024));
+                launch_batch(a, mode, d_values, d_query_offsets, d_thresholds, n_queries, width);
+                if (d_result_offsets)
+                    *d_result_offsets = a->roff.as<uint64_t>();
+                if (d_result_ids)
+                    *d_result_ids = a->out_ids.as<uint64_t>();
+                if (d_result_counts)
+                    *d_result_counts = mode == HIBF_GPU_QUERY_COUNT ? (width == 8 ? a->out_cnt.p : a->out_cntw.p)
+                                                                   : nullptr;
+            });
+    }
+
+    int hibf_gpu_agent_query_plain_d(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
+                                     uint64_t const * h_query_offsets, uint64_t n_queries,
+                                     uint64_t const * h_thresholds, int width)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !h_query_offsets || (n_queries && (!h_thresholds || !d_values)))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                check_mode(mode, width, h_thresholds, n_queries);
+                ensure_capacity(a, std::max<uint64_t>(n_queries, 1), std::max<uint64_t>(a->cap_tasks, 1024),
+                                std::max<uint64_t>(a->cap_results, 1024));
+                a->in_qoff.ensure((n_queries + 1) * 8);
+                a->in_thr.ensure(std::max<uint64_t>(n_queries, 1) * 8);
+                HG_CUDA(cudaMemcpyAsync(a->in_qoff.p, h_query_offsets, (n_queries + 1) * 8, cudaMemcpyHostToDevice,
+                                        a->stream));
+                if (n_queries)
+                    HG_CUDA(cudaMemcpyAsync(a->in_thr.p, h_thresholds, n_queries * 8, cudaMemcpyHostToDevice,
+                                            a->stream));
+                launch_plain(a, mode, d_values, h_query_offsets, a->in_qoff.as<uint64_t>(), a->in_thr.as<uint64_t>(),
+                             n_queries, width);
+            });
+    }
+
+    int hibf_gpu_agent_fetch_results(hibf_gpu_agent * a, uint64_t n_queries, int mode, int width,
+                                     uint64_t const ** result_offsets, uint64_t const ** result_ids,
+                                     void const ** result_counts)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !result_offsets || !result_ids)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (n_queries > a->cap_queries)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "more queries than the agent's last batch can hold");
+                check_mode(mode, width, nullptr, 0);
+                int const st = read_status(a);
+                if (st != HIBF_GPU_OK)
+                    fail(st, "device-side failure in the last batch");
+                a->h_roff.ensure((n_queries + 1) * 8);
+                HG_CUDA(cudaMemcpyAsync(a->h_roff.p, a->roff.p, (n_queries + 1) * 8, cudaMemcpyDeviceToHost,
+                                        a->stream));
+                HG_CUDA(cudaStreamSynchronize(a->stream));
+                uint64_t const nr = a->h_roff.as<uint64_t>()[n_queries];
+                a->h_ids.ensure(nr * 8);
+                a->h_cnt.ensure(nr * 8);
+                if (nr)
+                {
+                    HG_CUDA(cudaMemcpyAsync(a->h_ids.p, a->out_ids.p, nr * 8, cudaMemcpyDeviceToHost, a->stream));
+                    if (mode == HIBF_GPU_QUERY_COUNT)
+                        HG_CUDA(cudaMemcpyAsync(a->h_cnt.p, width == 8 ? a->out_cnt.p : a->out_cntw.p, nr * width,
+                                                cudaMemcpyDeviceToHost, a->stream));
+                }
+                HG_CUDA(cudaStreamSynchronize(a->stream));
+                *result_offsets = a->h_roff.as<uint64_t>();
+                *result_ids = a->h_ids.as<uint64_t>();
+                if (result_counts)
+                    *result_counts = mode == HIBF_GPU_QUERY_COUNT ? a->h_cnt.p : nullptr;
+            });
+    }
+
+    int hibf_gpu_agent_status(hibf_gpu_agent * a)
+    {
+        if (!a)
+            return HIBF_GPU_ERR_INVALID_ARG;
+        return guarded(
+            [&]
+            {
+                int const st = read_status(a);
+                if (st != HIBF_GPU_OK)
+                    fail(st, "device-side failure in the last batch");
+            });
+    }
+
+    int hibf_gpu_agent_last_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                (void)read_status(a);
+                if (tasks)
+                    *tasks = a->last_tasks;
+                if (value_visits)
+                    *value_visits = a->last_visits;
+            });
+    }
+
+} // extern "C"

@@ -1,0 +1,748 @@
+// ibf.cu -- single-level interleaved Bloom filter on the device: store, emplace/clear/widen kernels, the plain
+// (one launch per call) query kernels, and their C-ABI entry points (include/hibf_gb300.h).
+//
+// Reference interface: seqan::hibf::interleaved_bloom_filter (include/hibf/interleaved_bloom_filter.hpp,
+// src/interleaved_bloom_filter.cpp).
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.hpp"
+#include "count.cuh"
+#include "device.cuh"
+
+namespace hibf_gb300
+{
+
+thread_local std::string g_last_error;
+
+void set_last_error(std::string msg)
+{
+    g_last_error = std::move(msg);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------------------------------------------
+
+// emplace (src/interleaved_bloom_filter.cpp:119-140).  One thread per value; atomicOr makes concurrent inserts
+// order-independent.  With occupancy tracking, a value counts for its bin when one of its bits was newly set.
+__global__ void k_emplace(uint64_t * __restrict__ words, uint64_t bin_size, uint32_t row_words, uint32_t shift,
+                          uint32_t h, uint64_t const * __restrict__ values, uint64_t const * __restrict__ bins,
+                          uint64_t n, uint64_t bin, uint64_t n_bins, unsigned long long * occupancy,
+                          int * bad_bin)
+{
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        uint64_t const v = values[i];
+        uint64_t const b = bins ? bins[i] : bin;
+        if (b >= n_bins)
+        {
+            *bad_bin = 1; // device-supplied bin index out of range: skipped, reported by hibf_gpu_ibf_status
+            continue;
+        }
+        uint64_t const bit = 1ull << (b & 63u);
+        uint64_t const wofs = b >> 6;
+        bool exists = true;
+        for (uint32_t k = 0; k < h; ++k)
+        {
+            uint64_t const r = hash_row(v, c_hash_seeds[k], shift, bin_size);
+            unsigned long long * w = reinterpret_cast<unsigned long long *>(words + r * row_words + wofs);
+            unsigned long long const old = atomicOr(w, static_cast<unsigned long long>(bit));
+            exists = exists && (old & bit);
+        }
+        if (occupancy && !exists)
+            atomicAdd(occupancy + b, 1ull);
+    }
+}
+
+// clear(bin) (src/interleaved_bloom_filter.cpp:142-148): clear one bit of every row.
+__global__ void k_clear_bin(uint64_t * __restrict__ words, uint64_t bin_size, uint32_t row_words, uint64_t word,
+                            uint64_t keep)
+{
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t r = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; r < bin_size; r += stride)
+        atomicAnd(reinterpret_cast<unsigned long long *>(words + r * row_words + word), keep);
+}
+
+// clear(range) (include/hibf/interleaved_bloom_filter.hpp:283-297): per row, clear the listed bins word by word.
+__global__ void k_clear_words(uint64_t * __restrict__ words, uint64_t bin_size, uint32_t row_words,
+                              uint32_t const * __restrict__ widx, uint64_t const * __restrict__ keep, uint32_t nw)
+{
+    uint64_t const total = bin_size * nw;
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < total; i += stride)
+    {
+        uint64_t const r = i / nw;
+        uint32_t const e = static_cast<uint32_t>(i % nw);
+        atomicAnd(reinterpret_cast<unsigned long long *>(words + r * row_words + widx[e]), keep[e]);
+    }
+}
+
+// increase_bin_number_to (src/interleaved_bloom_filter.cpp:163-202): old row r becomes the first words of new row r.
+__global__ void k_widen(uint64_t * __restrict__ dst, uint32_t dst_row_words, uint64_t const * __restrict__ src,
+                        uint32_t src_row_words, uint32_t copy_words, uint64_t bin_size)
+{
+    uint64_t const total = bin_size * dst_row_words;
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < total; i += stride)
+    {
+        uint64_t const r = i / dst_row_words;
+        uint32_t const w = static_cast<uint32_t>(i % dst_row_words);
+        dst[i] = w < copy_words ? src[r * src_row_words + w] : 0u;
+    }
+}
+
+// bulk_contains (src/interleaved_bloom_filter.cpp:204-291) for many values: out[v * bin_words + j] = AND of word j
+// of the h rows.  LPV lanes per value, one row word per lane per pass (strided when the row is wider than a warp).
+template <int LPV>
+__global__ void k_bulk_contains(row_params rp, uint64_t const * __restrict__ values, uint64_t n,
+                                uint64_t * __restrict__ out)
+{
+    constexpr int G = 32 / LPV;
+    int const lane = threadIdx.x & 31;
+    int const g = lane / LPV;
+    int const j = lane % LPV;
+    uint64_t const warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
+    uint64_t const nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t base = warp * G; base < n; base += nwarps * G)
+    {
+        uint64_t const i = base + g;
+        if (i >= n)
+            continue;
+        uint64_t const v = values[i];
+        uint64_t off[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+            off[k] = (static_cast<uint32_t>(k) < rp.hash_funs)
+                       ? hash_row(v, c_hash_seeds[k], rp.hash_shift, rp.bin_size) * rp.row_words
+                       : 0u;
+        for (uint32_t w = j; w < rp.bin_words; w += LPV)
+        {
+            uint64_t x = ~0ull;
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                if (static_cast<uint32_t>(k) < rp.hash_funs)
+                    x &= __ldg(rp.words + off[k] + w);
+            out[i * rp.bin_words + w] = x;
+        }
+    }
+}
+
+// bulk_count over n values into one counting vector: every warp counts a contiguous chunk into the block's shared
+// counters, the block adds them to 64-bit global totals.
+__global__ void k_bulk_count(row_params rp, uint32_t lpv_log2, uint64_t const * __restrict__ values, uint64_t n,
+                             uint64_t chunk, unsigned long long * __restrict__ totals, uint32_t n_counters)
+{
+    extern __shared__ uint32_t s_counts[];
+    for (uint32_t i = threadIdx.x; i < n_counters; i += blockDim.x)
+        s_counts[i] = 0;
+    __syncthreads();
+    int const lane = threadIdx.x & 31;
+    uint64_t const warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
+    uint64_t const nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t start = warp * chunk; start < n; start += nwarps * chunk)
+    {
+        uint64_t const len = (n - start) < chunk ? (n - start) : chunk;
+        warp_count_any<true>(rp, lpv_log2, values + start, len, s_counts, lane);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n_counters; i += blockDim.x)
+        if (s_counts[i])
+            atomicAdd(totals + i, static_cast<unsigned long long>(s_counts[i]));
+}
+
+// Reduce exact totals modulo the counter width (the reference's counting_vector wraps).
+__global__ void k_store_counts(unsigned long long const * __restrict__ totals, uint64_t bins, int width, void * out)
+{
+    for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; b < bins;
+         b += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        uint64_t const t = totals[b];
+        switch (width)
+        {
+        case 1:
+            static_cast<uint8_t *>(out)[b] = static_cast<uint8_t>(t);
+            break;
+        case 2:
+            static_cast<uint16_t *>(out)[b] = static_cast<uint16_t>(t);
+            break;
+        case 4:
+            static_cast<uint32_t *>(out)[b] = static_cast<uint32_t>(t);
+            break;
+        default:
+            static_cast<uint64_t *>(out)[b] = t;
+        }
+    }
+}
+
+int sm_count()
+{
+    static int n = []
+    {
+        int dev = 0, c = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) !=
+                                                      cudaSuccess)
+            return 132;
+        return c;
+    }();
+    return n;
+}
+
+inline unsigned grid_for(uint64_t work, unsigned block)
+{
+    uint64_t const want = (work + block - 1) / block;
+    uint64_t const cap = static_cast<uint64_t>(sm_count()) * 16u;
+    return static_cast<unsigned>(std::max<uint64_t>(1, std::min(want, cap)));
+}
+
+} // namespace hibf_gb300
+
+using namespace hibf_gb300;
+
+// -----------------------------------------------------------------------------------------------------------------
+// Object
+// -----------------------------------------------------------------------------------------------------------------
+struct hibf_gpu_ibf
+{
+    uint64_t bins{};
+    uint64_t bin_size{};
+    uint64_t hash_funs{};
+    uint64_t bin_words{};
+    uint64_t row_words{};
+    uint32_t shift{};
+    bool track_occupancy{};
+    dbuf store;     // bin_size * row_words words
+    dbuf occupancy; // technical_bins counters
+    dbuf totals;    // technical_bins 64-bit totals (bulk_count scratch)
+    dbuf io;        // staging for host-pointer calls
+    dbuf io2;
+    dbuf flag; // device int: an emplace saw a bin index out of range
+    cudaStream_t stream{};
+    int status{HIBF_GPU_OK};
+    std::mutex mu;
+
+    row_params rp() const
+    {
+        return row_params{store.as<uint64_t>(), bin_size, static_cast<uint32_t>(row_words),
+                          static_cast<uint32_t>(bin_words), shift, static_cast<uint32_t>(hash_funs)};
+    }
+    uint32_t lpv_log2() const
+    {
+        return lanes_per_value_log2(bin_words);
+    }
+    uint64_t technical_bins() const
+    {
+        return bin_words * 64u;
+    }
+};
+
+namespace
+{
+
+cudaStream_t pick(hibf_gpu_ibf * f, void * s)
+{
+    return s ? static_cast<cudaStream_t>(s) : f->stream;
+}
+
+void launch_emplace(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t const * d_bins, uint64_t n, uint64_t bin,
+                    cudaStream_t s)
+{
+    if (n == 0)
+        return;
+    unsigned const block = 256;
+    k_emplace<<<grid_for(n, block), block, 0, s>>>(
+        f->store.as<uint64_t>(), f->bin_size, static_cast<uint32_t>(f->row_words), f->shift,
+        static_cast<uint32_t>(f->hash_funs), d_values, d_bins, n, bin, f->bins,
+        f->track_occupancy ? f->occupancy.as<unsigned long long>() : nullptr, f->flag.as<int>());
+    HG_CUDA(cudaGetLastError());
+}
+
+void launch_count(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int width, void * d_out, cudaStream_t s)
+{
+    uint64_t const nc = 64u * (f->bin_words <= 32 ? (1u << f->lpv_log2()) : f->bin_words);
+    f->totals.ensure(nc * sizeof(unsigned long long));
+    HG_CUDA(cudaMemsetAsync(f->totals.p, 0, nc * sizeof(unsigned long long), s));
+    if (n)
+    {
+        unsigned const block = 256;
+        uint64_t const chunk = 2048;
+        uint64_t const warps = (n + chunk - 1) / chunk;
+        unsigned const grid = static_cast<unsigned>(
+            std::max<uint64_t>(1, std::min<uint64_t>((warps + 7) / 8, static_cast<uint64_t>(sm_count()) * 4u)));
+        size_t const smem = nc * sizeof(uint32_t);
+        if (smem > 48 * 1024)
+            HG_CUDA(cudaFuncSetAttribute(k_bulk_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+        k_bulk_count<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk,
+                                               f->totals.as<unsigned long long>(), static_cast<uint32_t>(nc));
+        HG_CUDA(cudaGetLastError());
+    }
+    k_store_counts<<<grid_for(f->bins, 256), 256, 0, s>>>(f->totals.as<unsigned long long>(), f->bins, width, d_out);
+    HG_CUDA(cudaGetLastError());
+}
+
+void launch_contains(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, uint64_t * d_out, cudaStream_t s)
+{
+    if (n == 0)
+        return;
+    unsigned const block = 256;
+    uint32_t const l = f->lpv_log2();
+    uint64_t const lanes = n << l;
+    unsigned const grid = grid_for(lanes, block);
+    row_params const rp = f->rp();
+    switch (l)
+    {
+    case 0:
+        k_bulk_contains<1><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    case 1:
+        k_bulk_contains<2><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    case 2:
+        k_bulk_contains<4><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    case 3:
+        k_bulk_contains<8><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    case 4:
+        k_bulk_contains<16><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    default:
+        k_bulk_contains<32><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
+    }
+    HG_CUDA(cudaGetLastError());
+}
+
+int width_ok(int width)
+{
+    return width == 1 || width == 2 || width == 4 || width == 8;
+}
+
+} // namespace
+
+extern "C"
+{
+
+    char const * hibf_gpu_last_error(void)
+    {
+        return g_last_error.c_str();
+    }
+
+    int hibf_gpu_abi_version(void)
+    {
+        return HIBF_GPU_ABI_VERSION;
+    }
+
+    int hibf_gpu_device_count(int * count)
+    {
+        return guarded(
+            [&]
+            {
+                int n = 0;
+                cudaError_t e = cudaGetDeviceCount(&n);
+                if (e != cudaSuccess)
+                {
+                    (void)cudaGetLastError();
+                    n = 0;
+                }
+                if (count)
+                    *count = n;
+            });
+    }
+
+    int hibf_gpu_ibf_create(uint64_t bins, uint64_t bin_size, uint64_t hash_funs, int track_occupancy,
+                            hibf_gpu_ibf ** out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "out is null");
+                *out = nullptr;
+                if (bins == 0)
+                    fail(HIBF_GPU_ERR_LOGIC, "The number of bins must be > 0.");
+                if (hash_funs == 0 || hash_funs > 5)
+                    fail(HIBF_GPU_ERR_LOGIC, "The number of hash functions must be > 0 and <= 5.");
+                if (bin_size == 0)
+                    fail(HIBF_GPU_ERR_LOGIC, "The size of a bin must be > 0.");
+                require_device();
+                auto f = new hibf_gpu_ibf{};
+                try
+                {
+                    f->bins = bins;
+                    f->bin_size = bin_size;
+                    f->hash_funs = hash_funs;
+                    f->bin_words = (bins + 63u) / 64u;
+                    f->row_words = padded_row_words(f->bin_words);
+                    f->shift = static_cast<uint32_t>(__builtin_clzll(bin_size));
+                    f->track_occupancy = track_occupancy != 0;
+                    HG_CUDA(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
+                    size_t const bytes = bin_size * f->row_words * sizeof(uint64_t);
+                    f->store.ensure(bytes);
+                    HG_CUDA(cudaMemsetAsync(f->store.p, 0, bytes, f->stream));
+                    f->flag.ensure(sizeof(int));
+                    HG_CUDA(cudaMemsetAsync(f->flag.p, 0, sizeof(int), f->stream));
+                    f->occupancy.ensure(f->technical_bins() * sizeof(uint64_t));
+                    HG_CUDA(cudaMemsetAsync(f->occupancy.p, 0, f->technical_bins() * sizeof(uint64_t), f->stream));
+                    HG_CUDA(cudaStreamSynchronize(f->stream));
+                }
+                catch (...)
+                {
+                    if (f->stream)
+                        cudaStreamDestroy(f->stream);
+                    delete f;
+                    throw;
+                }
+                *out = f;
+            });
+    }
+
+    int hibf_gpu_ibf_destroy(hibf_gpu_ibf * f)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f)
+                    return;
+                cudaStreamSynchronize(f->stream);
+                cudaStreamDestroy(f->stream);
+                delete f;
+            });
+    }
+
+    int hibf_gpu_ibf_info(hibf_gpu_ibf const * f, uint64_t out[5])
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                out[0] = f->bins;
+                out[1] = f->bin_size;
+                out[2] = f->hash_funs;
+                out[3] = f->bin_words * 64u * f->bin_size;
+                out[4] = f->row_words * 8u;
+            });
+    }
+
+    int hibf_gpu_ibf_emplace_d(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t const * d_bins, uint64_t n,
+                               uint64_t bin, void * stream)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && !d_values))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (!d_bins && bin >= f->bins)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bin index out of range");
+                launch_emplace(f, d_values, d_bins, n, bin, pick(f, stream));
+            });
+    }
+
+    int hibf_gpu_ibf_emplace(hibf_gpu_ibf * f, uint64_t const * values, uint64_t n, uint64_t bin)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && !values))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (bin >= f->bins)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bin index out of range");
+                std::lock_guard<std::mutex> lk(f->mu);
+                f->io.ensure(n * 8);
+                HG_CUDA(cudaMemcpyAsync(f->io.p, values, n * 8, cudaMemcpyHostToDevice, f->stream));
+                launch_emplace(f, f->io.as<uint64_t>(), nullptr, n, bin, f->stream);
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_emplace_binned(hibf_gpu_ibf * f, uint64_t const * values, uint64_t const * bins, uint64_t n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && (!values || !bins)))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                for (uint64_t i = 0; i < n; ++i)
+                    if (bins[i] >= f->bins)
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "bin index out of range");
+                std::lock_guard<std::mutex> lk(f->mu);
+                f->io.ensure(n * 8);
+                f->io2.ensure(n * 8);
+                HG_CUDA(cudaMemcpyAsync(f->io.p, values, n * 8, cudaMemcpyHostToDevice, f->stream));
+                HG_CUDA(cudaMemcpyAsync(f->io2.p, bins, n * 8, cudaMemcpyHostToDevice, f->stream));
+                launch_emplace(f, f->io.as<uint64_t>(), f->io2.as<uint64_t>(), n, 0, f->stream);
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_clear(hibf_gpu_ibf * f, uint64_t bin)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (bin >= f->bins)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bin index out of range");
+                std::lock_guard<std::mutex> lk(f->mu);
+                k_clear_bin<<<grid_for(f->bin_size, 256), 256, 0, f->stream>>>(
+                    f->store.as<uint64_t>(), f->bin_size, static_cast<uint32_t>(f->row_words), bin >> 6,
+                    ~(1ull << (bin & 63u)));
+                HG_CUDA(cudaGetLastError());
+                HG_CUDA(cudaMemsetAsync(f->occupancy.as<uint64_t>() + bin, 0, sizeof(uint64_t), f->stream));
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_clear_range(hibf_gpu_ibf * f, uint64_t const * bins, uint64_t n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && !bins))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::vector<uint64_t> masks(f->bin_words, 0);
+                for (uint64_t i = 0; i < n; ++i)
+                {
+                    if (bins[i] >= f->technical_bins())
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "bin index out of range");
+                    masks[bins[i] >> 6] |= 1ull << (bins[i] & 63u);
+                }
+                std::vector<uint32_t> widx;
+                std::vector<uint64_t> keep;
+                for (uint64_t w = 0; w < f->bin_words; ++w)
+                    if (masks[w])
+                    {
+                        widx.push_back(static_cast<uint32_t>(w));
+                        keep.push_back(~masks[w]);
+                    }
+                if (widx.empty())
+                    return;
+                std::lock_guard<std::mutex> lk(f->mu);
+                f->io.ensure(widx.size() * 4);
+                f->io2.ensure(keep.size() * 8);
+                HG_CUDA(cudaMemcpyAsync(f->io.p, widx.data(), widx.size() * 4, cudaMemcpyHostToDevice, f->stream));
+                HG_CUDA(cudaMemcpyAsync(f->io2.p, keep.data(), keep.size() * 8, cudaMemcpyHostToDevice, f->stream));
+                uint32_t const nw = static_cast<uint32_t>(widx.size());
+                k_clear_words<<<grid_for(f->bin_size * nw, 256), 256, 0, f->stream>>>(
+                    f->store.as<uint64_t>(), f->bin_size, static_cast<uint32_t>(f->row_words), f->io.as<uint32_t>(),
+                    f->io2.as<uint64_t>(), nw);
+                HG_CUDA(cudaGetLastError());
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_try_increase_bin_number_to(hibf_gpu_ibf * f, uint64_t new_bins, int * increased)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || !increased)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                uint64_t const nbw = (new_bins + 63u) / 64u;
+                *increased = 0;
+                if (new_bins < f->bins || nbw > f->bin_words)
+                    return;
+                f->bins = new_bins;
+                *increased = 1;
+            });
+    }
+
+    int hibf_gpu_ibf_increase_bin_number_to(hibf_gpu_ibf * f, uint64_t new_bins)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (new_bins < f->bins)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "The number of new bins must be >= the current number of bins.");
+                uint64_t const nbw = (new_bins + 63u) / 64u;
+                if (nbw <= f->bin_words)
+                {
+                    f->bins = new_bins;
+                    return;
+                }
+                std::lock_guard<std::mutex> lk(f->mu);
+                uint64_t const nrw = padded_row_words(nbw);
+                dbuf fresh;
+                fresh.ensure(f->bin_size * nrw * 8);
+                k_widen<<<grid_for(f->bin_size * nrw, 256), 256, 0, f->stream>>>(
+                    fresh.as<uint64_t>(), static_cast<uint32_t>(nrw), f->store.as<uint64_t>(),
+                    static_cast<uint32_t>(f->row_words), static_cast<uint32_t>(f->bin_words), f->bin_size);
+                HG_CUDA(cudaGetLastError());
+                dbuf occ;
+                occ.ensure(nbw * 64 * 8);
+                HG_CUDA(cudaMemsetAsync(occ.p, 0, nbw * 64 * 8, f->stream));
+                HG_CUDA(cudaMemcpyAsync(occ.p, f->occupancy.p, f->technical_bins() * 8, cudaMemcpyDeviceToDevice,
+                                        f->stream));
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+                std::swap(f->store.p, fresh.p);
+                std::swap(f->store.bytes, fresh.bytes);
+                std::swap(f->occupancy.p, occ.p);
+                std::swap(f->occupancy.bytes, occ.bytes);
+                f->bins = new_bins;
+                f->bin_words = nbw;
+                f->row_words = nrw;
+            });
+    }
+
+    int hibf_gpu_ibf_bulk_contains_d(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, uint64_t * d_out,
+                                     void * stream)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && (!d_values || !d_out)))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                launch_contains(f, d_values, n, d_out, pick(f, stream));
+            });
+    }
+
+    int hibf_gpu_ibf_bulk_contains(hibf_gpu_ibf * f, uint64_t const * values, uint64_t n, uint64_t * out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && (!values || !out)))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (n == 0)
+                    return;
+                std::lock_guard<std::mutex> lk(f->mu);
+                f->io.ensure(n * 8);
+                f->io2.ensure(n * f->bin_words * 8);
+                HG_CUDA(cudaMemcpyAsync(f->io.p, values, n * 8, cudaMemcpyHostToDevice, f->stream));
+                launch_contains(f, f->io.as<uint64_t>(), n, f->io2.as<uint64_t>(), f->stream);
+                HG_CUDA(cudaMemcpyAsync(out, f->io2.p, n * f->bin_words * 8, cudaMemcpyDeviceToHost, f->stream));
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_bulk_count_d(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int width, void * d_out,
+                                  void * stream)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && !d_values) || !d_out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (!width_ok(width))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "width must be 1, 2, 4 or 8");
+                launch_count(f, d_values, n, width, d_out, pick(f, stream));
+            });
+    }
+
+    int hibf_gpu_ibf_bulk_count(hibf_gpu_ibf * f, uint64_t const * values, uint64_t n, int width, void * out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && !values) || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (!width_ok(width))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "width must be 1, 2, 4 or 8");
+                std::lock_guard<std::mutex> lk(f->mu);
+                f->io.ensure(n * 8);
+                f->io2.ensure(f->bins * 8);
+                if (n)
+                    HG_CUDA(cudaMemcpyAsync(f->io.p, values, n * 8, cudaMemcpyHostToDevice, f->stream));
+                launch_count(f, f->io.as<uint64_t>(), n, width, f->io2.p, f->stream);
+                HG_CUDA(cudaMemcpyAsync(out, f->io2.p, f->bins * width, cudaMemcpyDeviceToHost, f->stream));
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_membership_for(hibf_gpu_ibf * f, uint64_t const * values, uint64_t n, uint16_t threshold,
+                                    uint64_t * out_ids, uint64_t * n_out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && !values) || !out_ids || !n_out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::vector<uint16_t> counts(f->bins);
+                int const st = hibf_gpu_ibf_bulk_count(f, values, n, 2, counts.data());
+                if (st != HIBF_GPU_OK)
+                    fail(st, g_last_error);
+                uint64_t m = 0;
+                for (uint64_t b = 0; b < f->bins; ++b)
+                    if (counts[b] >= threshold)
+                        out_ids[m++] = b;
+                *n_out = m;
+            });
+    }
+
+    int hibf_gpu_ibf_upload_words(hibf_gpu_ibf * f, uint64_t const * words, uint64_t n_words)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || !words)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (n_words != f->bin_words * f->bin_size)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "word count does not match the filter");
+                std::lock_guard<std::mutex> lk(f->mu);
+                HG_CUDA(cudaMemcpy2DAsync(f->store.p, f->row_words * 8, words, f->bin_words * 8, f->bin_words * 8,
+                                          f->bin_size, cudaMemcpyHostToDevice, f->stream));
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_download_words(hibf_gpu_ibf * f, uint64_t * words, uint64_t n_words)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || !words)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (n_words != f->bin_words * f->bin_size)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "word count does not match the filter");
+                std::lock_guard<std::mutex> lk(f->mu);
+                HG_CUDA(cudaMemcpy2DAsync(words, f->bin_words * 8, f->store.p, f->row_words * 8, f->bin_words * 8,
+                                          f->bin_size, cudaMemcpyDeviceToHost, f->stream));
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_download_occupancy(hibf_gpu_ibf * f, uint64_t * out, uint64_t n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (n != f->technical_bins())
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "occupancy has technical_bins entries");
+                std::lock_guard<std::mutex> lk(f->mu);
+                HG_CUDA(cudaMemcpyAsync(out, f->occupancy.p, n * 8, cudaMemcpyDeviceToHost, f->stream));
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+            });
+    }
+
+    int hibf_gpu_ibf_status(hibf_gpu_ibf * f)
+    {
+        if (!f)
+            return HIBF_GPU_ERR_INVALID_ARG;
+        cudaError_t const e = cudaStreamSynchronize(f->stream);
+        if (e != cudaSuccess)
+        {
+            set_last_error(cudaGetErrorString(e));
+            return HIBF_GPU_ERR_CUDA;
+        }
+        int bad = 0;
+        if (cudaMemcpy(&bad, f->flag.p, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && bad)
+        {
+            cudaMemset(f->flag.p, 0, sizeof(int));
+            set_last_error("an emplace received a bin index out of range; those values were skipped");
+            return HIBF_GPU_ERR_INVALID_ARG;
+        }
+        return f->status;
+    }
+
+} // extern "C"

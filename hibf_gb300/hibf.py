@@ -1,0 +1,265 @@
+"""hierarchical_interleaved_bloom_filter -- device-resident HIBF (reference:
+include/hibf/hierarchical_interleaved_bloom_filter.hpp, src/hierarchical_interleaved_bloom_filter.cpp).
+
+    hibf = hierarchical_interleaved_bloom_filter.from_tables(...)     # tables of a built HIBF (+ its words)
+    hibf = hierarchical_interleaved_bloom_filter(config, layout_text)  # built from a layout (hibf_gb300.build)
+    agent = hibf.membership_agent()
+    ids = agent.membership_for(values, threshold)   # user bins in the reference's traversal order
+    agent.sort_results()                            # ascending, as HIBF.hpp:380-383
+    counts = hibf.counting_agent(width=2).bulk_count(values, threshold)
+    offs, ids, cnts = agent.query_batch(values, query_offsets, thresholds)   # one persistent launch
+
+Tables use the reference's conventions: next_ibf_id[k][b] (self for non-merged bins) and
+ibf_bin_to_user_bin_id[k][b] with BIN_MERGED / BIN_DELETED sentinels; IBF 0 is the root.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+_DT = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}
+
+
+def _u64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint64).reshape(-1))
+
+
+def traversal_rank(n_user_bins: int, bins, next_ibf, user_bin) -> np.ndarray:
+    """Position of every user bin in the order membership_for reports it (HIBF.hpp:322-355): bins scanned in
+    order, merged bins descended in place.  A user bin occurs in one place, so sorting a result by this rank gives
+    the reference's unsorted output."""
+    bins = [int(b) for b in bins]
+    off = np.zeros(len(bins) + 1, np.int64)
+    off[1:] = np.cumsum(bins)
+    nxt, ub = _u64(next_ibf), _u64(user_bin)
+    rank = np.full(n_user_bins, np.iinfo(np.int64).max, np.int64)
+    r = 0
+    stack = [(0, 0)]
+    seen = 0
+    while stack:
+        k, b = stack.pop()
+        seen += 1
+        if seen > 4 * (off[-1] + 1):
+            break
+        if b >= bins[k]:
+            continue
+        stack.append((k, b + 1))
+        i = off[k] + b
+        u = int(ub[i])
+        if u == N.BIN_MERGED:
+            c = int(nxt[i])
+            if c != k:
+                stack.append((c, 0))
+        elif u != N.BIN_DELETED and (b + 1 == bins[k] or int(ub[i + 1]) != u):
+            if rank[u] == np.iinfo(np.int64).max:
+                rank[u] = r
+                r += 1
+    return rank
+
+
+class hierarchical_interleaved_bloom_filter:
+    def __init__(self, *args, **kwargs):
+        self._h = None
+        if args or kwargs:
+            from .build import build_from_layout
+
+            built = build_from_layout(*args, **kwargs)
+            self._adopt(built)
+
+    def _adopt(self, other: "hierarchical_interleaved_bloom_filter") -> None:
+        self.__dict__.update(other.__dict__)
+        other._h = None
+
+    @classmethod
+    def from_tables(cls, n_user_bins, bins, bin_size, hash_funs, next_ibf, user_bin, words=None):
+        self = cls.__new__(cls)
+        self._h = None
+        bins, bsz, hf = _u64(bins), _u64(bin_size), _u64(np.broadcast_to(np.asarray(hash_funs, np.uint64),
+                                                                          np.shape(bins)))
+        nxt, ub = _u64(next_ibf), _u64(user_bin)
+        h = ctypes.c_void_p()
+        N.call("hibf_gpu_hibf_create", int(n_user_bins), bins.size, bins.ctypes.data, bsz.ctypes.data,
+               hf.ctypes.data, nxt.ctypes.data, ub.ctypes.data, ctypes.byref(h))
+        self._h = h
+        self.number_of_user_bins = int(n_user_bins)
+        self.bins, self.bin_size, self.hash_funs = bins, bsz, hf
+        self.next_ibf_id, self.ibf_bin_to_user_bin_id = nxt, ub
+        self._rank = None
+        if words is not None:
+            for k, w in enumerate(words):
+                self.set_words(k, w)
+        return self
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            try:
+                N.lib().hibf_gpu_hibf_destroy(self._h)
+            except Exception:
+                pass
+            self._h = None
+
+    # -- structure --------------------------------------------------------------------------------------------
+    @property
+    def n_ibfs(self) -> int:
+        return int(self.bins.size)
+
+    def info(self) -> dict:
+        out = (ctypes.c_uint64 * 4)()
+        N.call("hibf_gpu_hibf_info", self._h, out)
+        return dict(n_user_bins=out[0], n_ibfs=out[1], max_depth=out[2], device_bytes=out[3])
+
+    def ibf_words(self, k: int) -> int:
+        return int((int(self.bins[k]) + 63) // 64 * int(self.bin_size[k]))
+
+    def set_words(self, k: int, words) -> None:
+        w = _u64(words)
+        N.call("hibf_gpu_hibf_upload_words", self._h, k, w.ctypes.data, w.size)
+
+    def words(self, k: int) -> np.ndarray:
+        out = np.zeros(self.ibf_words(k), np.uint64)
+        N.call("hibf_gpu_hibf_download_words", self._h, k, out.ctypes.data, out.size)
+        return out
+
+    def emplace(self, k: int, values, bin: int) -> None:
+        v = _u64(values)
+        N.call("hibf_gpu_hibf_emplace", self._h, k, v.ctypes.data, v.size, int(bin))
+
+    def traversal_rank(self) -> np.ndarray:
+        if self._rank is None:
+            self._rank = traversal_rank(self.number_of_user_bins, self.bins, self.next_ibf_id,
+                                        self.ibf_bin_to_user_bin_id)
+        return self._rank
+
+    def tables(self) -> dict:
+        return dict(n_user_bins=self.number_of_user_bins, bins=self.bins, bin_size=self.bin_size,
+                    hash_funs=self.hash_funs, next_ibf=self.next_ibf_id, user_bin=self.ibf_bin_to_user_bin_id)
+
+    # -- agents -----------------------------------------------------------------------------------------------
+    def membership_agent(self) -> "membership_agent_type":
+        return membership_agent_type(self)
+
+    def counting_agent(self, width: int = 2) -> "counting_agent_type":
+        return counting_agent_type(self, width)
+
+
+class _agent_base:
+    def __init__(self, hibf: hierarchical_interleaved_bloom_filter):
+        self.hibf = hibf
+        a = ctypes.c_void_p()
+        N.call("hibf_gpu_agent_create", hibf._h, ctypes.byref(a))
+        self._a = a
+
+    def __del__(self):
+        if getattr(self, "_a", None):
+            try:
+                N.lib().hibf_gpu_agent_destroy(self._a)
+            except Exception:
+                pass
+            self._a = None
+
+    def reserve(self, max_queries, max_values, max_tasks, max_results) -> None:
+        N.call("hibf_gpu_agent_reserve", self._a, max_queries, max_values, max_tasks, max_results)
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        N.call("hibf_gpu_agent_set_stream", self._a, stream_ptr)
+
+    def last_work(self) -> tuple[int, int]:
+        t, v = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        N.call("hibf_gpu_agent_last_work", self._a, ctypes.byref(t), ctypes.byref(v))
+        return t.value, v.value
+
+    def status(self) -> None:
+        N.call("hibf_gpu_agent_status", self._a)
+
+    def query_batch(self, values, query_offsets, thresholds, mode=N.QUERY_MEMBERSHIP, width=2):
+        """All queries in one persistent launch.  Returns (offsets, ids, counts) as numpy copies; ids ascending per
+        query; counts (mode COUNT) are the non-zero entries of each dense counting vector."""
+        v, qo = _u64(values), _u64(query_offsets)
+        nq = qo.size - 1
+        t = _u64(thresholds)
+        ro, ri, rc = N.u64p(), N.u64p(), ctypes.c_void_p()
+        N.call("hibf_gpu_agent_query_batch", self._a, mode, v.ctypes.data if v.size else None, qo.ctypes.data, nq,
+               t.ctypes.data if nq else None, width, ctypes.byref(ro), ctypes.byref(ri), ctypes.byref(rc))
+        offs = np.ctypeslib.as_array(ro, shape=(nq + 1,)).copy()
+        nr = int(offs[-1])
+        ids = np.ctypeslib.as_array(ri, shape=(nr,)).copy() if nr else np.zeros(0, np.uint64)
+        cnts = None
+        if mode == N.QUERY_COUNT:
+            cnts = np.zeros(nr, _DT[width])
+            if nr:
+                ctypes.memmove(cnts.ctypes.data, rc.value, nr * width)
+        return offs, ids, cnts
+
+    def query_batch_device(self, d_values: int, d_query_offsets: int, n_queries: int, d_thresholds: int,
+                           mode=N.QUERY_MEMBERSHIP, width=2):
+        """Inputs already on the device (raw pointers, e.g. torch tensor data_ptr()).  Asynchronous on the agent's
+        stream; returns device pointers (offsets, ids, counts) into the agent's buffers."""
+        ro, ri, rc = N.u64p(), N.u64p(), ctypes.c_void_p()
+        N.call("hibf_gpu_agent_query_batch_d", self._a, mode, d_values, d_query_offsets, n_queries, d_thresholds,
+               width, ctypes.byref(ro), ctypes.byref(ri), ctypes.byref(rc))
+        return (ctypes.cast(ro, ctypes.c_void_p).value, ctypes.cast(ri, ctypes.c_void_p).value, rc.value)
+
+    def fetch_results(self, n_queries: int, mode=N.QUERY_MEMBERSHIP, width=2):
+        """Host copies (offsets, ids, counts) of the last device batch (query_batch_device / query_plain_device)."""
+        ro, ri, rc = N.u64p(), N.u64p(), ctypes.c_void_p()
+        N.call("hibf_gpu_agent_fetch_results", self._a, n_queries, mode, width, ctypes.byref(ro), ctypes.byref(ri),
+               ctypes.byref(rc))
+        offs = np.ctypeslib.as_array(ro, shape=(n_queries + 1,)).copy()
+        nr = int(offs[-1])
+        ids = np.ctypeslib.as_array(ri, shape=(nr,)).copy() if nr else np.zeros(0, np.uint64)
+        cnts = None
+        if mode == N.QUERY_COUNT:
+            cnts = np.zeros(nr, _DT[width])
+            if nr:
+                ctypes.memmove(cnts.ctypes.data, rc.value, nr * width)
+        return offs, ids, cnts
+
+    def query_plain_device(self, d_values: int, query_offsets, thresholds, mode=N.QUERY_MEMBERSHIP, width=2):
+        """The plain form: one launch per query (values on the device, offsets/thresholds on the host)."""
+        qo, t = _u64(query_offsets), _u64(thresholds)
+        N.call("hibf_gpu_agent_query_plain_d", self._a, mode, d_values, qo.ctypes.data, qo.size - 1,
+               t.ctypes.data if t.size else None, width)
+
+
+class membership_agent_type(_agent_base):
+    def __init__(self, hibf):
+        super().__init__(hibf)
+        self.result_buffer = np.zeros(0, np.uint64)
+
+    def membership_for(self, values, threshold: int) -> np.ndarray:
+        """User bins whose summed counts reach `threshold`, in the reference's traversal order."""
+        v = _u64(values)
+        ids, n = N.u64p(), ctypes.c_uint64(0)
+        N.call("hibf_gpu_agent_membership_for", self._a, v.ctypes.data if v.size else None, v.size, int(threshold),
+               ctypes.byref(ids), ctypes.byref(n))
+        res = np.ctypeslib.as_array(ids, shape=(n.value,)).copy() if n.value else np.zeros(0, np.uint64)
+        rank = self.hibf.traversal_rank()
+        self.result_buffer = res[np.argsort(rank[res.astype(np.int64)], kind="stable")] if res.size else res
+        return self.result_buffer
+
+    def sort_results(self) -> np.ndarray:
+        self.result_buffer = np.sort(self.result_buffer)
+        return self.result_buffer
+
+
+class counting_agent_type(_agent_base):
+    def __init__(self, hibf, width: int = 2):
+        super().__init__(hibf)
+        self.width = width
+
+    def bulk_count(self, values, threshold: int) -> np.ndarray:
+        """Dense counting vector of number_of_user_bins counters; entries below `threshold` are 0."""
+        v = _u64(values)
+        p = ctypes.c_void_p()
+        N.call("hibf_gpu_agent_bulk_count", self._a, v.ctypes.data if v.size else None, v.size, int(threshold),
+               self.width, ctypes.byref(p))
+        out = np.zeros(self.hibf.number_of_user_bins, _DT[self.width])
+        ctypes.memmove(out.ctypes.data, p.value, out.nbytes)
+        return out
+
+    def query_batch(self, values, query_offsets, thresholds, mode=N.QUERY_COUNT, width=None):
+        return super().query_batch(values, query_offsets, thresholds, mode, self.width if width is None else width)

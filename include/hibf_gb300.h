@@ -1,0 +1,205 @@
+/* hibf_gb300.h -- C ABI of the GB300-native HIBF build/query path.
+ *
+ * This is the drop-in boundary: plain pointers, sizes and status codes, no C++ or torch types.  A seqan::hibf
+ * build keeps its host-side config, layout DP, HyperLogLog sketching and serialization; it hands the device the
+ * interleaved bit store and the per-IBF tables, routes emplace() through the batched insert entry points, and
+ * replaces its agents' query calls with the entry points below.  Each declaration names the reference interface it
+ * replaces (file:line inside the seqan/hibf tree).
+ *
+ * Conventions
+ *   - Functions without a suffix take HOST pointers and are synchronous, like the reference's member functions.
+ *   - Functions ending in _d take DEVICE pointers and a cudaStream_t passed as void*; they are asynchronous and
+ *     report device-side failures (result overflow, a bounded wait that expired) through the owning object's
+ *     status, read with hibf_gpu_agent_status / hibf_gpu_ibf_status after the stream has been synchronised.
+ *   - Every function returns an int status (enum hibf_gpu_status).  hibf_gpu_last_error() describes the last
+ *     failure of the calling thread.
+ *   - Counter widths are given in bytes (1, 2, 4, 8) and select counting_agent<uint8_t .. uint64_t>; counts wrap
+ *     modulo 2^(8*width) exactly as the reference's counting_vector does.
+ *   - The library never falls back to a CPU path: without a usable CUDA device every call that needs one fails
+ *     with HIBF_GPU_ERR_NO_DEVICE.
+ */
+#ifndef HIBF_GB300_H
+#define HIBF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HIBF_GPU_ABI_VERSION 1
+
+enum hibf_gpu_status
+{
+    HIBF_GPU_OK = 0,
+    HIBF_GPU_ERR_INVALID_ARG = 1,   /* std::invalid_argument in the reference (config.cpp:66-129, IBF.cpp:165) */
+    HIBF_GPU_ERR_LOGIC = 2,         /* std::logic_error in the reference (IBF.cpp:41-46)                       */
+    HIBF_GPU_ERR_OUT_OF_MEMORY = 3, /* device or pinned-host allocation failed                                */
+    HIBF_GPU_ERR_NO_DEVICE = 4,     /* no CUDA device / driver                                                 */
+    HIBF_GPU_ERR_CUDA = 5,          /* any other CUDA runtime error                                            */
+    HIBF_GPU_ERR_OVERFLOW = 6,      /* result or task capacity of a batch exceeded; nothing was lost silently */
+    HIBF_GPU_ERR_TIMEOUT = 7,       /* a bounded device-side wait expired; the context stays usable           */
+    HIBF_GPU_ERR_ADMISSION = 8,     /* request rejected by the serving loop's memory admission cap            */
+    HIBF_GPU_ERR_CYCLE = 9          /* a merged bin leads back into its own subtree (descent depth exceeded)  */
+};
+
+/* Sentinels of ibf_bin_to_user_bin_id (include/hibf/hierarchical_interleaved_bloom_filter.hpp:32-40). */
+#define HIBF_GPU_BIN_MERGED UINT64_MAX
+#define HIBF_GPU_BIN_DELETED (UINT64_MAX - 1u)
+
+const char * hibf_gpu_last_error(void);
+int hibf_gpu_abi_version(void);
+/* Number of usable CUDA devices (0 when none); selects nothing. */
+int hibf_gpu_device_count(int * count);
+
+/* ============================================================================================================ */
+/* Single-level interleaved Bloom filter: seqan::hibf::interleaved_bloom_filter                                  */
+/* ============================================================================================================ */
+typedef struct hibf_gpu_ibf hibf_gpu_ibf;
+
+/* interleaved_bloom_filter(bin_count, bin_size, hash_function_count, track_occupancy)
+ * (include/hibf/interleaved_bloom_filter.hpp:225-228, src/interleaved_bloom_filter.cpp:32-53).
+ * Zeroed device bit store of bin_size rows x technical_bins bits, technical_bins = 64 * ceil(bins / 64).
+ * HIBF_GPU_ERR_LOGIC for bins == 0, hash_funs not in [1,5] or bin_size == 0. */
+int hibf_gpu_ibf_create(uint64_t bins, uint64_t bin_size, uint64_t hash_funs, int track_occupancy,
+                        hibf_gpu_ibf ** out);
+int hibf_gpu_ibf_destroy(hibf_gpu_ibf * ibf);
+
+/* bin_count(), bin_size(), hash_function_count(), bit_size() (interleaved_bloom_filter.hpp:395-425);
+ * out[4] = device row stride in bytes (rows are padded so that none straddles a 32-byte sector). */
+int hibf_gpu_ibf_info(hibf_gpu_ibf const * ibf, uint64_t out[5]);
+
+/* emplace(value, bin) for n values into one bin (src/interleaved_bloom_filter.cpp:119-140; the insert_iterator IBF
+ * branch, include/hibf/misc/insert_iterator.hpp:60-81).  Bits are set with atomicOr, so the result does not depend
+ * on the order of the values. */
+int hibf_gpu_ibf_emplace(hibf_gpu_ibf * ibf, uint64_t const * values, uint64_t n, uint64_t bin);
+/* emplace(values[i], bins[i]) for i < n. */
+int hibf_gpu_ibf_emplace_binned(hibf_gpu_ibf * ibf, uint64_t const * values, uint64_t const * bins, uint64_t n);
+/* Device-pointer form; d_bins == NULL means every value goes to `bin`. */
+int hibf_gpu_ibf_emplace_d(hibf_gpu_ibf * ibf, uint64_t const * d_values, uint64_t const * d_bins, uint64_t n,
+                           uint64_t bin, void * stream);
+
+/* clear(bin_index) (src/interleaved_bloom_filter.cpp:142-148) and clear(range) (interleaved_bloom_filter.hpp:283-297). */
+int hibf_gpu_ibf_clear(hibf_gpu_ibf * ibf, uint64_t bin);
+int hibf_gpu_ibf_clear_range(hibf_gpu_ibf * ibf, uint64_t const * bins, uint64_t n);
+
+/* try_increase_bin_number_to / increase_bin_number_to (src/interleaved_bloom_filter.cpp:150-202). */
+int hibf_gpu_ibf_try_increase_bin_number_to(hibf_gpu_ibf * ibf, uint64_t new_bins, int * increased);
+int hibf_gpu_ibf_increase_bin_number_to(hibf_gpu_ibf * ibf, uint64_t new_bins);
+
+/* containment_agent_type::bulk_contains (src/interleaved_bloom_filter.cpp:204-291) for n values:
+ * out receives n * ceil(bins/64) words, the bit_vector words of each value's result. */
+int hibf_gpu_ibf_bulk_contains(hibf_gpu_ibf * ibf, uint64_t const * values, uint64_t n, uint64_t * out);
+int hibf_gpu_ibf_bulk_contains_d(hibf_gpu_ibf * ibf, uint64_t const * d_values, uint64_t n, uint64_t * d_out,
+                                 void * stream);
+
+/* counting_agent_type<value_t>::bulk_count (include/hibf/interleaved_bloom_filter.hpp:652-665): one counting vector
+ * of `bins` counters of `width` bytes over all n values. */
+int hibf_gpu_ibf_bulk_count(hibf_gpu_ibf * ibf, uint64_t const * values, uint64_t n, int width, void * out);
+int hibf_gpu_ibf_bulk_count_d(hibf_gpu_ibf * ibf, uint64_t const * d_values, uint64_t n, int width, void * d_out,
+                              void * stream);
+
+/* membership_agent_type::membership_for (include/hibf/interleaved_bloom_filter.hpp:744-764): ascending bin ids whose
+ * uint16 count reaches `threshold`.  out_ids needs room for `bins` ids; *n_out receives the count. */
+int hibf_gpu_ibf_membership_for(hibf_gpu_ibf * ibf, uint64_t const * values, uint64_t n, uint16_t threshold,
+                                uint64_t * out_ids, uint64_t * n_out);
+
+/* The bit store in the reference's bit_vector word layout (row r = words [r*ceil(bins/64), ...)), for
+ * serialization through the host (interleaved_bloom_filter.hpp:471-485, bit_vector.hpp:885-925). */
+int hibf_gpu_ibf_upload_words(hibf_gpu_ibf * ibf, uint64_t const * words, uint64_t n_words);
+int hibf_gpu_ibf_download_words(hibf_gpu_ibf * ibf, uint64_t * words, uint64_t n_words);
+/* occupancy vector (interleaved_bloom_filter.hpp:433-437): technical_bins counters. */
+int hibf_gpu_ibf_download_occupancy(hibf_gpu_ibf * ibf, uint64_t * out, uint64_t n);
+/* Status of the last asynchronous (_d) call on this filter. */
+int hibf_gpu_ibf_status(hibf_gpu_ibf * ibf);
+
+/* ============================================================================================================ */
+/* Hierarchical interleaved Bloom filter: seqan::hibf::hierarchical_interleaved_bloom_filter                     */
+/* ============================================================================================================ */
+typedef struct hibf_gpu_hibf hibf_gpu_hibf;
+
+/* The HIBF's tables (hierarchical_interleaved_bloom_filter.hpp:208-238) plus one empty IBF per entry of ibf_vector,
+ * sized like construct_ibf does (src/build/construct_ibf.cpp:52-55):
+ *   bins[k], bin_sizes[k], hash_funs[k]       interleaved_bloom_filter(bin_count, bin_size, hash_function_count)
+ *   next_ibf_id / user_bin_id                 next_ibf_id[k][b] and ibf_bin_to_user_bin_id[k][b], flattened in IBF
+ *                                             order, sum(bins) entries each; HIBF_GPU_BIN_MERGED / _DELETED sentinels
+ * IBF 0 is the root.  n_user_bins must be below 2^32 - 2. */
+int hibf_gpu_hibf_create(uint64_t n_user_bins, uint64_t n_ibfs, uint64_t const * bins, uint64_t const * bin_sizes,
+                         uint64_t const * hash_funs, uint64_t const * next_ibf_id, uint64_t const * user_bin_id,
+                         hibf_gpu_hibf ** out);
+int hibf_gpu_hibf_destroy(hibf_gpu_hibf * h);
+/* out: n_user_bins, n_ibfs, max depth, total device bytes of the bit stores. */
+int hibf_gpu_hibf_info(hibf_gpu_hibf const * h, uint64_t out[4]);
+/* Per IBF: bins, technical bins, bin_size, hash_funs, device row stride in bytes. */
+int hibf_gpu_hibf_ibf_info(hibf_gpu_hibf const * h, uint64_t ibf, uint64_t out[5]);
+
+/* emplace into IBF `ibf` (insert_into_ibf, src/build/insert_into_ibf.cpp:28-84): host values into one bin, or
+ * device values with per-value bins (d_bins) or one bin. */
+int hibf_gpu_hibf_emplace(hibf_gpu_hibf * h, uint64_t ibf, uint64_t const * values, uint64_t n, uint64_t bin);
+int hibf_gpu_hibf_emplace_d(hibf_gpu_hibf * h, uint64_t ibf, uint64_t const * d_values, uint64_t const * d_bins,
+                            uint64_t n, uint64_t bin, void * stream);
+/* Words of IBF `ibf` in the reference's bit_vector layout (for serialization or a host-built HIBF). */
+int hibf_gpu_hibf_upload_words(hibf_gpu_hibf * h, uint64_t ibf, uint64_t const * words, uint64_t n_words);
+int hibf_gpu_hibf_download_words(hibf_gpu_hibf * h, uint64_t ibf, uint64_t * words, uint64_t n_words);
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* Agents (hierarchical_interleaved_bloom_filter.hpp:241-247).  An agent owns its device workspace, result       */
+/* buffers and stream; like the reference's agents, use one per thread.  Results returned by pointer stay valid   */
+/* until the agent's next call, as the reference's `const &` results do.                                          */
+/* ------------------------------------------------------------------------------------------------------------ */
+typedef struct hibf_gpu_agent hibf_gpu_agent;
+
+int hibf_gpu_agent_create(hibf_gpu_hibf * h, hibf_gpu_agent ** out);
+int hibf_gpu_agent_destroy(hibf_gpu_agent * a);
+/* Run the agent's work on this stream (cudaStream_t as void*); NULL restores the agent's own stream. */
+int hibf_gpu_agent_set_stream(hibf_gpu_agent * a, void * stream);
+/* Capacities of the device workspace; calls that need more grow it (host calls) or fail with OVERFLOW (_d). */
+int hibf_gpu_agent_reserve(hibf_gpu_agent * a, uint64_t max_queries, uint64_t max_values, uint64_t max_tasks,
+                           uint64_t max_results);
+
+/* membership_agent_type::membership_for + sort_results (hierarchical_interleaved_bloom_filter.hpp:322-439) for one
+ * query: the plain form, one device launch per call.  *ids points at the agent's sorted result buffer. */
+int hibf_gpu_agent_membership_for(hibf_gpu_agent * a, uint64_t const * values, uint64_t n, uint16_t threshold,
+                                  uint64_t const ** ids, uint64_t * n_ids);
+/* counting_agent_type<value_t>::bulk_count (hierarchical_interleaved_bloom_filter.hpp:463-566) for one query:
+ * *counts points at the agent's dense vector of n_user_bins counters of `width` bytes.  threshold must be > 0. */
+int hibf_gpu_agent_bulk_count(hibf_gpu_agent * a, uint64_t const * values, uint64_t n, uint64_t threshold,
+                              int width, void const ** counts);
+
+/* Batched queries, one persistent launch for all of them.  Queries are CSR: values[query_offsets[q] ..
+ * query_offsets[q+1]).  mode HIBF_GPU_QUERY_MEMBERSHIP uses the uint16 thresholds of membership_for;
+ * HIBF_GPU_QUERY_COUNT the size_t thresholds of bulk_count with counters of `width` bytes (thresholds > 0).
+ * Results are CSR per query, ascending user-bin ids, and for COUNT the count of each listed user bin (the
+ * dense counting vector's non-zero entries; every other entry is 0).  Host form: *result_offsets (n_queries+1),
+ * *result_ids and *result_counts (width bytes each; NULL for MEMBERSHIP) point into agent-owned host memory. */
+#define HIBF_GPU_QUERY_MEMBERSHIP 1
+#define HIBF_GPU_QUERY_COUNT 2
+int hibf_gpu_agent_query_batch(hibf_gpu_agent * a, int mode, uint64_t const * values,
+                               uint64_t const * query_offsets, uint64_t n_queries, uint64_t const * thresholds,
+                               int width, uint64_t const ** result_offsets, uint64_t const ** result_ids,
+                               void const ** result_counts);
+/* Device form: inputs already in HBM; results stay in the agent's device buffers (returned as device pointers).
+ * Asynchronous on the agent's stream; hibf_gpu_agent_status() after synchronising gives OVERFLOW / TIMEOUT. */
+int hibf_gpu_agent_query_batch_d(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
+                                 uint64_t const * d_query_offsets, uint64_t n_queries, uint64_t const * d_thresholds,
+                                 int width, uint64_t const ** d_result_offsets, uint64_t const ** d_result_ids,
+                                 void const ** d_result_counts);
+/* Plain form of the batch: one launch per query (the baseline the persistent launch is measured against). */
+int hibf_gpu_agent_query_plain_d(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
+                                 uint64_t const * h_query_offsets, uint64_t n_queries, uint64_t const * h_thresholds,
+                                 int width);
+/* Copies the results of the agent's last batch (_d or plain) into agent-owned host memory; synchronises. */
+int hibf_gpu_agent_fetch_results(hibf_gpu_agent * a, uint64_t n_queries, int mode, int width,
+                                 uint64_t const ** result_offsets, uint64_t const ** result_ids,
+                                 void const ** result_counts);
+int hibf_gpu_agent_status(hibf_gpu_agent * a);
+/* Number of (query, IBF) tasks the last batch processed and the number of query values they covered
+ * (sum over tasks of the query length): the work the roofline is computed from. */
+int hibf_gpu_agent_last_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HIBF_GB300_H */

@@ -1,0 +1,258 @@
+"""Generates the golden vectors in tests/golden from the REFERENCE itself.
+
+Run where the seqan/hibf source tree is available (default /root/reference, or HIBF_REFERENCE_DIR):
+
+    python tests/golden/make_golden.py
+
+It compiles the reference's own sources against the cereal/simde stand-ins (oracle/Makefile target `ref`) and drives
+them through oracle/ref_driver.cpp:
+
+  ibf_cases.npz      random IBF cases: emplace inputs, the digest of the reference's bit store, bulk_contains words,
+                     bulk_count for counter widths 1/2/4/8 (wraparound included), membership_for at several
+                     thresholds, occupancy, clear / clear(range) / increase_bin_number_to sequences.
+  hibf_<name>.npz    small HIBFs built by the reference (HIBF(config)): the layout it computed, its tables and bit
+                     words, queries, and the reference's outputs (membership in traversal order and sorted, dense
+                     uint16/uint32/uint8 counting vectors, per-query digests).
+  c3_layout.txt      the layout the reference computes (HyperLogLog sketches + DP) for the 8,192-user-bin workload
+                     (sizes log-normal(2e5, 1.5) clipped to [1e3, 5e7], h=2, fpr 0.05, tmax 64, sketch_bits 12, seed 1).
+  c1_reference.npz   the 64-user-bin workload (log-uniform [1e3, 1e5], h=2, fpr 0.05, tmax 64): layout, per-IBF
+                     digests and tables, 10,000 queries' outputs digests.
+
+Nothing here is read by the product; tests compare the oracle and the GPU path against these files.
+"""
+
+from __future__ import annotations
+
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from hibf_gb300 import synthetic as S  # noqa: E402
+from oracle.bindings import Reference, build_reference, ref_cfg  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+MERGED = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def digest_words(w: np.ndarray) -> int:
+    # same fold as hg_digest_step, vectorised poorly but fine for fixture sizes
+    return S.digest(w.tolist())
+
+
+IBF_CASES = [
+    # bins, bin_size, h, track_occupancy, n_insert, n_query
+    (64, 1024, 2, 0, 3000, 400),
+    (73, 1019, 3, 0, 3000, 400),
+    (1, 100, 1, 0, 200, 100),
+    (128, 512, 2, 1, 3000, 400),
+    (1024, 4096, 3, 0, 20000, 300),
+    (200, 777, 5, 0, 4000, 300),
+    (65, 64, 4, 1, 2000, 300),
+    (12, 8192, 2, 0, 500, 200),
+    (192, 1500, 2, 0, 4000, 300),  # 3 words per row: padded on the device
+    (2047, 333, 2, 0, 6000, 200),  # 32 words per row
+    (2100, 100, 2, 0, 6000, 100),  # 33 words per row: wider than a warp
+    (8, 64, 1, 0, 6000, 2000),     # tiny filter: counts above 255 wrap in uint8
+]
+
+
+def make_ibf_cases(R: Reference):
+    out = {}
+    for ci, (bins, bsz, h, track, n_ins, n_q) in enumerate(IBF_CASES):
+        rng = np.random.default_rng(1000 + ci)
+        vals = rng.integers(0, 2**64, n_ins, dtype=np.uint64)
+        bns = rng.integers(0, bins, n_ins).astype(np.uint64)
+        q = np.concatenate([vals[: n_q // 2], rng.integers(0, 2**64, n_q - n_q // 2, dtype=np.uint64)])
+        ibf = R.ibf(bins, bsz, h, bool(track))
+        ibf.emplace(vals, bns)
+        p = f"c{ci}_"
+        out[p + "params"] = np.array([bins, bsz, h, track], np.uint64)
+        out[p + "values"] = vals
+        out[p + "bins"] = bns
+        out[p + "queries"] = q
+        out[p + "digest"] = np.array([digest_words(ibf.words())], np.uint64)
+        out[p + "contains"] = ibf.bulk_contains(q)
+        for w in (1, 2, 4, 8):
+            out[p + f"count{w}"] = ibf.bulk_count(q, w)
+        for t in (0, 1, 2, 3, 50):
+            out[p + f"member{t}"] = ibf.membership_for(q, t)
+        if track:
+            out[p + "occupancy"] = ibf.occupancy()
+        # clear(bin), clear(range), then widen
+        ibf.clear(bins // 2)
+        out[p + "after_clear"] = ibf.bulk_count(q, 4)
+        rb = np.unique(rng.integers(0, bins, 5)).astype(np.uint64)
+        ibf.clear_range(rb)
+        out[p + "clear_range_bins"] = rb
+        out[p + "after_clear_range"] = ibf.bulk_count(q, 4)
+        if track:
+            out[p + "occupancy_after_clear"] = ibf.occupancy()
+        new_bins = bins + 70
+        ibf.increase_bin_number_to(new_bins)
+        out[p + "widened_bins"] = np.array([new_bins], np.uint64)
+        out[p + "widened_digest"] = np.array([digest_words(ibf.words())], np.uint64)
+        out[p + "widened_count"] = ibf.bulk_count(q, 2)
+    out["n_cases"] = np.array([len(IBF_CASES)], np.uint64)
+    np.savez_compressed(OUT / "ibf_cases.npz", **out)
+
+
+def hibf_case(R: Reference, name: str, cfg, values, offsets, queries, mem_t, cnt_t, widths=(2,), synthetic_seed=None):
+    t0 = time.time()
+    if synthetic_seed is None:
+        layout = R.layout(cfg, values, offsets)
+        H = R.hibf(cfg, values, offsets)
+    else:
+        layout = R.layout(cfg, None, offsets, seed=synthetic_seed, synthetic=True)
+        H = R.hibf(cfg, None, offsets, seed=synthetic_seed, synthetic=True)
+    T = H.tables(with_words=True)
+    qv, qo = queries
+    nq = qo.size - 1
+    nub = int(cfg.number_of_user_bins)
+    unsorted, sorted_, dense = [], [], {w: [] for w in widths}
+    for i in range(nq):
+        v = qv[qo[i]:qo[i + 1]]
+        unsorted.append(H.membership_for(v, int(mem_t[i]), sort=False))
+        sorted_.append(np.sort(unsorted[-1]))
+        for w in widths:
+            dense[w].append(H.bulk_count(v, int(cnt_t[i]), w))
+    lens = np.array([u.size for u in unsorted], np.uint64)
+    moff = np.zeros(nq + 1, np.uint64)
+    np.cumsum(lens, out=moff[1:])
+    out = dict(n_user_bins=np.array([nub], np.uint64), bins=T["bins"], bin_size=T["bin_size"],
+               hash_funs=T["hash_funs"], next_ibf=T["next_ibf"], user_bin=T["user_bin"], digests=T["digests"],
+               words=np.concatenate(T["words"]), layout=np.frombuffer(layout.encode(), np.uint8),
+               config=np.array([cfg.number_of_hash_functions, cfg.tmax, cfg.sketch_bits], np.uint64),
+               fpr=np.array([cfg.maximum_fpr, cfg.relaxed_fpr, cfg.alpha, cfg.max_rearrangement_ratio], np.float64),
+               flags=np.array([cfg.disable_estimate_union, cfg.disable_rearrangement], np.uint64),
+               q_values=qv, q_offsets=qo, mem_t=np.asarray(mem_t, np.uint64), cnt_t=np.asarray(cnt_t, np.uint64),
+               mem_offsets=moff, mem_unsorted=np.concatenate(unsorted) if nq else np.zeros(0, np.uint64),
+               mem_sorted=np.concatenate(sorted_) if nq else np.zeros(0, np.uint64))
+    if values is not None:
+        out["ub_values"] = np.asarray(values, np.uint64)
+        out["ub_offsets"] = np.asarray(offsets, np.uint64)
+    else:
+        out["ub_offsets"] = np.asarray(offsets, np.uint64)
+        out["synthetic_seed"] = np.array([synthetic_seed], np.uint64)
+    for w in widths:
+        out[f"count{w}"] = np.stack(dense[w]) if nq else np.zeros((0, nub))
+    np.savez_compressed(OUT / f"hibf_{name}.npz", **out)
+    print(f"hibf_{name}: {len(T['bins'])} IBFs, {sum(x.size for x in T['words'])} words, {nq} queries, "
+          f"{time.time() - t0:.1f}s")
+
+
+def csr(lists):
+    v = np.concatenate([np.asarray(x, np.uint64) for x in lists]) if lists else np.zeros(0, np.uint64)
+    o = np.zeros(len(lists) + 1, np.uint64)
+    np.cumsum([len(x) for x in lists], out=o[1:])
+    return v, o
+
+
+def make_hibf_cases(R: Reference):
+    # test/snippet/hibf/hierarchical_interleaved_bloom_filter.cpp and the unit test small example
+    ubs = [[1, 2, 3, 4, 5, 6, 7, 8, 9, 10], [1, 2, 3, 4, 5]]
+    v, o = csr(ubs)
+    q = csr([[1, 2, 3, 4, 5], [1, 2, 3, 4, 5], [1, 2, 3, 4, 5]])
+    hibf_case(R, "snippet", ref_cfg(2), v, o, q, [2, 6, 2], [1, 6, 1], widths=(2, 8))
+    # test/snippet/readme.cpp
+    ubs = [[1, 2, 3, 4, 5, 6, 7, 8, 9, 10], [1, 2, 3, 4, 5], [3, 9, 11]]
+    v, o = csr(ubs)
+    q = csr([[3, 9, 12, 14], list(range(15))])
+    hibf_case(R, "readme", ref_cfg(3), v, o, q, [2, 5], [2, 5])
+    # test/unit/hibf/hierarchical_interleaved_bloom_filter_test.cpp:112 three_level_hibf
+    n = 4097
+    ubs = [list(range(i * 16, i * 16 + 20)) for i in range(n)]
+    v, o = csr(ubs)
+    qs = []
+    for ub in range(0, 4096, 100):
+        s = ub * 16
+        qs += [list(range(s + 16, s + 20)), list(range(s + 5, s + 9))]
+    cfg = ref_cfg(n, fpr=0.001, threads=4, tmax=64, disable_estimate_union=True, disable_rearrangement=True)
+    hibf_case(R, "three_level", cfg, v, o, csr(qs), [4] * len(qs), [1] * len(qs))
+    # :164 unevenly_sized_and_unique_user_bins
+    ubs = [list(range((i + 1) ** 2, (i + 2) ** 2 - 1)) for i in range(500)]
+    v, o = csr(ubs)
+    qs = [list(range((ub + 1) ** 2 + 5, (ub + 1) ** 2 + 9)) for ub in range(5, 499, 20)]
+    qs.append(list(range(1, 251000)))
+    cfg = ref_cfg(500, fpr=0.001, threads=4, tmax=64, disable_estimate_union=True, disable_rearrangement=True)
+    hibf_case(R, "uneven", cfg, v, o, csr(qs), [4] * (len(qs) - 1) + [1], [1] * len(qs), widths=(2, 4))
+    # :198 evenly_sized_and_highly_similar_user_bins
+    ubs = [list(range(i * 5, i * 5 + 35)) for i in range(1000)]
+    v, o = csr(ubs)
+    qs = [list(range(ub * 5, ub * 5 + 5)) for ub in range(6, 994, 20)]
+    cfg = ref_cfg(1000, fpr=0.001, threads=4, tmax=64, disable_estimate_union=True, disable_rearrangement=True)
+    hibf_case(R, "similar", cfg, v, o, csr(qs), [5] * len(qs), [1] * len(qs))
+    # :233 counting_agent_same_bins
+    ubs = [list(range(500))] * 500
+    v, o = csr(ubs)
+    cfg = ref_cfg(500, fpr=0.001, threads=4, tmax=64, disable_estimate_union=True, disable_rearrangement=True)
+    hibf_case(R, "same", cfg, v, o, csr([list(range(500))]), [1], [1], widths=(2, 4))
+    # synthetic, 64 user bins (the small workload's shape at reduced sizes), with uint8 wraparound queries
+    sizes = S.user_bin_sizes(7, 64, S.SIZES_LOG_UNIFORM, 0, 0, 50, 2000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(7, S.QUERIES_HALF_ONE_BIN, 100, 100, 0, 0, 1, 2, 64)
+    qv, qo, thr = S.queries(spec, offs, 0, 400)
+    spec2 = S.query_spec(8, S.QUERIES_HALF_ONE_BIN, 700, 700, 0, 0, 1, 2, 64)
+    qv2, qo2, thr2 = S.queries(spec2, offs, 0, 40)
+    qv = np.concatenate([qv, qv2])
+    qo = np.concatenate([qo, qo2[1:] + qo[-1]])
+    mem_t = np.concatenate([thr, np.full(40, 3, np.uint64)])
+    cnt_t = np.concatenate([thr, np.ones(40, np.uint64)])
+    cfg = ref_cfg(64, h=2, fpr=0.05, tmax=64)
+    hibf_case(R, "synth64", cfg, None, offs, (qv, qo), mem_t, cnt_t, widths=(1, 2, 4), synthetic_seed=7)
+    # synthetic, 600 user bins, three levels with tmax 64, h=3, fpr 0.02, mixed queries
+    sizes = S.user_bin_sizes(11, 600, S.SIZES_LOG_NORMAL, 300.0, 1.2, 20, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(11, S.QUERIES_MIXED, 20, 300, 70, 2, 7, 10, 600)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(600, h=3, fpr=0.02, tmax=64)
+    hibf_case(R, "synth600", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=11)
+
+
+def make_c1(R: Reference):
+    """The 64-user-bin workload at full size: everything except the bit words (which are 2.9 MB)."""
+    sizes = S.user_bin_sizes(1, 64, S.SIZES_LOG_UNIFORM, 0, 0, 1000, 100000)
+    offs = S.offsets_of(sizes)
+    cfg = ref_cfg(64, h=2, fpr=0.05, tmax=64, threads=1)
+    layout = R.layout(cfg, None, offs, seed=1, synthetic=True)
+    H = R.hibf(cfg, None, offs, seed=1, synthetic=True)
+    T = H.tables(with_words=False)
+    spec = S.query_spec(1, S.QUERIES_HALF_ONE_BIN, 250, 250, 0, 0, 1, 2, 64)
+    qv, qo, thr = S.queries(spec, offs, 0, 10000)
+    res = H.query_batch(qv, qo, thr, thr, threads=8)
+    np.savez_compressed(OUT / "c1_reference.npz", ub_offsets=offs, layout=np.frombuffer(layout.encode(), np.uint8),
+                        bins=T["bins"], bin_size=T["bin_size"], hash_funs=T["hash_funs"], next_ibf=T["next_ibf"],
+                        user_bin=T["user_bin"], digests=T["digests"], thresholds=thr, **res)
+    print("c1_reference:", len(T["bins"]), "IBFs")
+
+
+def make_c3_layout(R: Reference):
+    sizes = S.user_bin_sizes(1, 8192, S.SIZES_LOG_NORMAL, 200000.0, 1.5, 1000, 50000000)
+    offs = S.offsets_of(sizes)
+    cfg = ref_cfg(8192, h=2, fpr=0.05, tmax=64, threads=8, sketch_bits=12)
+    t0 = time.time()
+    layout = R.layout(cfg, None, offs, seed=1, synthetic=True)
+    (OUT / "c3_layout.txt").write_text(layout)
+    print(f"c3_layout: {time.time() - t0:.0f}s")
+
+
+def main(argv):
+    build_reference()
+    R = Reference()
+    which = set(argv) or {"ibf", "hibf", "c1", "c3"}
+    if "ibf" in which:
+        make_ibf_cases(R)
+    if "hibf" in which:
+        make_hibf_cases(R)
+    if "c1" in which:
+        make_c1(R)
+    if "c3" in which:
+        make_c3_layout(R)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
