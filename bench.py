@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""bench.py -- HIBF query throughput on GB300 (batched persistent launch vs plain per-query launches).
+
+Default workload (hibf8192): 8,192 user bins (log-normal sizes, median 2e5, sigma 1.5, clipped [1e3, 5e7]; 4.9e9
+values; layout from the reference's DP), h=2, fpr 0.05, tmax 64; one step = membership_for + sort_results for
+1,000,000 queries of length U[20, 2000] (70% from 1-3 user bins with 2% noise, 30% uniform), threshold
+ceil(0.7 * length).  Inputs (8 GB of query values) and the index (13.4 GB) are both larger than L2.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload hibf8192|hibf64]
+
+Prints one JSON line (rank 0).  Under torchrun each rank holds its own replica and answers the full batch
+(replicas only, weak scaling); the step time is the maximum over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "HIBF query values/s on 1 GB300, batched vs plain (bit-exact); p99 serve latency"
+WORKLOAD_DESC = {
+    "hibf8192": "HIBF 8,192 user bins (log-normal median 2e5 sigma 1.5, [1e3,5e7]), h=2, fpr 0.05, tmax 64; "
+                "1e6 queries len U[20,2000] (70% from 1-3 UBs, 2% noise), t=ceil(0.7 len); membership_for",
+    "hibf64": "HIBF 64 user bins (log-uniform [1e3,1e5]), h=2, fpr 0.05, tmax 64; 10,000 queries of 250 values "
+              "(half from one UB), t=125; membership_for",
+}
+REASON_KEYS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["hibf8192", "hibf64"], default="hibf8192")
+    ap.add_argument("--queries", type=int, default=0, help="override the number of queries per step")
+    ap.add_argument("--plain-queries", type=int, default=2000, help="queries timed in the plain form")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end measurement (0: --steps)")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms while running."""
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.1)
+        self.proc.terminate()
+        self.proc.wait()
+        self.file.seek(0)
+        rows = [r.strip().split(",") for r in self.file.read().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        for r in rows:
+            if len(r) < 8:
+                continue
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except ValueError:
+                continue
+            for k, v in zip(REASON_KEYS, r[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(k)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_value_visit():
+    """DRAM bytes per (value, IBF) visit of the query kernel from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / "traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("k_query_bytes_per_value_visit="):
+            return float(line.split("=", 1)[1])
+    return None
+
+
+# ------------------------------------------------------------------------------------------------------------------
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_index(wl):
+    from hibf_gb300 import build as B
+
+    offs = wl.user_bin_offsets()
+    cfg = B.config(number_of_user_bins=wl.n_user_bins, number_of_hash_functions=wl.h, maximum_fpr=wl.fpr)
+    t0 = time.perf_counter()
+    hibf = B.build_synthetic(cfg, wl.layout_text(), wl.query.seed, offs)
+    return hibf, offs, time.perf_counter() - t0
+
+
+def oracle_from_device(hibf):
+    """The C oracle holding the device-built bit store (downloaded in place)."""
+    from hibf_gb300 import _native as N
+    from oracle.bindings import Oracle, build_oracle
+
+    build_oracle()
+    OH = Oracle().hibf(hibf.tables())
+    for k in range(hibf.n_ibfs):
+        addr, n = OH.data_ptr(k)
+        N.call("hibf_gpu_hibf_download_words", hibf._h, k, addr, n)
+    return OH
+
+
+def cpu_sample(OH, wl, offs, budget_s, threads, first=0):
+    """Times the oracle's membership_for + sort_results on a bounded sample of the workload's queries."""
+    probe = min(wl.n_queries, 400)
+    qo, thr = wl.query_offsets(first, probe)
+    v = wl.queries_host(offs, first, probe, qo)
+    t0 = time.perf_counter()
+    OH.run_queries(v, qo, thr, thr, mode=1, threads=threads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    n = int(min(wl.n_queries - first, max(probe, probe * budget_s / dt)))
+    qo, thr = wl.query_offsets(first, n)
+    v = wl.queries_host(offs, first, n, qo)
+    t0 = time.perf_counter()
+    pairs, chk = OH.run_queries(v, qo, thr, thr, mode=1, threads=threads)
+    dt = time.perf_counter() - t0
+    return dict(values=int(qo[-1]), queries=n, seconds=dt, value_visits=pairs, checksum=chk, qo=qo, thr=thr, v=v)
+
+
+# ------------------------------------------------------------------------------------------------------------------
+def run_ours(args, wl, rank, world, local):
+    import torch
+
+    from hibf_gb300 import _native as N
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    hibf, offs, build_s = build_index(wl)
+    nq = args.queries or wl.n_queries
+    qo, thr = wl.query_offsets(0, nq)
+    nv = int(qo[-1])
+    d_ub = torch.from_numpy(offs.view(np.int64)).cuda()
+    d_qo = torch.from_numpy(qo.view(np.int64)).cuda()
+    d_thr = torch.from_numpy(thr.view(np.int64)).cuda()
+    d_v = torch.empty(max(nv, 1), dtype=torch.int64, device="cuda")
+    wl.queries_device(d_ub.data_ptr(), 0, nq, d_qo.data_ptr(), d_v.data_ptr())
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.Stream()
+    agent = hibf.membership_agent()
+    agent.reserve(nq, nv, nq * 8 + 65536, nq * 8 + 65536)
+    agent.set_stream(stream.cuda_stream)
+    agent.capture_batch_device(d_v.data_ptr(), d_qo.data_ptr(), nq, d_thr.data_ptr())
+    for _ in range(max(args.warmup, 3)):
+        agent.replay()
+    stream.synchronize()
+    agent.status()
+
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0] or 0)
+    clocks = ClockSampler(gpu_index)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        agent.replay()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    agent.status()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    tasks, visits = agent.last_work()
+    kms = []
+    for _ in range(3):
+        agent.replay()
+        stream.synchronize()
+        kms.append(agent.kernel_ms())
+    kernel_ms = sum(kms) / len(kms)
+    launches_per_step = 8
+    res_offs, res_ids, _ = agent.fetch_results(nq)
+
+    # plain form: one launch per query on the first P queries
+    P = min(args.plain_queries, nq)
+    pa = hibf.membership_agent()
+    pa.reserve(P, nv, 65536, P * 8 + 65536)
+    pa.set_stream(stream.cuda_stream)
+    pa.query_plain_device(d_v.data_ptr(), qo[:P + 1], thr[:P])  # warm-up
+    stream.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    pa.query_plain_device(d_v.data_ptr(), qo[:P + 1], thr[:P])
+    p1.record(stream)
+    p1.synchronize()
+    plain_s = p0.elapsed_time(p1) / 1e3
+    plain_offs, plain_ids, _ = pa.fetch_results(P)
+    plain_equal = bool(np.array_equal(plain_offs, res_offs[:P + 1]) and
+                       np.array_equal(plain_ids, res_ids[:int(res_offs[P])]))
+    plain_vps = float(qo[P]) / plain_s
+
+    # end to end through the C ABI host call: pinned host inputs -> H2D -> batch -> D2H results
+    h_v = torch.empty(max(nv, 1), dtype=torch.int64, pin_memory=True)
+    h_v.copy_(d_v)
+    hv = h_v.numpy().view(np.uint64)[:nv]
+    ea = hibf.membership_agent()
+    ea.reserve(nq, nv, nq * 8 + 65536, nq * 8 + 65536)
+    for _ in range(2):
+        ea.query_batch(hv, qo, thr)
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        eo, ei, _ = ea.query_batch(hv, qo, thr)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_equal = bool(np.array_equal(eo, res_offs) and np.array_equal(ei, res_ids))
+    h2d = nv * 8 + (nq + 1) * 8 + nq * 8
+    d2h = (nq + 1) * 8 + int(eo[-1]) * 8 + 8 * 8 + 16
+
+    out = None
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        bytes_per_visit = wl.h * 1 * 32  # h rows of ceil(64/256) = 1 sector each (all IBFs have 64 bins)
+        achieved = visits * bytes_per_visit / (kernel_ms / 1e3) / 1e9
+        tpv = traffic_per_value_visit()
+        cpu = None
+        parity = {"plain_equals_batch": plain_equal, "e2e_equals_batch": e2e_equal}
+        if not args.no_cpu:
+            OH = oracle_from_device(hibf)
+            threads = os.cpu_count() or 1
+            s = cpu_sample(OH, wl, offs, args.cpu_seconds, threads)
+            cpu = {"value": s["values"] / s["seconds"], "unit": "values/s", "cores": threads, "kind": "port",
+                   "sample": f"first {s['queries']} queries ({s['values']} values) of the batch, membership_for + "
+                             f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads"}
+            o_off, o_ids = OH.membership_batch(s["v"], s["qo"], s["thr"], threads=threads)
+            n = s["queries"]
+            parity["oracle_sample_queries"] = n
+            parity["oracle_sample_equal"] = bool(np.array_equal(o_off, res_offs[:n + 1]) and
+                                                 np.array_equal(o_ids, res_ids[:int(res_offs[n])]))
+        value = world * nv / (ms / 1e3)
+        out = {
+            "metric": METRIC, "value": value, "unit": "values/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic: seeded splitmix64 user bins and queries (include/hibf_gb300_synthetic.h)",
+            "config": {"workload": WORKLOAD_DESC[wl.name], "name": wl.name, "n_user_bins": wl.n_user_bins,
+                       "queries_per_step": nq, "values_per_step": nv, "n_ibfs": hibf.n_ibfs,
+                       "index_bytes": int(hibf.info()["device_bytes"]), "parallelism": f"replicas x{world}",
+                       "l2": "inputs (values) and the index are larger than L2; no flush",
+                       "form": "one persistent launch per batch, CUDA-graph replay"},
+            "queries_per_s": world * nq / (ms / 1e3),
+            "e2e": {"value": world * nv / e2e_s, "unit": "values/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                    "call": "hibf_gpu_agent_query_batch (host buffers, pinned)"},
+            "plain": {"values_per_s": plain_vps, "queries": P, "form": "one launch per query"},
+            "batched_vs_plain": value / world / plain_vps,
+            "gpu_launches": launches_per_step * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "peak_kind": peak_kind,
+                         "traffic": (tpv * visits) if tpv is not None else None,
+                         "kernel": "k_query", "kernel_ms": kernel_ms, "value_visits": visits, "tasks": tasks,
+                         "algorithmic_bytes_per_value_visit": bytes_per_visit},
+            "cpu_baseline": cpu, "clocks": clk, "build_s": build_s, "parity": parity,
+        }
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def run_reference(args, wl, rank, world, local):
+    """The reference CPU path on the host cores: the C restatement of the reference's query (oracle/hibf_oracle.c)
+    with all host threads.  The index bits are built on the device and downloaded once (set-up, not timed)."""
+    if rank != 0:
+        return None
+    import torch
+
+    torch.cuda.set_device(local)
+    hibf, offs, _ = build_index(wl)
+    OH = oracle_from_device(hibf)
+    del hibf
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, min(args.cpu_seconds, 60.0 / max(1, args.steps + args.warmup)))
+    first = 0
+    for _ in range(args.warmup):
+        s = cpu_sample(OH, wl, offs, per_step, threads, first)
+        first = (first + s["queries"]) % max(1, wl.n_queries - 1)
+    vals, secs, nqs = 0, 0.0, 0
+    for _ in range(args.steps):
+        s = cpu_sample(OH, wl, offs, per_step, threads, first)
+        first = (first + s["queries"]) % max(1, wl.n_queries - 1)
+        vals += s["values"]
+        secs += s["seconds"]
+        nqs += s["queries"]
+    value = vals / secs
+    sample = (f"{args.steps} steps of ~{per_step:.1f} s, {nqs} queries ({vals} values) in total, membership_for + "
+              f"sort_results")
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "values/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic: seeded splitmix64 user bins and queries (include/hibf_gb300_synthetic.h)",
+            "config": {"workload": WORKLOAD_DESC[wl.name], "name": wl.name, "n_user_bins": wl.n_user_bins},
+            "cpu_baseline": {"value": value, "unit": "values/s", "cores": threads, "kind": "port",
+                             "sample": sample + "; oracle/hibf_oracle.c (the reference's sources are not on this host)"},
+            "e2e": {"value": value, "unit": "values/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    from hibf_gb300.workloads import WORKLOADS
+
+    wl = WORKLOADS[args.workload]
+    out = run_reference(args, wl, rank, world, local) if args.impl == "reference" else \
+        run_ours(args, wl, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

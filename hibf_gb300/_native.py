@@ -49,6 +49,15 @@ class InvalidArgument(HibfGpuError, ValueError):
     """std::invalid_argument of the reference."""
 
 
+class BuildConfig(ctypes.Structure):
+    """hibf_gpu_build_config (the fields of seqan::hibf::config the build uses)."""
+
+    _fields_ = [("number_of_user_bins", u64), ("number_of_hash_functions", u64), ("maximum_fpr", ctypes.c_double),
+                ("relaxed_fpr", ctypes.c_double), ("threads", u64), ("user_bins_disjoint", ci)]
+
+
+INPUT_FN = ctypes.CFUNCTYPE(None, vp, u64, vp)
+
 # (name, restype, argtypes); restype None means the int status convention.
 _SIGS = [
     ("hibf_gpu_last_error", ctypes.c_char_p, []),
@@ -79,6 +88,13 @@ _SIGS = [
     ("hibf_gpu_hibf_ibf_info", None, [vp, u64, u64p]),
     ("hibf_gpu_hibf_emplace", None, [vp, u64, vp, u64, u64]),
     ("hibf_gpu_hibf_emplace_d", None, [vp, u64, vp, vp, u64, u64, vp]),
+    ("hibf_gpu_hibf_get_tables", None, [vp, vp, vp, vp, vp, vp]),
+    ("hibf_gpu_sink_push", None, [vp, vp, u64]),
+    ("hibf_gpu_hibf_build", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, INPUT_FN, vp, ctypes.POINTER(vp)]),
+    ("hibf_gpu_hibf_build_synthetic", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, u64, vp,
+                                             ctypes.POINTER(vp)]),
+    ("hibf_gpu_plan_disjoint", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, vp, u64p, u64p, vp, vp, vp,
+                                      vp, vp, vp]),
     ("hibf_gpu_hibf_upload_words", None, [vp, u64, vp, u64]),
     ("hibf_gpu_hibf_download_words", None, [vp, u64, vp, u64]),
     ("hibf_gpu_agent_create", None, [vp, ctypes.POINTER(vp)]),
@@ -96,6 +112,16 @@ _SIGS = [
      [vp, u64, ci, ci, ctypes.POINTER(u64p), ctypes.POINTER(u64p), ctypes.POINTER(vp)]),
     ("hibf_gpu_agent_status", None, [vp]),
     ("hibf_gpu_agent_last_work", None, [vp, u64p, u64p]),
+    ("hibf_gpu_agent_capture_batch_d", None, [vp, ci, vp, vp, u64, vp, ci]),
+    ("hibf_gpu_agent_replay", None, [vp]),
+    ("hibf_gpu_agent_kernel_ms", None, [vp, ctypes.POINTER(ctypes.c_float)]),
+    ("hibf_gpu_synth_user_bin_offsets", None, [u64, ci, ctypes.c_double, ctypes.c_double, u64, u64, u64, vp]),
+    ("hibf_gpu_synth_query_offsets", None, [u64, ci, u64, u64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                            ctypes.c_uint32, u64, u64, u64, vp, vp]),
+    ("hibf_gpu_synth_queries", None, [u64, ci, u64, u64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.c_uint32, u64, vp, u64, u64, vp, vp]),
+    ("hibf_gpu_synth_queries_d", None, [u64, ci, u64, u64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.c_uint32, u64, vp, u64, u64, vp, vp, vp]),
 ]
 
 _lib = None

@@ -1,0 +1,702 @@
+// build.cu -- host orchestration of an HIBF build from a layout, with every insert done on the device.
+//
+// Restates the reference's build driver (src/hierarchical_interleaved_bloom_filter.cpp:40-209; src/build/*.cpp;
+// include/hibf/build/*.hpp) on top of the device bit stores:
+//   layout text  -> layout records            (src/layout/layout.cpp:60-145)
+//   records      -> IBF graph                 (src/layout/graph.cpp:19-125)
+//   graph        -> per-IBF sizes and tables  (construct_ibf.cpp:26-64, bin_size_in_bits.hpp:35-45,
+//                                              compute_fpr_correction.cpp:16-38, update_user_bins.hpp:19-25)
+//   contents     -> device inserts            (insert_into_ibf.cpp:28-84; merged bins receive the union of their
+//                                              subtree, i.e. every user bin below them)
+// IBFs are numbered in depth-first pre-order with children in layout order (the reference numbers them in a
+// randomised order, HIBF.cpp:111-116; numbering does not change any bit or query result).
+//
+// Split user bins are chunked in the order their distinct values first appear (stream order).  The reference
+// chunks in the iteration order of its hash set (robin_hood::unordered_flat_set, insert_into_ibf.cpp:34-47), which
+// changes which of the split bins a value lands in, not the sizes, tables or the bins of any unsplit user bin.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/hibf_gb300_synthetic.h"
+#include "common.hpp"
+#include "device.cuh"
+#include "hibf_internal.cuh"
+
+namespace hibf_gb300
+{
+namespace build
+{
+
+struct user_bin_rec
+{
+    std::vector<uint64_t> prev;
+    uint64_t storage{};
+    uint64_t ntb{};
+    uint64_t idx{};
+};
+
+struct max_bin_rec
+{
+    std::vector<uint64_t> prev;
+    uint64_t id{};
+};
+
+struct layout_t
+{
+    uint64_t top_max{};
+    std::vector<max_bin_rec> max_bins;
+    std::vector<user_bin_rec> user_bins;
+};
+
+static std::vector<uint64_t> parse_list(std::string const & s, char sep)
+{
+    std::vector<uint64_t> out;
+    size_t i = 0;
+    while (i < s.size())
+    {
+        size_t j = s.find(sep, i);
+        if (j == std::string::npos)
+            j = s.size();
+        if (j > i)
+            out.push_back(std::stoull(s.substr(i, j - i)));
+        i = j + 1;
+    }
+    return out;
+}
+
+// The layout file format of src/layout/layout.cpp:60-145 (an optional @HIBF_CONFIG block is skipped).
+layout_t parse_layout(char const * text)
+{
+    layout_t L;
+    std::string const t(text ? text : "");
+    size_t pos = 0;
+    auto next_line = [&](std::string & line) -> bool
+    {
+        if (pos >= t.size())
+            return false;
+        size_t e = t.find('\n', pos);
+        if (e == std::string::npos)
+            e = t.size();
+        line = t.substr(pos, e - pos);
+        if (!line.empty() && line.back() == '\r')
+            line.pop_back();
+        pos = e + 1;
+        return true;
+    };
+    std::string line;
+    std::string const key = "fullest_technical_bin_idx:";
+    bool have_top = false;
+    while (next_line(line))
+    {
+        if (line.empty() || line[0] == '@')
+            continue;
+        if (line.rfind("#TOP_LEVEL_IBF", 0) == 0)
+        {
+            size_t const k = line.find(key);
+            if (k == std::string::npos)
+                fail(HIBF_GPU_ERR_INVALID_ARG, "layout: malformed top-level header");
+            L.top_max = std::stoull(line.substr(k + key.size()));
+            have_top = true;
+            continue;
+        }
+        if (line.rfind("#LOWER_LEVEL_IBF_", 0) == 0)
+        {
+            size_t const sp = line.find(' ');
+            size_t const k = line.find(key);
+            if (sp == std::string::npos || k == std::string::npos)
+                fail(HIBF_GPU_ERR_INVALID_ARG, "layout: malformed lower-level header");
+            max_bin_rec m;
+            m.prev = parse_list(line.substr(17, sp - 17), ';');
+            m.id = std::stoull(line.substr(k + key.size()));
+            if (m.prev.empty())
+                fail(HIBF_GPU_ERR_INVALID_ARG, "layout: lower-level header without bin indices");
+            L.max_bins.push_back(std::move(m));
+            continue;
+        }
+        if (line[0] == '#')
+            continue; // column names
+        size_t const t1 = line.find('\t');
+        size_t const t2 = line.find('\t', t1 + 1);
+        if (t1 == std::string::npos || t2 == std::string::npos)
+            fail(HIBF_GPU_ERR_INVALID_ARG, "layout: malformed user bin line");
+        user_bin_rec r;
+        r.idx = std::stoull(line.substr(0, t1));
+        std::vector<uint64_t> bins = parse_list(line.substr(t1 + 1, t2 - t1 - 1), ';');
+        std::vector<uint64_t> ntb = parse_list(line.substr(t2 + 1), ';');
+        if (bins.empty() || ntb.empty())
+            fail(HIBF_GPU_ERR_INVALID_ARG, "layout: malformed user bin line");
+        r.storage = bins.back();
+        bins.pop_back();
+        r.prev = std::move(bins);
+        r.ntb = ntb.back();
+        L.user_bins.push_back(std::move(r));
+    }
+    if (!have_top)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "layout: missing #TOP_LEVEL_IBF header");
+    return L;
+}
+
+struct node_t
+{
+    std::vector<size_t> children;
+    size_t parent{SIZE_MAX};
+    uint64_t parent_bin_index{};
+    uint64_t max_bin_index{};
+    uint64_t ntb{};
+    int64_t favourite{-1};
+    std::vector<user_bin_rec> records;
+};
+
+// graph::graph (src/layout/graph.cpp:19-125).
+std::vector<node_t> make_graph(layout_t const & L)
+{
+    std::vector<node_t> g(1);
+    g[0].max_bin_index = L.top_max;
+    for (auto const & mb : L.max_bins)
+    {
+        size_t parent = 0;
+        for (size_t i = 0; i + 1 < mb.prev.size(); ++i)
+        {
+            for (size_t c : g[parent].children)
+                if (g[c].parent_bin_index == mb.prev[i])
+                {
+                    parent = c;
+                    break;
+                }
+        }
+        node_t n;
+        n.parent = parent;
+        n.parent_bin_index = mb.prev.back();
+        n.max_bin_index = mb.id;
+        g.push_back(std::move(n));
+        size_t const id = g.size() - 1;
+        g[parent].children.push_back(id);
+        if (g[parent].max_bin_index == mb.prev.back())
+            g[parent].favourite = static_cast<int64_t>(g[parent].children.size() - 1);
+    }
+    for (auto const & r : L.user_bins)
+    {
+        size_t cur = 0;
+        for (uint64_t bin : r.prev)
+        {
+            g[cur].ntb = std::max(g[cur].ntb, bin + 1);
+            size_t nxt = SIZE_MAX;
+            for (size_t c : g[cur].children)
+                if (g[c].parent_bin_index == bin)
+                {
+                    nxt = c;
+                    break;
+                }
+            if (nxt == SIZE_MAX)
+                fail(HIBF_GPU_ERR_INVALID_ARG, "layout: user bin refers to a lower-level IBF without a header");
+            cur = nxt;
+        }
+        g[cur].ntb = std::max(g[cur].ntb, r.storage + r.ntb);
+        if (r.storage == g[cur].max_bin_index)
+            g[cur].records.insert(g[cur].records.begin(), r);
+        else
+            g[cur].records.push_back(r);
+    }
+    return g;
+}
+
+// bin_size_in_bits (include/hibf/build/bin_size_in_bits.hpp:35-45).
+uint64_t bin_size_in_bits(double fpr, uint64_t hash_count, uint64_t elements)
+{
+    double const numerator = -static_cast<double>(elements * hash_count);
+    double const denominator = std::log(1 - std::exp(std::log(fpr) / static_cast<double>(hash_count)));
+    return static_cast<uint64_t>(std::ceil(numerator / denominator));
+}
+
+// compute_fpr_correction (src/layout/compute_fpr_correction.cpp:16-38).
+std::vector<double> fpr_correction(double fpr, uint64_t hash_count, uint64_t t_max)
+{
+    uint64_t const max_tb = ((t_max + 63) >> 6) << 6;
+    std::vector<double> c(max_tb + 1, 0.0);
+    c[1] = 1.0;
+    double const h = static_cast<double>(hash_count);
+    double const numerator = std::log1p(-std::exp(std::log(fpr) / h));
+    for (uint64_t split = 2; split <= max_tb; ++split)
+    {
+        double const log_target_fpr = std::log1p(-std::exp(std::log1p(-fpr) / static_cast<double>(split)));
+        c[split] = numerator / std::log1p(-std::exp(log_target_fpr / h));
+    }
+    return c;
+}
+
+struct plan_t
+{
+    std::vector<node_t> g;
+    std::vector<size_t> order;  // IBF index -> graph node
+    std::vector<size_t> ibf_of; // graph node -> IBF index
+    std::vector<uint64_t> bins, bin_size, hash_funs, next_ibf, user_bin, tb_off;
+    std::vector<uint64_t> parent_ibf, parent_bin;
+    // per user bin: leaf IBF, leaf record, and the (IBF, merged bin) pairs of its ancestors
+    std::vector<size_t> ub_leaf;
+    std::vector<user_bin_rec> ub_rec;
+    std::vector<std::vector<std::pair<uint64_t, uint64_t>>> ub_merged;
+};
+
+// Sizes every IBF like construct_ibf (src/build/construct_ibf.cpp:26-64): the max bin's content is the favourite
+// child's union (merged max bin, relaxed fpr, one bin) or the max record's distinct values split over its
+// technical bins (maximum fpr, times the fpr correction for split bins).  `distinct[u]` = distinct values of user
+// bin u; `subtree_union(node)` = distinct values under a node.
+template <typename union_fn>
+plan_t make_plan(hibf_gpu_build_config const & cfg, layout_t const & L, std::vector<uint64_t> const & distinct,
+                 union_fn && subtree_union)
+{
+    plan_t P;
+    P.g = make_graph(L);
+    auto & g = P.g;
+    // pre-order numbering
+    std::vector<size_t> st{0};
+    P.ibf_of.assign(g.size(), SIZE_MAX);
+    while (!st.empty())
+    {
+        size_t const n = st.back();
+        st.pop_back();
+        P.ibf_of[n] = P.order.size();
+        P.order.push_back(n);
+        for (auto it = g[n].children.rbegin(); it != g[n].children.rend(); ++it)
+            st.push_back(*it);
+    }
+    size_t const n_ibfs = P.order.size();
+    uint64_t const h = cfg.number_of_hash_functions;
+    std::vector<double> const corr = fpr_correction(cfg.maximum_fpr, h, g[0].ntb);
+    P.tb_off.assign(n_ibfs + 1, 0);
+    P.parent_ibf.assign(n_ibfs, 0);
+    P.parent_bin.assign(n_ibfs, 0);
+    for (size_t k = 0; k < n_ibfs; ++k)
+    {
+        node_t const & nd = g[P.order[k]];
+        if (nd.ntb == 0)
+            fail(HIBF_GPU_ERR_INVALID_ARG, "layout: an IBF has no technical bins");
+        uint64_t kmers = 0, nb = 1;
+        double fpr = cfg.maximum_fpr;
+        if (nd.favourite >= 0)
+        {
+            kmers = subtree_union(nd.children[static_cast<size_t>(nd.favourite)]);
+            nb = 1;
+            fpr = cfg.relaxed_fpr;
+        }
+        else
+        {
+            if (nd.records.empty())
+                fail(HIBF_GPU_ERR_INVALID_ARG, "layout: an IBF has neither a merged nor a user max bin");
+            user_bin_rec const & r = nd.records[0];
+            if (r.idx >= distinct.size())
+                fail(HIBF_GPU_ERR_INVALID_ARG, "layout: user bin index out of range");
+            kmers = distinct[r.idx];
+            nb = r.ntb;
+        }
+        uint64_t const per_bin = (kmers + nb - 1) / nb;
+        uint64_t const bits = bin_size_in_bits(fpr, h, per_bin);
+        uint64_t const size = nb == 1 ? bits : static_cast<uint64_t>(std::ceil(static_cast<double>(bits) * corr.at(nb)));
+        if (size == 0)
+            fail(HIBF_GPU_ERR_LOGIC, "The size of a bin must be > 0.");
+        P.bins.push_back(nd.ntb);
+        P.bin_size.push_back(size);
+        P.hash_funs.push_back(h);
+        P.tb_off[k + 1] = P.tb_off[k] + nd.ntb;
+        if (nd.parent != SIZE_MAX)
+        {
+            P.parent_ibf[k] = P.ibf_of[nd.parent];
+            P.parent_bin[k] = nd.parent_bin_index;
+        }
+    }
+    // tables (HIBF.cpp:47-55, update_user_bins.hpp:19-25)
+    P.next_ibf.assign(P.tb_off[n_ibfs], 0);
+    P.user_bin.assign(P.tb_off[n_ibfs], HIBF_GPU_BIN_MERGED);
+    for (size_t k = 0; k < n_ibfs; ++k)
+    {
+        node_t const & nd = g[P.order[k]];
+        for (uint64_t b = 0; b < nd.ntb; ++b)
+            P.next_ibf[P.tb_off[k] + b] = k;
+        for (size_t c : nd.children)
+            P.next_ibf[P.tb_off[k] + g[c].parent_bin_index] = P.ibf_of[c];
+        for (auto const & r : nd.records)
+            for (uint64_t b = r.storage; b < r.storage + r.ntb; ++b)
+                P.user_bin[P.tb_off[k] + b] = r.idx;
+    }
+    // per user bin placement
+    size_t const nub = cfg.number_of_user_bins;
+    P.ub_leaf.assign(nub, SIZE_MAX);
+    P.ub_rec.assign(nub, user_bin_rec{});
+    P.ub_merged.assign(nub, {});
+    for (size_t k = 0; k < n_ibfs; ++k)
+    {
+        size_t const n = P.order[k];
+        for (auto const & r : g[n].records)
+        {
+            if (r.idx >= nub)
+                fail(HIBF_GPU_ERR_INVALID_ARG, "layout: user bin index out of range");
+            if (P.ub_leaf[r.idx] != SIZE_MAX)
+                fail(HIBF_GPU_ERR_INVALID_ARG, "layout: a user bin occurs twice");
+            P.ub_leaf[r.idx] = k;
+            P.ub_rec[r.idx] = r;
+            size_t cur = n;
+            while (g[cur].parent != SIZE_MAX)
+            {
+                P.ub_merged[r.idx].push_back({P.ibf_of[g[cur].parent], g[cur].parent_bin_index});
+                cur = g[cur].parent;
+            }
+        }
+    }
+    for (size_t u = 0; u < nub; ++u)
+        if (P.ub_leaf[u] == SIZE_MAX)
+            fail(HIBF_GPU_ERR_INVALID_ARG, "layout: a user bin is missing");
+    return P;
+}
+
+// Distinct values under each node when user bins are pairwise disjoint: sums of their sizes.
+std::vector<uint64_t> disjoint_unions(plan_t const & P, std::vector<uint64_t> const & distinct, layout_t const & L)
+{
+    (void)L;
+    std::vector<uint64_t> sum(P.g.size(), 0);
+    // accumulate user bins into their leaf node and every ancestor
+    for (size_t u = 0; u < P.ub_leaf.size(); ++u)
+    {
+        size_t n = P.order[P.ub_leaf[u]];
+        while (true)
+        {
+            sum[n] += distinct[u];
+            if (P.g[n].parent == SIZE_MAX)
+                break;
+            n = P.g[n].parent;
+        }
+    }
+    return sum;
+}
+
+// ---- device inserts -------------------------------------------------------------------------------------------
+struct alignas(16) insert_job
+{
+    uint64_t start;  // first value (stream position for synthetic jobs, buffer offset otherwise)
+    uint64_t n;      // number of values
+    uint64_t chunk;  // values per technical bin for split user bins; 0: all values into first_bin
+    uint32_t ibf;
+    uint32_t first_bin;
+};
+
+// Inserts every job's values; job j covers flattened positions [end[j] - n_j, end[j]).  Values come from the
+// splitmix64 stream (values == nullptr) or from a device buffer.
+__global__ void k_insert_jobs(dev_node const * __restrict__ nodes, insert_job const * __restrict__ jobs,
+                              uint64_t const * __restrict__ job_end, uint32_t n_jobs, uint64_t total,
+                              uint64_t seed, uint64_t const * __restrict__ values)
+{
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    if (i >= total)
+        return;
+    // first job with end > i
+    uint32_t lo = 0, hi = n_jobs;
+    while (lo < hi)
+    {
+        uint32_t const mid = (lo + hi) >> 1;
+        if (job_end[mid] > i)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    uint32_t j = lo;
+    for (; i < total; i += stride)
+    {
+        while (job_end[j] <= i)
+            ++j;
+        insert_job const jb = jobs[j];
+        uint64_t const local = i - (job_end[j] - jb.n);
+        uint64_t const v = values ? values[jb.start + local] : hg_stream_at(seed, jb.start + local);
+        uint64_t const b = jb.first_bin + (jb.chunk ? local / jb.chunk : 0u);
+        dev_node const nd = nodes[jb.ibf];
+        if (b >= nd.bins)
+            continue;
+        unsigned long long const bit = 1ull << (b & 63u);
+        uint64_t * const base = const_cast<uint64_t *>(nd.words) + (b >> 6);
+        for (uint32_t k = 0; k < nd.hash_funs; ++k)
+        {
+            uint64_t const r = hash_row(v, c_hash_seeds[k], nd.hash_shift, nd.bin_size);
+            atomicOr(reinterpret_cast<unsigned long long *>(base + r * nd.row_words), bit);
+        }
+    }
+}
+
+void run_jobs(hibf_gpu_hibf * h, std::vector<insert_job> const & jobs, uint64_t seed, uint64_t const * d_values,
+              cudaStream_t s)
+{
+    if (jobs.empty())
+        return;
+    std::vector<uint64_t> end(jobs.size());
+    uint64_t acc = 0;
+    for (size_t j = 0; j < jobs.size(); ++j)
+    {
+        acc += jobs[j].n;
+        end[j] = acc;
+    }
+    if (acc == 0)
+        return;
+    dbuf dj, de;
+    dj.ensure(jobs.size() * sizeof(insert_job));
+    de.ensure(end.size() * 8);
+    HG_CUDA(cudaMemcpyAsync(dj.p, jobs.data(), jobs.size() * sizeof(insert_job), cudaMemcpyHostToDevice, s));
+    HG_CUDA(cudaMemcpyAsync(de.p, end.data(), end.size() * 8, cudaMemcpyHostToDevice, s));
+    unsigned const block = 256;
+    uint64_t const want = (acc + block - 1) / block;
+    unsigned const grid = static_cast<unsigned>(std::min<uint64_t>(want, static_cast<uint64_t>(sm_count()) * 16));
+    k_insert_jobs<<<grid, block, 0, s>>>(h->d_nodes.as<dev_node>(), dj.as<insert_job>(), de.as<uint64_t>(),
+                                         static_cast<uint32_t>(jobs.size()), acc, seed, d_values);
+    HG_CUDA(cudaGetLastError());
+    HG_CUDA(cudaStreamSynchronize(s));
+}
+
+hibf_gpu_hibf * create_from_plan(plan_t const & P, uint64_t n_user_bins)
+{
+    hibf_gpu_hibf * h = nullptr;
+    int const st = hibf_gpu_hibf_create(n_user_bins, P.bins.size(), P.bins.data(), P.bin_size.data(),
+                                        P.hash_funs.data(), P.next_ibf.data(), P.user_bin.data(), &h);
+    if (st != HIBF_GPU_OK)
+        fail(st, "hibf_gpu_hibf_create failed");
+    return h;
+}
+
+void validate(hibf_gpu_build_config const * cfg)
+{
+    if (!cfg)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "null config");
+    // config::validate_and_set_defaults (src/config.cpp:64-130), the fields this build uses
+    if (cfg->number_of_user_bins == 0)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "[HIBF CONFIG ERROR] You did not set the required config::number_of_user_bins.");
+    if (cfg->number_of_hash_functions == 0 || cfg->number_of_hash_functions > 5)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "[HIBF CONFIG ERROR] config::number_of_hash_functions must be in [1,5].");
+    if (!(cfg->maximum_fpr > 0.0 && cfg->maximum_fpr < 1.0))
+        fail(HIBF_GPU_ERR_INVALID_ARG, "[HIBF CONFIG ERROR] config::maximum_fpr must be in (0.0,1.0).");
+    if (!(cfg->relaxed_fpr > 0.0 && cfg->relaxed_fpr < 1.0))
+        fail(HIBF_GPU_ERR_INVALID_ARG, "[HIBF CONFIG ERROR] config::relaxed_fpr must be in (0.0,1.0).");
+    if (cfg->relaxed_fpr < cfg->maximum_fpr)
+        fail(HIBF_GPU_ERR_INVALID_ARG,
+             "[HIBF CONFIG ERROR] config::relaxed_fpr must be greater than or equal to config::maximum_fpr.");
+}
+
+} // namespace build
+} // namespace hibf_gb300
+
+using namespace hibf_gb300;
+using namespace hibf_gb300::build;
+
+struct hibf_gpu_sink
+{
+    std::vector<uint64_t> values;
+};
+
+extern "C"
+{
+
+    int hibf_gpu_sink_push(hibf_gpu_sink * sink, uint64_t const * values, uint64_t n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!sink || (n && !values))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                sink->values.insert(sink->values.end(), values, values + n);
+            });
+    }
+
+    int hibf_gpu_plan_disjoint(hibf_gpu_build_config const * cfg, char const * layout_text,
+                               uint64_t const * user_bin_sizes, uint64_t * n_ibfs, uint64_t * total_bins,
+                               uint64_t * bins, uint64_t * bin_sizes, uint64_t * next_ibf_id, uint64_t * user_bin_id,
+                               uint64_t * parent_ibf, uint64_t * parent_bin)
+    {
+        return guarded(
+            [&]
+            {
+                validate(cfg);
+                if (!user_bin_sizes || !n_ibfs || !total_bins)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                layout_t const L = parse_layout(layout_text);
+                std::vector<uint64_t> const distinct(user_bin_sizes, user_bin_sizes + cfg->number_of_user_bins);
+                std::vector<uint64_t> sums;
+                plan_t const P = make_plan(*cfg, L, distinct,
+                                           [&](size_t node)
+                                           {
+                                               (void)node;
+                                               return uint64_t{1}; // placeholder: only placements are used
+                                           });
+                // second pass with the subtree sums now that placements are known
+                sums = disjoint_unions(P, distinct, L);
+                plan_t const Q = make_plan(*cfg, L, distinct,
+                                           [&](size_t node)
+                                           {
+                                               return sums[node];
+                                           });
+                *n_ibfs = Q.bins.size();
+                *total_bins = Q.tb_off.back();
+                if (bins)
+                    std::copy(Q.bins.begin(), Q.bins.end(), bins);
+                if (bin_sizes)
+                    std::copy(Q.bin_size.begin(), Q.bin_size.end(), bin_sizes);
+                if (next_ibf_id)
+                    std::copy(Q.next_ibf.begin(), Q.next_ibf.end(), next_ibf_id);
+                if (user_bin_id)
+                    std::copy(Q.user_bin.begin(), Q.user_bin.end(), user_bin_id);
+                if (parent_ibf)
+                    std::copy(Q.parent_ibf.begin(), Q.parent_ibf.end(), parent_ibf);
+                if (parent_bin)
+                    std::copy(Q.parent_bin.begin(), Q.parent_bin.end(), parent_bin);
+            });
+    }
+
+    int hibf_gpu_hibf_build_synthetic(hibf_gpu_build_config const * cfg, char const * layout_text, uint64_t seed,
+                                      uint64_t const * user_bin_offsets, hibf_gpu_hibf ** out)
+    {
+        return guarded(
+            [&]
+            {
+                validate(cfg);
+                if (!user_bin_offsets || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *out = nullptr;
+                uint64_t const nub = cfg->number_of_user_bins;
+                std::vector<uint64_t> distinct(nub);
+                for (uint64_t u = 0; u < nub; ++u)
+                    distinct[u] = user_bin_offsets[u + 1] - user_bin_offsets[u];
+                layout_t const L = parse_layout(layout_text);
+                plan_t const P0 = make_plan(*cfg, L, distinct, [](size_t) { return uint64_t{1}; });
+                std::vector<uint64_t> const sums = disjoint_unions(P0, distinct, L);
+                plan_t const P = make_plan(*cfg, L, distinct, [&](size_t node) { return sums[node]; });
+                hibf_gpu_hibf * h = create_from_plan(P, nub);
+                try
+                {
+                    std::vector<insert_job> jobs;
+                    for (uint64_t u = 0; u < nub; ++u)
+                    {
+                        uint64_t const n = distinct[u];
+                        user_bin_rec const & r = P.ub_rec[u];
+                        insert_job leaf{user_bin_offsets[u], n, 0, static_cast<uint32_t>(P.ub_leaf[u]),
+                                        static_cast<uint32_t>(r.storage)};
+                        if (r.ntb > 1)
+                            leaf.chunk = (n + r.ntb - 1) / r.ntb;
+                        jobs.push_back(leaf);
+                        for (auto const & [ibf, bin] : P.ub_merged[u])
+                            jobs.push_back(insert_job{user_bin_offsets[u], n, 0, static_cast<uint32_t>(ibf),
+                                                      static_cast<uint32_t>(bin)});
+                    }
+                    run_jobs(h, jobs, seed, nullptr, h->stream);
+                }
+                catch (...)
+                {
+                    hibf_gpu_hibf_destroy(h);
+                    throw;
+                }
+                *out = h;
+            });
+    }
+
+    int hibf_gpu_hibf_build(hibf_gpu_build_config const * cfg, char const * layout_text, hibf_gpu_input_fn input_fn,
+                            void * user, hibf_gpu_hibf ** out)
+    {
+        return guarded(
+            [&]
+            {
+                validate(cfg);
+                if (!input_fn || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument (config::input_fn is required)");
+                *out = nullptr;
+                uint64_t const nub = cfg->number_of_user_bins;
+                // Read every user bin once: its distinct values in first-appearance order (the set the reference
+                // builds with compute_kmers, src/build/compute_kmers.cpp:23-32).
+                std::vector<std::vector<uint64_t>> sets(nub);
+                std::vector<uint64_t> distinct(nub);
+                for (uint64_t u = 0; u < nub; ++u)
+                {
+                    hibf_gpu_sink sink;
+                    input_fn(user, u, &sink);
+                    std::unordered_set<uint64_t> seen;
+                    seen.reserve(sink.values.size() * 2);
+                    for (uint64_t v : sink.values)
+                        if (seen.insert(v).second)
+                            sets[u].push_back(v);
+                    distinct[u] = sets[u].size();
+                }
+                layout_t const L = parse_layout(layout_text);
+                plan_t const P0 = make_plan(*cfg, L, distinct, [](size_t) { return uint64_t{1}; });
+                // exact distinct counts of subtree unions (merged max bins), or sums for disjoint user bins
+                std::vector<uint64_t> sums;
+                if (cfg->user_bins_disjoint)
+                    sums = disjoint_unions(P0, distinct, L);
+                else
+                {
+                    sums.assign(P0.g.size(), 0);
+                    std::vector<std::vector<uint64_t>> members(P0.g.size());
+                    for (uint64_t u = 0; u < nub; ++u)
+                    {
+                        size_t n = P0.order[P0.ub_leaf[u]];
+                        while (true)
+                        {
+                            members[n].push_back(u);
+                            if (P0.g[n].parent == SIZE_MAX)
+                                break;
+                            n = P0.g[n].parent;
+                        }
+                    }
+                    for (size_t n = 0; n < P0.g.size(); ++n)
+                    {
+                        // only favourite children are sized by their union
+                        bool needed = false;
+                        if (P0.g[n].parent != SIZE_MAX)
+                        {
+                            node_t const & p = P0.g[P0.g[n].parent];
+                            needed = p.favourite >= 0 && p.children[static_cast<size_t>(p.favourite)] == n;
+                        }
+                        if (!needed)
+                            continue;
+                        std::unordered_set<uint64_t> un;
+                        for (uint64_t u : members[n])
+                            un.insert(sets[u].begin(), sets[u].end());
+                        sums[n] = un.size();
+                    }
+                }
+                plan_t const P = make_plan(*cfg, L, distinct, [&](size_t node) { return sums[node]; });
+                hibf_gpu_hibf * h = create_from_plan(P, nub);
+                try
+                {
+                    // all distinct values, concatenated, uploaded once
+                    std::vector<uint64_t> off(nub + 1, 0);
+                    for (uint64_t u = 0; u < nub; ++u)
+                        off[u + 1] = off[u] + sets[u].size();
+                    dbuf dv;
+                    dv.ensure(off[nub] * 8);
+                    for (uint64_t u = 0; u < nub; ++u)
+                        if (!sets[u].empty())
+                            HG_CUDA(cudaMemcpyAsync(dv.as<uint64_t>() + off[u], sets[u].data(), sets[u].size() * 8,
+                                                    cudaMemcpyHostToDevice, h->stream));
+                    std::vector<insert_job> jobs;
+                    for (uint64_t u = 0; u < nub; ++u)
+                    {
+                        uint64_t const n = sets[u].size();
+                        user_bin_rec const & r = P.ub_rec[u];
+                        insert_job leaf{off[u], n, 0, static_cast<uint32_t>(P.ub_leaf[u]),
+                                        static_cast<uint32_t>(r.storage)};
+                        if (r.ntb > 1)
+                            leaf.chunk = (n + r.ntb - 1) / r.ntb;
+                        jobs.push_back(leaf);
+                        for (auto const & [ibf, bin] : P.ub_merged[u])
+                            jobs.push_back(
+                                insert_job{off[u], n, 0, static_cast<uint32_t>(ibf), static_cast<uint32_t>(bin)});
+                    }
+                    run_jobs(h, jobs, 0, dv.as<uint64_t>(), h->stream);
+                }
+                catch (...)
+                {
+                    hibf_gpu_hibf_destroy(h);
+                    throw;
+                }
+                *out = h;
+            });
+    }
+
+} // extern "C"

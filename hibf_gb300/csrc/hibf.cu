@@ -27,12 +27,12 @@
 #include "common.hpp"
 #include "count.cuh"
 #include "device.cuh"
+#include "hibf_internal.cuh"
 
 namespace hibf_gb300
 {
 
 void set_last_error(std::string msg);
-int sm_count();
 
 namespace
 {
@@ -62,20 +62,6 @@ constexpr unsigned long long E_OVERFLOW_REC = 1ull;
 constexpr unsigned long long E_OVERFLOW_TASK = 2ull;
 constexpr unsigned long long E_TIMEOUT = 4ull;
 constexpr unsigned long long E_CYCLE = 8ull;
-
-struct alignas(16) dev_node
-{
-    uint64_t const * words;
-    uint64_t bin_size;
-    uint32_t bins;
-    uint32_t bin_words;
-    uint32_t row_words;
-    uint32_t hash_shift;
-    uint32_t hash_funs;
-    uint32_t desc_offset;
-    uint32_t lpv_log2;
-    uint32_t pad;
-};
 
 struct query_params
 {
@@ -595,28 +581,13 @@ unsigned grid_cap(uint64_t work, unsigned block, unsigned per_sm = 16)
 
 using namespace hibf_gb300;
 
-struct hibf_gpu_hibf
-{
-    uint64_t n_user_bins{};
-    uint64_t n_ibfs{};
-    uint32_t max_depth{};
-    uint32_t counters_per_warp{};
-    uint64_t total_bytes{};
-    std::vector<dev_node> nodes;           // host copy
-    std::vector<std::unique_ptr<dbuf>> stores;
-    std::vector<uint64_t> bins, bin_size, hash_funs, bin_words, row_words;
-    dbuf d_nodes;
-    dbuf d_descs;
-    dbuf io;
-    cudaStream_t stream{};
-    std::mutex mu;
-};
-
 struct hibf_gpu_agent
 {
     hibf_gpu_hibf * h{};
     cudaStream_t own{};
     cudaStream_t stream{};
+    cudaEvent_t ev_k0{}, ev_k1{}; // around the persistent query kernel of the last batch
+    cudaGraphExec_t graph{};      // captured launch sequence of one batch (hibf_gpu_agent_capture_batch_d)
     int status{HIBF_GPU_OK};
     uint64_t last_tasks{}, last_visits{};
     uint64_t cap_queries{}, cap_tasks{}, cap_results{};
@@ -756,8 +727,10 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         uint64_t const full = static_cast<uint64_t>(sm_count()) * static_cast<uint64_t>(a->max_blocks_per_sm);
         uint64_t const want = (nq + 7) / 8;
         unsigned const grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min(full, want)));
+        HG_CUDA(cudaEventRecord(a->ev_k0, s));
         k_query<<<grid, 256, query_smem(h), s>>>(p);
         HG_CUDA(cudaGetLastError());
+        HG_CUDA(cudaEventRecord(a->ev_k1, s));
     }
     launch_postprocess(a, nq, mode, width);
 }
@@ -987,6 +960,8 @@ extern "C"
                 {
                     h->n_user_bins = n_user_bins;
                     h->n_ibfs = n_ibfs;
+                    h->next_ibf_id.assign(next_ibf_id, next_ibf_id + off[n_ibfs]);
+                    h->user_bin_id.assign(user_bin_id, user_bin_id + off[n_ibfs]);
                     h->max_depth = max_depth;
                     HG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
                     uint32_t cpw = 64;
@@ -1068,6 +1043,27 @@ extern "C"
                 out[1] = h->n_ibfs;
                 out[2] = h->max_depth;
                 out[3] = h->total_bytes;
+            });
+    }
+
+    int hibf_gpu_hibf_get_tables(hibf_gpu_hibf const * h, uint64_t * bins, uint64_t * bin_sizes, uint64_t * hash_funs,
+                                 uint64_t * next_ibf_id, uint64_t * user_bin_id)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (bins)
+                    std::copy(h->bins.begin(), h->bins.end(), bins);
+                if (bin_sizes)
+                    std::copy(h->bin_size.begin(), h->bin_size.end(), bin_sizes);
+                if (hash_funs)
+                    std::copy(h->hash_funs.begin(), h->hash_funs.end(), hash_funs);
+                if (next_ibf_id)
+                    std::copy(h->next_ibf_id.begin(), h->next_ibf_id.end(), next_ibf_id);
+                if (user_bin_id)
+                    std::copy(h->user_bin_id.begin(), h->user_bin_id.end(), user_bin_id);
             });
     }
 
@@ -1177,6 +1173,8 @@ extern "C"
                     a->h = h;
                     HG_CUDA(cudaStreamCreateWithFlags(&a->own, cudaStreamNonBlocking));
                     a->stream = a->own;
+                    HG_CUDA(cudaEventCreate(&a->ev_k0));
+                    HG_CUDA(cudaEventCreate(&a->ev_k1));
                     a->ctrl.ensure(C_WORDS * 8);
                     a->stats.ensure(2 * 8);
                     a->h_ctrl.ensure(C_WORDS * 8);
@@ -1205,6 +1203,10 @@ extern "C"
                 if (!a)
                     return;
                 cudaStreamSynchronize(a->stream);
+                if (a->graph)
+                    cudaGraphExecDestroy(a->graph);
+                cudaEventDestroy(a->ev_k0);
+                cudaEventDestroy(a->ev_k1);
                 cudaStreamDestroy(a->own);
                 delete a;
             });
@@ -1381,6 +1383,70 @@ extern "C"
                 *result_ids = a->h_ids.as<uint64_t>();
                 if (result_counts)
                     *result_counts = mode == HIBF_GPU_QUERY_COUNT ? a->h_cnt.p : nullptr;
+            });
+    }
+
+    int hibf_gpu_agent_capture_batch_d(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
+                                       uint64_t const * d_query_offsets, uint64_t n_queries,
+                                       uint64_t const * d_thresholds, int width)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !d_query_offsets || (n_queries && (!d_thresholds || !d_values)))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (n_queries >= 0xFFFFFFFFull)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "at most 2^32 - 1 queries per batch");
+                check_mode(mode, width, nullptr, 0);
+                ensure_capacity(a, std::max<uint64_t>(n_queries, 1), std::max<uint64_t>(a->cap_tasks, 1024),
+                                std::max<uint64_t>(a->cap_results, 1024));
+                HG_CUDA(cudaStreamSynchronize(a->stream));
+                if (a->graph)
+                {
+                    HG_CUDA(cudaGraphExecDestroy(a->graph));
+                    a->graph = nullptr;
+                }
+                (void)sm_count();
+                cudaGraph_t g = nullptr;
+                HG_CUDA(cudaStreamBeginCapture(a->stream, cudaStreamCaptureModeThreadLocal));
+                try
+                {
+                    launch_batch(a, mode, d_values, d_query_offsets, d_thresholds, n_queries, width);
+                }
+                catch (...)
+                {
+                    cudaStreamEndCapture(a->stream, &g);
+                    if (g)
+                        cudaGraphDestroy(g);
+                    throw;
+                }
+                HG_CUDA(cudaStreamEndCapture(a->stream, &g));
+                cudaError_t const e = cudaGraphInstantiate(&a->graph, g, 0);
+                cudaGraphDestroy(g);
+                HG_CUDA(e);
+            });
+    }
+
+    int hibf_gpu_agent_replay(hibf_gpu_agent * a)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !a->graph)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "no captured batch");
+                HG_CUDA(cudaGraphLaunch(a->graph, a->stream));
+            });
+    }
+
+    int hibf_gpu_agent_kernel_ms(hibf_gpu_agent * a, float * ms)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !ms)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                HG_CUDA(cudaEventSynchronize(a->ev_k1));
+                HG_CUDA(cudaEventElapsedTime(ms, a->ev_k0, a->ev_k1));
             });
     }
 

@@ -1,0 +1,52 @@
+// hibf_internal.cuh -- the HIBF object shared by the query (hibf.cu) and build (build.cu) translation units.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "common.hpp"
+
+namespace hibf_gb300
+{
+
+// One IBF of the hierarchy as the query kernel sees it.
+struct alignas(16) dev_node
+{
+    uint64_t const * words;
+    uint64_t bin_size;
+    uint32_t bins;
+    uint32_t bin_words;
+    uint32_t row_words;
+    uint32_t hash_shift;
+    uint32_t hash_funs;
+    uint32_t desc_offset;
+    uint32_t lpv_log2;
+    uint32_t pad;
+};
+
+
+int sm_count();
+
+} // namespace hibf_gb300
+
+struct hibf_gpu_hibf
+{
+    uint64_t n_user_bins{};
+    uint64_t n_ibfs{};
+    uint32_t max_depth{};
+    uint32_t counters_per_warp{};
+    uint64_t total_bytes{};
+    std::vector<hibf_gb300::dev_node> nodes;           // host copy
+    std::vector<std::unique_ptr<hibf_gb300::dbuf>> stores;
+    std::vector<uint64_t> bins, bin_size, hash_funs, bin_words, row_words;
+    hibf_gb300::dbuf d_nodes;
+    hibf_gb300::dbuf d_descs;
+    hibf_gb300::dbuf io;
+    // the tables as given (reference conventions), for hibf_gpu_hibf_get_tables
+    std::vector<uint64_t> next_ibf_id, user_bin_id;
+    cudaStream_t stream{};
+    std::mutex mu;
+};
+

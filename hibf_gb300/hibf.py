@@ -203,6 +203,21 @@ class _agent_base:
                width, ctypes.byref(ro), ctypes.byref(ri), ctypes.byref(rc))
         return (ctypes.cast(ro, ctypes.c_void_p).value, ctypes.cast(ri, ctypes.c_void_p).value, rc.value)
 
+    def capture_batch_device(self, d_values: int, d_query_offsets: int, n_queries: int, d_thresholds: int,
+                             mode=N.QUERY_MEMBERSHIP, width=2) -> None:
+        """Captures one batch on fixed device buffers into a CUDA graph; replay() launches it."""
+        N.call("hibf_gpu_agent_capture_batch_d", self._a, mode, d_values, d_query_offsets, n_queries, d_thresholds,
+               width)
+
+    def replay(self) -> None:
+        N.call("hibf_gpu_agent_replay", self._a)
+
+    def kernel_ms(self) -> float:
+        """Device time of the persistent query kernel of the last batch."""
+        ms = ctypes.c_float(0)
+        N.call("hibf_gpu_agent_kernel_ms", self._a, ctypes.byref(ms))
+        return float(ms.value)
+
     def fetch_results(self, n_queries: int, mode=N.QUERY_MEMBERSHIP, width=2):
         """Host copies (offsets, ids, counts) of the last device batch (query_batch_device / query_plain_device)."""
         ro, ri, rc = N.u64p(), N.u64p(), ctypes.c_void_p()

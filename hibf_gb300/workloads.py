@@ -1,0 +1,82 @@
+"""The benchmark workloads, by what they are (seeded synthetic data, see include/hibf_gb300_synthetic.h).
+
+hibf64     64 user bins, sizes log-uniform in [1e3, 1e5], h=2, fpr 0.05, tmax 64; 10,000 queries of 250 values, half
+           from one user bin, half uniform; threshold 125.
+hibf8192   8,192 user bins, sizes log-normal (median 2e5, sigma 1.5) clipped to [1e3, 5e7], h=2, fpr 0.05, tmax 64,
+           layout from the reference's DP over HyperLogLog sketches (sketch_bits 12); 1,000,000 queries of length
+           U[20, 2000], 70% drawn from 1-3 user bins with 2% noise, 30% uniform; threshold ceil(0.7 * length).
+
+Layouts were computed by the reference (tests/golden/make_golden.py) and are read from tests/golden.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import _native as N
+from . import synthetic as S
+
+GOLDEN = Path(__file__).resolve().parents[1] / "tests" / "golden"
+
+
+@dataclass
+class workload:
+    name: str
+    n_user_bins: int
+    size_law: int
+    size_p0: float
+    size_p1: float
+    size_lo: int
+    size_hi: int
+    h: int
+    fpr: float
+    tmax: int
+    n_queries: int
+    query: S.query_spec
+    layout_file: str | None
+
+    def user_bin_offsets(self) -> np.ndarray:
+        off = np.zeros(self.n_user_bins + 1, np.uint64)
+        N.call("hibf_gpu_synth_user_bin_offsets", self.query.seed, self.size_law, self.size_p0, self.size_p1,
+               self.size_lo, self.size_hi, self.n_user_bins, off.ctypes.data)
+        return off
+
+    def layout_text(self) -> str:
+        if self.layout_file is None:
+            raise FileNotFoundError(f"{self.name}: no layout file")
+        p = GOLDEN / self.layout_file
+        if p.suffix == ".npz":
+            return bytes(np.load(p)["layout"]).decode()
+        return p.read_text()
+
+    def query_offsets(self, first: int, n: int):
+        q = self.query
+        qo = np.zeros(n + 1, np.uint64)
+        thr = np.zeros(n, np.uint64)
+        N.call("hibf_gpu_synth_query_offsets", q.seed, q.law, q.len_lo, q.len_hi, q.mix_pct, q.noise_pct, q.thr_num,
+               q.thr_den, q.n_user_bins, first, n, qo.ctypes.data, thr.ctypes.data)
+        return qo, thr
+
+    def queries_device(self, d_ub_offsets: int, first: int, n: int, d_qoff: int, d_values: int, stream=None):
+        q = self.query
+        N.call("hibf_gpu_synth_queries_d", q.seed, q.law, q.len_lo, q.len_hi, q.mix_pct, q.noise_pct, q.thr_num,
+               q.thr_den, q.n_user_bins, d_ub_offsets, first, n, d_qoff, d_values, stream)
+
+    def queries_host(self, ub_offsets: np.ndarray, first: int, n: int, qoff: np.ndarray) -> np.ndarray:
+        q = self.query
+        vals = np.zeros(int(qoff[-1]), np.uint64)
+        N.call("hibf_gpu_synth_queries", q.seed, q.law, q.len_lo, q.len_hi, q.mix_pct, q.noise_pct, q.thr_num,
+               q.thr_den, q.n_user_bins, ub_offsets.ctypes.data, first, n, qoff.ctypes.data, vals.ctypes.data)
+        return vals
+
+
+HIBF64 = workload("hibf64", 64, S.SIZES_LOG_UNIFORM, 0.0, 0.0, 1000, 100000, 2, 0.05, 64, 10000,
+                  S.query_spec(1, S.QUERIES_HALF_ONE_BIN, 250, 250, 0, 0, 1, 2, 64), "c1_reference.npz")
+HIBF8192 = workload("hibf8192", 8192, S.SIZES_LOG_NORMAL, 200000.0, 1.5, 1000, 50000000, 2, 0.05, 64, 1000000,
+                    S.query_spec(1, S.QUERIES_MIXED, 20, 2000, 70, 2, 7, 10, 8192), "c3_layout.txt")
+
+WORKLOADS = {w.name: w for w in (HIBF64, HIBF8192)}

@@ -139,9 +139,49 @@ int hibf_gpu_hibf_ibf_info(hibf_gpu_hibf const * h, uint64_t ibf, uint64_t out[5
 int hibf_gpu_hibf_emplace(hibf_gpu_hibf * h, uint64_t ibf, uint64_t const * values, uint64_t n, uint64_t bin);
 int hibf_gpu_hibf_emplace_d(hibf_gpu_hibf * h, uint64_t ibf, uint64_t const * d_values, uint64_t const * d_bins,
                             uint64_t n, uint64_t bin, void * stream);
+/* The tables as given at creation (reference conventions): bins / bin_sizes / hash_funs have n_ibfs entries,
+ * next_ibf_id / user_bin_id sum(bins) entries.  Any pointer may be NULL. */
+int hibf_gpu_hibf_get_tables(hibf_gpu_hibf const * h, uint64_t * bins, uint64_t * bin_sizes, uint64_t * hash_funs,
+                             uint64_t * next_ibf_id, uint64_t * user_bin_id);
 /* Words of IBF `ibf` in the reference's bit_vector layout (for serialization or a host-built HIBF). */
 int hibf_gpu_hibf_upload_words(hibf_gpu_hibf * h, uint64_t ibf, uint64_t const * words, uint64_t n_words);
 int hibf_gpu_hibf_download_words(hibf_gpu_hibf * h, uint64_t ibf, uint64_t * words, uint64_t n_words);
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* Build from a layout (hierarchical_interleaved_bloom_filter(config&, layout::layout const&),                   */
+/* hierarchical_interleaved_bloom_filter.hpp:205; src/hierarchical_interleaved_bloom_filter.cpp:40-253).         */
+/* The host parses the layout file text (src/layout/layout.cpp:60-145), builds the IBF graph                      */
+/* (src/layout/graph.cpp:19-125), sizes every IBF like construct_ibf (src/build/construct_ibf.cpp:26-64) and      */
+/* fills the tables; every insert runs on the device.  IBFs are numbered depth-first in layout order.              */
+/* ------------------------------------------------------------------------------------------------------------ */
+typedef struct hibf_gpu_build_config
+{
+    uint64_t number_of_user_bins;      /* config::number_of_user_bins      */
+    uint64_t number_of_hash_functions; /* config::number_of_hash_functions */
+    double maximum_fpr;                /* config::maximum_fpr              */
+    double relaxed_fpr;                /* config::relaxed_fpr              */
+    uint64_t threads;                  /* config::threads (host work)      */
+    int user_bins_disjoint;            /* user bins share no value: unions are sized by sums, no host set union */
+} hibf_gpu_build_config;
+
+/* config::input_fn (config.hpp:111): for user bin `user_bin` the callback pushes its values into the sink,
+ * the insert_iterator of the reference (include/hibf/misc/insert_iterator.hpp:24-111). */
+typedef struct hibf_gpu_sink hibf_gpu_sink;
+typedef void (*hibf_gpu_input_fn)(void * user, uint64_t user_bin, hibf_gpu_sink * sink);
+int hibf_gpu_sink_push(hibf_gpu_sink * sink, uint64_t const * values, uint64_t n);
+
+int hibf_gpu_hibf_build(hibf_gpu_build_config const * cfg, char const * layout_text, hibf_gpu_input_fn input_fn,
+                        void * user, hibf_gpu_hibf ** out);
+/* The same build for the seeded synthetic workloads of include/hibf_gb300_synthetic.h: user bin u holds stream
+ * positions [user_bin_offsets[u], user_bin_offsets[u+1]) of the splitmix64 stream `seed`, generated on the device. */
+int hibf_gpu_hibf_build_synthetic(hibf_gpu_build_config const * cfg, char const * layout_text, uint64_t seed,
+                                  uint64_t const * user_bin_offsets, hibf_gpu_hibf ** out);
+/* Host-only planning for pairwise disjoint user bins of the given distinct sizes: the IBF count and total bins
+ * (first call with NULL arrays), then sizes, tables and each IBF's parent (IBF, bin).  No device needed. */
+int hibf_gpu_plan_disjoint(hibf_gpu_build_config const * cfg, char const * layout_text,
+                           uint64_t const * user_bin_sizes, uint64_t * n_ibfs, uint64_t * total_bins, uint64_t * bins,
+                           uint64_t * bin_sizes, uint64_t * next_ibf_id, uint64_t * user_bin_id,
+                           uint64_t * parent_ibf, uint64_t * parent_bin);
 
 /* ------------------------------------------------------------------------------------------------------------ */
 /* Agents (hierarchical_interleaved_bloom_filter.hpp:241-247).  An agent owns its device workspace, result       */
@@ -194,9 +234,38 @@ int hibf_gpu_agent_fetch_results(hibf_gpu_agent * a, uint64_t n_queries, int mod
                                  uint64_t const ** result_offsets, uint64_t const ** result_ids,
                                  void const ** result_counts);
 int hibf_gpu_agent_status(hibf_gpu_agent * a);
+/* Captures one batch's launch sequence (control reset, persistent kernel, compaction) on fixed device buffers into
+ * a CUDA graph owned by the agent; hibf_gpu_agent_replay launches it on the agent's stream. */
+int hibf_gpu_agent_capture_batch_d(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
+                                   uint64_t const * d_query_offsets, uint64_t n_queries, uint64_t const * d_thresholds,
+                                   int width);
+int hibf_gpu_agent_replay(hibf_gpu_agent * a);
+/* Device time of the persistent query kernel of the agent's last batch (CUDA events on the agent's stream). */
+int hibf_gpu_agent_kernel_ms(hibf_gpu_agent * a, float * ms);
 /* Number of (query, IBF) tasks the last batch processed and the number of query values they covered
  * (sum over tasks of the query length): the work the roofline is computed from. */
 int hibf_gpu_agent_last_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits);
+
+/* ============================================================================================================ */
+/* Seeded synthetic workloads (include/hibf_gb300_synthetic.h), for benchmarks and tests                        */
+/* ============================================================================================================ */
+/* offsets[0..n_user_bins]: prefix sums of the user bin sizes (law: HG_SIZES_LOG_UNIFORM / _LOG_NORMAL). */
+int hibf_gpu_synth_user_bin_offsets(uint64_t seed, int law, double p0, double p1, uint64_t lo, uint64_t hi,
+                                    uint64_t n_user_bins, uint64_t * offsets);
+/* query_offsets[0..n_queries] and thresholds[0..n_queries) of queries first_query .. first_query+n_queries-1. */
+int hibf_gpu_synth_query_offsets(uint64_t seed, int law, uint64_t len_lo, uint64_t len_hi, uint32_t mix_pct,
+                                 uint32_t noise_pct, uint32_t thr_num, uint32_t thr_den, uint64_t n_user_bins,
+                                 uint64_t first_query, uint64_t n_queries, uint64_t * query_offsets,
+                                 uint64_t * thresholds);
+/* Query values on the host, or on the device (one thread per query). */
+int hibf_gpu_synth_queries(uint64_t seed, int law, uint64_t len_lo, uint64_t len_hi, uint32_t mix_pct,
+                           uint32_t noise_pct, uint32_t thr_num, uint32_t thr_den, uint64_t n_user_bins,
+                           uint64_t const * user_bin_offsets, uint64_t first_query, uint64_t n_queries,
+                           uint64_t const * query_offsets, uint64_t * values);
+int hibf_gpu_synth_queries_d(uint64_t seed, int law, uint64_t len_lo, uint64_t len_hi, uint32_t mix_pct,
+                             uint32_t noise_pct, uint32_t thr_num, uint32_t thr_den, uint64_t n_user_bins,
+                             uint64_t const * d_user_bin_offsets, uint64_t first_query, uint64_t n_queries,
+                             uint64_t const * d_query_offsets, uint64_t * d_values, void * stream);
 
 #ifdef __cplusplus
 }

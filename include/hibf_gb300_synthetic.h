@@ -98,7 +98,6 @@ enum hg_query_law
     HG_QUERIES_MIXED = 1
 };
 
-#if !defined(__CUDA_ARCH__)
 /* Host only (libm).  Size of user bin i. */
 static inline uint64_t hg_user_bin_size(uint64_t seed, int law, double p0, double p1, uint64_t lo, uint64_t hi,
                                         uint64_t i)
@@ -124,7 +123,6 @@ static inline uint64_t hg_user_bin_size(uint64_t seed, int law, double p0, doubl
         n = (double)hi;
     return (uint64_t)n;
 }
-#endif
 
 /* Query parameters. */
 typedef struct hg_query_spec

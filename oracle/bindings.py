@@ -206,6 +206,11 @@ class OracleHIBF:
         assert w.size == n, (w.size, n)
         ctypes.memmove(self.L.orc_ibf_data(p), w.ctypes.data, n * 8)
 
+    def data_ptr(self, k) -> tuple[int, int]:
+        """(address, word count) of IBF k's bit store, for filling it in place."""
+        p = self._ibf_ptr(k)
+        return ctypes.cast(self.L.orc_ibf_data(p), ctypes.c_void_p).value, int(self.L.orc_ibf_nwords(p))
+
     def words(self, k) -> np.ndarray:
         p = self._ibf_ptr(k)
         n = self.L.orc_ibf_nwords(p)

@@ -1,0 +1,105 @@
+"""GPU build from a layout (hibf_gpu_hibf_build / _build_synthetic) against the reference's own builds.
+
+For the layouts the reference computed (tests/golden), the device build must reproduce, for every IBF matched by its
+path of merged bins: the bin count, bin size and bin-to-user-bin table, and -- for IBFs that store no split user
+bin -- the exact bit words (digest).  IBFs with split user bins differ from the reference only in which split bin a
+value lands in (stream order vs the reference's hash-set order); for them every inserted value must be found in its
+user bin's bins, and query results are checked against the C oracle run on the downloaded bits.
+"""
+
+import numpy as np
+import pytest
+
+import hibf_gb300 as hg
+from hibf_gb300 import build as B
+from hibf_gb300 import synthetic as S
+from tests import golden_io as G
+from tests.hibf_canon import canonical, split_free
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(d, input_fn=None):
+    h, tmax, sketch = (int(x) for x in d["config"])
+    fpr, rfpr, alpha, ratio = (float(x) for x in d["fpr"])
+    return B.config(input_fn=input_fn, number_of_user_bins=d["n_ub"], number_of_hash_functions=h, maximum_fpr=fpr,
+                    relaxed_fpr=rfpr)
+
+
+def _compare_with_reference(H, d):
+    ref_t = G.tables(d)
+    ref = canonical(ref_t)
+    got = canonical(H.tables())
+    assert set(ref) == set(got)
+    n_exact = 0
+    for path, (bins, size, row, k_ref) in ref.items():
+        gb, gs, grow, k_got = got[path]
+        assert (bins, size, row) == (gb, gs, grow), path
+        if split_free(ref_t, k_ref):
+            assert S.digest(H.words(k_got).tolist()) == int(d["digests"][k_ref]), path
+            n_exact += 1
+    return n_exact
+
+
+def _queries_vs_oracle(H, oracle, d):
+    t = H.tables()
+    t["words"] = [H.words(k) for k in range(H.n_ibfs)]
+    O = oracle.hibf(t)
+    qv, qo = d["q_values"], d["q_offsets"]
+    offs, ids, _ = H.membership_agent().query_batch(qv, qo, d["mem_t"])
+    o_off, o_ids = O.membership_batch(qv, qo, d["mem_t"], threads=4)
+    np.testing.assert_array_equal(offs, o_off)
+    np.testing.assert_array_equal(ids, o_ids)
+
+
+@pytest.mark.parametrize("name", ["synth64", "synth600"])
+def test_build_synthetic_matches_reference(gpu_lib, oracle, name):
+    d = G.hibf_case(name)
+    seed = int(d["synthetic_seed"][0])
+    H = B.build_synthetic(_cfg(d), d["layout_text"], seed, d["ub_offsets"])
+    _compare_with_reference(H, d)
+    _queries_vs_oracle(H, oracle, d)
+    # no false negatives: every value of every user bin is counted in its user bin
+    offs = d["ub_offsets"]
+    ca = H.counting_agent(4)
+    for ub in range(0, d["n_ub"], max(1, d["n_ub"] // 20)):
+        v = S.user_bin_values(seed, offs, ub)
+        assert int(ca.bulk_count(v, 1)[ub]) >= v.size
+
+
+@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "similar", "same"])
+def test_build_input_fn_matches_reference(gpu_lib, oracle, name):
+    d = G.hibf_case(name)
+    vals, offs = d["ub_values"], d["ub_offsets"]
+
+    def input_fn(ub, it):
+        it.push(vals[offs[ub]:offs[ub + 1]])
+
+    H = hg.hierarchical_interleaved_bloom_filter(_cfg(d, input_fn), d["layout_text"])
+    n_exact = _compare_with_reference(H, d)
+    assert n_exact >= 1
+    _queries_vs_oracle(H, oracle, d)
+
+
+def test_build_matches_reference_unit_expectations(gpu_lib):
+    # hierarchical_interleaved_bloom_filter_test.cpp:112 three_level_hibf, built here from the reference's layout
+    d = G.hibf_case("three_level")
+    vals, offs = d["ub_values"], d["ub_offsets"]
+    H = hg.hierarchical_interleaved_bloom_filter(
+        _cfg(d, lambda ub, it: it.push(vals[offs[ub]:offs[ub + 1]])), d["layout_text"])
+    a = H.membership_agent()
+    for ub in range(0, 4096, 100):
+        s = ub * 16
+        a.membership_for(np.arange(s + 16, s + 20), 4)
+        assert a.sort_results().tolist() == [ub, ub + 1]
+        assert a.membership_for(np.arange(s + 5, s + 9), 4).tolist() == [ub]
+
+
+def test_build_c1_structure(gpu_lib):
+    """The 64-user-bin workload built from the reference's layout: same IBF sizes and tables as the reference."""
+    z = np.load(G.GOLDEN / "c1_reference.npz")
+    cfg = B.config(number_of_user_bins=64, number_of_hash_functions=2, maximum_fpr=0.05)
+    H = B.build_synthetic(cfg, bytes(z["layout"]).decode(), 1, z["ub_offsets"])
+    ref = canonical(dict(bins=z["bins"], bin_size=z["bin_size"], next_ibf=z["next_ibf"], user_bin=z["user_bin"]))
+    got = canonical(H.tables())
+    assert {p: v[:3] for p, v in ref.items()} == {p: v[:3] for p, v in got.items()}

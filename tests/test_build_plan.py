@@ -1,0 +1,77 @@
+"""The host part of the build (layout parsing, IBF graph, sizing, tables) against the reference's own builds.
+
+CPU only: hibf_gpu_plan_disjoint computes sizes and tables without a device.  For the synthetic workloads (pairwise
+disjoint user bins) every IBF -- matched by its path of merged bins -- must have the reference's bin count, bin size
+and bin-to-user-bin table, given the layout the reference computed."""
+
+import numpy as np
+import pytest
+
+from hibf_gb300 import build as B
+from hibf_gb300 import synthetic as S
+from tests import golden_io as G
+from tests.hibf_canon import canonical
+
+
+def _cfg(d):
+    h, tmax, sketch = (int(x) for x in d["config"])
+    fpr, rfpr, alpha, ratio = (float(x) for x in d["fpr"])
+    return B.config(number_of_user_bins=d["n_ub"], number_of_hash_functions=h, maximum_fpr=fpr, relaxed_fpr=rfpr)
+
+
+@pytest.mark.parametrize("name", ["synth64", "synth600"])
+def test_plan_matches_reference_tables(name):
+    d = G.hibf_case(name)
+    sizes = np.diff(d["ub_offsets"].astype(np.int64)).astype(np.uint64)
+    plan = B.plan_disjoint(_cfg(d), d["layout_text"], sizes)
+    ref = canonical(G.tables(d))
+    got = canonical(plan)
+    assert set(ref) == set(got)
+    for path in ref:
+        assert ref[path][:3] == got[path][:3], path
+
+
+def test_plan_c1_matches_reference():
+    z = np.load(G.GOLDEN / "c1_reference.npz")
+    sizes = np.diff(z["ub_offsets"].astype(np.int64)).astype(np.uint64)
+    cfg = B.config(number_of_user_bins=64, number_of_hash_functions=2, maximum_fpr=0.05)
+    plan = B.plan_disjoint(cfg, bytes(z["layout"]).decode(), sizes)
+    ref = canonical(dict(bins=z["bins"], bin_size=z["bin_size"], next_ibf=z["next_ibf"], user_bin=z["user_bin"]))
+    got = canonical(plan)
+    assert {p: v[:3] for p, v in ref.items()} == {p: v[:3] for p, v in got.items()}
+
+
+def test_plan_c3_layout():
+    """The 8,192-user-bin layout: 606 IBFs over three levels, every user bin placed once."""
+    text = (G.GOLDEN / "c3_layout.txt").read_text()
+    sizes = S.user_bin_sizes(1, 8192, S.SIZES_LOG_NORMAL, 200000.0, 1.5, 1000, 50000000)
+    plan = B.plan_disjoint(B.config(number_of_user_bins=8192), text, sizes)
+    assert plan["bins"].size == 606
+    ub = plan["user_bin"]
+    ids = np.unique(ub[ub < np.uint64(8192)])
+    assert ids.size == 8192
+    assert int(plan["bins"][0]) == 64
+
+
+def test_layout_errors():
+    with pytest.raises(B.N.InvalidArgument):
+        B.plan_disjoint(B.config(number_of_user_bins=2), "no header\n", [1, 1])
+    with pytest.raises(B.N.InvalidArgument):
+        B.plan_disjoint(B.config(number_of_user_bins=2, maximum_fpr=1.5), "#TOP_LEVEL_IBF fullest_technical_bin_idx:0\n", [1, 1])
+
+
+def test_config_validation_mirrors_reference():
+    c = B.config(input_fn=lambda u, it: None, number_of_user_bins=100)
+    c.validate_and_set_defaults()
+    assert c.tmax == 64
+    c = B.config(input_fn=lambda u, it: None, number_of_user_bins=10, tmax=65)
+    c.validate_and_set_defaults()
+    assert c.tmax == 128 and c.warnings
+    for bad in (dict(number_of_user_bins=0), dict(number_of_user_bins=2, number_of_hash_functions=6),
+                dict(number_of_user_bins=2, maximum_fpr=0.0), dict(number_of_user_bins=2, relaxed_fpr=0.01),
+                dict(number_of_user_bins=2, threads=0), dict(number_of_user_bins=2, sketch_bits=4),
+                dict(number_of_user_bins=2, alpha=-1.0), dict(number_of_user_bins=2, empty_bin_fraction=1.0)):
+        with pytest.raises(ValueError):
+            B.config(input_fn=lambda u, it: None, **bad).validate_and_set_defaults()
+    with pytest.raises(ValueError):
+        B.config(number_of_user_bins=2).validate_and_set_defaults()
