@@ -727,10 +727,15 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         uint64_t const full = static_cast<uint64_t>(sm_count()) * static_cast<uint64_t>(a->max_blocks_per_sm);
         uint64_t const want = (nq + 7) / 8;
         unsigned const grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min(full, want)));
-        HG_CUDA(cudaEventRecord(a->ev_k0, s));
+        // inside a stream capture an event record only orders work unless it is marked external; external records
+        // become event-record nodes of the graph, so replays time the kernel too
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        HG_CUDA(cudaStreamIsCapturing(s, &cap));
+        unsigned const rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
+        HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
         k_query<<<grid, 256, query_smem(h), s>>>(p);
         HG_CUDA(cudaGetLastError());
-        HG_CUDA(cudaEventRecord(a->ev_k1, s));
+        HG_CUDA(cudaEventRecordWithFlags(a->ev_k1, s, rec_flags));
     }
     launch_postprocess(a, nq, mode, width);
 }
