@@ -77,6 +77,7 @@ _SIGS = [
     ("hibf_gpu_ibf_bulk_contains_d", None, [vp, vp, u64, vp, vp]),
     ("hibf_gpu_ibf_bulk_count", None, [vp, vp, u64, ci, vp]),
     ("hibf_gpu_ibf_bulk_count_d", None, [vp, vp, u64, ci, vp, vp]),
+    ("hibf_gpu_ibf_bulk_count_noalloc_d", None, [vp, vp, u64, ci, vp, vp]),
     ("hibf_gpu_ibf_membership_for", None, [vp, vp, u64, ctypes.c_uint16, vp, u64p]),
     ("hibf_gpu_ibf_upload_words", None, [vp, vp, u64]),
     ("hibf_gpu_ibf_download_words", None, [vp, vp, u64]),

@@ -323,6 +323,35 @@ int width_ok(int width)
     return width == 1 || width == 2 || width == 4 || width == 8;
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// bulk_count without allocation.  The 64-bit per-bin totals that bulk_count accumulates live in this fixed array
+// instead of a cudaMalloc'd buffer.  Every device that loads the library holds it (128 KiB) until the process exits.
+// ---------------------------------------------------------------------------------------------------------------
+constexpr uint64_t kNoAllocMaxCounters = HIBF_GPU_NOALLOC_MAX_BINS;
+static __device__ __align__(256) unsigned long long g_noalloc_totals[kNoAllocMaxCounters];
+
+// Device address of g_noalloc_totals per device.  In host code the array's name is only a host-side stand-in, so
+// the address is looked up once per device (cudaGetSymbolAddress, with that device current) and cached.
+constexpr int kMaxDevices = 256;
+std::mutex g_noalloc_mu;
+unsigned long long * g_noalloc_addr[kMaxDevices] = {};
+
+unsigned long long * noalloc_totals()
+{
+    int dev = 0;
+    HG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev])
+    {
+        void * p = nullptr;
+        HG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_totals));
+        g_noalloc_addr[dev] = static_cast<unsigned long long *>(p);
+    }
+    return g_noalloc_addr[dev];
+}
+
 } // namespace
 
 extern "C"
@@ -743,6 +772,48 @@ extern "C"
             return HIBF_GPU_ERR_INVALID_ARG;
         }
         return f->status;
+    }
+
+    // Same result as hibf_gpu_ibf_bulk_count_d, for callers that cannot allocate device memory.  The counting
+    // scratch is the static array above: this call makes no cudaMalloc, cudaFree or other allocating call.  The first
+    // call on a device looks up the array's device address (issue it before any stream capture); calls that overlap
+    // on the GPU share the array and race; the totals are cleared at the start of every call.
+    int hibf_gpu_ibf_bulk_count_noalloc_d(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int width,
+                                          void * d_out, void * stream)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || (n && !d_values) || !d_out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (!width_ok(width))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "width must be 1, 2, 4 or 8");
+                uint64_t const nc = 64u * (f->bin_words <= 32 ? (1u << f->lpv_log2()) : f->bin_words);
+                if (nc > kNoAllocMaxCounters)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "hibf_gpu_ibf_bulk_count_noalloc_d supports at most " +
+                                                       std::to_string(kNoAllocMaxCounters) +
+                                                       " bins; use hibf_gpu_ibf_bulk_count_d");
+                cudaStream_t const s = pick(f, stream);
+                unsigned long long * totals = noalloc_totals();
+                HG_CUDA(cudaMemsetAsync(totals, 0, nc * sizeof(unsigned long long), s));
+                if (n)
+                {
+                    unsigned const block = 256;
+                    uint64_t const chunk = 2048;
+                    uint64_t const warps = (n + chunk - 1) / chunk;
+                    unsigned const grid = static_cast<unsigned>(std::max<uint64_t>(
+                        1, std::min<uint64_t>((warps + 7) / 8, static_cast<uint64_t>(sm_count()) * 4u)));
+                    size_t const smem = nc * sizeof(uint32_t);
+                    if (smem > 48 * 1024)
+                        HG_CUDA(cudaFuncSetAttribute(k_bulk_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     static_cast<int>(smem)));
+                    k_bulk_count<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk, totals,
+                                                           static_cast<uint32_t>(nc));
+                    HG_CUDA(cudaGetLastError());
+                }
+                k_store_counts<<<grid_for(f->bins, 256), 256, 0, s>>>(totals, f->bins, width, d_out);
+                HG_CUDA(cudaGetLastError());
+            });
     }
 
 } // extern "C"

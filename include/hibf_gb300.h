@@ -100,6 +100,17 @@ int hibf_gpu_ibf_bulk_count(hibf_gpu_ibf * ibf, uint64_t const * values, uint64_
 int hibf_gpu_ibf_bulk_count_d(hibf_gpu_ibf * ibf, uint64_t const * d_values, uint64_t n, int width, void * d_out,
                               void * stream);
 
+/* No counterpart in the reference.  hibf_gpu_ibf_bulk_count_d for callers that cannot allocate device memory:
+ * a process whose device memory is all held by its own pool (a framework's caching allocator), or a loop where
+ * cudaMalloc's implicit device-wide synchronisation is not acceptable.  The counting scratch is a fixed static
+ * device array of HIBF_GPU_NOALLOC_MAX_BINS 64-bit totals (128 KiB, held by every device that loads the library
+ * until exit); filters with more bins are rejected with HIBF_GPU_ERR_INVALID_ARG.  The call allocates nothing.
+ * Its first call on a device looks the array's address up (make that call before any stream capture).  All calls
+ * share the array: calls that overlap on the GPU race; each call clears the totals it uses first. */
+#define HIBF_GPU_NOALLOC_MAX_BINS 16384
+int hibf_gpu_ibf_bulk_count_noalloc_d(hibf_gpu_ibf * ibf, uint64_t const * d_values, uint64_t n, int width,
+                                      void * d_out, void * stream);
+
 /* membership_agent_type::membership_for (include/hibf/interleaved_bloom_filter.hpp:744-764): ascending bin ids whose
  * uint16 count reaches `threshold`.  out_ids needs room for `bins` ids; *n_out receives the count. */
 int hibf_gpu_ibf_membership_for(hibf_gpu_ibf * ibf, uint64_t const * values, uint64_t n, uint16_t threshold,
