@@ -52,6 +52,10 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end measurement (0: --steps)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--l2-fetch", type=int, default=-1,
+                    help="set the context's L2 fetch granularity hint (bytes) before the run; -1 leaves it")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="scale every user bin's size (same layout); < 1 gives a smaller index for profiling")
     return ap.parse_args()
 
 
@@ -129,10 +133,14 @@ def dist_env():
     return rank, world, local
 
 
-def build_index(wl):
+def build_index(wl, scale=1.0):
     from hibf_gb300 import build as B
 
     offs = wl.user_bin_offsets()
+    if scale != 1.0:
+        sizes = np.maximum(1, np.floor(np.diff(offs.astype(np.float64)) * scale)).astype(np.uint64)
+        offs = np.zeros(sizes.size + 1, np.uint64)
+        np.cumsum(sizes, out=offs[1:])
     cfg = B.config(number_of_user_bins=wl.n_user_bins, number_of_hash_functions=wl.h, maximum_fpr=wl.fpr)
     t0 = time.perf_counter()
     hibf = B.build_synthetic(cfg, wl.layout_text(), wl.query.seed, offs)
@@ -176,11 +184,13 @@ def run_ours(args, wl, rank, world, local):
     from hibf_gb300 import _native as N
 
     torch.cuda.set_device(local)
+    if args.l2_fetch >= 0:
+        N.call("hibf_gpu_set_l2_fetch_granularity", args.l2_fetch)
     if world > 1:
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    hibf, offs, build_s = build_index(wl)
+    hibf, offs, build_s = build_index(wl, args.scale)
     nq = args.queries or wl.n_queries
     qo, thr = wl.query_offsets(0, nq)
     nv = int(qo[-1])
@@ -224,6 +234,7 @@ def run_ours(args, wl, rank, world, local):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     tasks, visits = agent.last_work()
+    executed = agent.last_work_executed()
     kms = []
     for _ in range(3):
         agent.replay()
@@ -273,7 +284,8 @@ def run_ours(args, wl, rank, world, local):
     if rank == 0:
         hbm, peak_kind = peaks()
         bytes_per_visit = wl.h * 1 * 32  # h rows of ceil(64/256) = 1 sector each (all IBFs have 64 bins)
-        achieved = visits * bytes_per_visit / (kernel_ms / 1e3) / 1e9
+        # bytes the executed work needs: a task stops reading values once its IBF can no longer report (exact)
+        achieved = executed * bytes_per_visit / (kernel_ms / 1e3) / 1e9
         tpv = traffic_per_value_visit()
         cpu = None
         parity = {"plain_equals_batch": plain_equal, "e2e_equals_batch": e2e_equal}
@@ -298,6 +310,7 @@ def run_ours(args, wl, rank, world, local):
             "config": {"workload": WORKLOAD_DESC[wl.name], "name": wl.name, "n_user_bins": wl.n_user_bins,
                        "queries_per_step": nq, "values_per_step": nv, "n_ibfs": hibf.n_ibfs,
                        "index_bytes": int(hibf.info()["device_bytes"]), "parallelism": f"replicas x{world}",
+                       "size_scale": args.scale, "l2_fetch_granularity": args.l2_fetch,
                        "l2": "inputs (values) and the index are larger than L2; no flush",
                        "form": "one persistent launch per batch, CUDA-graph replay"},
             "queries_per_s": world * nq / (ms / 1e3),
@@ -309,8 +322,9 @@ def run_ours(args, wl, rank, world, local):
             "gpu_launches": launches_per_step * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "peak_kind": peak_kind,
-                         "traffic": (tpv * visits) if tpv is not None else None,
-                         "kernel": "k_query", "kernel_ms": kernel_ms, "value_visits": visits, "tasks": tasks,
+                         "traffic": (tpv * executed) if tpv is not None else None,
+                         "kernel": "k_query", "kernel_ms": kernel_ms, "value_visits": visits,
+                         "value_visits_executed": executed, "tasks": tasks,
                          "algorithmic_bytes_per_value_visit": bytes_per_visit},
             "cpu_baseline": cpu, "clocks": clk, "build_s": build_s, "parity": parity,
         }
@@ -327,7 +341,7 @@ def run_reference(args, wl, rank, world, local):
     import torch
 
     torch.cuda.set_device(local)
-    hibf, offs, _ = build_index(wl)
+    hibf, offs, _ = build_index(wl, args.scale)
     OH = oracle_from_device(hibf)
     del hibf
     threads = os.cpu_count() or 1

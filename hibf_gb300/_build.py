@@ -15,9 +15,10 @@ from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
-LIBDIR = PKG / "_lib"
-OBJDIR = PKG / "_build"
+LIBDIR = Path(os.environ.get("HIBF_GB300_LIBDIR", PKG / "_lib"))
+OBJDIR = LIBDIR.parent / (LIBDIR.name + "_obj") if "HIBF_GB300_LIBDIR" in os.environ else PKG / "_build"
 LIB = LIBDIR / "libhibf_gb300.so"
+EXTRA_FLAGS = os.environ.get("HIBF_GB300_NVCC_FLAGS", "").split()
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -40,9 +41,9 @@ def _compile(src: Path) -> Path:
     deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.hpp")) + list((PKG.parent / "include").glob("*.h"))
     if obj.exists() and all(obj.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *EXTRA_FLAGS, "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
-        cmd = [nvcc(), "-x", "cu", *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc(), "-x", "cu", *ARCH, *NVCC_FLAGS, *EXTRA_FLAGS, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
@@ -52,8 +53,8 @@ def _compile(src: Path) -> Path:
 
 
 def build(verbose: bool = False) -> Path:
-    LIBDIR.mkdir(exist_ok=True)
-    OBJDIR.mkdir(exist_ok=True)
+    LIBDIR.mkdir(parents=True, exist_ok=True)
+    OBJDIR.mkdir(parents=True, exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 1))) as ex:
         objs = list(ex.map(_compile, srcs))

@@ -10,7 +10,7 @@ import ctypes
 import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libhibf_gb300.so"
+LIB_PATH = Path(os.environ.get("HIBF_GB300_LIB", Path(__file__).resolve().parent / "_lib" / "libhibf_gb300.so"))
 
 u64 = ctypes.c_uint64
 u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -112,7 +112,9 @@ _SIGS = [
     ("hibf_gpu_agent_fetch_results", None,
      [vp, u64, ci, ci, ctypes.POINTER(u64p), ctypes.POINTER(u64p), ctypes.POINTER(vp)]),
     ("hibf_gpu_agent_status", None, [vp]),
+    ("hibf_gpu_set_l2_fetch_granularity", None, [ci]),
     ("hibf_gpu_agent_last_work", None, [vp, u64p, u64p]),
+    ("hibf_gpu_agent_last_work_executed", None, [vp, u64p]),
     ("hibf_gpu_agent_capture_batch_d", None, [vp, ci, vp, vp, u64, vp, ci]),
     ("hibf_gpu_agent_replay", None, [vp]),
     ("hibf_gpu_agent_kernel_ms", None, [vp, ctypes.POINTER(ctypes.c_float)]),

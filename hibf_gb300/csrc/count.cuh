@@ -26,15 +26,26 @@ struct row_params
     uint32_t hash_funs;
 };
 
+// `added` (warp-uniform) masks went into the planes since the last flush, so planes k with 2^k > added are zero and
+// are not transposed.
 template <int LPV, int K, bool ATOMIC>
-__device__ __forceinline__ void planes_flush_to(uint64_t (&P)[K], uint32_t * out, int lane)
+__device__ __forceinline__ void planes_flush_to(uint64_t (&P)[K], uint32_t * out, int lane, int added)
 {
+    int const kmax = 32 - __clz(added);
     uint32_t lo[K], hi[K];
 #pragma unroll
     for (int k = 0; k < K; ++k)
     {
-        lo[k] = warp_transpose32(static_cast<uint32_t>(P[k]), lane);
-        hi[k] = warp_transpose32(static_cast<uint32_t>(P[k] >> 32), lane);
+        if (k < kmax)
+        {
+            lo[k] = warp_transpose32(static_cast<uint32_t>(P[k]), lane);
+            hi[k] = warp_transpose32(static_cast<uint32_t>(P[k] >> 32), lane);
+        }
+        else
+        {
+            lo[k] = 0;
+            hi[k] = 0;
+        }
         P[k] = 0;
     }
 #pragma unroll
@@ -66,8 +77,10 @@ __device__ __forceinline__ void planes_flush_to(uint64_t (&P)[K], uint32_t * out
     }
 }
 
-// One warp counts vals[0, n) into counts[0, 64 * LPV).  ATOMIC: counters shared with other warps.
-template <int LPV, int K, bool ATOMIC>
+// One warp counts vals[0, n) into counts[0, 64 * LPV) with H hash functions.  ATOMIC: counters shared with other
+// warps.  Each lane keeps U values' H row offsets and 4 x H row words in registers, so the loads of four values are in
+// flight together.
+template <int LPV, int H, int K, bool ATOMIC>
 __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const * __restrict__ vals, uint64_t n,
                                            uint32_t * counts, int lane)
 {
@@ -79,7 +92,6 @@ __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const
     int const g = lane / LPV;
     int const j = lane % LPV;
     bool const wj = static_cast<uint32_t>(j) < rp.bin_words;
-    uint32_t const h = rp.hash_funs;
     uint64_t const * __restrict__ words = rp.words + j;
 
     uint64_t P[K];
@@ -90,57 +102,68 @@ __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const
 
     for (uint64_t base = 0; base < n; base += BLOCK)
     {
-        uint64_t off[U][5];
+        uint64_t off[U][H];
 #pragma unroll
         for (int u = 0; u < U; ++u)
         {
             uint64_t const idx = base + static_cast<uint64_t>(u * 32 + lane);
             uint64_t const v = idx < n ? vals[idx] : 0u;
 #pragma unroll
-            for (int i = 0; i < 5; ++i)
-                off[u][i] = (static_cast<uint32_t>(i) < h)
-                              ? hash_row(v, c_hash_seeds[i], rp.hash_shift, rp.bin_size) * rp.row_words
-                              : 0u;
+            for (int i = 0; i < H; ++i)
+                off[u][i] = hash_row(v, c_hash_seeds[i], rp.hash_shift, rp.bin_size) * rp.row_words;
         }
-#pragma unroll
-        for (int s = 0; s < STEPS; s += 4)
+        // one group: four masks per lane (four sub-steps of LPV-lane groups), their h loads issued together
+        auto group = [&](int s)
         {
-            uint64_t w[4][5];
+            uint64_t w[4][H];
             bool ok[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t)
             {
                 int const step = s + t;
-                int const u = step / LPV;
+                int const u = U == 1 ? 0 : step / LPV;
                 int const src = (step % LPV) * G + g;
                 ok[t] = wj && (base + static_cast<uint64_t>(u * 32 + src) < n);
 #pragma unroll
-                for (int i = 0; i < 5; ++i)
+                for (int i = 0; i < H; ++i)
                 {
                     uint64_t o = off[u][i];
                     if constexpr (LPV > 1)
                         o = __shfl_sync(kFullMask, o, src);
-                    w[t][i] = (ok[t] && static_cast<uint32_t>(i) < h) ? __ldg(words + o) : ~0ull;
+                    w[t][i] = ok[t] ? __ldg(words + o) : 0ull;
                 }
             }
             uint64_t m[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t)
             {
-                uint64_t x = w[t][0] & w[t][1] & w[t][2] & w[t][3] & w[t][4];
-                m[t] = ok[t] ? x : 0u;
+                uint64_t x = w[t][0];
+#pragma unroll
+                for (int i = 1; i < H; ++i)
+                    x &= w[t][i];
+                m[t] = x;
             }
             planes_add4<K>(P, m[0], m[1], m[2], m[3]);
             acc += 4;
             if (acc > (1 << K) - 1 - 4)
             {
-                planes_flush_to<LPV, K, ATOMIC>(P, counts, lane);
+                planes_flush_to<LPV, K, ATOMIC>(P, counts, lane, acc);
                 acc = 0;
             }
+        };
+        if constexpr (STEPS <= 4)
+        {
+            group(0);
+        }
+        else
+        {
+#pragma unroll 1
+            for (int s = 0; s < STEPS; s += 4)
+                group(s);
         }
     }
     if (acc)
-        planes_flush_to<LPV, K, ATOMIC>(P, counts, lane);
+        planes_flush_to<LPV, K, ATOMIC>(P, counts, lane, acc);
 }
 
 // Rows wider than a warp (bin_words > 32): lanes stride over the words, set bits are added one by one.
@@ -173,7 +196,45 @@ __device__ __forceinline__ void warp_count_wide(row_params const & rp, uint64_t 
     }
 }
 
-// Dispatch on the node's lanes-per-value (log2).  K = 7 planes: flush every 124 masks per lane.
+template <int H, bool ATOMIC>
+__device__ __forceinline__ void warp_count_lpv(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
+                                               uint64_t n, uint32_t * counts, int lane)
+{
+    switch (lpv_log2)
+    {
+    case 0:
+        warp_count<1, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    case 1:
+        warp_count<2, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    case 2:
+        warp_count<4, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    case 3:
+        warp_count<8, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    case 4:
+        warp_count<16, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        break;
+    default:
+        warp_count<32, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+    }
+}
+
+// Dispatch on lanes-per-value for a compile-time hash function count (rows wider than a warp use the generic loop).
+template <int H, bool ATOMIC>
+__device__ __forceinline__ void warp_count_h(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
+                                             uint64_t n, uint32_t * counts, int lane)
+{
+    if (rp.bin_words > 32)
+        warp_count_wide(rp, vals, n, counts, lane);
+    else
+        warp_count_lpv<H, ATOMIC>(rp, lpv_log2, vals, n, counts, lane);
+}
+
+// Dispatch on the node's hash function count and lanes-per-value (log2).  K = 7 planes: flush every 124 masks per
+// lane.
 template <bool ATOMIC>
 __device__ __forceinline__ void warp_count_any(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
                                                uint64_t n, uint32_t * counts, int lane)
@@ -183,25 +244,22 @@ __device__ __forceinline__ void warp_count_any(row_params const & rp, uint32_t l
         warp_count_wide(rp, vals, n, counts, lane);
         return;
     }
-    switch (lpv_log2)
+    switch (rp.hash_funs)
     {
-    case 0:
-        warp_count<1, 7, ATOMIC>(rp, vals, n, counts, lane);
-        break;
     case 1:
-        warp_count<2, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count_lpv<1, ATOMIC>(rp, lpv_log2, vals, n, counts, lane);
         break;
     case 2:
-        warp_count<4, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count_lpv<2, ATOMIC>(rp, lpv_log2, vals, n, counts, lane);
         break;
     case 3:
-        warp_count<8, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count_lpv<3, ATOMIC>(rp, lpv_log2, vals, n, counts, lane);
         break;
     case 4:
-        warp_count<16, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count_lpv<4, ATOMIC>(rp, lpv_log2, vals, n, counts, lane);
         break;
     default:
-        warp_count<32, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count_lpv<5, ATOMIC>(rp, lpv_log2, vals, n, counts, lane);
     }
 }
 

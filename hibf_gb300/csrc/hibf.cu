@@ -43,6 +43,23 @@ constexpr uint32_t F_RUN_END = 4u;
 constexpr uint32_t F_HEAD = 8u;
 
 constexpr unsigned long long kEmpty = ~0ull;
+// tasks shorter than this are counted in one stage (the reachability checks would cost more than they save)
+constexpr uint64_t kEarlyExitMinValues = 256;
+// checkpoints (percent of the task's values) after which the task stops if no segment can reach the threshold
+#ifndef HIBF_EE_FIRST
+#    define HIBF_EE_FIRST 30
+#endif
+#ifndef HIBF_EE_STEP
+#    define HIBF_EE_STEP 10
+#endif
+#ifndef HIBF_EE_STAGES
+#    define HIBF_EE_STAGES 7
+#endif
+constexpr uint64_t kEarlyExitFirst = HIBF_EE_FIRST;
+constexpr uint64_t kEarlyExitStep = HIBF_EE_STEP;
+constexpr int kEarlyExitStages = HIBF_EE_STAGES;
+// stats words: tasks, value visits the reference's traversal implies, value visits executed
+constexpr int kStats = 3;
 constexpr uint32_t kNodeBits = 26;
 constexpr uint32_t kNodeMask = (1u << kNodeBits) - 1u;
 
@@ -119,8 +136,50 @@ __device__ unsigned long long wait_for_task(query_params const & p, unsigned lon
     }
 }
 
+// Whether some summation segment of IBF `nd` can still report or descend: its counts so far plus `remaining` for each
+// of its bins (a value adds at most one to every bin) reach the threshold, or could exceed the counter range (then
+// the wrapped sum is not bounded).  When no segment can, the task's outcome is already fixed -- nothing reported,
+// nothing descended -- exactly as if every value had been counted.
+__device__ bool any_segment_reachable(query_params const & p, dev_node const & nd, uint32_t const * counts,
+                                      uint64_t remaining, uint64_t thr, int lane)
+{
+    uint2 const * d = p.descs + nd.desc_offset;
+    unsigned long long carry = 0;
+    for (uint32_t c = 0; c < nd.bins; c += 32)
+    {
+        uint32_t const b = c + lane;
+        bool const valid = b < nd.bins;
+        uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
+        unsigned long long x = valid ? static_cast<unsigned long long>(counts[b]) + remaining : 0ull;
+        bool f = valid && (ds.y & F_HEAD);
+        if (lane == 0 && !f)
+            x += carry;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
+            int const fy = __shfl_up_sync(kFullMask, static_cast<int>(f), o);
+            if (lane >= o)
+            {
+                if (!f)
+                    x += y;
+                f = f || fy;
+            }
+        }
+        bool const ends = valid && (ds.y & (F_RUN_END | F_MERGED));
+        if (__any_sync(kFullMask, ends && (x >= thr || x > p.count_mask)))
+            return true;
+        unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
+        uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
+        carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
+    }
+    return false;
+}
+
+template <int H>
 __device__ void process_task(query_params const & p, unsigned long long task, uint32_t * counts, int lane,
-                             unsigned long long & n_tasks, unsigned long long & n_visits)
+                             unsigned long long & n_tasks, unsigned long long & n_visits,
+                             unsigned long long & n_executed)
 {
     uint64_t const q = task >> 32;
     uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
@@ -135,8 +194,42 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
         counts[i] = 0;
     __syncwarp();
     row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
-    warp_count_any<false>(rp, nd.lpv_log2, p.values + b0, n, counts, lane);
+    // Count in stages; after each stage stop if no segment can reach the threshold any more (exact: see above).
+    uint64_t done = 0;
+    bool hopeless = !any_segment_reachable(p, nd, counts, n, thr, lane);
+    if (!hopeless && n >= kEarlyExitMinValues)
+    {
+        for (int s = 0; s < kEarlyExitStages; ++s)
+        {
+            uint64_t const stop = n * (kEarlyExitFirst + s * kEarlyExitStep) / 100u;
+            warp_count_h<H, false>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
+            done = stop;
+            __syncwarp();
+            if (!any_segment_reachable(p, nd, counts, n - done, thr, lane))
+            {
+                hopeless = true;
+                break;
+            }
+        }
+    }
+    if (!hopeless)
+    {
+        warp_count_h<H, false>(rp, nd.lpv_log2, p.values + b0 + done, n - done, counts, lane);
+        done = n;
+    }
     __syncwarp();
+    if (hopeless)
+    {
+        if (lane == 0)
+        {
+            __threadfence();
+            atomicAdd(p.ctrl + C_PENDING, ~0ull); // retires without results or children
+            ++n_tasks;
+            n_visits += n;
+            n_executed += done;
+        }
+        return;
+    }
 
     uint2 const * d = p.descs + nd.desc_offset;
     unsigned long long carry = 0;
@@ -237,10 +330,18 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
         atomicAdd(p.ctrl + C_PENDING, ~0ull); // this task retires
         ++n_tasks;
         n_visits += n;
+        n_executed += done;
     }
 }
 
-__global__ void __launch_bounds__(256) k_query(query_params p)
+// H = the hierarchy's hash function count (one value for all IBFs, as in the reference's build).
+// HIBF_QUERY_MIN_BLOCKS blocks of eight warps per SM bound the register budget (2: 128 registers per thread,
+// measured fastest: the kernel is limited by the memory system's random-access rate, not by occupancy).
+#ifndef HIBF_QUERY_MIN_BLOCKS
+#    define HIBF_QUERY_MIN_BLOCKS 2
+#endif
+template <int H>
+__global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_params p)
 {
     extern __shared__ uint32_t s_counts[];
     int const lane = threadIdx.x & 31;
@@ -256,7 +357,7 @@ __global__ void __launch_bounds__(256) k_query(query_params p)
         }
         __syncthreads();
     }
-    unsigned long long n_tasks = 0, n_visits = 0;
+    unsigned long long n_tasks = 0, n_visits = 0, n_executed = 0;
     for (;;)
     {
         unsigned long long idx = 0;
@@ -280,12 +381,13 @@ __global__ void __launch_bounds__(256) k_query(query_params p)
             if (task == kEmpty)
                 break;
         }
-        process_task(p, task, counts, lane, n_tasks, n_visits);
+        process_task<H>(p, task, counts, lane, n_tasks, n_visits, n_executed);
     }
     if (lane == 0 && n_tasks)
     {
         atomicAdd(p.stats + 0, n_tasks);
         atomicAdd(p.stats + 1, n_visits);
+        atomicAdd(p.stats + 2, n_executed);
     }
 }
 
@@ -293,7 +395,7 @@ __global__ void k_init_ctrl(unsigned long long * ctrl, unsigned long long * stat
 {
     if (threadIdx.x < C_WORDS)
         ctrl[threadIdx.x] = threadIdx.x == C_PENDING ? n_queries : 0ull;
-    if (threadIdx.x < 2)
+    if (threadIdx.x < kStats)
         stats[threadIdx.x] = 0;
 }
 
@@ -569,6 +671,25 @@ __global__ void k_hibf_emplace(uint64_t * __restrict__ words, uint64_t bin_size,
     }
 }
 
+using query_kernel_t = void (*)(query_params);
+
+query_kernel_t query_kernel(uint32_t h)
+{
+    switch (h)
+    {
+    case 1:
+        return k_query<1>;
+    case 2:
+        return k_query<2>;
+    case 3:
+        return k_query<3>;
+    case 4:
+        return k_query<4>;
+    default:
+        return k_query<5>;
+    }
+}
+
 unsigned grid_cap(uint64_t work, unsigned block, unsigned per_sm = 16)
 {
     uint64_t const want = (work + block - 1) / block;
@@ -589,7 +710,7 @@ struct hibf_gpu_agent
     cudaEvent_t ev_k0{}, ev_k1{}; // around the persistent query kernel of the last batch
     cudaGraphExec_t graph{};      // captured launch sequence of one batch (hibf_gpu_agent_capture_batch_d)
     int status{HIBF_GPU_OK};
-    uint64_t last_tasks{}, last_visits{};
+    uint64_t last_tasks{}, last_visits{}, last_executed{};
     uint64_t cap_queries{}, cap_tasks{}, cap_results{};
     int max_blocks_per_sm{};
     // device workspace
@@ -733,7 +854,7 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         HG_CUDA(cudaStreamIsCapturing(s, &cap));
         unsigned const rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
-        k_query<<<grid, 256, query_smem(h), s>>>(p);
+        query_kernel(h->hash_count)<<<grid, 256, query_smem(h), s>>>(p);
         HG_CUDA(cudaGetLastError());
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k1, s, rec_flags));
     }
@@ -758,7 +879,7 @@ void launch_plain(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         p.self_init = 1;
         HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u) * 8, s));
         p.task_cap = std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u);
-        k_query<<<1, 256, query_smem(h), s>>>(p);
+        query_kernel(h->hash_count)<<<1, 256, query_smem(h), s>>>(p);
         HG_CUDA(cudaGetLastError());
     }
     launch_postprocess(a, nq, mode, width);
@@ -767,12 +888,13 @@ void launch_plain(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
 int read_status(hibf_gpu_agent * a)
 {
     HG_CUDA(cudaMemcpyAsync(a->h_ctrl.p, a->ctrl.p, C_WORDS * 8, cudaMemcpyDeviceToHost, a->stream));
-    HG_CUDA(cudaMemcpyAsync(a->h_stats.p, a->stats.p, 2 * 8, cudaMemcpyDeviceToHost, a->stream));
+    HG_CUDA(cudaMemcpyAsync(a->h_stats.p, a->stats.p, kStats * 8, cudaMemcpyDeviceToHost, a->stream));
     HG_CUDA(cudaStreamSynchronize(a->stream));
     unsigned long long const * c = a->h_ctrl.as<unsigned long long>();
     unsigned long long const * st = a->h_stats.as<unsigned long long>();
     a->last_tasks = st[0];
     a->last_visits = st[1];
+    a->last_executed = st[2];
     unsigned long long const e = c[C_ERROR];
     if (e & E_TIMEOUT)
         return HIBF_GPU_ERR_TIMEOUT;
@@ -886,6 +1008,10 @@ extern "C"
                         fail(HIBF_GPU_ERR_LOGIC, "The size of a bin must be > 0.");
                     off[k + 1] = off[k] + bins[k];
                 }
+                for (uint64_t k = 1; k < n_ibfs; ++k)
+                    if (hash_funs[k] != hash_funs[0])
+                        fail(HIBF_GPU_ERR_INVALID_ARG,
+                             "all IBFs of a hierarchy must use the same number of hash functions");
                 if (off[n_ibfs] >= 0xFFFFFFFFull)
                     fail(HIBF_GPU_ERR_INVALID_ARG, "too many technical bins in total");
                 // per-bin descriptors
@@ -1000,6 +1126,7 @@ extern "C"
                         h->stores.push_back(std::move(st));
                     }
                     h->counters_per_warp = cpw;
+                    h->hash_count = static_cast<uint32_t>(hash_funs[0]);
                     if (static_cast<size_t>(8) * cpw * 4 > 200 * 1024)
                         fail(HIBF_GPU_ERR_INVALID_ARG, "an IBF is too wide for the query kernel's shared counters");
                     h->d_nodes.ensure(n_ibfs * sizeof(dev_node));
@@ -1010,7 +1137,8 @@ extern "C"
                                             cudaMemcpyHostToDevice, h->stream));
                     HG_CUDA(cudaStreamSynchronize(h->stream));
                     size_t const smem = query_smem(h);
-                    HG_CUDA(cudaFuncSetAttribute(k_query, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    HG_CUDA(cudaFuncSetAttribute(query_kernel(h->hash_count),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  static_cast<int>(std::max<size_t>(smem, 48 * 1024))));
                 }
                 catch (...)
@@ -1181,11 +1309,12 @@ extern "C"
                     HG_CUDA(cudaEventCreate(&a->ev_k0));
                     HG_CUDA(cudaEventCreate(&a->ev_k1));
                     a->ctrl.ensure(C_WORDS * 8);
-                    a->stats.ensure(2 * 8);
+                    a->stats.ensure(kStats * 8);
                     a->h_ctrl.ensure(C_WORDS * 8);
-                    a->h_stats.ensure(2 * 8);
+                    a->h_stats.ensure(kStats * 8);
                     int nb = 0;
-                    HG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_query, 256, query_smem(h)));
+                    HG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, query_kernel(h->hash_count), 256,
+                                                                          query_smem(h)));
                     a->max_blocks_per_sm = std::max(1, nb);
                     ensure_capacity(a, 1024, 4096, 4096);
                 }
@@ -1455,6 +1584,18 @@ extern "C"
             });
     }
 
+    int hibf_gpu_set_l2_fetch_granularity(int bytes)
+    {
+        return guarded(
+            [&]
+            {
+                if (bytes < 0 || bytes > 128)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "L2 fetch granularity must be in [0, 128] bytes");
+                require_device();
+                HG_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, static_cast<size_t>(bytes)));
+            });
+    }
+
     int hibf_gpu_agent_status(hibf_gpu_agent * a)
     {
         if (!a)
@@ -1465,6 +1606,18 @@ extern "C"
                 int const st = read_status(a);
                 if (st != HIBF_GPU_OK)
                     fail(st, "device-side failure in the last batch");
+            });
+    }
+
+    int hibf_gpu_agent_last_work_executed(hibf_gpu_agent * a, uint64_t * value_visits_executed)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !value_visits_executed)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                (void)read_status(a);
+                *value_visits_executed = a->last_executed;
             });
     }
 

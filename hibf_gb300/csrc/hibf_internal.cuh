@@ -36,6 +36,7 @@ struct hibf_gpu_hibf
     uint64_t n_user_bins{};
     uint64_t n_ibfs{};
     uint32_t max_depth{};
+    uint32_t hash_count{}; // number of hash functions, the same for every IBF
     uint32_t counters_per_warp{};
     uint64_t total_bytes{};
     std::vector<hibf_gb300::dev_node> nodes;           // host copy

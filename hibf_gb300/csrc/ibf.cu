@@ -135,8 +135,10 @@ __global__ void k_bulk_contains(row_params rp, uint64_t const * __restrict__ val
 
 // bulk_count over n values into one counting vector: every warp counts a contiguous chunk into the block's shared
 // counters, the block adds them to 64-bit global totals.
-__global__ void k_bulk_count(row_params rp, uint32_t lpv_log2, uint64_t const * __restrict__ values, uint64_t n,
-                             uint64_t chunk, unsigned long long * __restrict__ totals, uint32_t n_counters)
+template <int H>
+__global__ void __launch_bounds__(256, 4)
+    k_bulk_count(row_params rp, uint32_t lpv_log2, uint64_t const * __restrict__ values, uint64_t n, uint64_t chunk,
+                 unsigned long long * __restrict__ totals, uint32_t n_counters)
 {
     extern __shared__ uint32_t s_counts[];
     for (uint32_t i = threadIdx.x; i < n_counters; i += blockDim.x)
@@ -148,7 +150,7 @@ __global__ void k_bulk_count(row_params rp, uint32_t lpv_log2, uint64_t const * 
     for (uint64_t start = warp * chunk; start < n; start += nwarps * chunk)
     {
         uint64_t const len = (n - start) < chunk ? (n - start) : chunk;
-        warp_count_any<true>(rp, lpv_log2, values + start, len, s_counts, lane);
+        warp_count_h<H, true>(rp, lpv_log2, values + start, len, s_counts, lane);
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < n_counters; i += blockDim.x)
@@ -177,6 +179,26 @@ __global__ void k_store_counts(unsigned long long const * __restrict__ totals, u
         default:
             static_cast<uint64_t *>(out)[b] = t;
         }
+    }
+}
+
+using bulk_count_kernel_t = void (*)(row_params, uint32_t, uint64_t const *, uint64_t, uint64_t,
+                                     unsigned long long *, uint32_t);
+
+bulk_count_kernel_t bulk_count_kernel(uint64_t h)
+{
+    switch (h)
+    {
+    case 1:
+        return k_bulk_count<1>;
+    case 2:
+        return k_bulk_count<2>;
+    case 3:
+        return k_bulk_count<3>;
+    case 4:
+        return k_bulk_count<4>;
+    default:
+        return k_bulk_count<5>;
     }
 }
 
@@ -276,9 +298,9 @@ void launch_count(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int w
             std::max<uint64_t>(1, std::min<uint64_t>((warps + 7) / 8, static_cast<uint64_t>(sm_count()) * 4u)));
         size_t const smem = nc * sizeof(uint32_t);
         if (smem > 48 * 1024)
-            HG_CUDA(cudaFuncSetAttribute(k_bulk_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            HG_CUDA(cudaFuncSetAttribute(bulk_count_kernel(f->hash_funs), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
-        k_bulk_count<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk,
+        bulk_count_kernel(f->hash_funs)<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk,
                                                f->totals.as<unsigned long long>(), static_cast<uint32_t>(nc));
         HG_CUDA(cudaGetLastError());
     }
@@ -805,9 +827,9 @@ extern "C"
                         1, std::min<uint64_t>((warps + 7) / 8, static_cast<uint64_t>(sm_count()) * 4u)));
                     size_t const smem = nc * sizeof(uint32_t);
                     if (smem > 48 * 1024)
-                        HG_CUDA(cudaFuncSetAttribute(k_bulk_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        HG_CUDA(cudaFuncSetAttribute(bulk_count_kernel(f->hash_funs), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      static_cast<int>(smem)));
-                    k_bulk_count<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk, totals,
+                    bulk_count_kernel(f->hash_funs)<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk, totals,
                                                            static_cast<uint32_t>(nc));
                     HG_CUDA(cudaGetLastError());
                 }

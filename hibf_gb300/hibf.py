@@ -172,6 +172,11 @@ class _agent_base:
         N.call("hibf_gpu_agent_last_work", self._a, ctypes.byref(t), ctypes.byref(v))
         return t.value, v.value
 
+    def last_work_executed(self) -> int:
+        v = ctypes.c_uint64(0)
+        N.call("hibf_gpu_agent_last_work_executed", self._a, ctypes.byref(v))
+        return v.value
+
     def status(self) -> None:
         N.call("hibf_gpu_agent_status", self._a)
 

@@ -245,6 +245,10 @@ int hibf_gpu_agent_fetch_results(hibf_gpu_agent * a, uint64_t n_queries, int mod
                                  uint64_t const ** result_offsets, uint64_t const ** result_ids,
                                  void const ** result_counts);
 int hibf_gpu_agent_status(hibf_gpu_agent * a);
+/* Hint for the L2 fetch granularity of the calling process's CUDA context (cudaLimitMaxL2FetchGranularity, bytes in
+ * [0, 128]).  Random 8-32 byte row reads waste bandwidth when L2 fetches more than a sector; the limit applies to
+ * every kernel of the context and ends with it. */
+int hibf_gpu_set_l2_fetch_granularity(int bytes);
 /* Captures one batch's launch sequence (control reset, persistent kernel, compaction) on fixed device buffers into
  * a CUDA graph owned by the agent; hibf_gpu_agent_replay launches it on the agent's stream. */
 int hibf_gpu_agent_capture_batch_d(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
@@ -256,6 +260,9 @@ int hibf_gpu_agent_kernel_ms(hibf_gpu_agent * a, float * ms);
 /* Number of (query, IBF) tasks the last batch processed and the number of query values they covered
  * (sum over tasks of the query length): the work the roofline is computed from. */
 int hibf_gpu_agent_last_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits);
+/* The query values the last batch actually read: a (query, IBF) task stops reading once no bin segment of the IBF
+ * can reach the threshold any more (its result is then already fixed), so this is at most value_visits. */
+int hibf_gpu_agent_last_work_executed(hibf_gpu_agent * a, uint64_t * value_visits_executed);
 
 /* ============================================================================================================ */
 /* Seeded synthetic workloads (include/hibf_gb300_synthetic.h), for benchmarks and tests                        */
