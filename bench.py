@@ -52,6 +52,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end measurement (0: --steps)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--l2-fetch", type=int, default=-1,
                     help="set the context's L2 fetch granularity hint (bytes) before the run; -1 leaves it")
     ap.add_argument("--scale", type=float, default=1.0,
@@ -280,6 +281,19 @@ def run_ours(args, wl, rank, world, local):
     h2d = nv * 8 + (nq + 1) * 8 + nq * 8
     d2h = (nq + 1) * 8 + int(eo[-1]) * 8 + 8 * 8 + 16
 
+    # serving: open-loop Poisson arrivals against the resident index (continuous batching, 4 slots, 4 GiB cap)
+    serving = []
+    if not args.no_serve:
+        from hibf_gb300.serve import server
+
+        pool_q = min(nq, 100_000)
+        pool_v = hv[:int(qo[pool_q])]
+        srv = server(hibf, slots=4, max_batch_queries=65536, max_batch_values=1 << 27, admission_bytes=4 << 30)
+        for load, dur in ((1e4, 2.0), (1e5, 1.0), (1e6, 1.0)):
+            serving.append(srv.open_loop(pool_v, qo[:pool_q + 1], offered_qps=load, duration_s=dur,
+                                         max_request_queries=4096, thr_lo=0.5, thr_hi=0.9, seed=int(load)))
+        srv.close()
+
     out = None
     if rank == 0:
         hbm, peak_kind = peaks()
@@ -327,6 +341,9 @@ def run_ours(args, wl, rank, world, local):
                          "value_visits_executed": executed, "tasks": tasks,
                          "algorithmic_bytes_per_value_visit": bytes_per_visit},
             "cpu_baseline": cpu, "clocks": clk, "build_s": build_s, "parity": parity,
+            "serving": serving, "p99_serve_latency_ms": serving[-1]["p99_ms"] if serving else None,
+            "serving_config": "open-loop Poisson, request sizes log-uniform 1-4096 queries from the batch's first "
+                              "100k queries, thresholds U(0.5,0.9)*len, 4 slots, 4 GiB admission cap",
         }
     if world > 1:
         torch.distributed.destroy_process_group()

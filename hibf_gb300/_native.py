@@ -113,11 +113,22 @@ _SIGS = [
      [vp, u64, ci, ci, ctypes.POINTER(u64p), ctypes.POINTER(u64p), ctypes.POINTER(vp)]),
     ("hibf_gpu_agent_status", None, [vp]),
     ("hibf_gpu_set_l2_fetch_granularity", None, [ci]),
+    ("hibf_gpu_agent_selftest_wait_limit", None, [vp, ctypes.c_double]),
     ("hibf_gpu_agent_last_work", None, [vp, u64p, u64p]),
     ("hibf_gpu_agent_last_work_executed", None, [vp, u64p]),
     ("hibf_gpu_agent_capture_batch_d", None, [vp, ci, vp, vp, u64, vp, ci]),
     ("hibf_gpu_agent_replay", None, [vp]),
     ("hibf_gpu_agent_kernel_ms", None, [vp, ctypes.POINTER(ctypes.c_float)]),
+    ("hibf_gpu_server_create", None, [vp, ci, u64, u64, u64, ctypes.POINTER(vp)]),
+    ("hibf_gpu_server_destroy", None, [vp]),
+    ("hibf_gpu_server_submit", None, [vp, vp, vp, u64, vp, ctypes.c_double, ci, u64p]),
+    ("hibf_gpu_server_wait", None, [vp, u64, ctypes.c_double, ctypes.POINTER(ci), ctypes.POINTER(u64p),
+                                    ctypes.POINTER(u64p), ctypes.POINTER(ctypes.c_double)]),
+    ("hibf_gpu_server_release", None, [vp, u64]),
+    ("hibf_gpu_server_now", ctypes.c_double, []),
+    ("hibf_gpu_server_stats", None, [vp, u64p]),
+    ("hibf_gpu_server_open_loop", None, [vp, vp, vp, u64, ctypes.c_double, ctypes.c_double, u64, ctypes.c_double,
+                                         ctypes.c_double, u64, ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_synth_user_bin_offsets", None, [u64, ci, ctypes.c_double, ctypes.c_double, u64, u64, u64, vp]),
     ("hibf_gpu_synth_query_offsets", None, [u64, ci, u64, u64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                             ctypes.c_uint32, u64, u64, u64, vp, vp]),

@@ -33,6 +33,7 @@ inline void cuda_check(cudaError_t e, char const * what)
 {
     if (e == cudaSuccess)
         return;
+    (void)cudaGetLastError(); // a non-sticky error (e.g. a failed allocation) must not resurface at a later check
     int st = HIBF_GPU_ERR_CUDA;
     if (e == cudaErrorMemoryAllocation)
         st = HIBF_GPU_ERR_OUT_OF_MEMORY;

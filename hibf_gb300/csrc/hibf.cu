@@ -1584,6 +1584,34 @@ extern "C"
             });
     }
 
+    int hibf_gpu_agent_selftest_wait_limit(hibf_gpu_agent * a, double limit_ms)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !(limit_ms > 0) || limit_ms > 10000)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "limit must be in (0, 10000] ms");
+                cudaStream_t s = a->stream;
+                ensure_capacity(a, 1, std::max<uint64_t>(a->cap_tasks, 1024), std::max<uint64_t>(a->cap_results, 1024));
+                a->in_values.ensure(8);
+                a->in_qoff.ensure(16);
+                a->in_thr.ensure(8);
+                HG_CUDA(cudaMemsetAsync(a->in_qoff.p, 0, 16, s));
+                // no query, but one task announced that nobody will ever push: every worker's wait must expire
+                k_init_ctrl<<<1, 32, 0, s>>>(a->ctrl.as<unsigned long long>(), a->stats.as<unsigned long long>(), 1);
+                HG_CUDA(cudaGetLastError());
+                HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, a->cap_tasks * 8, s));
+                query_params p = base_params(a, a->in_values.as<uint64_t>(), a->in_qoff.as<uint64_t>(),
+                                             a->in_thr.as<uint64_t>(), 0, 0xFFFFu);
+                p.wait_limit_ns = static_cast<uint64_t>(limit_ms * 1e6);
+                query_kernel(a->h->hash_count)<<<1, 256, query_smem(a->h), s>>>(p);
+                HG_CUDA(cudaGetLastError());
+                int const st = read_status(a);
+                if (st != HIBF_GPU_ERR_TIMEOUT)
+                    fail(HIBF_GPU_ERR_CUDA, "the bounded wait did not report a timeout");
+            });
+    }
+
     int hibf_gpu_set_l2_fetch_granularity(int bytes)
     {
         return guarded(

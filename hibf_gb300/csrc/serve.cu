@@ -1,0 +1,652 @@
+// serve.cu -- continuous-batching query server over a resident HIBF, and an open-loop load driver.
+//
+// The server keeps the HIBF on the device and owns `slots` agents, each with its own stream and buffers.  Requests
+// (CSR batches of queries from callers) wait in a FIFO.  A loop thread admits them: whenever a slot is free it
+// coalesces waiting requests, oldest first, into one batch bounded by the slot's capacity and by the device-memory
+// admission cap (inputs, task queue, records and result lists of all batches in flight).  Batches on different
+// slots overlap on the device; a request that arrives while others run joins the next batch a free slot takes.
+// Results are split back per request; a batch's results equal each request's results alone because queries are
+// independent.  A request that alone needs more than the admission cap is rejected (HIBF_GPU_ERR_ADMISSION).
+//
+// Reference: the reference has no server; its agents answer one query per call (hierarchical_interleaved_bloom_filter
+// .hpp:322-439).  This is the serving loop the batched device path enables.
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/hibf_gb300_synthetic.h"
+#include "common.hpp"
+
+namespace hibf_gb300
+{
+namespace serve
+{
+
+using clock_t_ = std::chrono::steady_clock;
+
+inline double now_s()
+{
+    return std::chrono::duration<double>(clock_t_::now().time_since_epoch()).count();
+}
+
+struct request
+{
+    uint64_t id{};
+    uint64_t nq{}, nv{};
+    uint64_t const * values{}; // the request's values, offsets (relative, qoff[0] = 0) and thresholds: either the
+    uint64_t const * qoff{};   // caller's buffers (kept alive by the caller until the request is released) or the
+    uint64_t const * thr{};    // copies below
+    std::vector<uint64_t> own_values, own_qoff, own_thr;
+    double t_arrival{};                      // when the request counts as arrived (caller's clock, seconds)
+    double t_done{};
+    int status{HIBF_GPU_OK};
+    std::atomic<bool> done{false}; // set by the loop thread after the results, read by waiters
+    bool solo{false}; // run alone (after a batch overflowed)
+    std::vector<uint64_t> res_off, res_ids;
+};
+
+struct slot
+{
+    hibf_gpu_agent * agent{};
+    cudaStream_t stream{};
+    cudaEvent_t ev{};
+    int phase{0}; // 0 idle, 1 kernels + offsets in flight, 2 ids in flight
+    std::vector<request *> reqs;
+    uint64_t nq{}, nv{}, bytes{};
+    uint64_t nr{};
+    dbuf d_values, d_qoff, d_thr;
+    hbuf h_values, h_qoff, h_thr, h_roff, h_ids;
+    uint64_t const * d_roff{};
+    uint64_t const * d_ids{};
+};
+
+} // namespace serve
+} // namespace hibf_gb300
+
+using namespace hibf_gb300;
+using namespace hibf_gb300::serve;
+
+struct hibf_gpu_server
+{
+    hibf_gpu_hibf * h{};
+    uint64_t max_queries{}, max_values{}, admission_bytes{};
+    std::vector<std::unique_ptr<slot>> slots;
+    std::deque<request *> waiting;
+    std::unordered_map<uint64_t, std::unique_ptr<request>> reqs;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread loop;
+    std::atomic<bool> stop{false};
+    uint64_t inflight_bytes{};
+    uint64_t next_id{1};
+    int device{};
+    std::string loop_error;
+    // counters
+    uint64_t batches{}, batched_queries{}, rejected{};
+};
+
+namespace
+{
+
+// Device bytes a batch needs: inputs, task queue, records and result lists (the agent's workspace for it).
+uint64_t batch_bytes(uint64_t nq, uint64_t nv)
+{
+    return nv * 8 + (nq + 1) * 8 + nq * 8 + nq * 8 * 8 + nq * 16 * (4 + 4 + 8 + 8 + 8 + 8);
+}
+
+void start_batch(hibf_gpu_server * S, slot & sl)
+{
+    // gather inputs into pinned staging, offsets relative to the batch
+    uint64_t nq = 0, nv = 0;
+    for (request * r : sl.reqs)
+    {
+        nq += r->nq;
+        nv += r->nv;
+    }
+    sl.nq = nq;
+    sl.nv = nv;
+    uint64_t * hv = sl.h_values.as<uint64_t>();
+    uint64_t * ho = sl.h_qoff.as<uint64_t>();
+    uint64_t * ht = sl.h_thr.as<uint64_t>();
+    uint64_t q = 0, v = 0;
+    ho[0] = 0;
+    for (request * r : sl.reqs)
+    {
+        std::memcpy(hv + v, r->values, r->nv * 8);
+        for (uint64_t i = 0; i < r->nq; ++i)
+        {
+            ho[q + i + 1] = v + r->qoff[i + 1];
+            ht[q + i] = r->thr[i];
+        }
+        q += r->nq;
+        v += r->nv;
+    }
+    HG_CUDA(cudaMemcpyAsync(sl.d_values.p, hv, std::max<uint64_t>(nv, 1) * 8, cudaMemcpyHostToDevice, sl.stream));
+    HG_CUDA(cudaMemcpyAsync(sl.d_qoff.p, ho, (nq + 1) * 8, cudaMemcpyHostToDevice, sl.stream));
+    HG_CUDA(cudaMemcpyAsync(sl.d_thr.p, ht, std::max<uint64_t>(nq, 1) * 8, cudaMemcpyHostToDevice, sl.stream));
+    void const * cnt = nullptr;
+    int const st = hibf_gpu_agent_query_batch_d(sl.agent, HIBF_GPU_QUERY_MEMBERSHIP, sl.d_values.as<uint64_t>(),
+                                                sl.d_qoff.as<uint64_t>(), nq, sl.d_thr.as<uint64_t>(), 2, &sl.d_roff,
+                                                &sl.d_ids, &cnt);
+    if (st != HIBF_GPU_OK)
+        fail(st, "batch launch failed");
+    HG_CUDA(cudaMemcpyAsync(sl.h_roff.p, sl.d_roff, (nq + 1) * 8, cudaMemcpyDeviceToHost, sl.stream));
+    HG_CUDA(cudaEventRecord(sl.ev, sl.stream));
+    sl.phase = 1;
+    ++S->batches;
+    S->batched_queries += nq;
+}
+
+// Advances a slot whose event has fired.  Returns true when its requests completed (or were requeued).
+bool advance_slot(hibf_gpu_server * S, slot & sl, std::vector<request *> & requeue)
+{
+    if (sl.phase == 1)
+    {
+        int const st = hibf_gpu_agent_status(sl.agent);
+        if (st == HIBF_GPU_ERR_OVERFLOW)
+        {
+            // rerun every request alone; a request that overflows alone fails
+            for (request * r : sl.reqs)
+            {
+                if (sl.reqs.size() == 1 || r->solo)
+                {
+                    r->status = HIBF_GPU_ERR_OVERFLOW;
+                    r->done = true;
+                    r->t_done = now_s();
+                }
+                else
+                {
+                    r->solo = true;
+                    requeue.push_back(r);
+                }
+            }
+            return true;
+        }
+        if (st != HIBF_GPU_OK)
+        {
+            for (request * r : sl.reqs)
+            {
+                r->status = st;
+                r->done = true;
+                r->t_done = now_s();
+            }
+            return true;
+        }
+        sl.nr = sl.h_roff.as<uint64_t>()[sl.nq];
+        if (sl.nr)
+            HG_CUDA(cudaMemcpyAsync(sl.h_ids.p, sl.d_ids, sl.nr * 8, cudaMemcpyDeviceToHost, sl.stream));
+        HG_CUDA(cudaEventRecord(sl.ev, sl.stream));
+        sl.phase = 2;
+        return false;
+    }
+    // phase 2: results on the host -> split per request
+    uint64_t const * ro = sl.h_roff.as<uint64_t>();
+    uint64_t const * ids = sl.h_ids.as<uint64_t>();
+    double const t = now_s();
+    uint64_t q = 0;
+    for (request * r : sl.reqs)
+    {
+        uint64_t const base = ro[q];
+        r->res_off.resize(r->nq + 1);
+        for (uint64_t i = 0; i <= r->nq; ++i)
+            r->res_off[i] = ro[q + i] - base;
+        r->res_ids.assign(ids + base, ids + ro[q + r->nq]);
+        r->status = HIBF_GPU_OK;
+        r->done = true;
+        r->t_done = t;
+        q += r->nq;
+    }
+    return true;
+}
+
+void server_loop(hibf_gpu_server * S)
+{
+    cudaSetDevice(S->device);
+    std::vector<request *> requeue;
+    while (!S->stop.load())
+    {
+        bool progressed = false;
+        // completions
+        for (auto & slp : S->slots)
+        {
+            slot & sl = *slp;
+            if (sl.phase == 0)
+                continue;
+            cudaError_t const e = cudaEventQuery(sl.ev);
+            if (e == cudaErrorNotReady)
+                continue;
+            if (e != cudaSuccess)
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->loop_error = cudaGetErrorString(e);
+                for (request * r : sl.reqs)
+                {
+                    r->status = HIBF_GPU_ERR_CUDA;
+                    r->done = true;
+                }
+                sl.reqs.clear();
+                sl.phase = 0;
+                S->cv_done.notify_all();
+                continue;
+            }
+            bool finished = false;
+            try
+            {
+                finished = advance_slot(S, sl, requeue);
+            }
+            catch (status_error const & err)
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->loop_error = err.what();
+                for (request * r : sl.reqs)
+                {
+                    r->status = err.status;
+                    r->done = true;
+                }
+                finished = true;
+            }
+            progressed = true;
+            if (finished)
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->inflight_bytes -= sl.bytes;
+                for (auto it = requeue.rbegin(); it != requeue.rend(); ++it)
+                    S->waiting.push_front(*it);
+                requeue.clear();
+                sl.reqs.clear();
+                sl.phase = 0;
+                S->cv_done.notify_all();
+            }
+        }
+        // admission: fill free slots with the oldest waiting requests
+        for (auto & slp : S->slots)
+        {
+            slot & sl = *slp;
+            if (sl.phase != 0)
+                continue;
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                uint64_t nq = 0, nv = 0;
+                while (!S->waiting.empty())
+                {
+                    request * r = S->waiting.front();
+                    uint64_t const b = batch_bytes(nq + r->nq, nv + r->nv);
+                    bool const fits_slot = nq + r->nq <= S->max_queries && nv + r->nv <= S->max_values;
+                    bool const fits_cap = S->inflight_bytes + b <= S->admission_bytes;
+                    if (sl.reqs.empty() && !fits_slot)
+                    {
+                        // cannot run even alone in a slot
+                        S->waiting.pop_front();
+                        r->status = HIBF_GPU_ERR_ADMISSION;
+                        r->done = true;
+                        r->t_done = now_s();
+                        ++S->rejected;
+                        S->cv_done.notify_all();
+                        continue;
+                    }
+                    if (!fits_slot || !fits_cap || (r->solo && !sl.reqs.empty()))
+                        break;
+                    S->waiting.pop_front();
+                    sl.reqs.push_back(r);
+                    nq += r->nq;
+                    nv += r->nv;
+                    if (r->solo)
+                        break;
+                }
+                if (sl.reqs.empty())
+                    continue;
+                sl.bytes = batch_bytes(nq, nv);
+                S->inflight_bytes += sl.bytes;
+            }
+            try
+            {
+                start_batch(S, sl);
+            }
+            catch (status_error const & err)
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->loop_error = err.what();
+                for (request * r : sl.reqs)
+                {
+                    r->status = err.status;
+                    r->done = true;
+                }
+                S->inflight_bytes -= sl.bytes;
+                sl.reqs.clear();
+                sl.phase = 0;
+                S->cv_done.notify_all();
+            }
+            progressed = true;
+        }
+        if (!progressed)
+        {
+            bool busy = false;
+            for (auto & slp : S->slots)
+                busy = busy || slp->phase != 0;
+            if (busy)
+                std::this_thread::yield();
+            else
+            {
+                std::unique_lock<std::mutex> lk(S->mu);
+                S->cv_work.wait_for(lk, std::chrono::microseconds(200),
+                                    [&] { return S->stop.load() || !S->waiting.empty(); });
+            }
+        }
+    }
+}
+
+} // namespace
+
+extern "C"
+{
+
+    int hibf_gpu_server_create(hibf_gpu_hibf * h, int n_slots, uint64_t max_batch_queries, uint64_t max_batch_values,
+                               uint64_t admission_bytes, hibf_gpu_server ** out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || !out || n_slots <= 0 || max_batch_queries == 0 || max_batch_values == 0)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                *out = nullptr;
+                auto S = std::make_unique<hibf_gpu_server>();
+                S->h = h;
+                S->max_queries = max_batch_queries;
+                S->max_values = max_batch_values;
+                S->admission_bytes = admission_bytes;
+                HG_CUDA(cudaGetDevice(&S->device));
+                for (int i = 0; i < n_slots; ++i)
+                {
+                    auto sl = std::make_unique<slot>();
+                    int st = hibf_gpu_agent_create(h, &sl->agent);
+                    if (st != HIBF_GPU_OK)
+                        fail(st, "agent creation failed");
+                    HG_CUDA(cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking));
+                    HG_CUDA(cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming));
+                    st = hibf_gpu_agent_set_stream(sl->agent, sl->stream);
+                    if (st != HIBF_GPU_OK)
+                        fail(st, "agent stream");
+                    uint64_t const mq = max_batch_queries, mv = max_batch_values;
+                    st = hibf_gpu_agent_reserve(sl->agent, mq, mv, mq * 8 + 4096, mq * 16 + 4096);
+                    if (st != HIBF_GPU_OK)
+                        fail(st, "agent reserve");
+                    sl->d_values.ensure(mv * 8);
+                    sl->d_qoff.ensure((mq + 1) * 8);
+                    sl->d_thr.ensure(mq * 8);
+                    sl->h_values.ensure(mv * 8);
+                    sl->h_qoff.ensure((mq + 1) * 8);
+                    sl->h_thr.ensure(mq * 8);
+                    sl->h_roff.ensure((mq + 1) * 8);
+                    sl->h_ids.ensure((mq * 16 + 4096) * 8);
+                    S->slots.push_back(std::move(sl));
+                }
+                hibf_gpu_server * raw = S.release();
+                raw->loop = std::thread(server_loop, raw);
+                *out = raw;
+            });
+    }
+
+    int hibf_gpu_server_destroy(hibf_gpu_server * S)
+    {
+        return guarded(
+            [&]
+            {
+                if (!S)
+                    return;
+                S->stop.store(true);
+                S->cv_work.notify_all();
+                if (S->loop.joinable())
+                    S->loop.join();
+                for (auto & sl : S->slots)
+                {
+                    cudaStreamSynchronize(sl->stream);
+                    hibf_gpu_agent_destroy(sl->agent);
+                    cudaEventDestroy(sl->ev);
+                    cudaStreamDestroy(sl->stream);
+                }
+                delete S;
+            });
+    }
+
+    // Submits a request.  copy != 0: the data is copied and the caller's buffers may be reused on return; copy == 0:
+    // the server reads the caller's buffers until the request is released (query_offsets[0] must be 0).
+    // arrival_s: the request's arrival time on the server's steady clock (hibf_gpu_server_now), < 0 for "now".
+    int hibf_gpu_server_submit(hibf_gpu_server * S, uint64_t const * values, uint64_t const * query_offsets,
+                               uint64_t n_queries, uint64_t const * thresholds, double arrival_s, int copy,
+                               uint64_t * id)
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !query_offsets || (n_queries && !thresholds) || !id)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                auto r = std::make_unique<request>();
+                r->nq = n_queries;
+                r->nv = query_offsets[n_queries] - query_offsets[0];
+                if (r->nv && !values)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null values");
+                for (uint64_t i = 0; i < n_queries; ++i)
+                {
+                    if (thresholds[i] > 0xFFFFu)
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "membership thresholds are uint16");
+                    if (query_offsets[i + 1] < query_offsets[i])
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "query offsets must be non-decreasing");
+                }
+                if (copy)
+                {
+                    r->own_values.assign(values + query_offsets[0], values + query_offsets[0] + r->nv);
+                    r->own_qoff.resize(n_queries + 1);
+                    for (uint64_t i = 0; i <= n_queries; ++i)
+                        r->own_qoff[i] = query_offsets[i] - query_offsets[0];
+                    r->own_thr.assign(thresholds, thresholds + n_queries);
+                    r->values = r->own_values.data();
+                    r->qoff = r->own_qoff.data();
+                    r->thr = r->own_thr.data();
+                }
+                else
+                {
+                    if (query_offsets[0] != 0)
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "borrowed requests need query_offsets[0] == 0");
+                    r->values = values;
+                    r->qoff = query_offsets;
+                    r->thr = thresholds;
+                }
+                r->t_arrival = arrival_s >= 0 ? arrival_s : now_s();
+                std::lock_guard<std::mutex> lk(S->mu);
+                r->id = S->next_id++;
+                *id = r->id;
+                S->waiting.push_back(r.get());
+                S->reqs.emplace(r->id, std::move(r));
+                S->cv_work.notify_one();
+            });
+    }
+
+    // Waits (up to timeout_ms; < 0 forever) for a request.  On completion *status holds its status and the result
+    // pointers (valid until hibf_gpu_server_release) its sorted membership lists per query.
+    int hibf_gpu_server_wait(hibf_gpu_server * S, uint64_t id, double timeout_ms, int * status,
+                             uint64_t const ** result_offsets, uint64_t const ** result_ids, double * latency_s)
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !status)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::unique_lock<std::mutex> lk(S->mu);
+                auto it = S->reqs.find(id);
+                if (it == S->reqs.end())
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "unknown request id");
+                request * r = it->second.get();
+                auto pred = [&] { return r->done.load(); };
+                if (timeout_ms < 0)
+                    S->cv_done.wait(lk, pred);
+                else if (!S->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), pred))
+                    fail(HIBF_GPU_ERR_TIMEOUT, "request not finished within the timeout");
+                *status = r->status;
+                if (result_offsets)
+                    *result_offsets = r->res_off.data();
+                if (result_ids)
+                    *result_ids = r->res_ids.data();
+                if (latency_s)
+                    *latency_s = r->t_done - r->t_arrival;
+            });
+    }
+
+    int hibf_gpu_server_release(hibf_gpu_server * S, uint64_t id)
+    {
+        return guarded(
+            [&]
+            {
+                if (!S)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(S->mu);
+                auto it = S->reqs.find(id);
+                if (it == S->reqs.end() || !it->second->done)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "unknown or unfinished request");
+                S->reqs.erase(it);
+            });
+    }
+
+    double hibf_gpu_server_now(void)
+    {
+        return now_s();
+    }
+
+    // out: batches, batched queries, rejected requests, bytes in flight
+    int hibf_gpu_server_stats(hibf_gpu_server * S, uint64_t out[4])
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(S->mu);
+                out[0] = S->batches;
+                out[1] = S->batched_queries;
+                out[2] = S->rejected;
+                out[3] = S->inflight_bytes;
+            });
+    }
+
+    // Open-loop load: requests arrive as a Poisson process (rate = offered queries/s / mean request size), request
+    // sizes log-uniform in [1, max_request_queries], queries drawn cyclically from a pool (CSR, host), per-request
+    // thresholds ceil(f * length) with f uniform in [thr_lo, thr_hi].  Runs `duration_s`, then waits for every
+    // request.  out: achieved queries/s, p50, p99, p99.9 latency (s), requests, queries, rejected, mean batch size.
+    int hibf_gpu_server_open_loop(hibf_gpu_server * S, uint64_t const * pool_values, uint64_t const * pool_offsets,
+                                  uint64_t pool_queries, double offered_qps, double duration_s,
+                                  uint64_t max_request_queries, double thr_lo, double thr_hi, uint64_t seed,
+                                  double out[8])
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !pool_values || !pool_offsets || pool_queries == 0 || offered_qps <= 0 || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                std::mt19937_64 rng(seed);
+                std::uniform_real_distribution<double> U(0.0, 1.0);
+                double const lmax = std::log(static_cast<double>(max_request_queries));
+                // mean of floor(exp(U(0, lmax))) ~ (max - 1) / lmax
+                double const mean_size = max_request_queries > 1
+                                             ? (static_cast<double>(max_request_queries) - 1.0) / lmax
+                                             : 1.0;
+                double const req_rate = offered_qps / mean_size;
+                struct plan
+                {
+                    double t;
+                    uint64_t q0, nq;
+                    double f;
+                };
+                std::vector<plan> plans;
+                double t = 0;
+                uint64_t q = 0;
+                while (true)
+                {
+                    t += -std::log(1.0 - U(rng)) / req_rate;
+                    if (t > duration_s)
+                        break;
+                    uint64_t nq = static_cast<uint64_t>(std::floor(std::exp(U(rng) * lmax)));
+                    nq = std::max<uint64_t>(1, std::min(nq, max_request_queries));
+                    nq = std::min(nq, pool_queries);
+                    plans.push_back(plan{t, q % pool_queries, nq, thr_lo + (thr_hi - thr_lo) * U(rng)});
+                    q += nq;
+                }
+                // build request payloads ahead of time (contiguous pool slices, wrapping)
+                std::vector<std::vector<uint64_t>> offs(plans.size()), thrs(plans.size());
+                std::vector<std::vector<uint64_t>> vals(plans.size());
+                for (size_t i = 0; i < plans.size(); ++i)
+                {
+                    auto & p = plans[i];
+                    offs[i].push_back(0);
+                    for (uint64_t k = 0; k < p.nq; ++k)
+                    {
+                        uint64_t const qi = (p.q0 + k) % pool_queries;
+                        uint64_t const b = pool_offsets[qi], e = pool_offsets[qi + 1];
+                        vals[i].insert(vals[i].end(), pool_values + b, pool_values + e);
+                        offs[i].push_back(vals[i].size());
+                        thrs[i].push_back(static_cast<uint64_t>(std::ceil(p.f * static_cast<double>(e - b))));
+                    }
+                }
+                std::vector<uint64_t> ids(plans.size(), 0);
+                double const t0 = now_s() + 0.01;
+                for (size_t i = 0; i < plans.size(); ++i)
+                {
+                    double const ta = t0 + plans[i].t;
+                    while (now_s() < ta)
+                        ;
+                    int const st = hibf_gpu_server_submit(S, vals[i].data(), offs[i].data(), plans[i].nq,
+                                                          thrs[i].data(), ta, 0, &ids[i]);
+                    if (st != HIBF_GPU_OK)
+                        fail(st, "submit failed");
+                }
+                std::vector<double> lat;
+                lat.reserve(plans.size());
+                uint64_t nqs = 0, rej = 0;
+                double t_end = t0;
+                for (size_t i = 0; i < plans.size(); ++i)
+                {
+                    int st = 0;
+                    double l = 0;
+                    int const w = hibf_gpu_server_wait(S, ids[i], 600000.0, &st, nullptr, nullptr, &l);
+                    if (w != HIBF_GPU_OK)
+                        fail(w, "wait failed");
+                    if (st == HIBF_GPU_OK)
+                    {
+                        lat.push_back(l);
+                        nqs += plans[i].nq;
+                        t_end = std::max(t_end, t0 + plans[i].t + l);
+                    }
+                    else
+                        ++rej;
+                    hibf_gpu_server_release(S, ids[i]);
+                }
+                std::sort(lat.begin(), lat.end());
+                auto pct = [&](double p) -> double
+                {
+                    if (lat.empty())
+                        return 0.0;
+                    size_t const k = std::min(lat.size() - 1, static_cast<size_t>(std::ceil(p * lat.size())) - 1);
+                    return lat[k];
+                };
+                uint64_t st4[4];
+                hibf_gpu_server_stats(S, st4);
+                out[0] = static_cast<double>(nqs) / std::max(1e-9, t_end - t0);
+                out[1] = pct(0.50);
+                out[2] = pct(0.99);
+                out[3] = pct(0.999);
+                out[4] = static_cast<double>(plans.size());
+                out[5] = static_cast<double>(nqs);
+                out[6] = static_cast<double>(rej);
+                out[7] = st4[0] ? static_cast<double>(st4[1]) / static_cast<double>(st4[0]) : 0.0;
+            });
+    }
+
+} // extern "C"

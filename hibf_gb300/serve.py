@@ -1,0 +1,89 @@
+"""Continuous-batching query server over a resident HIBF (hibf_gpu_server_* in the C ABI).
+
+    srv = server(hibf, slots=4, max_batch_queries=65536, max_batch_values=1 << 26, admission_bytes=4 << 30)
+    rid = srv.submit(values, query_offsets, thresholds)
+    status, offsets, ids, latency_s = srv.wait_result(rid, n_queries)
+    stats = srv.open_loop(pool_values, pool_offsets, offered_qps=1e5, duration_s=1.0)
+
+Requests arriving while batches run are admitted as slots and admission memory free up; their batches overlap on
+the device.  Each request's results equal the same queries answered alone.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+
+def _u64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint64).reshape(-1))
+
+
+class server:
+    def __init__(self, hibf, slots: int = 4, max_batch_queries: int = 65536, max_batch_values: int = 1 << 26,
+                 admission_bytes: int = 4 << 30):
+        self._s = None
+        self.hibf = hibf  # keeps the HIBF alive
+        s = ctypes.c_void_p()
+        N.call("hibf_gpu_server_create", hibf._h, slots, max_batch_queries, max_batch_values, admission_bytes,
+               ctypes.byref(s))
+        self._s = s
+
+    def close(self) -> None:
+        if getattr(self, "_s", None):
+            N.call("hibf_gpu_server_destroy", self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, values, query_offsets, thresholds, arrival_s: float = -1.0) -> int:
+        v, qo, t = _u64(values), _u64(query_offsets), _u64(thresholds)
+        rid = ctypes.c_uint64(0)
+        N.call("hibf_gpu_server_submit", self._s, v.ctypes.data if v.size else None, qo.ctypes.data, qo.size - 1,
+               t.ctypes.data if t.size else None, arrival_s, 1, ctypes.byref(rid))
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: float = -1.0):
+        """(status, offsets pointer, ids pointer, latency_s); the pointers stay valid until release(rid)."""
+        st = ctypes.c_int(0)
+        ro, ri = N.u64p(), N.u64p()
+        lat = ctypes.c_double(0)
+        N.call("hibf_gpu_server_wait", self._s, rid, timeout_ms, ctypes.byref(st), ctypes.byref(ro),
+               ctypes.byref(ri), ctypes.byref(lat))
+        return st.value, ro, ri, lat.value
+
+    def release(self, rid: int) -> None:
+        N.call("hibf_gpu_server_release", self._s, rid)
+
+    def wait_result(self, rid: int, n_queries: int, timeout_ms: float = -1.0):
+        """(status, offsets (n_queries + 1), ids, latency_s) as numpy copies; releases the request."""
+        st, ro, ri, lat = self.wait(rid, timeout_ms)
+        offs = ids = None
+        if st == N.OK:
+            offs = np.ctypeslib.as_array(ro, shape=(n_queries + 1,)).copy()
+            nr = int(offs[-1])
+            ids = np.ctypeslib.as_array(ri, shape=(nr,)).copy() if nr else np.zeros(0, np.uint64)
+        N.call("hibf_gpu_server_release", self._s, rid)
+        return st, offs, ids, lat
+
+    def stats(self) -> dict:
+        out = (ctypes.c_uint64 * 4)()
+        N.call("hibf_gpu_server_stats", self._s, out)
+        return dict(batches=out[0], batched_queries=out[1], rejected=out[2], inflight_bytes=out[3])
+
+    def open_loop(self, pool_values, pool_offsets, offered_qps: float, duration_s: float = 1.0,
+                  max_request_queries: int = 4096, thr_lo: float = 0.5, thr_hi: float = 0.9, seed: int = 1) -> dict:
+        v, qo = _u64(pool_values), _u64(pool_offsets)
+        out = (ctypes.c_double * 8)()
+        N.call("hibf_gpu_server_open_loop", self._s, v.ctypes.data, qo.ctypes.data, qo.size - 1, offered_qps,
+               duration_s, max_request_queries, thr_lo, thr_hi, seed, out)
+        return dict(offered_qps=offered_qps, achieved_qps=out[0], p50_ms=out[1] * 1e3, p99_ms=out[2] * 1e3,
+                    p999_ms=out[3] * 1e3, requests=int(out[4]), queries=int(out[5]), rejected=int(out[6]),
+                    mean_batch_queries=out[7], duration_s=duration_s)

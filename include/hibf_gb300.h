@@ -249,6 +249,10 @@ int hibf_gpu_agent_status(hibf_gpu_agent * a);
  * [0, 128]).  Random 8-32 byte row reads waste bandwidth when L2 fetches more than a sector; the limit applies to
  * every kernel of the context and ends with it. */
 int hibf_gpu_set_l2_fetch_granularity(int bytes);
+/* Failure-detection self-test of the work queue's bounded wait: runs the persistent kernel with one announced task
+ * that is never pushed, so every worker's wait must expire after limit_ms and the batch must report
+ * HIBF_GPU_ERR_TIMEOUT through the device status word.  Returns OK when it did; the context stays usable. */
+int hibf_gpu_agent_selftest_wait_limit(hibf_gpu_agent * a, double limit_ms);
 /* Captures one batch's launch sequence (control reset, persistent kernel, compaction) on fixed device buffers into
  * a CUDA graph owned by the agent; hibf_gpu_agent_replay launches it on the agent's stream. */
 int hibf_gpu_agent_capture_batch_d(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
@@ -263,6 +267,37 @@ int hibf_gpu_agent_last_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * va
 /* The query values the last batch actually read: a (query, IBF) task stops reading once no bin segment of the IBF
  * can reach the threshold any more (its result is then already fixed), so this is at most value_visits. */
 int hibf_gpu_agent_last_work_executed(hibf_gpu_agent * a, uint64_t * value_visits_executed);
+
+/* ============================================================================================================ */
+/* Continuous-batching server over a resident HIBF (no counterpart in the reference, whose agents answer one query   */
+/* per call).  A loop thread owns n_slots agents with their own streams; waiting requests are coalesced oldest-first */
+/* into one batch per free slot, bounded by the slot capacity (queries, values) and by admission_bytes, the device   */
+/* memory of inputs, task queues, records and result lists of all batches in flight.  Batches on different slots    */
+/* overlap on the device.  A request that cannot run even alone in a slot is rejected with HIBF_GPU_ERR_ADMISSION.   */
+/* Results are membership_for + sort_results per query, identical to the request answered alone.                    */
+/* ============================================================================================================ */
+typedef struct hibf_gpu_server hibf_gpu_server;
+int hibf_gpu_server_create(hibf_gpu_hibf * h, int n_slots, uint64_t max_batch_queries, uint64_t max_batch_values,
+                           uint64_t admission_bytes, hibf_gpu_server ** out);
+int hibf_gpu_server_destroy(hibf_gpu_server * s);
+/* copy != 0: inputs copied; copy == 0: the caller keeps them alive until hibf_gpu_server_release (offsets from 0).
+ * arrival_s: arrival time on hibf_gpu_server_now's clock (< 0: now); latencies are measured from it. */
+int hibf_gpu_server_submit(hibf_gpu_server * s, uint64_t const * values, uint64_t const * query_offsets,
+                           uint64_t n_queries, uint64_t const * thresholds, double arrival_s, int copy, uint64_t * id);
+/* Waits up to timeout_ms (< 0: forever); *status is the request's status; results valid until release. */
+int hibf_gpu_server_wait(hibf_gpu_server * s, uint64_t id, double timeout_ms, int * status,
+                         uint64_t const ** result_offsets, uint64_t const ** result_ids, double * latency_s);
+int hibf_gpu_server_release(hibf_gpu_server * s, uint64_t id);
+double hibf_gpu_server_now(void);
+/* out: batches launched, queries in them, requests rejected, device bytes admitted in flight. */
+int hibf_gpu_server_stats(hibf_gpu_server * s, uint64_t out[4]);
+/* Open-loop Poisson load from a pool of queries (host CSR): request sizes log-uniform in [1, max_request_queries],
+ * per-request thresholds ceil(f * length), f uniform in [thr_lo, thr_hi].  out: achieved queries/s, p50, p99, p99.9
+ * latency (seconds), requests, queries, rejected requests, mean queries per batch. */
+int hibf_gpu_server_open_loop(hibf_gpu_server * s, uint64_t const * pool_values, uint64_t const * pool_offsets,
+                              uint64_t pool_queries, double offered_qps, double duration_s,
+                              uint64_t max_request_queries, double thr_lo, double thr_hi, uint64_t seed,
+                              double out[8]);
 
 /* ============================================================================================================ */
 /* Seeded synthetic workloads (include/hibf_gb300_synthetic.h), for benchmarks and tests                        */
