@@ -242,6 +242,15 @@ def run_ours(args, wl, rank, world, local):
         stream.synchronize()
         kms.append(agent.kernel_ms())
     kernel_ms = sum(kms) / len(kms)
+    # the device's own random 8-byte read rate at the index's footprint (fully random, and 2 MiB-local)
+    import ctypes as _ct
+
+    probe = {}
+    fp = min(int(hibf.info()["device_bytes"]), 16 << 30)
+    for name, region in (("random", 0), ("window_2MiB", 2 << 20)):
+        rps = _ct.c_double(0)
+        N.call("hibf_gpu_probe_random_reads", fp, region, _ct.byref(rps))
+        probe[name] = rps.value
     launches_per_step = 8
     res_offs, res_ids, _ = agent.fetch_results(nq)
 
@@ -339,7 +348,11 @@ def run_ours(args, wl, rank, world, local):
                          "traffic": (tpv * executed) if tpv is not None else None,
                          "kernel": "k_query", "kernel_ms": kernel_ms, "value_visits": visits,
                          "value_visits_executed": executed, "tasks": tasks,
-                         "algorithmic_bytes_per_value_visit": bytes_per_visit},
+                         "algorithmic_bytes_per_value_visit": bytes_per_visit,
+                         "row_reads_per_s": executed * wl.h / (kernel_ms / 1e3),
+                         "random_read_ceiling": {"footprint_bytes": fp, "reads_per_s_random": probe["random"],
+                                                 "reads_per_s_2MiB_windows": probe["window_2MiB"],
+                                                 "probe": "hibf_gpu_probe_random_reads"}},
             "cpu_baseline": cpu, "clocks": clk, "build_s": build_s, "parity": parity,
             "serving": serving, "p99_serve_latency_ms": serving[-1]["p99_ms"] if serving else None,
             "serving_config": "open-loop Poisson, request sizes log-uniform 1-4096 queries from the batch's first "

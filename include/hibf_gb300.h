@@ -299,6 +299,11 @@ int hibf_gpu_server_open_loop(hibf_gpu_server * s, uint64_t const * pool_values,
                               uint64_t max_request_queries, double thr_lo, double thr_hi, uint64_t seed,
                               double out[8]);
 
+/* Diagnostic: the device's rate of independent random 8-byte reads over a buffer of footprint_bytes (region_bytes:
+ * reads confined to windows of that size, 0 = the whole buffer).  The practical ceiling for the query kernels'
+ * random row reads, which the copy-bandwidth peak overstates. */
+int hibf_gpu_probe_random_reads(uint64_t footprint_bytes, uint64_t region_bytes, double * reads_per_s);
+
 /* ============================================================================================================ */
 /* Seeded synthetic workloads (include/hibf_gb300_synthetic.h), for benchmarks and tests                        */
 /* ============================================================================================================ */
