@@ -92,6 +92,9 @@ _SIGS = [
     ("hibf_gpu_hibf_get_tables", None, [vp, vp, vp, vp, vp, vp]),
     ("hibf_gpu_sink_push", None, [vp, vp, u64]),
     ("hibf_gpu_hibf_build", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, INPUT_FN, vp, ctypes.POINTER(vp)]),
+    ("hibf_gpu_ibf_build", None, [ctypes.POINTER(BuildConfig), u64, ctypes.c_uint32, ci, INPUT_FN, vp,
+                                  ctypes.POINTER(vp)]),
+    ("hibf_gpu_ibf_plan", None, [ctypes.POINTER(BuildConfig), u64, ctypes.c_uint32, INPUT_FN, vp, u64p, u64p]),
     ("hibf_gpu_hibf_build_synthetic", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, u64, vp,
                                              ctypes.POINTER(vp)]),
     ("hibf_gpu_plan_disjoint", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, vp, u64p, u64p, vp, vp, vp,

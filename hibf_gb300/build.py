@@ -178,3 +178,38 @@ def plan_disjoint(configuration: config, layout_text: str, user_bin_sizes) -> di
     out["hash_funs"] = np.full(n.value, configuration.number_of_hash_functions, np.uint64)
     out["n_user_bins"] = configuration.number_of_user_bins
     return out
+
+
+def ibf_from_config(configuration: config, max_bin_elements: int = 0):
+    """interleaved_bloom_filter(config&, max_bin_elements) (include/hibf/interleaved_bloom_filter.hpp:241)."""
+    from .ibf import interleaved_bloom_filter
+
+    configuration.validate_and_set_defaults()
+    fn = configuration.input_fn
+
+    def trampoline(_user, ub, sink):
+        fn(int(ub), insert_iterator(sink))
+
+    cb = N.INPUT_FN(trampoline)
+    h = ctypes.c_void_p()
+    N.call("hibf_gpu_ibf_build", ctypes.byref(_cfg(configuration, False)), int(max_bin_elements),
+           configuration.sketch_bits, int(configuration.track_occupancy), cb, None, ctypes.byref(h))
+    obj = interleaved_bloom_filter.__new__(interleaved_bloom_filter)
+    obj._h = h
+    obj._pending_v, obj._pending_b = [], []
+    return obj
+
+
+def ibf_plan(configuration: config, max_bin_elements: int = 0) -> tuple[int, int]:
+    """Host part of interleaved_bloom_filter(config&, max_bin_elements): (bin size in bits, biggest user bin)."""
+    configuration.validate_and_set_defaults()
+    fn = configuration.input_fn
+
+    def trampoline(_user, ub, sink):
+        fn(int(ub), insert_iterator(sink))
+
+    cb = N.INPUT_FN(trampoline)
+    size, best = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    N.call("hibf_gpu_ibf_plan", ctypes.byref(_cfg(configuration, False)), int(max_bin_elements),
+           configuration.sketch_bits, cb, None, ctypes.byref(size), ctypes.byref(best))
+    return size.value, best.value

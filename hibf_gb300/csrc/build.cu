@@ -481,6 +481,64 @@ void validate(hibf_gpu_build_config const * cfg)
              "[HIBF CONFIG ERROR] config::relaxed_fpr must be greater than or equal to config::maximum_fpr.");
 }
 
+// ---- HyperLogLog, as the reference's IBF(config) constructor uses it to find the largest user bin ----------------
+// src/sketch/hyperloglog.cpp:28-118: registers of 2^bits bytes; a value's 64-bit wyhash picks the register with
+// its top `bits` bits and stores max(rank), rank = leading zeros of the remaining bits + 1; the estimate sums
+// 2^-register in single precision over eight lanes (register 8k + 7 - l goes to lane l, lanes added in order),
+// corrects with alpha * m^2, and falls back to linear counting when the raw estimate is at most 2.5 m.
+struct hll
+{
+    uint32_t bits;
+    uint64_t size;
+    uint64_t rank_mask;
+    double norm;
+    std::vector<uint8_t> reg;
+
+    explicit hll(uint32_t b) : bits{b}, size{1ull << b}, rank_mask{(1ull << b) - 1u}, reg(size, 0)
+    {
+        double alpha = 0;
+        if (size == 32)
+            alpha = 0.697;
+        else if (size == 64)
+            alpha = 0.709;
+        else
+            alpha = 0.7213 / (1.0 + 1.079 / static_cast<double>(size));
+        norm = alpha * static_cast<double>(size) * static_cast<double>(size);
+    }
+    void add(uint64_t v)
+    {
+        unsigned __int128 const r = static_cast<unsigned __int128>(v) * 0x9E3779B97F4A7C15ULL;
+        uint64_t const h = static_cast<uint64_t>(r) ^ static_cast<uint64_t>(r >> 64);
+        uint64_t const idx = h >> (64 - bits);
+        uint8_t const rank = static_cast<uint8_t>(__builtin_clzll((h << bits) | rank_mask) + 1);
+        reg[idx] = std::max(reg[idx], rank);
+    }
+    double estimate() const
+    {
+        float lane[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (uint64_t i = 0; i < size / 32; ++i)
+            for (uint64_t j = 0; j <= 24; j += 8)
+                for (int l = 0; l < 8; ++l)
+                {
+                    uint8_t const x = reg[i * 32 + j + 7 - l];
+                    lane[l] = lane[l] + 1.0f / static_cast<float>(1ull << x);
+                }
+        float sum = 0;
+        for (int l = 0; l < 8; ++l)
+            sum += lane[l];
+        double e = norm / static_cast<double>(sum);
+        if (e <= 2.5 * static_cast<double>(size))
+        {
+            uint32_t zeros = 0;
+            for (uint8_t x : reg)
+                zeros += x == 0;
+            if (zeros)
+                e = static_cast<double>(size) * std::log(static_cast<double>(size) / zeros);
+        }
+        return e;
+    }
+};
+
 } // namespace build
 } // namespace hibf_gb300
 
@@ -503,6 +561,91 @@ extern "C"
                 if (!sink || (n && !values))
                     fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
                 sink->values.insert(sink->values.end(), values, values + n);
+            });
+    }
+
+    int hibf_gpu_ibf_plan(hibf_gpu_build_config const * cfg, uint64_t max_bin_elements, uint32_t sketch_bits,
+                          hibf_gpu_input_fn input_fn, void * user, uint64_t * bin_size, uint64_t * biggest_user_bin)
+    {
+        return guarded(
+            [&]
+            {
+                validate(cfg);
+                if (!input_fn || !bin_size)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument (config::input_fn is required)");
+                if (sketch_bits < 5 || sketch_bits > 32)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "[HIBF CONFIG ERROR] config::sketch_bits must be in [5,32].");
+                // max_bin_size (src/interleaved_bloom_filter.cpp:81-101): the largest user bin by sketch estimate
+                // (the first one on ties), then its exact distinct count
+                uint64_t max_size = max_bin_elements;
+                uint64_t best = 0;
+                if (max_size == 0)
+                {
+                    uint64_t best_est = 0;
+                    for (uint64_t u = 0; u < cfg->number_of_user_bins; ++u)
+                    {
+                        hibf_gpu_sink sink;
+                        input_fn(user, u, &sink);
+                        hll sk(sketch_bits);
+                        for (uint64_t v : sink.values)
+                            sk.add(v);
+                        uint64_t const est = static_cast<uint64_t>(sk.estimate());
+                        if (est > best_est)
+                        {
+                            best_est = est;
+                            best = u;
+                        }
+                    }
+                    hibf_gpu_sink sink;
+                    input_fn(user, best, &sink);
+                    std::unordered_set<uint64_t> distinct(sink.values.begin(), sink.values.end());
+                    max_size = distinct.size();
+                }
+                *bin_size = bin_size_in_bits(cfg->maximum_fpr, cfg->number_of_hash_functions, max_size);
+                if (biggest_user_bin)
+                    *biggest_user_bin = best;
+            });
+    }
+
+    int hibf_gpu_ibf_build(hibf_gpu_build_config const * cfg, uint64_t max_bin_elements, uint32_t sketch_bits,
+                           int track_occupancy, hibf_gpu_input_fn input_fn, void * user, hibf_gpu_ibf ** out)
+    {
+        return guarded(
+            [&]
+            {
+                validate(cfg);
+                if (!input_fn || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument (config::input_fn is required)");
+                if (sketch_bits < 5 || sketch_bits > 32)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "[HIBF CONFIG ERROR] config::sketch_bits must be in [5,32].");
+                *out = nullptr;
+                uint64_t const nub = cfg->number_of_user_bins;
+                uint64_t bits = 0;
+                int const pst = hibf_gpu_ibf_plan(cfg, max_bin_elements, sketch_bits, input_fn, user, &bits, nullptr);
+                if (pst != HIBF_GPU_OK)
+                    fail(pst, hibf_gpu_last_error());
+                hibf_gpu_ibf * f = nullptr;
+                int const st = hibf_gpu_ibf_create(nub, bits, cfg->number_of_hash_functions, track_occupancy, &f);
+                if (st != HIBF_GPU_OK)
+                    fail(st, std::string("IBF construction failed: ") + hibf_gpu_last_error());
+                try
+                {
+                    // IBF.cpp:104-117: every user bin's values into its own bin
+                    for (uint64_t u = 0; u < nub; ++u)
+                    {
+                        hibf_gpu_sink sink;
+                        input_fn(user, u, &sink);
+                        int const e = hibf_gpu_ibf_emplace(f, sink.values.data(), sink.values.size(), u);
+                        if (e != HIBF_GPU_OK)
+                            fail(e, hibf_gpu_last_error());
+                    }
+                }
+                catch (...)
+                {
+                    hibf_gpu_ibf_destroy(f);
+                    throw;
+                }
+                *out = f;
             });
     }
 

@@ -187,6 +187,16 @@ int hibf_gpu_hibf_build(hibf_gpu_build_config const * cfg, char const * layout_t
  * positions [user_bin_offsets[u], user_bin_offsets[u+1]) of the splitmix64 stream `seed`, generated on the device. */
 int hibf_gpu_hibf_build_synthetic(hibf_gpu_build_config const * cfg, char const * layout_text, uint64_t seed,
                                   uint64_t const * user_bin_offsets, hibf_gpu_hibf ** out);
+/* interleaved_bloom_filter(config&, max_bin_elements) (interleaved_bloom_filter.hpp:241, src/interleaved_bloom_filter.cpp:
+ * 55-117): bin count = number_of_user_bins; bin size from max_bin_elements, or -- when 0 -- from the exact distinct
+ * count of the user bin with the largest HyperLogLog estimate (sketch_bits), the first such bin on ties; then user
+ * bin u's values go to bin u.  input_fn is called once per user bin for the sketches, once for the exact count and
+ * once for the inserts, as in the reference. */
+int hibf_gpu_ibf_build(hibf_gpu_build_config const * cfg, uint64_t max_bin_elements, uint32_t sketch_bits,
+                       int track_occupancy, hibf_gpu_input_fn input_fn, void * user, hibf_gpu_ibf ** out);
+/* The host part of that constructor alone (no device): the bin size in bits and the user bin it was taken from. */
+int hibf_gpu_ibf_plan(hibf_gpu_build_config const * cfg, uint64_t max_bin_elements, uint32_t sketch_bits,
+                      hibf_gpu_input_fn input_fn, void * user, uint64_t * bin_size, uint64_t * biggest_user_bin);
 /* Host-only planning for pairwise disjoint user bins of the given distinct sizes: the IBF count and total bins
  * (first call with NULL arrays), then sizes, tables and each IBF's parent (IBF, bin).  No device needed. */
 int hibf_gpu_plan_disjoint(hibf_gpu_build_config const * cfg, char const * layout_text,

@@ -15,6 +15,8 @@ them through oracle/ref_driver.cpp:
                      uint16/uint32/uint8 counting vectors, per-query digests).
   c3_layout.txt      the layout the reference computes (HyperLogLog sketches + DP) for the 8,192-user-bin workload
                      (sizes log-normal(2e5, 1.5) clipped to [1e3, 5e7], h=2, fpr 0.05, tmax 64, sketch_bits 12, seed 1).
+  ibf_config.npz     interleaved_bloom_filter(config&, max_bin_elements): bin size (largest user bin by HyperLogLog
+                     estimate, then its exact count), bit store digest, counts, for several configs.
   c1_reference.npz   the 64-user-bin workload (log-uniform [1e3, 1e5], h=2, fpr 0.05, tmax 64): layout, per-IBF
                      digests and tables, 10,000 queries' outputs digests.
 
@@ -213,6 +215,45 @@ def make_hibf_cases(R: Reference):
     hibf_case(R, "synth600", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=11)
 
 
+def make_ibf_config(R: Reference):
+    """interleaved_bloom_filter(config&, max_bin_elements): bin size, bit store digest, counts."""
+    out = {}
+    cases = []
+    # interleaved_bloom_filter_test.cpp:410-431
+    cases.append(([[1, 2, 3, 4, 5, 6, 7, 8, 9, 10], [1, 2, 3, 4, 5]], dict(), 0))
+    rng = np.random.default_rng(77)
+    ubs = [rng.integers(0, 50000, rng.integers(10, 3000)).tolist() for _ in range(40)]  # duplicates and overlaps
+    cases.append((ubs, dict(), 0))
+    cases.append((ubs, dict(h=3, fpr=0.01), 0))
+    cases.append((ubs, dict(sketch_bits=5), 0))
+    cases.append((ubs, dict(), 777))
+    cases.append((None, dict(h=2, fpr=0.05), 0))
+    stream_sizes = rng.integers(100, 20000, 70)
+    big = [S.stream_range(i, 0, int(n)).tolist() for i, n in enumerate(stream_sizes)]
+    cases[-1] = (big, dict(h=2, fpr=0.05), 0)
+    for ci, (ubs, kw, mbe) in enumerate(cases):
+        v, o = csr(ubs)
+        cfg = ref_cfg(len(ubs), **kw)
+        ibf = R.ibf_from_config(cfg, v, o, mbe)
+        q = np.concatenate([v[::3], np.arange(60000, 60500, dtype=np.uint64)])
+        p_ = f"c{ci}_"
+        if ubs is big:
+            # user bin i = the first stream_sizes[i] outputs of the splitmix64 stream seeded with i (regenerated)
+            out[p_ + "stream_sizes"] = stream_sizes.astype(np.uint64)
+        else:
+            out[p_ + "values"], out[p_ + "offsets"] = v, o
+        out[p_ + "kw"] = np.array([kw.get("h", 2), int(kw.get("fpr", 0.05) * 1e6), kw.get("sketch_bits", 12), mbe],
+                                  np.uint64)
+        out[p_ + "params"] = np.array([ibf.bins, ibf.bin_size, ibf.hash_funs], np.uint64)
+        out[p_ + "digest"] = np.array([digest_words(ibf.words())], np.uint64)
+        if ubs is not big:
+            out[p_ + "queries"] = q
+        out[p_ + "count2"] = ibf.bulk_count(q, 2)
+        out[p_ + "member"] = ibf.membership_for(q[:200], 2)
+    out["n_cases"] = np.array([len(cases)], np.uint64)
+    np.savez_compressed(OUT / "ibf_config.npz", **out)
+
+
 def make_c1(R: Reference):
     """The 64-user-bin workload at full size: everything except the bit words (which are 2.9 MB)."""
     sizes = S.user_bin_sizes(1, 64, S.SIZES_LOG_UNIFORM, 0, 0, 1000, 100000)
@@ -243,9 +284,11 @@ def make_c3_layout(R: Reference):
 def main(argv):
     build_reference()
     R = Reference()
-    which = set(argv) or {"ibf", "hibf", "c1", "c3"}
+    which = set(argv) or {"ibf", "ibfcfg", "hibf", "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
+    if "ibfcfg" in which:
+        make_ibf_config(R)
     if "hibf" in which:
         make_hibf_cases(R)
     if "c1" in which:

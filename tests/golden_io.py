@@ -47,3 +47,29 @@ def mem_lists(d, key="mem_sorted"):
 def tables(d):
     return dict(n_user_bins=d["n_ub"], bins=d["bins"], bin_size=d["bin_size"], hash_funs=d["hash_funs"],
                 next_ibf=d["next_ibf"], user_bin=d["user_bin"], words=d["word_list"])
+
+
+def ibf_config_cases():
+    """interleaved_bloom_filter(config&, max_bin_elements) cases; user bins as lists, kw as config fields."""
+    from hibf_gb300 import synthetic as S
+
+    z = np.load(GOLDEN / "ibf_config.npz")
+    out = []
+    for i in range(int(z["n_cases"][0])):
+        p = f"c{i}_"
+        d = {k[len(p):]: z[k] for k in z.files if k.startswith(p)}
+        if "stream_sizes" in d:  # user bin u = the first n_u outputs of the splitmix64 stream seeded with u
+            ubs = [S.stream_range(u, 0, int(n)) for u, n in enumerate(d["stream_sizes"])]
+            v = np.concatenate(ubs).astype(np.uint64)
+            d["queries"] = np.concatenate([v[::3], np.arange(60000, 60500, dtype=np.uint64)])
+        else:
+            v, o = d["values"], d["offsets"].astype(np.int64)
+            ubs = [v[o[u]:o[u + 1]] for u in range(o.size - 1)]
+        h, fpr_ppm, sketch, mbe = (int(x) for x in d["kw"])
+        d["user_bins"] = ubs
+        d["config"] = dict(number_of_user_bins=len(ubs), number_of_hash_functions=h, maximum_fpr=fpr_ppm / 1e6,
+                           sketch_bits=sketch)
+        d["max_bin_elements"] = mbe
+        d["index"] = i
+        out.append(d)
+    return out

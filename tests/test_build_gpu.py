@@ -102,3 +102,36 @@ def test_build_c1_structure(gpu_lib):
     ref = canonical(dict(bins=z["bins"], bin_size=z["bin_size"], next_ibf=z["next_ibf"], user_bin=z["user_bin"]))
     got = canonical(H.tables())
     assert {p: v[:3] for p, v in ref.items()} == {p: v[:3] for p, v in got.items()}
+
+
+@pytest.mark.parametrize("case", G.ibf_config_cases(), ids=lambda c: f"ibfcfg{c['index']}")
+def test_ibf_from_config_matches_reference(gpu_lib, case):
+    """interleaved_bloom_filter(config&, max_bin_elements): same bins, size, bit store, counts and memberships."""
+    ubs = case["user_bins"]
+    cfg = B.config(input_fn=lambda ub, it: it.push(ubs[ub]), **case["config"])
+    ibf = B.ibf_from_config(cfg, case["max_bin_elements"])
+    bins, size, h = (int(x) for x in case["params"])
+    assert (ibf.bin_count(), ibf.bin_size(), ibf.hash_function_count()) == (bins, size, h)
+    assert S.digest(ibf.words().tolist()) == int(case["digest"][0])
+    q = case["queries"]
+    np.testing.assert_array_equal(ibf.counting_agent(2).bulk_count(q), case["count2"])
+    np.testing.assert_array_equal(ibf.membership_agent().membership_for(q[:200], 2), case["member"])
+
+
+def test_ibf_from_config_unit_expectation(gpu_lib):
+    """interleaved_bloom_filter_test.cpp:65-98 (construction_from_config): 2 is in both user bins, 8 only in the first,
+    0 only in the second."""
+    ubs = [list(range(1, 11)), [0, 2, 3, 4, 5]]
+    ibf = B.ibf_from_config(B.config(input_fn=lambda ub, it: it.push(ubs[ub]), number_of_user_bins=2))
+    agent = ibf.containment_agent()
+    assert agent.bulk_contains(2).tolist() == [True, True]
+    assert agent.bulk_contains(8).tolist() == [True, False]
+    assert agent.bulk_contains(0).tolist() == [False, True]
+
+
+def test_ibf_from_config_membership_for(gpu_lib):
+    """interleaved_bloom_filter_test.cpp:410-431 (membership_for): querying 1..5 with threshold 2 hits both bins."""
+    ubs = [list(range(1, 11)), list(range(1, 6))]
+    ibf = B.ibf_from_config(B.config(input_fn=lambda ub, it: it.push(ubs[ub]), number_of_user_bins=2))
+    got = ibf.membership_agent().membership_for(np.arange(1, 6, dtype=np.uint64), 2)
+    assert got.tolist() == [0, 1]

@@ -75,3 +75,13 @@ def test_config_validation_mirrors_reference():
             B.config(input_fn=lambda u, it: None, **bad).validate_and_set_defaults()
     with pytest.raises(ValueError):
         B.config(number_of_user_bins=2).validate_and_set_defaults()
+
+
+@pytest.mark.parametrize("case", G.ibf_config_cases(), ids=lambda c: f"ibfcfg{c['index']}")
+def test_ibf_plan_matches_reference(case):
+    """interleaved_bloom_filter(config&, max_bin_elements): the bin size the reference chose -- from the biggest user
+    bin by HyperLogLog estimate (then counted exactly), or from max_bin_elements -- on the host, no device."""
+    ubs = case["user_bins"]
+    cfg = B.config(input_fn=lambda ub, it: it.push(ubs[ub]), **case["config"])
+    size, _biggest = B.ibf_plan(cfg, case["max_bin_elements"])
+    assert size == int(case["params"][1])
