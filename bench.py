@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end measurement (0: --steps)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel schedule")
+    ap.add_argument("--tune-queries", type=int, default=200_000, help="sample batch of the autotuner")
     ap.add_argument("--l2-fetch", type=int, default=-1,
                     help="set the context's L2 fetch granularity hint (bytes) before the run; -1 leaves it")
     ap.add_argument("--scale", type=float, default=1.0,
@@ -206,6 +208,19 @@ def run_ours(args, wl, rank, world, local):
     agent = hibf.membership_agent()
     agent.reserve(nq, nv, nq * 8 + 65536, nq * 8 + 65536)
     agent.set_stream(stream.cuda_stream)
+    # autotune the kernel schedule on the batch's first queries (results are checked identical across schedules)
+    tune = None
+    if not args.no_autotune:
+        ns = min(nq, args.tune_queries)
+        t0 = time.perf_counter()
+        trials = agent.autotune(d_v.data_ptr(), d_qo.data_ptr(), ns, d_thr.data_ptr(), reps=2)
+        keys = ("values_per_lane", "fetch_bytes", "counter_bits", "blocks_per_sm", "early_exit_first",
+                "early_exit_step", "early_exit_stages", "early_exit_min")
+        tune = {"sample_queries": ns, "seconds": time.perf_counter() - t0, "best": agent.tuning,
+                "default_kernel_ms": trials[0]["kernel_ms"],
+                "best_kernel_ms": min(t["kernel_ms"] for t in trials),
+                "trial_fields": list(keys) + ["kernel_ms"],
+                "trials": [[t[k] for k in keys] + [round(t["kernel_ms"], 4)] for t in trials]}
     agent.capture_batch_device(d_v.data_ptr(), d_qo.data_ptr(), nq, d_thr.data_ptr())
     for _ in range(max(args.warmup, 3)):
         agent.replay()
@@ -257,6 +272,7 @@ def run_ours(args, wl, rank, world, local):
     # plain form: one launch per query on the first P queries
     P = min(args.plain_queries, nq)
     pa = hibf.membership_agent()
+    pa.tuning = agent.tuning
     pa.reserve(P, nv, 65536, P * 8 + 65536)
     pa.set_stream(stream.cuda_stream)
     pa.query_plain_device(d_v.data_ptr(), qo[:P + 1], thr[:P])  # warm-up
@@ -277,6 +293,7 @@ def run_ours(args, wl, rank, world, local):
     h_v.copy_(d_v)
     hv = h_v.numpy().view(np.uint64)[:nv]
     ea = hibf.membership_agent()
+    ea.tuning = agent.tuning
     ea.reserve(nq, nv, nq * 8 + 65536, nq * 8 + 65536)
     for _ in range(2):
         ea.query_batch(hv, qo, thr)
@@ -353,7 +370,7 @@ def run_ours(args, wl, rank, world, local):
                          "random_read_ceiling": {"footprint_bytes": fp, "reads_per_s_random": probe["random"],
                                                  "reads_per_s_2MiB_windows": probe["window_2MiB"],
                                                  "probe": "hibf_gpu_probe_random_reads"}},
-            "cpu_baseline": cpu, "clocks": clk, "build_s": build_s, "parity": parity,
+            "cpu_baseline": cpu, "clocks": clk, "build_s": build_s, "parity": parity, "autotune": tune,
             "serving": serving, "p99_serve_latency_ms": serving[-1]["p99_ms"] if serving else None,
             "serving_config": "open-loop Poisson, request sizes log-uniform 1-4096 queries from the batch's first "
                               "100k queries, thresholds U(0.5,0.9)*len, 4 slots, 4 GiB admission cap",

@@ -58,7 +58,33 @@ class BuildConfig(ctypes.Structure):
 
 INPUT_FN = ctypes.CFUNCTYPE(None, vp, u64, vp)
 
-# (name, restype, argtypes); restype None means the int status convention.
+
+class Tuning(ctypes.Structure):
+    """hibf_gpu_tuning: schedule of the persistent query kernel (results never depend on it)."""
+
+    _fields_ = [(n, ctypes.c_uint32) for n in ("values_per_lane", "fetch_bytes", "counter_bits", "blocks_per_sm",
+                                                 "early_exit_first", "early_exit_step", "early_exit_stages",
+                                                 "early_exit_min")]
+
+    def as_dict(self) -> dict:
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "Tuning":
+        t = cls()
+        lib().hibf_gpu_tuning_default(ctypes.byref(t))
+        for k, v in d.items():
+            setattr(t, k, int(v))
+        return t
+
+
+class TuneTrial(ctypes.Structure):
+    _fields_ = [("tuning", Tuning), ("kernel_ms", ctypes.c_double)]
+
+
+TUNE_MEASURE_FN = ctypes.CFUNCTYPE(ci, ctypes.POINTER(Tuning), vp, ctypes.POINTER(ctypes.c_double))
+
+# (name, restype, argtypes); restype None means the int status convention, "void" no result.
 _SIGS = [
     ("hibf_gpu_last_error", ctypes.c_char_p, []),
     ("hibf_gpu_abi_version", ci, []),
@@ -122,6 +148,12 @@ _SIGS = [
     ("hibf_gpu_agent_capture_batch_d", None, [vp, ci, vp, vp, u64, vp, ci]),
     ("hibf_gpu_agent_replay", None, [vp]),
     ("hibf_gpu_agent_kernel_ms", None, [vp, ctypes.POINTER(ctypes.c_float)]),
+    ("hibf_gpu_tuning_default", "void", [ctypes.POINTER(Tuning)]),
+    ("hibf_gpu_agent_set_tuning", None, [vp, ctypes.POINTER(Tuning)]),
+    ("hibf_gpu_agent_get_tuning", None, [vp, ctypes.POINTER(Tuning)]),
+    ("hibf_gpu_tune_search", None, [ctypes.c_uint32, ctypes.c_uint32, TUNE_MEASURE_FN, vp,
+                                    ctypes.POINTER(TuneTrial), u64, u64p, ctypes.POINTER(Tuning)]),
+    ("hibf_gpu_agent_autotune", None, [vp, ci, vp, vp, u64, vp, ci, ci, ctypes.POINTER(TuneTrial), u64, u64p]),
     ("hibf_gpu_server_create", None, [vp, ci, u64, u64, u64, ctypes.POINTER(vp)]),
     ("hibf_gpu_server_destroy", None, [vp]),
     ("hibf_gpu_server_submit", None, [vp, vp, vp, u64, vp, ctypes.c_double, ci, u64p]),
@@ -165,7 +197,7 @@ def lib() -> ctypes.CDLL:
     L = ctypes.CDLL(str(LIB_PATH))
     for name, res, args in _SIGS:
         f = getattr(L, name)
-        f.restype = ci if res is None else res
+        f.restype = ci if res is None else (None if res == "void" else res)
         f.argtypes = args
     _lib = L
     return L

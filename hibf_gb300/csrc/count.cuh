@@ -27,8 +27,8 @@ struct row_params
 };
 
 // `added` (warp-uniform) masks went into the planes since the last flush, so planes k with 2^k > added are zero and
-// are not transposed.
-template <int LPV, int K, bool ATOMIC>
+// are not transposed.  Lane j of an LPV-lane group holds word W * j (+ the caller's offset of `out`) of its rows.
+template <int LPV, int K, bool ATOMIC, int W = 1>
 __device__ __forceinline__ void planes_flush_to(uint64_t (&P)[K], uint32_t * out, int lane, int added)
 {
     int const kmax = 32 - __clz(added);
@@ -65,39 +65,60 @@ __device__ __forceinline__ void planes_flush_to(uint64_t (&P)[K], uint32_t * out
         if constexpr (ATOMIC)
         {
             if (cl)
-                atomicAdd(out + 64 * j + lane, cl);
+                atomicAdd(out + 64 * W * j + lane, cl);
             if (ch)
-                atomicAdd(out + 64 * j + 32 + lane, ch);
+                atomicAdd(out + 64 * W * j + 32 + lane, ch);
         }
         else
         {
-            out[64 * j + lane] += cl;
-            out[64 * j + 32 + lane] += ch;
+            out[64 * W * j + lane] += cl;
+            out[64 * W * j + 32 + lane] += ch;
         }
     }
 }
 
-// One warp counts vals[0, n) into counts[0, 64 * LPV) with H hash functions.  ATOMIC: counters shared with other
-// warps.  Each lane keeps U values' H row offsets and 4 x H row words in registers, so the loads of four values are in
-// flight together.
-template <int LPV, int H, int K, bool ATOMIC>
+template <int W>
+__device__ __forceinline__ void load_row_words(uint64_t const * p, uint64_t (&w)[W])
+{
+    if constexpr (W == 1)
+    {
+        w[0] = __ldg(p);
+    }
+    else
+    {
+        ulonglong2 const x = __ldg(reinterpret_cast<ulonglong2 const *>(p));
+        w[0] = x.x;
+        w[1] = x.y;
+    }
+}
+
+// One warp counts vals[0, n) into counts[0, 64 * LPV * W) with H hash functions.  ATOMIC: counters shared with other
+// warps.  A row is read by LPV lanes, each loading W consecutive words (W = 2: one 16-byte load; the row stride
+// must then be even).  Each lane hashes U values per pass and keeps their H row offsets; the row words of
+// GS = 4 * UM masks per lane are loaded together, so GS * H * W loads per lane are in flight.  K planes count up to
+// 2^K - 1 masks between flushes.
+template <int LPV, int H, int K, bool ATOMIC, int UM = 1, int W = 1>
 __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const * __restrict__ vals, uint64_t n,
                                            uint32_t * counts, int lane)
 {
     constexpr int G = 32 / LPV;
-    constexpr int U = LPV >= 4 ? 1 : 4 / LPV;
+    constexpr int U = UM * (LPV >= 4 ? 1 : 4 / LPV);
     constexpr int STEPS = U * LPV;
+    constexpr int GS = 4 * UM;
     constexpr int BLOCK = 32 * U;
-    static_assert(STEPS % 4 == 0, "masks are consumed in groups of four");
+    static_assert(STEPS % GS == 0, "masks are consumed in groups of GS");
+    static_assert((1 << K) - 1 >= 2 * GS, "the planes must hold at least two groups between flushes");
     int const g = lane / LPV;
     int const j = lane % LPV;
-    bool const wj = static_cast<uint32_t>(j) < rp.bin_words;
-    uint64_t const * __restrict__ words = rp.words + j;
+    bool const wj = static_cast<uint32_t>(j * W) < rp.bin_words;
+    uint64_t const * __restrict__ words = rp.words + j * W;
 
-    uint64_t P[K];
+    uint64_t P[W][K];
 #pragma unroll
-    for (int k = 0; k < K; ++k)
-        P[k] = 0;
+    for (int e = 0; e < W; ++e)
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            P[e][k] = 0;
     int acc = 0;
 
     for (uint64_t base = 0; base < n; base += BLOCK)
@@ -112,13 +133,13 @@ __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const
             for (int i = 0; i < H; ++i)
                 off[u][i] = hash_row(v, c_hash_seeds[i], rp.hash_shift, rp.bin_size) * rp.row_words;
         }
-        // one group: four masks per lane (four sub-steps of LPV-lane groups), their h loads issued together
+        // one group: GS masks per lane (GS sub-steps of LPV-lane groups), their H * W loads issued together
         auto group = [&](int s)
         {
-            uint64_t w[4][H];
-            bool ok[4];
+            uint64_t w[GS][H][W];
+            bool ok[GS];
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
+            for (int t = 0; t < GS; ++t)
             {
                 int const step = s + t;
                 int const u = U == 1 ? 0 : step / LPV;
@@ -130,40 +151,59 @@ __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const
                     uint64_t o = off[u][i];
                     if constexpr (LPV > 1)
                         o = __shfl_sync(kFullMask, o, src);
-                    w[t][i] = ok[t] ? __ldg(words + o) : 0ull;
+                    if (ok[t])
+                        load_row_words<W>(words + o, w[t][i]);
+                    else
+#pragma unroll
+                        for (int e = 0; e < W; ++e)
+                            w[t][i][e] = 0ull;
                 }
             }
-            uint64_t m[4];
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
+            for (int t0 = 0; t0 < GS; t0 += 4)
             {
-                uint64_t x = w[t][0];
 #pragma unroll
-                for (int i = 1; i < H; ++i)
-                    x &= w[t][i];
-                m[t] = x;
-            }
-            planes_add4<K>(P, m[0], m[1], m[2], m[3]);
-            acc += 4;
-            if (acc > (1 << K) - 1 - 4)
-            {
-                planes_flush_to<LPV, K, ATOMIC>(P, counts, lane, acc);
-                acc = 0;
+                for (int e = 0; e < W; ++e)
+                {
+                    uint64_t m[4];
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+                    {
+                        uint64_t x = w[t0 + t][0][e];
+#pragma unroll
+                        for (int i = 1; i < H; ++i)
+                            x &= w[t0 + t][i][e];
+                        m[t] = x;
+                    }
+                    planes_add4<K>(P[e], m[0], m[1], m[2], m[3]);
+                }
+                acc += 4;
+                if (acc > (1 << K) - 1 - 4)
+                {
+#pragma unroll
+                    for (int e = 0; e < W; ++e)
+                        planes_flush_to<LPV, K, ATOMIC, W>(P[e], counts + 64 * e, lane, acc);
+                    acc = 0;
+                }
             }
         };
-        if constexpr (STEPS <= 4)
+        if constexpr (STEPS <= GS)
         {
             group(0);
         }
         else
         {
 #pragma unroll 1
-            for (int s = 0; s < STEPS; s += 4)
+            for (int s = 0; s < STEPS; s += GS)
                 group(s);
         }
     }
     if (acc)
-        planes_flush_to<LPV, K, ATOMIC>(P, counts, lane, acc);
+    {
+#pragma unroll
+        for (int e = 0; e < W; ++e)
+            planes_flush_to<LPV, K, ATOMIC, W>(P[e], counts + 64 * e, lane, acc);
+    }
 }
 
 // Rows wider than a warp (bin_words > 32): lanes stride over the words, set bits are added one by one.

@@ -4,18 +4,8 @@
 // Reference interface: seqan::hibf::hierarchical_interleaved_bloom_filter
 // (include/hibf/hierarchical_interleaved_bloom_filter.hpp, src/hierarchical_interleaved_bloom_filter.cpp).
 //
-// Query semantics (membership_for_impl HIBF.hpp:322-355, bulk_count_impl HIBF.hpp:463-496): for a query and an IBF,
-// count every value per technical bin, then scan the bins in order with a running sum in the counter type:
-//   deleted  -> keep the sum;   merged -> descend if sum >= t, reset;   last bin of a user bin -> report if sum >= t,
-//   reset.  We precompute per bin: MERGED, DELETED, RUN_END (last bin of a user bin's run) and HEAD (first bin of a
-// summation segment, i.e. bin 0 or the bin after a MERGED / RUN_END bin), which turns the scan into a segmented
-// prefix sum, done 32 bins at a time by a warp.  Counter wraparound: exact sums reduced modulo 2^(8*width) before
-// the comparison equal the reference's wrapping value_t sums.
-//
-// Work queue: task = (query, depth, IBF).  Claim indices below n_queries are the implicit root tasks; children are
-// appended behind them.  A worker that claims an index whose task is not written yet waits (bounded by a time
-// limit) until it appears or the count of unfinished tasks drops to zero.  Children are added to that count
-// before their parent retires, so zero means no task is queued or running anywhere.
+// The query kernel itself (semantics, work queue, tuning variants) is in query.cuh; this file holds the stores, the
+// result compaction passes, agents, the autotuner and their C-ABI entry points.
 
 #include <algorithm>
 #include <cstring>
@@ -28,6 +18,7 @@
 #include "count.cuh"
 #include "device.cuh"
 #include "hibf_internal.cuh"
+#include "query.cuh"
 
 namespace hibf_gb300
 {
@@ -37,359 +28,6 @@ void set_last_error(std::string msg);
 namespace
 {
 
-constexpr uint32_t F_MERGED = 1u;
-constexpr uint32_t F_DELETED = 2u;
-constexpr uint32_t F_RUN_END = 4u;
-constexpr uint32_t F_HEAD = 8u;
-
-constexpr unsigned long long kEmpty = ~0ull;
-// tasks shorter than this are counted in one stage (the reachability checks would cost more than they save)
-constexpr uint64_t kEarlyExitMinValues = 256;
-// checkpoints (percent of the task's values) after which the task stops if no segment can reach the threshold
-#ifndef HIBF_EE_FIRST
-#    define HIBF_EE_FIRST 30
-#endif
-#ifndef HIBF_EE_STEP
-#    define HIBF_EE_STEP 10
-#endif
-#ifndef HIBF_EE_STAGES
-#    define HIBF_EE_STAGES 7
-#endif
-constexpr uint64_t kEarlyExitFirst = HIBF_EE_FIRST;
-constexpr uint64_t kEarlyExitStep = HIBF_EE_STEP;
-constexpr int kEarlyExitStages = HIBF_EE_STAGES;
-// stats words: tasks, value visits the reference's traversal implies, value visits executed
-constexpr int kStats = 3;
-constexpr uint32_t kNodeBits = 26;
-constexpr uint32_t kNodeMask = (1u << kNodeBits) - 1u;
-
-// control words
-enum : int
-{
-    C_HEAD = 0,
-    C_TAIL = 1,
-    C_PENDING = 2,
-    C_NREC = 3,
-    C_ERROR = 4,
-    C_NLARGE = 5,
-    C_WORDS = 8
-};
-// error bits
-constexpr unsigned long long E_OVERFLOW_REC = 1ull;
-constexpr unsigned long long E_OVERFLOW_TASK = 2ull;
-constexpr unsigned long long E_TIMEOUT = 4ull;
-constexpr unsigned long long E_CYCLE = 8ull;
-
-struct query_params
-{
-    dev_node const * nodes;
-    uint2 const * descs; // .x = user bin or next IBF, .y = flags
-    uint64_t const * values;
-    uint64_t const * qoff;
-    uint64_t const * thr;
-    uint64_t count_mask;
-    uint64_t n_queries;
-    uint64_t q_base; // added to the query index in records and per-query counters (plain form)
-    uint32_t max_depth;
-    uint32_t counters_per_warp;
-    unsigned long long * tasks;
-    uint64_t task_cap;
-    unsigned long long * ctrl;
-    uint32_t * rec_q;
-    uint32_t * rec_ub;
-    unsigned long long * rec_cnt;
-    uint64_t rec_cap;
-    unsigned int * qcount;
-    unsigned long long * stats;
-    uint64_t wait_limit_ns;
-    int self_init; // single-block launch that resets its own control words first
-};
-
-__device__ __forceinline__ unsigned long long make_task(uint64_t q, uint32_t depth, uint32_t node)
-{
-    return (static_cast<unsigned long long>(q) << 32) | (static_cast<unsigned long long>(depth) << kNodeBits) | node;
-}
-
-__device__ unsigned long long wait_for_task(query_params const & p, unsigned long long slot)
-{
-    volatile unsigned long long * t = p.tasks + slot;
-    volatile unsigned long long * pending = p.ctrl + C_PENDING;
-    uint64_t start = 0;
-    for (uint32_t it = 0;; ++it)
-    {
-        unsigned long long v = *t;
-        if (v != kEmpty)
-            return v;
-        if (*pending == 0ull)
-        {
-            __threadfence();
-            return *t; // still empty: nothing is queued or running, the batch is done
-        }
-        if (it == 0)
-            start = globaltimer_ns();
-        else if ((it & 31u) == 0 && globaltimer_ns() - start > p.wait_limit_ns)
-        {
-            atomicOr(p.ctrl + C_ERROR, E_TIMEOUT);
-            return kEmpty;
-        }
-        __nanosleep(256);
-    }
-}
-
-// Whether some summation segment of IBF `nd` can still report or descend: its counts so far plus `remaining` for each
-// of its bins (a value adds at most one to every bin) reach the threshold, or could exceed the counter range (then
-// the wrapped sum is not bounded).  When no segment can, the task's outcome is already fixed -- nothing reported,
-// nothing descended -- exactly as if every value had been counted.
-__device__ bool any_segment_reachable(query_params const & p, dev_node const & nd, uint32_t const * counts,
-                                      uint64_t remaining, uint64_t thr, int lane)
-{
-    uint2 const * d = p.descs + nd.desc_offset;
-    unsigned long long carry = 0;
-    for (uint32_t c = 0; c < nd.bins; c += 32)
-    {
-        uint32_t const b = c + lane;
-        bool const valid = b < nd.bins;
-        uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
-        unsigned long long x = valid ? static_cast<unsigned long long>(counts[b]) + remaining : 0ull;
-        bool f = valid && (ds.y & F_HEAD);
-        if (lane == 0 && !f)
-            x += carry;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
-            int const fy = __shfl_up_sync(kFullMask, static_cast<int>(f), o);
-            if (lane >= o)
-            {
-                if (!f)
-                    x += y;
-                f = f || fy;
-            }
-        }
-        bool const ends = valid && (ds.y & (F_RUN_END | F_MERGED));
-        if (__any_sync(kFullMask, ends && (x >= thr || x > p.count_mask)))
-            return true;
-        unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
-        uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
-        carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
-    }
-    return false;
-}
-
-template <int H>
-__device__ void process_task(query_params const & p, unsigned long long task, uint32_t * counts, int lane,
-                             unsigned long long & n_tasks, unsigned long long & n_visits,
-                             unsigned long long & n_executed)
-{
-    uint64_t const q = task >> 32;
-    uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
-    uint32_t const k = static_cast<uint32_t>(task) & kNodeMask;
-    dev_node const nd = p.nodes[k];
-    uint64_t const b0 = p.qoff[q];
-    uint64_t const n = p.qoff[q + 1] - b0;
-    uint64_t const thr = p.thr[q];
-
-    uint32_t const ncount = nd.bin_words > 32 ? 64u * nd.bin_words : (64u << nd.lpv_log2);
-    for (uint32_t i = lane; i < ncount; i += 32)
-        counts[i] = 0;
-    __syncwarp();
-    row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
-    // Count in stages; after each stage stop if no segment can reach the threshold any more (exact: see above).
-    uint64_t done = 0;
-    bool hopeless = !any_segment_reachable(p, nd, counts, n, thr, lane);
-    if (!hopeless && n >= kEarlyExitMinValues)
-    {
-        for (int s = 0; s < kEarlyExitStages; ++s)
-        {
-            uint64_t const stop = n * (kEarlyExitFirst + s * kEarlyExitStep) / 100u;
-            warp_count_h<H, false>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
-            done = stop;
-            __syncwarp();
-            if (!any_segment_reachable(p, nd, counts, n - done, thr, lane))
-            {
-                hopeless = true;
-                break;
-            }
-        }
-    }
-    if (!hopeless)
-    {
-        warp_count_h<H, false>(rp, nd.lpv_log2, p.values + b0 + done, n - done, counts, lane);
-        done = n;
-    }
-    __syncwarp();
-    if (hopeless)
-    {
-        if (lane == 0)
-        {
-            __threadfence();
-            atomicAdd(p.ctrl + C_PENDING, ~0ull); // retires without results or children
-            ++n_tasks;
-            n_visits += n;
-            n_executed += done;
-        }
-        return;
-    }
-
-    uint2 const * d = p.descs + nd.desc_offset;
-    unsigned long long carry = 0;
-    unsigned const lt_mask = (1u << lane) - 1u;
-    uint64_t const gq = q + p.q_base;
-    for (uint32_t c = 0; c < nd.bins; c += 32)
-    {
-        uint32_t const b = c + lane;
-        bool const valid = b < nd.bins;
-        uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
-        unsigned long long x = valid ? counts[b] : 0ull;
-        bool f = valid && (ds.y & F_HEAD);
-        if (lane == 0 && !f)
-            x += carry;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
-            int const fy = __shfl_up_sync(kFullMask, static_cast<int>(f), o);
-            if (lane >= o)
-            {
-                if (!f)
-                    x += y;
-                f = f || fy;
-            }
-        }
-        uint64_t const sum = x & p.count_mask;
-        bool const pass = sum >= thr;
-        bool const emit_ub = valid && (ds.y & F_RUN_END) && pass;
-        bool const emit_child = valid && (ds.y & F_MERGED) && pass;
-
-        unsigned const rb = __ballot_sync(kFullMask, emit_ub);
-        if (rb)
-        {
-            unsigned const nr = __popc(rb);
-            unsigned long long base = 0;
-            if (lane == 0)
-            {
-                base = atomicAdd(p.ctrl + C_NREC, static_cast<unsigned long long>(nr));
-                atomicAdd(p.qcount + gq, nr);
-                if (base + nr > p.rec_cap)
-                    atomicOr(p.ctrl + C_ERROR, E_OVERFLOW_REC);
-            }
-            base = __shfl_sync(kFullMask, base, 0);
-            if (emit_ub)
-            {
-                unsigned long long const r = base + __popc(rb & lt_mask);
-                if (r < p.rec_cap)
-                {
-                    p.rec_q[r] = static_cast<uint32_t>(gq);
-                    p.rec_ub[r] = ds.x;
-                    p.rec_cnt[r] = sum;
-                }
-            }
-        }
-        unsigned const cb = __ballot_sync(kFullMask, emit_child);
-        if (cb)
-        {
-            unsigned const nc = __popc(cb);
-            if (depth + 1u > p.max_depth)
-            {
-                if (lane == 0)
-                    atomicOr(p.ctrl + C_ERROR, E_CYCLE);
-            }
-            else
-            {
-                unsigned long long base = 0;
-                if (lane == 0)
-                {
-                    atomicAdd(p.ctrl + C_PENDING, static_cast<unsigned long long>(nc));
-                    base = atomicAdd(p.ctrl + C_TAIL, static_cast<unsigned long long>(nc));
-                }
-                base = __shfl_sync(kFullMask, base, 0);
-                if (emit_child)
-                {
-                    unsigned long long const s = base + __popc(cb & lt_mask);
-                    if (s < p.task_cap)
-                    {
-                        atomicExch(p.tasks + s, make_task(q, depth + 1u, ds.x));
-                    }
-                    else
-                    {
-                        atomicOr(p.ctrl + C_ERROR, E_OVERFLOW_TASK);
-                        atomicAdd(p.ctrl + C_PENDING, ~0ull); // this child will never run
-                    }
-                    __threadfence();
-                }
-            }
-        }
-        unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
-        uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
-        carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
-    }
-    __syncwarp();
-    if (lane == 0)
-    {
-        __threadfence();
-        atomicAdd(p.ctrl + C_PENDING, ~0ull); // this task retires
-        ++n_tasks;
-        n_visits += n;
-        n_executed += done;
-    }
-}
-
-// H = the hierarchy's hash function count (one value for all IBFs, as in the reference's build).
-// HIBF_QUERY_MIN_BLOCKS blocks of eight warps per SM bound the register budget (2: 128 registers per thread,
-// measured fastest: the kernel is limited by the memory system's random-access rate, not by occupancy).
-#ifndef HIBF_QUERY_MIN_BLOCKS
-#    define HIBF_QUERY_MIN_BLOCKS 2
-#endif
-template <int H>
-__global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_params p)
-{
-    extern __shared__ uint32_t s_counts[];
-    int const lane = threadIdx.x & 31;
-    uint32_t * counts = s_counts + (threadIdx.x >> 5) * p.counters_per_warp;
-    if (p.self_init)
-    {
-        if (threadIdx.x == 0)
-        {
-            p.ctrl[C_HEAD] = 0;
-            p.ctrl[C_TAIL] = 0;
-            p.ctrl[C_PENDING] = p.n_queries;
-            __threadfence();
-        }
-        __syncthreads();
-    }
-    unsigned long long n_tasks = 0, n_visits = 0, n_executed = 0;
-    for (;;)
-    {
-        unsigned long long idx = 0;
-        if (lane == 0)
-            idx = atomicAdd(p.ctrl + C_HEAD, 1ull);
-        idx = __shfl_sync(kFullMask, idx, 0);
-        unsigned long long task;
-        if (idx < p.n_queries)
-        {
-            task = make_task(idx, 0u, 0u);
-        }
-        else
-        {
-            unsigned long long const slot = idx - p.n_queries;
-            if (slot >= p.task_cap)
-                break;
-            task = 0;
-            if (lane == 0)
-                task = wait_for_task(p, slot);
-            task = __shfl_sync(kFullMask, task, 0);
-            if (task == kEmpty)
-                break;
-        }
-        process_task<H>(p, task, counts, lane, n_tasks, n_visits, n_executed);
-    }
-    if (lane == 0 && n_tasks)
-    {
-        atomicAdd(p.stats + 0, n_tasks);
-        atomicAdd(p.stats + 1, n_visits);
-        atomicAdd(p.stats + 2, n_executed);
-    }
-}
 
 __global__ void k_init_ctrl(unsigned long long * ctrl, unsigned long long * stats, uint64_t n_queries)
 {
@@ -671,25 +309,6 @@ __global__ void k_hibf_emplace(uint64_t * __restrict__ words, uint64_t bin_size,
     }
 }
 
-using query_kernel_t = void (*)(query_params);
-
-query_kernel_t query_kernel(uint32_t h)
-{
-    switch (h)
-    {
-    case 1:
-        return k_query<1>;
-    case 2:
-        return k_query<2>;
-    case 3:
-        return k_query<3>;
-    case 4:
-        return k_query<4>;
-    default:
-        return k_query<5>;
-    }
-}
-
 unsigned grid_cap(uint64_t work, unsigned block, unsigned per_sm = 16)
 {
     uint64_t const want = (work + block - 1) / block;
@@ -712,7 +331,9 @@ struct hibf_gpu_agent
     int status{HIBF_GPU_OK};
     uint64_t last_tasks{}, last_visits{}, last_executed{};
     uint64_t cap_queries{}, cap_tasks{}, cap_results{};
-    int max_blocks_per_sm{};
+    hibf_gpu_tuning tune{};                // schedule of the persistent kernel
+    int variant{0};                        // kernel variant of `tune`
+    int max_blocks[kQueryVariants]{};      // resident 256-thread blocks per SM of each variant
     // device workspace
     dbuf ctrl, stats, tasks, rec_q, rec_ub, rec_cnt, qcount, cursor, roff, bsum, out_ids, out_cnt, out_cntw, large;
     // host-call staging
@@ -780,6 +401,10 @@ query_params base_params(hibf_gpu_agent * a, uint64_t const * d_values, uint64_t
     p.stats = a->stats.as<unsigned long long>();
     p.wait_limit_ns = 10ull * 1000 * 1000 * 1000;
     p.self_init = 0;
+    p.ee_first = a->tune.early_exit_first;
+    p.ee_step = a->tune.early_exit_step;
+    p.ee_stages = a->tune.early_exit_stages;
+    p.ee_min = a->tune.early_exit_min;
     return p;
 }
 
@@ -845,7 +470,9 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
     if (nq)
     {
         query_params p = base_params(a, d_values, d_qoff, d_thr, nq, mask_for(mode, width));
-        uint64_t const full = static_cast<uint64_t>(sm_count()) * static_cast<uint64_t>(a->max_blocks_per_sm);
+        int const fit = a->max_blocks[a->variant];
+        int const per_sm = a->tune.blocks_per_sm ? std::min<int>(fit, static_cast<int>(a->tune.blocks_per_sm)) : fit;
+        uint64_t const full = static_cast<uint64_t>(sm_count()) * static_cast<uint64_t>(per_sm);
         uint64_t const want = (nq + 7) / 8;
         unsigned const grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min(full, want)));
         // inside a stream capture an event record only orders work unless it is marked external; external records
@@ -854,7 +481,7 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         HG_CUDA(cudaStreamIsCapturing(s, &cap));
         unsigned const rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
-        query_kernel(h->hash_count)<<<grid, 256, query_smem(h), s>>>(p);
+        query_kernel(h->hash_count, a->variant)<<<grid, 256, query_smem(h), s>>>(p);
         HG_CUDA(cudaGetLastError());
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k1, s, rec_flags));
     }
@@ -879,7 +506,7 @@ void launch_plain(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         p.self_init = 1;
         HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u) * 8, s));
         p.task_cap = std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u);
-        query_kernel(h->hash_count)<<<1, 256, query_smem(h), s>>>(p);
+        query_kernel(h->hash_count, a->variant)<<<1, 256, query_smem(h), s>>>(p);
         HG_CUDA(cudaGetLastError());
     }
     launch_postprocess(a, nq, mode, width);
@@ -900,6 +527,8 @@ int read_status(hibf_gpu_agent * a)
         return HIBF_GPU_ERR_TIMEOUT;
     if (e & E_CYCLE)
         return HIBF_GPU_ERR_CYCLE;
+    if (e & E_VARIANT)
+        return HIBF_GPU_ERR_LOGIC;
     if (e & (E_OVERFLOW_REC | E_OVERFLOW_TASK))
         return HIBF_GPU_ERR_OVERFLOW;
     return HIBF_GPU_OK;
@@ -978,10 +607,291 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
     HG_CUDA(cudaStreamSynchronize(a->stream));
 }
 
+// Whether the tuned kernel variants apply: at most 3 hash functions and rows of at most 4 words.
+bool variants_apply(uint32_t hash_count, uint64_t max_row_words)
+{
+    return hash_count <= 3 && max_row_words <= 4;
+}
+
+uint64_t max_bin_words(hibf_gpu_hibf const * h)
+{
+    uint64_t m = 0;
+    for (uint64_t w : h->bin_words)
+        m = std::max(m, w);
+    return m;
+}
+
+// The kernel variant of a schedule (kVariantTable), or -1 when no kernel has that combination.
+int variant_of(hibf_gpu_tuning const & t)
+{
+    for (int v = 0; v < kQueryVariants; ++v)
+        if (t.values_per_lane == static_cast<uint32_t>(kVariantTable[v][0]) &&
+            t.fetch_bytes == static_cast<uint32_t>(8 * kVariantTable[v][1]) &&
+            t.counter_bits == static_cast<uint32_t>(kVariantTable[v][2]))
+            return v;
+    return -1;
+}
+
+void check_tuning(hibf_gpu_tuning const & t, hibf_gpu_hibf const * h)
+{
+    int const v = variant_of(t);
+    if (v < 0)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "no query kernel for this (values_per_lane, fetch_bytes, counter_bits)");
+    if (v != 0 && !variants_apply(h->hash_count, max_bin_words(h)))
+        fail(HIBF_GPU_ERR_INVALID_ARG, "tuned kernel variants need at most 3 hash functions and rows of at most 4 "
+                                       "words; this hierarchy takes the default (1, 8, 7)");
+    if (t.blocks_per_sm > 32)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "blocks_per_sm must be in [0, 32]");
+    if (t.early_exit_stages)
+    {
+        uint64_t const last = t.early_exit_first + static_cast<uint64_t>(t.early_exit_stages - 1) * t.early_exit_step;
+        if (t.early_exit_first == 0 || last >= 100 || (t.early_exit_stages > 1 && t.early_exit_step == 0))
+            fail(HIBF_GPU_ERR_INVALID_ARG, "early-exit checkpoints must be increasing percentages in (0, 100)");
+    }
+}
+
+hibf_gpu_tuning with_schedule(hibf_gpu_tuning t, uint32_t first, uint32_t step)
+{
+    t.early_exit_first = first;
+    t.early_exit_step = step;
+    t.early_exit_stages = first == 0 ? 0u : (step == 0 ? 1u : (90u - first) / step + 1u); // checkpoints up to 90%
+    return t;
+}
+
+bool same_schedule(hibf_gpu_tuning const & a, hibf_gpu_tuning const & b)
+{
+    return a.early_exit_stages == b.early_exit_stages &&
+           (a.early_exit_stages == 0 || (a.early_exit_first == b.early_exit_first && a.early_exit_step == b.early_exit_step));
+}
+
+// Stage 1: every kernel variant at 1 block per SM and at as many as fit; stage 2: the early-exit checkpoints with
+// the fastest kernel; stage 3: the minimum task length for early exit.
+void tune_search(uint32_t hash_count, uint64_t max_row_words, hibf_gpu_tune_measure_fn measure, void * user,
+                 std::vector<hibf_gpu_tune_trial> & trials, hibf_gpu_tuning & best)
+{
+    hibf_gpu_tuning base{};
+    hibf_gpu_tuning_default(&base);
+    double best_ms = 0;
+    auto run = [&](hibf_gpu_tuning const & t)
+    {
+        double ms = 0;
+        int const st = measure(&t, user, &ms);
+        if (st != HIBF_GPU_OK)
+            fail(st, "autotune measurement failed");
+        if (!(ms >= 0))
+            fail(HIBF_GPU_ERR_INVALID_ARG, "autotune measurement returned a negative time");
+        trials.push_back(hibf_gpu_tune_trial{t, ms});
+        if (trials.size() == 1 || ms < best_ms)
+        {
+            best_ms = ms;
+            best = t;
+        }
+    };
+    for (int v = 0; v < kQueryVariants; ++v)
+    {
+        if (v != 0 && !variants_apply(hash_count, max_row_words))
+            break;
+        if (max_row_words < 2 && kVariantTable[v][1] != 1)
+            continue; // 16-byte fetches need rows of two or more words
+        for (uint32_t bps : {0u, 1u})
+        {
+            hibf_gpu_tuning t = base;
+            t.values_per_lane = static_cast<uint32_t>(kVariantTable[v][0]);
+            t.fetch_bytes = static_cast<uint32_t>(8 * kVariantTable[v][1]);
+            t.counter_bits = static_cast<uint32_t>(kVariantTable[v][2]);
+            t.blocks_per_sm = bps;
+            run(t);
+        }
+    }
+    hibf_gpu_tuning const k = best;
+    static constexpr uint32_t schedules[][2] = {{0, 0}, {10, 10}, {20, 10}, {30, 10}, {50, 10}, {30, 20}, {50, 20}};
+    for (auto const & sch : schedules)
+    {
+        hibf_gpu_tuning const t = with_schedule(k, sch[0], sch[1]);
+        if (!same_schedule(t, k))
+            run(t);
+    }
+    hibf_gpu_tuning const e = best;
+    if (e.early_exit_stages)
+        for (uint32_t m : {64u, 128u, 256u, 512u, 1024u})
+            if (m != e.early_exit_min)
+            {
+                hibf_gpu_tuning t = e;
+                t.early_exit_min = m;
+                run(t);
+            }
+}
+
+// Device measurement of one schedule for hibf_gpu_agent_autotune.
+struct autotune_ctx
+{
+    hibf_gpu_agent * a;
+    int mode, width, reps;
+    uint64_t const *values, *qoff, *thr;
+    uint64_t nq;
+    std::vector<uint64_t> ref_roff, ref_ids, ref_cnt, roff, ids, cnt;
+    bool have_ref{false};
+};
+
+void fetch_batch_results(autotune_ctx & c, std::vector<uint64_t> & roff, std::vector<uint64_t> & ids,
+                         std::vector<uint64_t> & cnt)
+{
+    hibf_gpu_agent * a = c.a;
+    roff.resize(c.nq + 1);
+    HG_CUDA(cudaMemcpyAsync(roff.data(), a->roff.p, (c.nq + 1) * 8, cudaMemcpyDeviceToHost, a->stream));
+    HG_CUDA(cudaStreamSynchronize(a->stream));
+    uint64_t const nr = roff[c.nq];
+    ids.resize(nr);
+    cnt.resize(c.mode == HIBF_GPU_QUERY_COUNT ? nr : 0);
+    if (nr)
+    {
+        HG_CUDA(cudaMemcpyAsync(ids.data(), a->out_ids.p, nr * 8, cudaMemcpyDeviceToHost, a->stream));
+        if (c.mode == HIBF_GPU_QUERY_COUNT)
+            HG_CUDA(cudaMemcpyAsync(cnt.data(), a->out_cnt.p, nr * 8, cudaMemcpyDeviceToHost, a->stream));
+    }
+    HG_CUDA(cudaStreamSynchronize(a->stream));
+}
+
+int autotune_measure(hibf_gpu_tuning const * t, void * user, double * kernel_ms)
+{
+    return guarded(
+        [&]
+        {
+            autotune_ctx & c = *static_cast<autotune_ctx *>(user);
+            hibf_gpu_agent * a = c.a;
+            a->tune = *t;
+            a->variant = variant_of(*t);
+            std::vector<double> ms;
+            for (int r = -1; r < c.reps; ++r)
+            {
+                launch_batch(a, c.mode, c.values, c.qoff, c.thr, c.nq, c.width);
+                int const st = read_status(a);
+                if (st != HIBF_GPU_OK)
+                    fail(st, "autotune batch failed (reserve enough tasks and results for the sample)");
+                if (r < 0)
+                {
+                    auto & roff = c.have_ref ? c.roff : c.ref_roff;
+                    auto & ids = c.have_ref ? c.ids : c.ref_ids;
+                    auto & cnt = c.have_ref ? c.cnt : c.ref_cnt;
+                    fetch_batch_results(c, roff, ids, cnt);
+                    if (c.have_ref && (roff != c.ref_roff || ids != c.ref_ids || cnt != c.ref_cnt))
+                        fail(HIBF_GPU_ERR_LOGIC, "a kernel schedule changed the query results");
+                    c.have_ref = true;
+                    continue;
+                }
+                float k = 0;
+                HG_CUDA(cudaEventElapsedTime(&k, a->ev_k0, a->ev_k1));
+                ms.push_back(k);
+            }
+            std::sort(ms.begin(), ms.end());
+            *kernel_ms = ms.empty() ? 0.0 : ms[ms.size() / 2];
+        });
+}
+
 } // namespace
 
 extern "C"
 {
+    void hibf_gpu_tuning_default(hibf_gpu_tuning * t)
+    {
+        if (!t)
+            return;
+        t->values_per_lane = 1;
+        t->fetch_bytes = 8;
+        t->counter_bits = 7;
+        t->blocks_per_sm = 0;
+        t->early_exit_first = 30;
+        t->early_exit_step = 10;
+        t->early_exit_stages = 7;
+        t->early_exit_min = 256;
+    }
+
+    int hibf_gpu_agent_set_tuning(hibf_gpu_agent * a, hibf_gpu_tuning const * t)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !t)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                check_tuning(*t, a->h);
+                a->tune = *t;
+                a->variant = variant_of(*t);
+                if (a->graph)
+                {
+                    HG_CUDA(cudaGraphExecDestroy(a->graph));
+                    a->graph = nullptr;
+                }
+            });
+    }
+
+    int hibf_gpu_agent_get_tuning(hibf_gpu_agent * a, hibf_gpu_tuning * t)
+    {
+        if (!a || !t)
+            return HIBF_GPU_ERR_INVALID_ARG;
+        *t = a->tune;
+        return HIBF_GPU_OK;
+    }
+
+    int hibf_gpu_tune_search(uint32_t hash_count, uint32_t max_row_words, hibf_gpu_tune_measure_fn measure,
+                             void * user, hibf_gpu_tune_trial * trials, uint64_t cap, uint64_t * n_trials,
+                             hibf_gpu_tuning * best)
+    {
+        return guarded(
+            [&]
+            {
+                if (!measure || !best || hash_count == 0 || hash_count > 5)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                std::vector<hibf_gpu_tune_trial> all;
+                tune_search(hash_count, max_row_words, measure, user, all, *best);
+                if (n_trials)
+                    *n_trials = all.size();
+                if (trials)
+                    std::copy_n(all.begin(), std::min<uint64_t>(cap, all.size()), trials);
+            });
+    }
+
+    int hibf_gpu_agent_autotune(hibf_gpu_agent * a, int mode, uint64_t const * d_values,
+                                uint64_t const * d_query_offsets, uint64_t n_queries, uint64_t const * d_thresholds,
+                                int width, int reps, hibf_gpu_tune_trial * trials, uint64_t cap, uint64_t * n_trials)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !d_query_offsets || !d_thresholds || n_queries == 0 || reps < 1 || reps > 100)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                check_mode(mode, width, nullptr, n_queries);
+                ensure_capacity(a, n_queries, std::max<uint64_t>(a->cap_tasks, n_queries * 4 + 1024),
+                                std::max<uint64_t>(a->cap_results, n_queries * 4 + 1024));
+                if (a->graph)
+                {
+                    HG_CUDA(cudaGraphExecDestroy(a->graph));
+                    a->graph = nullptr;
+                }
+                autotune_ctx c{a, mode, width, reps, d_values, d_query_offsets, d_thresholds, n_queries, {}, {}, {},
+                               {}, {}, {}};
+                hibf_gpu_tuning const before = a->tune;
+                std::vector<hibf_gpu_tune_trial> all;
+                hibf_gpu_tuning best{};
+                try
+                {
+                    tune_search(a->h->hash_count, max_bin_words(a->h), autotune_measure, &c, all, best);
+                }
+                catch (...)
+                {
+                    a->tune = before;
+                    a->variant = variant_of(before);
+                    throw;
+                }
+                a->tune = best;
+                a->variant = variant_of(best);
+                if (n_trials)
+                    *n_trials = all.size();
+                if (trials)
+                    std::copy_n(all.begin(), std::min<uint64_t>(cap, all.size()), trials);
+            });
+    }
+
+
 
     int hibf_gpu_hibf_create(uint64_t n_user_bins, uint64_t n_ibfs, uint64_t const * bins,
                              uint64_t const * bin_sizes, uint64_t const * hash_funs, uint64_t const * next_ibf_id,
@@ -1137,9 +1047,10 @@ extern "C"
                                             cudaMemcpyHostToDevice, h->stream));
                     HG_CUDA(cudaStreamSynchronize(h->stream));
                     size_t const smem = query_smem(h);
-                    HG_CUDA(cudaFuncSetAttribute(query_kernel(h->hash_count),
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 static_cast<int>(std::max<size_t>(smem, 48 * 1024))));
+                    for (int v = 0; v < kQueryVariants; ++v)
+                        HG_CUDA(cudaFuncSetAttribute(query_kernel(h->hash_count, v),
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     static_cast<int>(std::max<size_t>(smem, 48 * 1024))));
                 }
                 catch (...)
                 {
@@ -1312,10 +1223,14 @@ extern "C"
                     a->stats.ensure(kStats * 8);
                     a->h_ctrl.ensure(C_WORDS * 8);
                     a->h_stats.ensure(kStats * 8);
-                    int nb = 0;
-                    HG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, query_kernel(h->hash_count), 256,
-                                                                          query_smem(h)));
-                    a->max_blocks_per_sm = std::max(1, nb);
+                    for (int v = 0; v < kQueryVariants; ++v)
+                    {
+                        int nb = 0;
+                        HG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, query_kernel(h->hash_count, v), 256,
+                                                                              query_smem(h)));
+                        a->max_blocks[v] = std::max(1, nb);
+                    }
+                    hibf_gpu_tuning_default(&a->tune);
                     ensure_capacity(a, 1024, 4096, 4096);
                 }
                 catch (...)
@@ -1604,7 +1519,7 @@ extern "C"
                 query_params p = base_params(a, a->in_values.as<uint64_t>(), a->in_qoff.as<uint64_t>(),
                                              a->in_thr.as<uint64_t>(), 0, 0xFFFFu);
                 p.wait_limit_ns = static_cast<uint64_t>(limit_ms * 1e6);
-                query_kernel(a->h->hash_count)<<<1, 256, query_smem(a->h), s>>>(p);
+                query_kernel(a->h->hash_count, a->variant)<<<1, 256, query_smem(a->h), s>>>(p);
                 HG_CUDA(cudaGetLastError());
                 int const st = read_status(a);
                 if (st != HIBF_GPU_ERR_TIMEOUT)

@@ -1,0 +1,487 @@
+// query.cuh -- the persistent (query, IBF) work-queue kernel of the HIBF query, templated on the hash function count
+// H and on a tuning variant V (values hashed per lane, register counter width, bytes fetched per lane).
+//
+// Query semantics (membership_for_impl HIBF.hpp:322-355, bulk_count_impl HIBF.hpp:463-496): for a query and an IBF,
+// count every value per technical bin, then scan the bins in order with a running sum in the counter type:
+//   deleted  -> keep the sum;   merged -> descend if sum >= t, reset;   last bin of a user bin -> report if sum >= t,
+//   reset.  Per bin the host precomputes MERGED, DELETED, RUN_END (last bin of a user bin's run) and HEAD (first bin
+// of a summation segment: bin 0 or the bin after a MERGED / RUN_END bin), which turns the scan into a segmented
+// prefix sum, done 32 bins at a time by a warp.  Counter wraparound: exact sums reduced modulo 2^(8*width) before
+// the comparison equal the reference's wrapping value_t sums.
+//
+// Work queue: task = (query, depth, IBF).  Claim indices below n_queries are the implicit root tasks; children are
+// appended behind them.  A worker that claims an index whose task is not written yet waits (bounded by a time
+// limit) until it appears or the count of unfinished tasks drops to zero.  Children are added to that count
+// before their parent retires, so zero means no task is queued or running anywhere.
+//
+// The kernels are instantiated per H in query_h<H>.cu (one translation unit each, compiled in parallel); the host
+// side (hibf.cu) picks one through query_kernel(h, variant).
+#pragma once
+
+#include "count.cuh"
+#include "device.cuh"
+#include "hibf_internal.cuh"
+
+namespace hibf_gb300
+{
+
+constexpr uint32_t F_MERGED = 1u;
+constexpr uint32_t F_DELETED = 2u;
+constexpr uint32_t F_RUN_END = 4u;
+constexpr uint32_t F_HEAD = 8u;
+
+constexpr unsigned long long kEmpty = ~0ull;
+// stats words: tasks, value visits the reference's traversal implies, value visits executed
+constexpr int kStats = 3;
+constexpr uint32_t kNodeBits = 26;
+constexpr uint32_t kNodeMask = (1u << kNodeBits) - 1u;
+
+// control words
+enum : int
+{
+    C_HEAD = 0,
+    C_TAIL = 1,
+    C_PENDING = 2,
+    C_NREC = 3,
+    C_ERROR = 4,
+    C_NLARGE = 5,
+    C_WORDS = 8
+};
+// error bits
+constexpr unsigned long long E_OVERFLOW_REC = 1ull;
+constexpr unsigned long long E_OVERFLOW_TASK = 2ull;
+constexpr unsigned long long E_TIMEOUT = 4ull;
+constexpr unsigned long long E_CYCLE = 8ull;
+constexpr unsigned long long E_VARIANT = 16ull; // a tuned variant met a row of more than 4 words (host rejects this)
+
+// Tuning variants of the counting loop (compile-time), one kernel each:
+//   UM  values hashed per lane per pass, as a multiple of max(1, 4 / lanes-per-row): more row loads in flight
+//   K   width in bits of the per-lane bit-sliced counters (flushed to shared memory every 2^K - 4 masks)
+//   W   64-bit words fetched per lane per row (1: 8-byte loads; 2: 16-byte loads, half the lanes per row)
+// Every variant computes the same exact counts; only the schedule differs.
+constexpr int kQueryVariants = 6;
+// {UM, W, K} of variant V; variant 0 is the default schedule.
+constexpr int kVariantTable[kQueryVariants][3] = {{1, 1, 7}, {2, 1, 7}, {1, 1, 5}, {2, 1, 5}, {1, 2, 7}, {1, 2, 5}};
+template <int V>
+struct qvariant
+{
+    static constexpr int UM = kVariantTable[V][0];
+    static constexpr int W = kVariantTable[V][1];
+    static constexpr int K = kVariantTable[V][2];
+};
+
+struct query_params
+{
+    dev_node const * nodes;
+    uint2 const * descs; // .x = user bin or next IBF, .y = flags
+    uint64_t const * values;
+    uint64_t const * qoff;
+    uint64_t const * thr;
+    uint64_t count_mask;
+    uint64_t n_queries;
+    uint64_t q_base; // added to the query index in records and per-query counters (plain form)
+    uint32_t max_depth;
+    uint32_t counters_per_warp;
+    unsigned long long * tasks;
+    uint64_t task_cap;
+    unsigned long long * ctrl;
+    uint32_t * rec_q;
+    uint32_t * rec_ub;
+    unsigned long long * rec_cnt;
+    uint64_t rec_cap;
+    unsigned int * qcount;
+    unsigned long long * stats;
+    uint64_t wait_limit_ns;
+    int self_init; // single-block launch that resets its own control words first
+    // early exit: after counting first + s * step percent of a task's values (s < stages), stop when no segment can
+    // reach the threshold any more; tasks shorter than ee_min values are counted in one stage
+    uint32_t ee_first;
+    uint32_t ee_step;
+    uint32_t ee_stages;
+    uint32_t ee_min;
+};
+
+using query_kernel_t = void (*)(query_params);
+
+__device__ __forceinline__ unsigned long long make_task(uint64_t q, uint32_t depth, uint32_t node)
+{
+    return (static_cast<unsigned long long>(q) << 32) | (static_cast<unsigned long long>(depth) << kNodeBits) | node;
+}
+
+__device__ inline unsigned long long wait_for_task(query_params const & p, unsigned long long slot)
+{
+    volatile unsigned long long * t = p.tasks + slot;
+    volatile unsigned long long * pending = p.ctrl + C_PENDING;
+    uint64_t start = 0;
+    for (uint32_t it = 0;; ++it)
+    {
+        unsigned long long v = *t;
+        if (v != kEmpty)
+            return v;
+        if (*pending == 0ull)
+        {
+            __threadfence();
+            return *t; // still empty: nothing is queued or running, the batch is done
+        }
+        if (it == 0)
+            start = globaltimer_ns();
+        else if ((it & 31u) == 0 && globaltimer_ns() - start > p.wait_limit_ns)
+        {
+            atomicOr(p.ctrl + C_ERROR, E_TIMEOUT);
+            return kEmpty;
+        }
+        __nanosleep(256);
+    }
+}
+
+// Whether some summation segment of IBF `nd` can still report or descend: its counts so far plus `remaining` for each
+// of its bins (a value adds at most one to every bin) reach the threshold, or could exceed the counter range (then
+// the wrapped sum is not bounded).  When no segment can, the task's outcome is already fixed -- nothing reported,
+// nothing descended -- exactly as if every value had been counted.
+__device__ inline bool any_segment_reachable(query_params const & p, dev_node const & nd, uint32_t const * counts,
+                                             uint64_t remaining, uint64_t thr, int lane)
+{
+    uint2 const * d = p.descs + nd.desc_offset;
+    unsigned long long carry = 0;
+    for (uint32_t c = 0; c < nd.bins; c += 32)
+    {
+        uint32_t const b = c + lane;
+        bool const valid = b < nd.bins;
+        uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
+        unsigned long long x = valid ? static_cast<unsigned long long>(counts[b]) + remaining : 0ull;
+        bool f = valid && (ds.y & F_HEAD);
+        if (lane == 0 && !f)
+            x += carry;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
+            int const fy = __shfl_up_sync(kFullMask, static_cast<int>(f), o);
+            if (lane >= o)
+            {
+                if (!f)
+                    x += y;
+                f = f || fy;
+            }
+        }
+        bool const ends = valid && (ds.y & (F_RUN_END | F_MERGED));
+        if (__any_sync(kFullMask, ends && (x >= thr || x > p.count_mask)))
+            return true;
+        unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
+        uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
+        carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
+    }
+    return false;
+}
+
+// Counting with variant V.  Variant 0 handles every row width; the tuned variants only rows of up to 4 words (the
+// host offers them only for such hierarchies, and process_task refuses wider rows).
+template <int H, int V>
+__device__ __forceinline__ void count_variant(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
+                                              uint64_t n, uint32_t * counts, int lane)
+{
+    using Q = qvariant<V>;
+    switch (lpv_log2)
+    {
+    case 0:
+        warp_count<1, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane);
+        break;
+    case 1:
+        if constexpr (Q::W == 2)
+            warp_count<1, H, Q::K, false, Q::UM, 2>(rp, vals, n, counts, lane);
+        else
+            warp_count<2, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane);
+        break;
+    case 2:
+        if constexpr (Q::W == 2)
+            warp_count<2, H, Q::K, false, Q::UM, 2>(rp, vals, n, counts, lane);
+        else
+            warp_count<4, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane);
+        break;
+    default:
+        if constexpr (V == 0)
+            warp_count_h<H, false>(rp, lpv_log2, vals, n, counts, lane);
+    }
+}
+
+template <int H, int V>
+__device__ void process_task(query_params const & p, unsigned long long task, uint32_t * counts, int lane,
+                             unsigned long long & n_tasks, unsigned long long & n_visits,
+                             unsigned long long & n_executed)
+{
+    uint64_t const q = task >> 32;
+    uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
+    uint32_t const k = static_cast<uint32_t>(task) & kNodeMask;
+    dev_node const nd = p.nodes[k];
+    uint64_t const b0 = p.qoff[q];
+    uint64_t const n = p.qoff[q + 1] - b0;
+    uint64_t const thr = p.thr[q];
+
+    if (V != 0 && nd.lpv_log2 > 2)
+    {
+        if (lane == 0)
+        {
+            atomicOr(p.ctrl + C_ERROR, E_VARIANT);
+            __threadfence();
+            atomicAdd(p.ctrl + C_PENDING, ~0ull);
+        }
+        return;
+    }
+    uint32_t const ncount = nd.bin_words > 32 ? 64u * nd.bin_words : (64u << nd.lpv_log2);
+    for (uint32_t i = lane; i < ncount; i += 32)
+        counts[i] = 0;
+    __syncwarp();
+    row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
+    // Count in stages; after each stage stop if no segment can reach the threshold any more (exact: see above).
+    uint64_t done = 0;
+    bool hopeless = !any_segment_reachable(p, nd, counts, n, thr, lane);
+    if (!hopeless && n >= p.ee_min)
+    {
+        for (uint32_t s = 0; s < p.ee_stages; ++s)
+        {
+            uint64_t const stop = n * (p.ee_first + s * p.ee_step) / 100u;
+            if (stop <= done)
+                continue;
+            count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
+            done = stop;
+            __syncwarp();
+            if (!any_segment_reachable(p, nd, counts, n - done, thr, lane))
+            {
+                hopeless = true;
+                break;
+            }
+        }
+    }
+    if (!hopeless)
+    {
+        count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, n - done, counts, lane);
+        done = n;
+    }
+    __syncwarp();
+    if (hopeless)
+    {
+        if (lane == 0)
+        {
+            __threadfence();
+            atomicAdd(p.ctrl + C_PENDING, ~0ull); // retires without results or children
+            ++n_tasks;
+            n_visits += n;
+            n_executed += done;
+        }
+        return;
+    }
+
+    uint2 const * d = p.descs + nd.desc_offset;
+    unsigned long long carry = 0;
+    unsigned const lt_mask = (1u << lane) - 1u;
+    uint64_t const gq = q + p.q_base;
+    for (uint32_t c = 0; c < nd.bins; c += 32)
+    {
+        uint32_t const b = c + lane;
+        bool const valid = b < nd.bins;
+        uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
+        unsigned long long x = valid ? counts[b] : 0ull;
+        bool f = valid && (ds.y & F_HEAD);
+        if (lane == 0 && !f)
+            x += carry;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
+            int const fy = __shfl_up_sync(kFullMask, static_cast<int>(f), o);
+            if (lane >= o)
+            {
+                if (!f)
+                    x += y;
+                f = f || fy;
+            }
+        }
+        uint64_t const sum = x & p.count_mask;
+        bool const pass = sum >= thr;
+        bool const emit_ub = valid && (ds.y & F_RUN_END) && pass;
+        bool const emit_child = valid && (ds.y & F_MERGED) && pass;
+
+        unsigned const rb = __ballot_sync(kFullMask, emit_ub);
+        if (rb)
+        {
+            unsigned const nr = __popc(rb);
+            unsigned long long base = 0;
+            if (lane == 0)
+            {
+                base = atomicAdd(p.ctrl + C_NREC, static_cast<unsigned long long>(nr));
+                atomicAdd(p.qcount + gq, nr);
+                if (base + nr > p.rec_cap)
+                    atomicOr(p.ctrl + C_ERROR, E_OVERFLOW_REC);
+            }
+            base = __shfl_sync(kFullMask, base, 0);
+            if (emit_ub)
+            {
+                unsigned long long const r = base + __popc(rb & lt_mask);
+                if (r < p.rec_cap)
+                {
+                    p.rec_q[r] = static_cast<uint32_t>(gq);
+                    p.rec_ub[r] = ds.x;
+                    p.rec_cnt[r] = sum;
+                }
+            }
+        }
+        unsigned const cb = __ballot_sync(kFullMask, emit_child);
+        if (cb)
+        {
+            unsigned const nc = __popc(cb);
+            if (depth + 1u > p.max_depth)
+            {
+                if (lane == 0)
+                    atomicOr(p.ctrl + C_ERROR, E_CYCLE);
+            }
+            else
+            {
+                unsigned long long base = 0;
+                if (lane == 0)
+                {
+                    atomicAdd(p.ctrl + C_PENDING, static_cast<unsigned long long>(nc));
+                    base = atomicAdd(p.ctrl + C_TAIL, static_cast<unsigned long long>(nc));
+                }
+                base = __shfl_sync(kFullMask, base, 0);
+                if (emit_child)
+                {
+                    unsigned long long const s = base + __popc(cb & lt_mask);
+                    if (s < p.task_cap)
+                    {
+                        atomicExch(p.tasks + s, make_task(q, depth + 1u, ds.x));
+                    }
+                    else
+                    {
+                        atomicOr(p.ctrl + C_ERROR, E_OVERFLOW_TASK);
+                        atomicAdd(p.ctrl + C_PENDING, ~0ull); // this child will never run
+                    }
+                    __threadfence();
+                }
+            }
+        }
+        unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
+        uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
+        carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
+    }
+    __syncwarp();
+    if (lane == 0)
+    {
+        __threadfence();
+        atomicAdd(p.ctrl + C_PENDING, ~0ull); // this task retires
+        ++n_tasks;
+        n_visits += n;
+        n_executed += done;
+    }
+}
+
+// H = the hierarchy's hash function count (one value for all IBFs, as in the reference's build).
+// HIBF_QUERY_MIN_BLOCKS blocks of eight warps per SM bound the register budget (2: 128 registers per thread,
+// measured fastest: the kernel is limited by the memory system's random-access rate, not by occupancy).
+#ifndef HIBF_QUERY_MIN_BLOCKS
+#    define HIBF_QUERY_MIN_BLOCKS 2
+#endif
+template <int H, int V>
+__global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_params p)
+{
+    extern __shared__ uint32_t s_counts[];
+    int const lane = threadIdx.x & 31;
+    uint32_t * counts = s_counts + (threadIdx.x >> 5) * p.counters_per_warp;
+    if (p.self_init)
+    {
+        if (threadIdx.x == 0)
+        {
+            p.ctrl[C_HEAD] = 0;
+            p.ctrl[C_TAIL] = 0;
+            p.ctrl[C_PENDING] = p.n_queries;
+            __threadfence();
+        }
+        __syncthreads();
+    }
+    unsigned long long n_tasks = 0, n_visits = 0, n_executed = 0;
+    for (;;)
+    {
+        unsigned long long idx = 0;
+        if (lane == 0)
+            idx = atomicAdd(p.ctrl + C_HEAD, 1ull);
+        idx = __shfl_sync(kFullMask, idx, 0);
+        unsigned long long task;
+        if (idx < p.n_queries)
+        {
+            task = make_task(idx, 0u, 0u);
+        }
+        else
+        {
+            unsigned long long const slot = idx - p.n_queries;
+            if (slot >= p.task_cap)
+                break;
+            task = 0;
+            if (lane == 0)
+                task = wait_for_task(p, slot);
+            task = __shfl_sync(kFullMask, task, 0);
+            if (task == kEmpty)
+                break;
+        }
+        process_task<H, V>(p, task, counts, lane, n_tasks, n_visits, n_executed);
+    }
+    if (lane == 0 && n_tasks)
+    {
+        atomicAdd(p.stats + 0, n_tasks);
+        atomicAdd(p.stats + 1, n_visits);
+        atomicAdd(p.stats + 2, n_executed);
+    }
+}
+
+// The kernel of variant v (0 <= v < kQueryVariants; H > 3 has the default variant only).
+template <int H>
+query_kernel_t query_kernel_variant(int v)
+{
+    if constexpr (H > 3)
+    {
+        (void)v;
+        return k_query<H, 0>;
+    }
+    else
+    {
+        switch (v)
+        {
+        case 1:
+            return k_query<H, 1>;
+        case 2:
+            return k_query<H, 2>;
+        case 3:
+            return k_query<H, 3>;
+        case 4:
+            return k_query<H, 4>;
+        case 5:
+            return k_query<H, 5>;
+        default:
+            return k_query<H, 0>;
+        }
+    }
+}
+
+// Defined in query_h1.cu .. query_h5.cu.
+query_kernel_t query_kernel_h1(int v);
+query_kernel_t query_kernel_h2(int v);
+query_kernel_t query_kernel_h3(int v);
+query_kernel_t query_kernel_h4(int v);
+query_kernel_t query_kernel_h5(int v);
+
+inline query_kernel_t query_kernel(uint32_t h, int v)
+{
+    switch (h)
+    {
+    case 1:
+        return query_kernel_h1(v);
+    case 2:
+        return query_kernel_h2(v);
+    case 3:
+        return query_kernel_h3(v);
+    case 4:
+        return query_kernel_h4(v);
+    default:
+        return query_kernel_h5(v);
+    }
+}
+
+} // namespace hibf_gb300

@@ -1,0 +1,11 @@
+// query_h2.cu -- the HIBF query kernels for hierarchies with 2 hash function(s), every tuning variant.
+// One translation unit per hash function count keeps the instantiations compiling in parallel.
+#include "query.cuh"
+
+namespace hibf_gb300
+{
+query_kernel_t query_kernel_h2(int v)
+{
+    return query_kernel_variant<2>(v);
+}
+} // namespace hibf_gb300

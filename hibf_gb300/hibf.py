@@ -223,6 +223,29 @@ class _agent_base:
         N.call("hibf_gpu_agent_kernel_ms", self._a, ctypes.byref(ms))
         return float(ms.value)
 
+    @property
+    def tuning(self) -> dict:
+        """The persistent kernel's schedule (hibf_gpu_tuning fields)."""
+        t = N.Tuning()
+        N.call("hibf_gpu_agent_get_tuning", self._a, ctypes.byref(t))
+        return t.as_dict()
+
+    @tuning.setter
+    def tuning(self, value: dict) -> None:
+        t = N.Tuning.from_dict(value)
+        N.call("hibf_gpu_agent_set_tuning", self._a, ctypes.byref(t))
+
+    def autotune(self, d_values: int, d_query_offsets: int, n_queries: int, d_thresholds: int,
+                 mode=N.QUERY_MEMBERSHIP, width=2, reps=3) -> list[dict]:
+        """Times every schedule the search visits on a device-resident sample batch, keeps the fastest on this agent
+        and returns the trials [{**tuning, "kernel_ms": ms}] (results are checked identical across schedules)."""
+        cap = 64
+        trials = (N.TuneTrial * cap)()
+        n = ctypes.c_uint64(0)
+        N.call("hibf_gpu_agent_autotune", self._a, mode, d_values, d_query_offsets, n_queries, d_thresholds, width,
+               reps, trials, cap, ctypes.byref(n))
+        return [dict(trials[i].tuning.as_dict(), kernel_ms=trials[i].kernel_ms) for i in range(min(cap, n.value))]
+
     def fetch_results(self, n_queries: int, mode=N.QUERY_MEMBERSHIP, width=2):
         """Host copies (offsets, ids, counts) of the last device batch (query_batch_device / query_plain_device)."""
         ro, ri, rc = N.u64p(), N.u64p(), ctypes.c_void_p()
@@ -283,3 +306,32 @@ class counting_agent_type(_agent_base):
 
     def query_batch(self, values, query_offsets, thresholds, mode=N.QUERY_COUNT, width=None):
         return super().query_batch(values, query_offsets, thresholds, mode, self.width if width is None else width)
+
+
+def tune_search(hash_count: int, max_row_words: int, measure) -> tuple[dict, list[dict]]:
+    """The autotuner's search with a caller-supplied measure(tuning: dict) -> ms (no device involved): returns the
+    fastest schedule and every trial in measurement order."""
+    err = []
+
+    def cb(tp, _user, out):
+        try:
+            out[0] = float(measure(tp.contents.as_dict()))
+            return N.OK
+        except Exception as e:  # reported through the status code
+            err.append(e)
+            return N.ERR_INVALID_ARG
+
+    fn = N.TUNE_MEASURE_FN(cb)
+    cap = 64
+    trials = (N.TuneTrial * cap)()
+    n = ctypes.c_uint64(0)
+    best = N.Tuning()
+    try:
+        N.call("hibf_gpu_tune_search", hash_count, max_row_words, fn, None, trials, cap, ctypes.byref(n),
+               ctypes.byref(best))
+    except N.HibfGpuError:
+        if err:
+            raise err[0]
+        raise
+    return best.as_dict(), [dict(trials[i].tuning.as_dict(), kernel_ms=trials[i].kernel_ms)
+                            for i in range(min(cap, n.value))]

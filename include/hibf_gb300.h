@@ -279,6 +279,47 @@ int hibf_gpu_agent_last_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * va
 int hibf_gpu_agent_last_work_executed(hibf_gpu_agent * a, uint64_t * value_visits_executed);
 
 /* ============================================================================================================ */
+/* Schedule of the persistent query kernel and its autotuner (no counterpart in the reference).  Every schedule     */
+/* computes the same exact counts, so results do not depend on it; only the time does.                              */
+/* ============================================================================================================ */
+typedef struct hibf_gpu_tuning
+{
+    uint32_t values_per_lane;   /* 1 or 2: values each lane hashes per pass, times max(1, 4 / lanes per row) */
+    uint32_t fetch_bytes;       /* 8 or 16: bytes each lane loads of a row (16: one 128-bit load; rows of >= 2 words) */
+    uint32_t counter_bits;      /* 5 or 7: width of the per-lane bit-sliced counters between shared-memory flushes */
+    uint32_t blocks_per_sm;     /* persistent blocks of 256 threads per SM; 0 = as many as fit */
+    uint32_t early_exit_first;  /* percent of a task's values counted before its first early-exit check */
+    uint32_t early_exit_step;   /* percent between later checks */
+    uint32_t early_exit_stages; /* number of checks (0: none; first + (stages - 1) * step must stay below 100) */
+    uint32_t early_exit_min;    /* tasks with fewer values are counted in one stage */
+} hibf_gpu_tuning;
+/* (values_per_lane, fetch_bytes, counter_bits) in {(1,8,7) (2,8,7) (1,8,5) (2,8,5) (1,16,7) (1,16,5)}; hierarchies
+ * with more than 3 hash functions or rows of more than 4 words (over 256 technical bins) take (1,8,7) only. */
+void hibf_gpu_tuning_default(hibf_gpu_tuning * t);
+/* Sets the agent's schedule for later batches (a captured graph is dropped: capture again). */
+int hibf_gpu_agent_set_tuning(hibf_gpu_agent * a, hibf_gpu_tuning const * t);
+int hibf_gpu_agent_get_tuning(hibf_gpu_agent * a, hibf_gpu_tuning * t);
+typedef struct hibf_gpu_tune_trial
+{
+    hibf_gpu_tuning tuning;
+    double kernel_ms; /* median device time of the persistent kernel over the repetitions */
+} hibf_gpu_tune_trial;
+/* Measures `tuning` (writes *kernel_ms); returns a status. */
+typedef int (*hibf_gpu_tune_measure_fn)(hibf_gpu_tuning const * tuning, void * user, double * kernel_ms);
+/* The autotuner's search, independent of the device: every kernel variant the hierarchy admits (given its hash
+ * function count and its widest row in 64-bit words; the 16-byte fetch only for rows of >= 2 words) at 1 and at the
+ * maximum blocks per SM, then the early-exit schedule and its minimum task length by coordinate descent.  Writes up
+ * to cap trials in measurement order, *n_trials (all of them) and *best (the fastest). */
+int hibf_gpu_tune_search(uint32_t hash_count, uint32_t max_row_words, hibf_gpu_tune_measure_fn measure, void * user,
+                         hibf_gpu_tune_trial * trials, uint64_t cap, uint64_t * n_trials, hibf_gpu_tuning * best);
+/* Autotunes the agent on a sample batch in HBM (as hibf_gpu_agent_query_batch_d): each trial is one warm-up and
+ * `reps` timed launches; every trial's results must equal the first's (else HIBF_GPU_ERR_LOGIC).  Leaves the best
+ * schedule set on the agent. */
+int hibf_gpu_agent_autotune(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint64_t const * d_query_offsets,
+                            uint64_t n_queries, uint64_t const * d_thresholds, int width, int reps,
+                            hibf_gpu_tune_trial * trials, uint64_t cap, uint64_t * n_trials);
+
+/* ============================================================================================================ */
 /* Continuous-batching server over a resident HIBF (no counterpart in the reference, whose agents answer one query   */
 /* per call).  A loop thread owns n_slots agents with their own streams; waiting requests are coalesced oldest-first */
 /* into one batch per free slot, bounded by the slot capacity (queries, values) and by admission_bytes, the device   */

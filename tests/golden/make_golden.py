@@ -215,6 +215,23 @@ def make_hibf_cases(R: Reference):
     hibf_case(R, "synth600", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=11)
 
 
+def make_hibf_wide_cases(R: Reference):
+    """Hierarchies whose IBFs have rows of 2 and 4 words (tmax 128 and 256), for the 16-byte-fetch kernels."""
+    # the 65,536-user-bin workload's shape at reduced sizes: h=3, fpr 0.02, tmax 256, log-normal sizes (sigma 2)
+    sizes = S.user_bin_sizes(13, 1000, S.SIZES_LOG_NORMAL, 60.0, 2.0, 5, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(13, S.QUERIES_MIXED, 50, 500, 70, 2, 6, 10, 1000)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(1000, h=3, fpr=0.02, tmax=256)
+    hibf_case(R, "synth_t256", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=13)
+    sizes = S.user_bin_sizes(17, 300, S.SIZES_LOG_NORMAL, 200.0, 1.5, 10, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(17, S.QUERIES_MIXED, 20, 400, 70, 2, 7, 10, 300)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(300, h=2, fpr=0.05, tmax=128)
+    hibf_case(R, "synth_t128", cfg, None, offs, (qv, qo), thr, thr, widths=(2, 4), synthetic_seed=17)
+
+
 def make_ibf_config(R: Reference):
     """interleaved_bloom_filter(config&, max_bin_elements): bin size, bit store digest, counts."""
     out = {}
@@ -281,12 +298,26 @@ def make_c3_layout(R: Reference):
     print(f"c3_layout: {time.time() - t0:.0f}s")
 
 
+def make_c4_layout(R: Reference):
+    """The 65,536-user-bin layout (h=3, fpr 0.02, tmax 256): reference DP over HyperLogLog sketches of the
+    synthetic user bins, streamed from the generator (about 4.8e10 values; no value is materialised)."""
+    sizes = S.user_bin_sizes(1, 65536, S.SIZES_LOG_NORMAL, 100000.0, 2.0, 500, 200000000)
+    offs = S.offsets_of(sizes)
+    cfg = ref_cfg(65536, h=3, fpr=0.02, tmax=256, threads=8, sketch_bits=12)
+    t0 = time.time()
+    layout = R.layout(cfg, None, offs, seed=1, synthetic=True)
+    (OUT / "c4_layout.txt").write_text(layout)
+    print(f"c4_layout: {time.time() - t0:.0f}s")
+
+
 def main(argv):
     build_reference()
     R = Reference()
-    which = set(argv) or {"ibf", "ibfcfg", "hibf", "c1", "c3"}
+    which = set(argv) or {"ibf", "ibfcfg", "hibf", "hibfwide", "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
+    if "hibfwide" in which:
+        make_hibf_wide_cases(R)
     if "ibfcfg" in which:
         make_ibf_config(R)
     if "hibf" in which:
@@ -295,6 +326,8 @@ def main(argv):
         make_c1(R)
     if "c3" in which:
         make_c3_layout(R)
+    if "c4" in which:  # not in the default set: about an hour of CPU
+        make_c4_layout(R)
 
 
 if __name__ == "__main__":

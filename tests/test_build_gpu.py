@@ -52,7 +52,7 @@ def _queries_vs_oracle(H, oracle, d):
     np.testing.assert_array_equal(ids, o_ids)
 
 
-@pytest.mark.parametrize("name", ["synth64", "synth600"])
+@pytest.mark.parametrize("name", ["synth64", "synth600", "synth_t128", "synth_t256"])
 def test_build_synthetic_matches_reference(gpu_lib, oracle, name):
     d = G.hibf_case(name)
     seed = int(d["synthetic_seed"][0])

@@ -147,3 +147,65 @@ def test_work_counters(gpu_lib):
     tasks, visits = a.last_work()
     assert tasks >= qo.size - 1
     assert visits >= int(qo[-1])
+
+
+KERNELS = [(1, 8, 7), (2, 8, 7), (1, 8, 5), (2, 8, 5), (1, 16, 7), (1, 16, 5)]
+EARLY_EXIT = [dict(early_exit_first=30, early_exit_step=10, early_exit_stages=7, early_exit_min=256),
+              dict(early_exit_stages=0),
+              dict(early_exit_first=10, early_exit_step=10, early_exit_stages=9, early_exit_min=16)]
+
+
+@pytest.mark.parametrize("name", ["synth600", "synth_t128", "synth_t256"])
+def test_every_schedule_gives_the_reference_results(gpu_lib, name):
+    """Each kernel variant (values per lane, fetch width, counter width) and early-exit schedule: bit-exact
+    membership lists and uint16 counts against the reference."""
+    d = G.hibf_case(name)
+    H = _gpu_hibf(d)
+    a = H.membership_agent()
+    qv, qo = d["q_values"], d["q_offsets"]
+    exp = G.mem_lists(d, "mem_sorted")
+    for vpl, fb, cb in KERNELS:
+        for ee in EARLY_EXIT:
+            for bps in (0, 1):
+                a.tuning = dict(values_per_lane=vpl, fetch_bytes=fb, counter_bits=cb, blocks_per_sm=bps, **ee)
+                offs, ids, _ = a.query_batch(qv, qo, d["mem_t"])
+                got = _split(offs, ids)
+                for i, (g, e) in enumerate(zip(got, exp)):
+                    np.testing.assert_array_equal(g, e, err_msg=f"{(vpl, fb, cb, bps, ee)} query {i}")
+        offs, ids, cnts = a.query_batch(qv, qo, d["cnt_t"], mode=N.QUERY_COUNT, width=2)
+        dense = np.zeros_like(d["count2"])
+        for i in range(offs.size - 1):
+            dense[i, ids[offs[i]:offs[i + 1]].astype(np.int64)] = cnts[offs[i]:offs[i + 1]]
+        np.testing.assert_array_equal(dense, d["count2"], err_msg=str((vpl, fb, cb)))
+
+
+def test_tuning_validation(gpu_lib):
+    a = _gpu_hibf(G.hibf_case("synth_t256")).membership_agent()
+    default = a.tuning
+    for bad in (dict(values_per_lane=2, fetch_bytes=16), dict(counter_bits=6), dict(blocks_per_sm=33),
+                dict(early_exit_first=95, early_exit_step=10, early_exit_stages=2),
+                dict(early_exit_first=0, early_exit_stages=3)):
+        with pytest.raises(hg.InvalidArgument):
+            a.tuning = dict(default, **bad)
+    assert a.tuning == default
+
+
+@pytest.mark.parametrize("name", ["synth600", "synth_t256"])
+def test_autotune_keeps_the_fastest_and_the_results(gpu_lib, name):
+    import torch
+
+    d = G.hibf_case(name)
+    H = _gpu_hibf(d)
+    a = H.membership_agent()
+    qv, qo, t = d["q_values"], d["q_offsets"], d["mem_t"]
+    dv = torch.from_numpy(qv.view(np.int64)).cuda()
+    dq = torch.from_numpy(qo.view(np.int64)).cuda()
+    dt = torch.from_numpy(t.astype(np.uint64).view(np.int64)).cuda()
+    torch.cuda.synchronize()
+    trials = a.autotune(dv.data_ptr(), dq.data_ptr(), qo.size - 1, dt.data_ptr(), reps=1)
+    assert len(trials) >= 12
+    best = min(trials, key=lambda tr: tr["kernel_ms"])
+    assert a.tuning == {k: v for k, v in best.items() if k != "kernel_ms"}
+    offs, ids, _ = a.query_batch(qv, qo, t)
+    for i, (g, e) in enumerate(zip(_split(offs, ids), G.mem_lists(d, "mem_sorted"))):
+        np.testing.assert_array_equal(g, e, err_msg=f"query {i}")
