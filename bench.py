@@ -37,6 +37,9 @@ WORKLOAD_DESC = {
     "hibf64": "HIBF 64 user bins (log-uniform [1e3,1e5]), h=2, fpr 0.05, tmax 64; 10,000 queries of 250 values "
               "(half from one UB), t=125; membership_for",
 }
+WORKLOAD_DESC["ibf1024"] = ("IBF 1,024 bins x 2^26 bits (8 GiB), h=3, emplace of 5e6 uniform values per bin; "
+                             "bulk_contains + bulk_count<uint16> over 2^24 query values, 50% present in a random bin")
+IBF1024 = dict(bins=1024, bin_size=1 << 26, h=3, values_per_bin=5_000_000, n_queries=1 << 24, seed=1)
 REASON_KEYS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
 
@@ -46,7 +49,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["hibf8192", "hibf64"], default="hibf8192")
+    ap.add_argument("--workload", choices=["hibf8192", "hibf64", "ibf1024"], default="hibf8192")
     ap.add_argument("--queries", type=int, default=0, help="override the number of queries per step")
     ap.add_argument("--plain-queries", type=int, default=2000, help="queries timed in the plain form")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
@@ -417,11 +420,239 @@ def run_reference(args, wl, rank, world, local):
             "e2e": {"value": value, "unit": "values/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def ibf_oracle_from_device(ibf, w):
+    """The C oracle's IBF holding the device-built bit store (downloaded in place)."""
+    from hibf_gb300 import _native as N
+    from oracle.bindings import Oracle, build_oracle
+
+    build_oracle()
+    O = Oracle().ibf(w["bins"], w["bin_size"], w["h"])
+    addr, n = O.data_ptr()
+    N.call("hibf_gpu_ibf_download_words", ibf._h, addr, n)
+    return O
+
+
+def ibf_cpu_sample(O, w, budget_s, threads):
+    """Times the oracle's bulk_count<uint16> + bulk_contains over a bounded sample of the query values."""
+    from hibf_gb300 import synthetic as S
+
+    n = 1 << 14
+    while True:
+        q = S.ibf_query_values(w["seed"], w["bins"], w["values_per_bin"], 0, n)
+        t0 = time.perf_counter()
+        cnt = O.bulk_count(q, 2, threads=threads)
+        con = O.bulk_contains(q, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt * 4 > budget_s or n >= w["n_queries"]:
+            return dict(values=n, seconds=dt, count=cnt, contains=con, q=q)
+        n = min(w["n_queries"], n * 4)
+
+
+def build_ibf1024(w, stream):
+    import torch
+
+    import hibf_gb300 as hg
+    from hibf_gb300 import _native as N
+
+    ibf = hg.interleaved_bloom_filter(hg.bin_count(w["bins"]), hg.bin_size(w["bin_size"]),
+                                      hg.hash_function_count(w["h"]))
+    torch.cuda.synchronize()
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b0.record(stream)
+    N.call("hibf_gpu_synth_ibf_emplace", ibf._h, w["seed"], w["values_per_bin"], 0, w["bins"], stream.cuda_stream)
+    b1.record(stream)
+    b1.synchronize()
+    return ibf, b0.elapsed_time(b1)
+
+
+def run_ibf_ours(args, rank, world, local):
+    import torch
+
+    from hibf_gb300 import _native as N
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    w = dict(IBF1024)
+    nq = args.queries or w["n_queries"]
+    stream = torch.cuda.Stream()
+    ibf, build_ms = build_ibf1024(w, stream)
+    bw = ibf.bin_words
+    d_q = torch.empty(nq, dtype=torch.int64, device="cuda")
+    N.call("hibf_gpu_synth_ibf_queries_d", w["seed"], w["bins"], w["values_per_bin"], 0, nq, d_q.data_ptr(),
+           stream.cuda_stream)
+    d_cnt = torch.empty(w["bins"], dtype=torch.int16, device="cuda")
+    d_con = torch.empty(nq * bw, dtype=torch.int64, device="cuda")
+    sp = stream.cuda_stream
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        N.call("hibf_gpu_ibf_bulk_count_d", ibf._h, d_q.data_ptr(), nq, 2, d_cnt.data_ptr(), sp)
+        if ev:
+            ev[1].record(stream)
+        N.call("hibf_gpu_ibf_bulk_contains_d", ibf._h, d_q.data_ptr(), nq, d_con.data_ptr(), sp)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    stream.synchronize()
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0] or 0)
+    clocks = ClockSampler(gpu_index)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for k in range(args.steps):
+        step(evs[k])
+    stream.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    count_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
+    contains_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
+    ms = sum(e[0].elapsed_time(e[2]) for e in evs) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # size-independent check at full size: the counts are the column sums of the contains bit vectors (mod 2^16)
+    c8 = d_con.view(torch.uint8).view(nq, bw * 8)
+    col = torch.zeros(bw * 64, dtype=torch.int64, device="cuda")
+    for k in range(8):
+        col.view(bw * 8, 8)[:, k] = ((c8 >> k) & 1).sum(dim=0, dtype=torch.int64)
+    col = (col[: w["bins"]] & 0xFFFF).to(torch.int32)
+    counts_equal_contains = bool(torch.equal(col, d_cnt.to(torch.int32) & 0xFFFF))
+
+    # end to end through the host entry points: pinned host values in, count vector and contains words out
+    h_q = torch.empty(nq, dtype=torch.int64, pin_memory=True)
+    h_q.copy_(d_q)
+    h_cnt = torch.empty(w["bins"], dtype=torch.int16, pin_memory=True)
+    h_con = torch.empty(nq * bw, dtype=torch.int64, pin_memory=True)
+
+    def host_step():
+        N.call("hibf_gpu_ibf_bulk_count", ibf._h, h_q.data_ptr(), nq, 2, h_cnt.data_ptr())
+        N.call("hibf_gpu_ibf_bulk_contains", ibf._h, h_q.data_ptr(), nq, h_con.data_ptr())
+
+    host_step()
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        host_step()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_equal = bool(torch.equal(h_cnt, d_cnt.cpu()))
+
+    out = None
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        rows = w["h"] * bw * 8  # h rows of bin_words words: 384 B per value
+        count_bytes = nq * (rows + 8)
+        contains_bytes = nq * (rows + 8 + bw * 8)
+        achieved = (count_bytes + contains_bytes) / (ms / 1e3) / 1e9
+        parity = {"counts_equal_contains_column_sums": counts_equal_contains, "e2e_equals_device": e2e_equal}
+        cpu = None
+        if not args.no_cpu:
+            O = ibf_oracle_from_device(ibf, w)
+            threads = os.cpu_count() or 1
+            smp = ibf_cpu_sample(O, w, args.cpu_seconds, threads)
+            n = smp["values"]
+            cpu = {"value": n / smp["seconds"], "unit": "values/s", "cores": threads, "kind": "port",
+                   "sample": f"first {n} query values, bulk_count<uint16> + bulk_contains, oracle/hibf_oracle.c with "
+                             f"{threads} OpenMP threads"}
+            dq = torch.from_numpy(smp["q"].view(np.int64)).cuda()
+            dc = torch.empty(w["bins"], dtype=torch.int16, device="cuda")
+            N.call("hibf_gpu_ibf_bulk_count_d", ibf._h, dq.data_ptr(), n, 2, dc.data_ptr(), None)
+            torch.cuda.synchronize()
+            parity["oracle_sample_values"] = n
+            parity["oracle_sample_count_equal"] = bool(np.array_equal(dc.cpu().numpy().view(np.uint16), smp["count"]))
+            parity["oracle_sample_contains_equal"] = bool(np.array_equal(
+                d_con[: n * bw].cpu().numpy().view(np.uint64).reshape(n, bw), smp["contains"]))
+        value = world * nq / (ms / 1e3)
+        out = {
+            "metric": "IBF bulk_contains + bulk_count<uint16> query values/s on 1 GB300 (bit-exact)",
+            "value": value, "unit": "values/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic: seeded splitmix64 bins and query values (include/hibf_gb300_synthetic.h)",
+            "config": {"workload": WORKLOAD_DESC["ibf1024"], "name": "ibf1024", "bins": w["bins"],
+                       "bin_size": w["bin_size"], "hash_functions": w["h"], "query_values_per_step": nq,
+                       "index_bytes": w["bins"] // 64 * 8 * w["bin_size"], "parallelism": f"replicas x{world}",
+                       "l2": "index (8 GiB) and outputs (2 GiB) larger than L2; no flush",
+                       "form": "one launch per call (bulk_count_d, bulk_contains_d)"},
+            "kernels": {"bulk_count_ms": count_ms, "bulk_contains_ms": contains_ms,
+                        "bulk_count_values_per_s": nq / (count_ms / 1e3),
+                        "bulk_contains_values_per_s": nq / (contains_ms / 1e3),
+                        "bulk_count_GBps": count_bytes / (count_ms / 1e3) / 1e9,
+                        "bulk_contains_GBps": contains_bytes / (contains_ms / 1e3) / 1e9},
+            "build": {"inserts": w["bins"] * w["values_per_bin"], "ms": build_ms,
+                      "inserts_per_s": w["bins"] * w["values_per_bin"] / (build_ms / 1e3),
+                      "algorithmic_GBps": w["bins"] * w["values_per_bin"] * w["h"] * 64 / (build_ms / 1e3) / 1e9,
+                      "bytes_per_insert": w["h"] * 64, "form": "hibf_gpu_synth_ibf_emplace (values generated on "
+                                                               "the device, atomicOr)"},
+            "e2e": {"value": world * nq / e2e_s, "unit": "values/s", "h2d_bytes_per_step": 2 * nq * 8,
+                    "d2h_bytes_per_step": w["bins"] * 2 + nq * bw * 8, "ms_per_step": e2e_s * 1e3,
+                    "call": "hibf_gpu_ibf_bulk_count + hibf_gpu_ibf_bulk_contains (pinned host buffers)"},
+            "gpu_launches": 4 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "algorithmic_bytes_per_value": {"bulk_count": rows + 8, "bulk_contains": rows + 8 + bw * 8}},
+            "cpu_baseline": cpu, "clocks": clk, "parity": parity,
+        }
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def run_ibf_reference(args, rank, world, local):
+    """The reference arm for the IBF workload: the oracle's bulk_count + bulk_contains on the host cores (bounded
+    samples), over the bit store built on the device (set-up, not timed)."""
+    if rank != 0:
+        return None
+    import torch
+
+    torch.cuda.set_device(local)
+    w = dict(IBF1024)
+    stream = torch.cuda.Stream()
+    ibf, _ = build_ibf1024(w, stream)
+    O = ibf_oracle_from_device(ibf, w)
+    del ibf
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, min(args.cpu_seconds, 60.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        ibf_cpu_sample(O, w, per_step, threads)
+    vals, secs = 0, 0.0
+    for _ in range(args.steps):
+        s = ibf_cpu_sample(O, w, per_step, threads)
+        vals += s["values"]
+        secs += s["seconds"]
+    value = vals / secs
+    return {"impl": "reference", "metric": "IBF bulk_contains + bulk_count<uint16> query values/s on 1 GB300 "
+                                           "(bit-exact)",
+            "value": value, "unit": "values/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": WORKLOAD_DESC["ibf1024"], "name": "ibf1024"},
+            "cpu_baseline": {"value": value, "unit": "values/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} samples of ~{per_step:.1f} s ({vals} values), oracle/hibf_oracle.c"},
+            "e2e": {"value": value, "unit": "values/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
     from hibf_gb300.workloads import WORKLOADS
 
+    if args.workload == "ibf1024":
+        out = run_ibf_reference(args, rank, world, local) if args.impl == "reference" else \
+            run_ibf_ours(args, rank, world, local)
+        if rank == 0 and out is not None:
+            print(json.dumps(out), flush=True)
+        return
     wl = WORKLOADS[args.workload]
     out = run_reference(args, wl, rank, world, local) if args.impl == "reference" else \
         run_ours(args, wl, rank, world, local)

@@ -170,6 +170,9 @@ _SIGS = [
                                             ctypes.c_uint32, u64, u64, u64, vp, vp]),
     ("hibf_gpu_synth_queries", None, [u64, ci, u64, u64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                       ctypes.c_uint32, u64, vp, u64, u64, vp, vp]),
+    ("hibf_gpu_synth_ibf_emplace", None, [vp, u64, u64, u64, u64, vp]),
+    ("hibf_gpu_synth_ibf_queries", None, [u64, u64, u64, u64, u64, vp]),
+    ("hibf_gpu_synth_ibf_queries_d", None, [u64, u64, u64, u64, u64, vp, vp]),
     ("hibf_gpu_synth_queries_d", None, [u64, ci, u64, u64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                         ctypes.c_uint32, u64, vp, u64, u64, vp, vp, vp]),
 ]

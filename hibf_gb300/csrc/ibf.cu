@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/hibf_gb300_synthetic.h"
 #include "common.hpp"
 #include "count.cuh"
 #include "device.cuh"
@@ -45,6 +46,32 @@ __global__ void k_emplace(uint64_t * __restrict__ words, uint64_t bin_size, uint
             *bad_bin = 1; // device-supplied bin index out of range: skipped, reported by hibf_gpu_ibf_status
             continue;
         }
+        uint64_t const bit = 1ull << (b & 63u);
+        uint64_t const wofs = b >> 6;
+        bool exists = true;
+        for (uint32_t k = 0; k < h; ++k)
+        {
+            uint64_t const r = hash_row(v, c_hash_seeds[k], shift, bin_size);
+            unsigned long long * w = reinterpret_cast<unsigned long long *>(words + r * row_words + wofs);
+            unsigned long long const old = atomicOr(w, static_cast<unsigned long long>(bit));
+            exists = exists && (old & bit);
+        }
+        if (occupancy && !exists)
+            atomicAdd(occupancy + b, 1ull);
+    }
+}
+
+// emplace of the synthetic single-level workload: value i of the launch is hg_ibf_bin_value of bin
+// first_bin + i / vpb, generated in place instead of read (same bits as k_emplace with those values).
+__global__ void k_synth_emplace(uint64_t * __restrict__ words, uint64_t bin_size, uint32_t row_words, uint32_t shift,
+                                uint32_t h, uint64_t seed, uint64_t vpb, uint64_t first_bin, uint64_t n,
+                                unsigned long long * occupancy)
+{
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        uint64_t const b = first_bin + i / vpb;
+        uint64_t const v = hg_ibf_bin_value(seed, vpb, b, i % vpb);
         uint64_t const bit = 1ull << (b & 63u);
         uint64_t const wofs = b >> 6;
         bool exists = true;
@@ -492,6 +519,30 @@ extern "C"
                 if (!d_bins && bin >= f->bins)
                     fail(HIBF_GPU_ERR_INVALID_ARG, "bin index out of range");
                 launch_emplace(f, d_values, d_bins, n, bin, pick(f, stream));
+            });
+    }
+
+    int hibf_gpu_synth_ibf_emplace(hibf_gpu_ibf * f, uint64_t seed, uint64_t values_per_bin, uint64_t first_bin,
+                                   uint64_t n_bins, void * stream)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || values_per_bin == 0)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                if (first_bin > f->bins || n_bins > f->bins - first_bin)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bin range out of range");
+                if (n_bins && values_per_bin > UINT64_MAX / n_bins)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "too many values");
+                uint64_t const n = n_bins * values_per_bin;
+                if (!n)
+                    return;
+                unsigned const block = 256;
+                k_synth_emplace<<<grid_for(n, block), block, 0, pick(f, stream)>>>(
+                    f->store.as<uint64_t>(), f->bin_size, static_cast<uint32_t>(f->row_words), f->shift,
+                    static_cast<uint32_t>(f->hash_funs), seed, values_per_bin, first_bin, n,
+                    f->track_occupancy ? f->occupancy.as<unsigned long long>() : nullptr);
+                HG_CUDA(cudaGetLastError());
             });
     }
 

@@ -25,6 +25,14 @@ __global__ void k_synth_queries(hg_query_spec spec, uint64_t const * __restrict_
         hg_query_values(&spec, ub_offsets, first + i, out + qoff[i]);
 }
 
+__global__ void k_synth_ibf_queries(uint64_t seed, uint64_t n_bins, uint64_t vpb, uint64_t first, uint64_t n,
+                                    uint64_t * __restrict__ out)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        out[i] = hg_ibf_query_value(seed, n_bins, vpb, first + i);
+}
+
 hg_query_spec make_spec(uint64_t seed, int law, uint64_t len_lo, uint64_t len_hi, uint32_t mix_pct,
                         uint32_t noise_pct, uint32_t thr_num, uint32_t thr_den, uint64_t n_user_bins)
 {
@@ -127,6 +135,39 @@ extern "C"
                 k_synth_queries<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(s, d_user_bin_offsets,
                                                                                       first_query, n_queries,
                                                                                       d_query_offsets, d_values);
+                HG_CUDA(cudaGetLastError());
+            });
+    }
+
+    int hibf_gpu_synth_ibf_queries(uint64_t seed, uint64_t n_bins, uint64_t values_per_bin, uint64_t first,
+                                   uint64_t n, uint64_t * values)
+    {
+        return guarded(
+            [&]
+            {
+                if ((n && !values) || n_bins == 0 || values_per_bin == 0)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                for (uint64_t i = 0; i < n; ++i)
+                    values[i] = hg_ibf_query_value(seed, n_bins, values_per_bin, first + i);
+            });
+    }
+
+    int hibf_gpu_synth_ibf_queries_d(uint64_t seed, uint64_t n_bins, uint64_t values_per_bin, uint64_t first,
+                                     uint64_t n, uint64_t * d_values, void * stream)
+    {
+        return guarded(
+            [&]
+            {
+                if ((n && !d_values) || n_bins == 0 || values_per_bin == 0)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                if (!n)
+                    return;
+                unsigned const block = 256;
+                unsigned const grid = static_cast<unsigned>(
+                    std::min<uint64_t>((n + block - 1) / block, static_cast<uint64_t>(sm_count()) * 16));
+                k_synth_ibf_queries<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(seed, n_bins,
+                                                                                          values_per_bin, first, n,
+                                                                                          d_values);
                 HG_CUDA(cudaGetLastError());
             });
     }

@@ -171,3 +171,25 @@ def queries(q: query_spec, offsets: np.ndarray, first: int, n: int):
     np.cumsum([v.size for v in vals], out=qoff[1:])
     thr = np.array([query_threshold(q, v.size) for v in vals], np.uint64)
     return (np.concatenate(vals) if vals else np.zeros(0, np.uint64)), qoff, thr
+
+
+# -- single-level IBF workload (hg_ibf_bin_value / hg_ibf_query_value) --------------------------------------------
+TAG_IBF_QUERIES = 0x4942465155
+
+
+def ibf_bin_values(seed: int, values_per_bin: int, b: int, first: int = 0, n: int | None = None) -> np.ndarray:
+    """Values first .. first+n-1 of bin b."""
+    n = values_per_bin - first if n is None else n
+    return stream_range(seed, b * values_per_bin + first, n)
+
+
+def ibf_query_values(seed: int, n_bins: int, values_per_bin: int, first: int, n: int) -> np.ndarray:
+    qs = subseed(seed, TAG_IBF_QUERIES)
+    k = 2 * np.arange(first, first + n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        r = mix64_np(np.uint64(qs) + (k + np.uint64(1)) * np.uint64(GAMMA))
+        r2 = mix64_np(np.uint64(qs) + (k + np.uint64(2)) * np.uint64(GAMMA))
+        b = (r >> np.uint64(1)) % np.uint64(n_bins)
+        j = r2 % np.uint64(values_per_bin)
+        present = mix64_np(np.uint64(seed) + (b * np.uint64(values_per_bin) + j + np.uint64(1)) * np.uint64(GAMMA))
+    return np.where((r & np.uint64(1)).astype(bool), present, r2)

@@ -375,6 +375,16 @@ int hibf_gpu_synth_queries_d(uint64_t seed, int law, uint64_t len_lo, uint64_t l
                              uint32_t noise_pct, uint32_t thr_num, uint32_t thr_den, uint64_t n_user_bins,
                              uint64_t const * d_user_bin_offsets, uint64_t first_query, uint64_t n_queries,
                              uint64_t const * d_query_offsets, uint64_t * d_values, void * stream);
+/* Single-level IBF workload (hg_ibf_bin_value / hg_ibf_query_value): emplace of bins [first_bin, first_bin +
+ * n_bins), bin b receiving its values_per_bin values generated on the device (asynchronous on `stream`; the same
+ * bits as hibf_gpu_ibf_emplace with those values). */
+int hibf_gpu_synth_ibf_emplace(hibf_gpu_ibf * ibf, uint64_t seed, uint64_t values_per_bin, uint64_t first_bin,
+                               uint64_t n_bins, void * stream);
+/* Query values first .. first+n-1 of that workload over n_bins bins, on the host or on the device. */
+int hibf_gpu_synth_ibf_queries(uint64_t seed, uint64_t n_bins, uint64_t values_per_bin, uint64_t first, uint64_t n,
+                               uint64_t * values);
+int hibf_gpu_synth_ibf_queries_d(uint64_t seed, uint64_t n_bins, uint64_t values_per_bin, uint64_t first, uint64_t n,
+                                 uint64_t * d_values, void * stream);
 
 #ifdef __cplusplus
 }

@@ -210,4 +210,26 @@ HG_HD void hg_query_values(hg_query_spec const * q, uint64_t const * offsets, ui
     }
 }
 
+/* ---------------------------------------------------------------------------------------------------------- */
+/* Single-level IBF workload: bin b holds stream outputs [b * values_per_bin, (b + 1) * values_per_bin) of       */
+/* `seed`.  Query value i: with probability 1/2 a uniformly chosen element of a uniformly chosen bin (present),  */
+/* otherwise a uniform random uint64 (absent except for false positives).                                        */
+/* ---------------------------------------------------------------------------------------------------------- */
+#define HG_TAG_IBF_QUERIES 0x4942465155ULL /* "IBFQU" */
+
+HG_HD uint64_t hg_ibf_bin_value(uint64_t seed, uint64_t values_per_bin, uint64_t bin, uint64_t j)
+{
+    return hg_stream_at(seed, bin * values_per_bin + j);
+}
+
+HG_HD uint64_t hg_ibf_query_value(uint64_t seed, uint64_t n_bins, uint64_t values_per_bin, uint64_t i)
+{
+    uint64_t const qs = hg_subseed(seed, HG_TAG_IBF_QUERIES);
+    uint64_t const r = hg_stream_at(qs, 2u * i);
+    uint64_t const r2 = hg_stream_at(qs, 2u * i + 1u);
+    if (r & 1u)
+        return hg_ibf_bin_value(seed, values_per_bin, (r >> 1) % n_bins, r2 % values_per_bin);
+    return r2;
+}
+
 #endif /* HIBF_GB300_SYNTHETIC_H */

@@ -77,6 +77,8 @@ class Oracle:
         L.orc_ibf_increase_bin_number_to.argtypes = [vp, u64]
         L.orc_ibf_bulk_contains_many.argtypes = [vp, vp, u64, vp]
         L.orc_ibf_bulk_count.argtypes = [vp, vp, u64, ctypes.c_int, vp]
+        L.orc_ibf_bulk_count_mt.argtypes = [vp, vp, u64, ctypes.c_int, vp, ctypes.c_int]
+        L.orc_ibf_bulk_contains_many_mt.argtypes = [vp, vp, u64, vp, ctypes.c_int]
         L.orc_ibf_membership.restype = u64
         L.orc_ibf_membership.argtypes = [vp, vp, u64, ctypes.c_uint16, vp]
         L.orc_hibf_new.restype = vp
@@ -156,16 +158,26 @@ class OracleIBF:
             raise MemoryError
         self.bins = n
 
-    def bulk_contains(self, values) -> np.ndarray:
+    def data_ptr(self) -> tuple[int, int]:
+        """(address, words) of the bit store, to fill it in place (e.g. from a device download)."""
+        return ctypes.cast(self.L.orc_ibf_data(self.h), ctypes.c_void_p).value, self.L.orc_ibf_nwords(self.h)
+
+    def bulk_contains(self, values, threads=1) -> np.ndarray:
         v = _u64(values)
         out = np.zeros((v.size, self.bin_words), np.uint64)
-        self.L.orc_ibf_bulk_contains_many(self.h, _ptr(v), v.size, _ptr(out))
+        if threads > 1:
+            self.L.orc_ibf_bulk_contains_many_mt(self.h, _ptr(v), v.size, _ptr(out), threads)
+        else:
+            self.L.orc_ibf_bulk_contains_many(self.h, _ptr(v), v.size, _ptr(out))
         return out
 
-    def bulk_count(self, values, width=2) -> np.ndarray:
+    def bulk_count(self, values, width=2, threads=1) -> np.ndarray:
         v = _u64(values)
         out = np.zeros(self.bins, _WIDTH_DTYPE[width])
-        self.L.orc_ibf_bulk_count(self.h, _ptr(v), v.size, width, _ptr(out))
+        if threads > 1:
+            self.L.orc_ibf_bulk_count_mt(self.h, _ptr(v), v.size, width, _ptr(out), threads)
+        else:
+            self.L.orc_ibf_bulk_count(self.h, _ptr(v), v.size, width, _ptr(out))
         return out
 
     def membership_for(self, values, threshold) -> np.ndarray:

@@ -9,6 +9,7 @@
 #define _POSIX_C_SOURCE 200809L
 #include "hibf_oracle.h"
 
+#include <omp.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -263,6 +264,42 @@ void orc_ibf_bulk_count(orc_ibf const * ibf, uint64_t const * values, uint64_t n
         store_width(out, b, counts[b], width);
     free(counts);
     free(scratch);
+}
+
+/* The same count over `threads` disjoint slices of the values with one counting vector each, summed at the end:
+ * addition modulo 2^(8*width) is associative, so this equals one counting_agent over all values. */
+void orc_ibf_bulk_count_mt(orc_ibf const * ibf, uint64_t const * values, uint64_t n, int width, void * out,
+                           int threads)
+{
+    if (threads < 1)
+        threads = 1;
+    uint64_t * total = (uint64_t *)calloc(ibf->bins, sizeof(uint64_t));
+#pragma omp parallel num_threads(threads)
+    {
+        uint64_t * counts = (uint64_t *)malloc(ibf->bins * sizeof(uint64_t));
+        uint64_t * scratch = (uint64_t *)malloc(ibf->bin_words * sizeof(uint64_t));
+        int const t = omp_get_thread_num();
+        int const nt = omp_get_num_threads();
+        uint64_t const lo = n * (uint64_t)t / (uint64_t)nt;
+        uint64_t const hi = n * (uint64_t)(t + 1) / (uint64_t)nt;
+        orc_count_raw(ibf, values + lo, hi - lo, counts, scratch);
+#pragma omp critical
+        for (uint64_t b = 0; b < ibf->bins; ++b)
+            total[b] += counts[b];
+        free(counts);
+        free(scratch);
+    }
+    for (uint64_t b = 0; b < ibf->bins; ++b)
+        store_width(out, b, total[b], width);
+    free(total);
+}
+
+void orc_ibf_bulk_contains_many_mt(orc_ibf const * ibf, uint64_t const * values, uint64_t n, uint64_t * out,
+                                   int threads)
+{
+#pragma omp parallel for num_threads(threads < 1 ? 1 : threads) schedule(static)
+    for (uint64_t i = 0; i < n; ++i)
+        orc_ibf_bulk_contains(ibf, values[i], out + i * ibf->bin_words);
 }
 
 /* IBF.hpp:744-764: uint16 bulk_count, then the ascending bin ids whose count reaches the threshold. */

@@ -71,6 +71,10 @@ void orc_ibf_bulk_contains(orc_ibf const * ibf, uint64_t value, uint64_t * out_w
 void orc_ibf_bulk_contains_many(orc_ibf const * ibf, uint64_t const * values, uint64_t n, uint64_t * out_words);
 /* width = sizeof(value_t) in bytes: 1, 2, 4 or 8.  `out` holds `bins` counters of that width. */
 void orc_ibf_bulk_count(orc_ibf const * ibf, uint64_t const * values, uint64_t n, int width, void * out);
+void orc_ibf_bulk_count_mt(orc_ibf const * ibf, uint64_t const * values, uint64_t n, int width, void * out,
+                           int threads);
+void orc_ibf_bulk_contains_many_mt(orc_ibf const * ibf, uint64_t const * values, uint64_t n, uint64_t * out,
+                                   int threads);
 uint64_t orc_ibf_membership(orc_ibf const * ibf, uint64_t const * values, uint64_t n, uint16_t threshold,
                             uint64_t * out);
 
