@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel schedule")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned scheduler measurement")
+    ap.add_argument("--sched-queries", type=int, default=65536, help="batch size of the learned scheduler test")
     ap.add_argument("--tune-queries", type=int, default=200_000, help="sample batch of the autotuner")
     ap.add_argument("--l2-fetch", type=int, default=-1,
                     help="set the context's L2 fetch granularity hint (bytes) before the run; -1 leaves it")
@@ -181,6 +183,83 @@ def cpu_sample(OH, wl, offs, budget_s, threads, first=0):
     pairs, chk = OH.run_queries(v, qo, thr, thr, mode=1, threads=threads)
     dt = time.perf_counter() - t0
     return dict(values=int(qo[-1]), queries=n, seconds=dt, value_visits=pairs, checksum=chk, qo=qo, thr=thr, v=v)
+
+
+def _ranks(x):
+    r = np.empty(x.size)
+    r[np.argsort(x, kind="stable")] = np.arange(x.size)
+    return r
+
+
+def learned_scheduler(hibf, tuning, d_v, d_qo, d_thr, qo, nq, n, stream):
+    """Trains the cost model on one sub-batch's measured per-query work and times another sub-batch's persistent
+    kernel with its root tasks in query order, in order of length, and in order of the model's prediction."""
+    import torch
+
+    from hibf_gb300.scheduler import cost_model
+
+    a = hibf.membership_agent()
+    a.tuning = tuning
+    a.reserve(n, int(qo[-1]), n * 8 + 65536, n * 8 + 65536)
+    a.set_stream(stream.cuda_stream)
+
+    def sub(first):
+        return d_v.data_ptr(), d_qo.data_ptr() + 8 * first, d_thr.data_ptr() + 8 * first
+
+    def feats_work(first):
+        v, q, t = sub(first)
+        f = torch.zeros(n * 6, dtype=torch.float32, device="cuda")
+        w = torch.zeros(n, dtype=torch.int64, device="cuda")
+        a.query_features(v, q, n, t, 16, f.data_ptr())
+        a.set_work_out(w.data_ptr(), n)
+        a.query_batch_device(v, q, n, t)
+        stream.synchronize()
+        a.status()
+        a.set_work_out(None)
+        return f, w
+
+    t0 = time.perf_counter()
+    f_tr, w_tr = feats_work(0)
+    model = cost_model(seed=1)
+    loss = model.train(f_tr.data_ptr(), w_tr.data_ptr(), n, steps=500, lr=1e-2)
+    train_s = time.perf_counter() - t0
+    first = nq // 2
+    f_te, w_te = feats_work(first)
+    pred = torch.empty(n, dtype=torch.float32, device="cuda")
+    model.predict(f_te.data_ptr(), n, pred.data_ptr(), stream.cuda_stream)
+    lengths = torch.from_numpy(np.diff(qo[first:first + n + 1]).astype(np.float32)).cuda()
+    o_len = torch.empty(n, dtype=torch.int32, device="cuda")
+    o_learned = torch.empty(n, dtype=torch.int32, device="cuda")
+    model.sort_desc(lengths.data_ptr(), n, o_len.data_ptr(), stream.cuda_stream)
+    t1 = time.perf_counter()
+    model.order(f_te.data_ptr(), n, o_learned.data_ptr(), stream.cuda_stream)
+    stream.synchronize()
+    order_s = time.perf_counter() - t1
+    work = w_te.cpu().numpy().astype(np.float64)
+    rho = lambda x: float(np.corrcoef(_ranks(x), _ranks(work))[0, 1])
+    v, q, t = sub(first)
+    times, results = {}, {}
+    for name, order in (("query_order", None), ("length_order", o_len), ("learned_order", o_learned)):
+        a.set_order(order.data_ptr() if order is not None else None, n)
+        ks = []
+        for _ in range(7):
+            a.query_batch_device(v, q, n, t)
+            stream.synchronize()
+            ks.append(a.kernel_ms())
+        a.status()
+        times[name] = float(np.median(ks[2:]))
+        o, i, _ = a.fetch_results(n)
+        results[name] = (o, i)
+    a.set_order(None)
+    same = all(np.array_equal(results[k][0], results["query_order"][0]) and
+               np.array_equal(results[k][1], results["query_order"][1]) for k in results)
+    return {"batch_queries": n, "train_queries": n, "train_steps": 500, "train_s": train_s, "train_mse": loss,
+            "order_s": order_s, "spearman_learned": rho(pred.cpu().numpy().astype(np.float64)),
+            "spearman_length": rho(np.diff(qo[first:first + n + 1]).astype(np.float64)),
+            "kernel_ms": times, "gain_vs_query_order": times["query_order"] / times["learned_order"],
+            "gain_vs_length_order": times["length_order"] / times["learned_order"], "results_identical": same,
+            "model": "6 features -> 32 -> 32 -> 1 ReLU MLP, full-batch Adam on log(1 + executed visits), "
+                     "hibf_gb300/csrc/cost_model.cu"}
 
 
 # ------------------------------------------------------------------------------------------------------------------
@@ -323,6 +402,10 @@ def run_ours(args, wl, rank, world, local):
                                          max_request_queries=4096, thr_lo=0.5, thr_hi=0.9, seed=int(load)))
         srv.close()
 
+    learned = None
+    if not args.no_learned and nq >= 2 * args.sched_queries:
+        learned = learned_scheduler(hibf, agent.tuning, d_v, d_qo, d_thr, qo, nq, args.sched_queries, stream)
+
     out = None
     if rank == 0:
         hbm, peak_kind = peaks()
@@ -374,6 +457,7 @@ def run_ours(args, wl, rank, world, local):
                                                  "reads_per_s_2MiB_windows": probe["window_2MiB"],
                                                  "probe": "hibf_gpu_probe_random_reads"}},
             "cpu_baseline": cpu, "clocks": clk, "build_s": build_s, "parity": parity, "autotune": tune,
+            "learned_scheduler": learned,
             "serving": serving, "p99_serve_latency_ms": serving[-1]["p99_ms"] if serving else None,
             "serving_config": "open-loop Poisson, request sizes log-uniform 1-4096 queries from the batch's first "
                               "100k queries, thresholds U(0.5,0.9)*len, 4 slots, 4 GiB admission cap",

@@ -153,6 +153,19 @@ _SIGS = [
     ("hibf_gpu_agent_get_tuning", None, [vp, ctypes.POINTER(Tuning)]),
     ("hibf_gpu_tune_search", None, [ctypes.c_uint32, ctypes.c_uint32, TUNE_MEASURE_FN, vp,
                                     ctypes.POINTER(TuneTrial), u64, u64p, ctypes.POINTER(Tuning)]),
+    ("hibf_gpu_agent_set_order_d", None, [vp, vp, u64]),
+    ("hibf_gpu_agent_set_work_out_d", None, [vp, vp, u64]),
+    ("hibf_gpu_agent_query_features_d", None, [vp, vp, vp, u64, vp, ctypes.c_uint32, vp]),
+    ("hibf_gpu_cost_model_create", None, [u64, ctypes.POINTER(vp)]),
+    ("hibf_gpu_cost_model_destroy", None, [vp]),
+    ("hibf_gpu_cost_model_get_params", None, [vp, vp]),
+    ("hibf_gpu_cost_model_set_params", None, [vp, vp]),
+    ("hibf_gpu_cost_model_loss_grad_d", None, [vp, vp, vp, u64, vp, ctypes.POINTER(ctypes.c_double)]),
+    ("hibf_gpu_cost_model_train_d", None, [vp, vp, vp, u64, ctypes.c_uint32, ctypes.c_float,
+                                           ctypes.POINTER(ctypes.c_double)]),
+    ("hibf_gpu_cost_model_predict_d", None, [vp, vp, u64, vp, vp]),
+    ("hibf_gpu_cost_model_order_d", None, [vp, vp, u64, vp, vp]),
+    ("hibf_gpu_sort_desc_d", None, [vp, vp, u64, vp, vp]),
     ("hibf_gpu_agent_autotune", None, [vp, ci, vp, vp, u64, vp, ci, ci, ctypes.POINTER(TuneTrial), u64, u64p]),
     ("hibf_gpu_server_create", None, [vp, ci, u64, u64, u64, ctypes.POINTER(vp)]),
     ("hibf_gpu_server_destroy", None, [vp]),

@@ -334,6 +334,10 @@ struct hibf_gpu_agent
     hibf_gpu_tuning tune{};                // schedule of the persistent kernel
     int variant{0};                        // kernel variant of `tune`
     int max_blocks[kQueryVariants]{};      // resident 256-thread blocks per SM of each variant
+    uint32_t const * order{};              // claim order of the root tasks (device; null = query order)
+    uint64_t order_n{};                    // its length: batches must have exactly this many queries
+    unsigned long long * qwork{};          // executed value visits per query (device; null = not recorded)
+    uint64_t qwork_n{};                    // its length: batches may have at most this many queries
     // device workspace
     dbuf ctrl, stats, tasks, rec_q, rec_ub, rec_cnt, qcount, cursor, roff, bsum, out_ids, out_cnt, out_cntw, large;
     // host-call staging
@@ -405,6 +409,8 @@ query_params base_params(hibf_gpu_agent * a, uint64_t const * d_values, uint64_t
     p.ee_step = a->tune.early_exit_step;
     p.ee_stages = a->tune.early_exit_stages;
     p.ee_min = a->tune.early_exit_min;
+    p.order = a->order;
+    p.qwork = a->qwork;
     return p;
 }
 
@@ -458,15 +464,26 @@ void launch_postprocess(hibf_gpu_agent * a, uint64_t nq, int mode, int width)
 }
 
 // One persistent launch over all queries plus compaction.  Asynchronous.
+void check_order_and_work(hibf_gpu_agent const * a, uint64_t nq, bool plain)
+{
+    if (a->order && !plain && a->order_n != nq)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "the claim order set on the agent has a different length than the batch");
+    if (a->qwork && a->qwork_n < nq)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "the per-query work array set on the agent is shorter than the batch");
+}
+
 void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint64_t const * d_qoff,
                   uint64_t const * d_thr, uint64_t nq, int width)
 {
     hibf_gpu_hibf * h = a->h;
+    check_order_and_work(a, nq, false);
     cudaStream_t s = a->stream;
     k_init_ctrl<<<1, 32, 0, s>>>(a->ctrl.as<unsigned long long>(), a->stats.as<unsigned long long>(), nq);
     HG_CUDA(cudaGetLastError());
     HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, a->cap_tasks * 8, s));
     HG_CUDA(cudaMemsetAsync(a->qcount.p, 0, std::max<uint64_t>(nq, 1) * 4, s));
+    if (a->qwork && nq)
+        HG_CUDA(cudaMemsetAsync(a->qwork, 0, nq * 8, s));
     if (nq)
     {
         query_params p = base_params(a, d_values, d_qoff, d_thr, nq, mask_for(mode, width));
@@ -493,16 +510,20 @@ void launch_plain(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
                   uint64_t const * d_qoff, uint64_t const * d_thr, uint64_t nq, int width)
 {
     hibf_gpu_hibf * h = a->h;
+    check_order_and_work(a, nq, true);
     cudaStream_t s = a->stream;
     k_init_ctrl<<<1, 32, 0, s>>>(a->ctrl.as<unsigned long long>(), a->stats.as<unsigned long long>(), 0);
     HG_CUDA(cudaGetLastError());
     HG_CUDA(cudaMemsetAsync(a->qcount.p, 0, std::max<uint64_t>(nq, 1) * 4, s));
+    if (a->qwork && nq)
+        HG_CUDA(cudaMemsetAsync(a->qwork, 0, nq * 8, s));
     uint64_t const mask = mask_for(mode, width);
     for (uint64_t q = 0; q < nq; ++q)
     {
         (void)h_qoff;
         query_params p = base_params(a, d_values, d_qoff + q, d_thr + q, 1, mask);
         p.q_base = q;
+        p.order = nullptr;
         p.self_init = 1;
         HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u) * 8, s));
         p.task_cap = std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u);
@@ -529,6 +550,8 @@ int read_status(hibf_gpu_agent * a)
         return HIBF_GPU_ERR_CYCLE;
     if (e & E_VARIANT)
         return HIBF_GPU_ERR_LOGIC;
+    if (e & E_ORDER)
+        return HIBF_GPU_ERR_INVALID_ARG;
     if (e & (E_OVERFLOW_REC | E_OVERFLOW_TASK))
         return HIBF_GPU_ERR_OVERFLOW;
     return HIBF_GPU_OK;
@@ -583,9 +606,11 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
             break;
         unsigned long long const * c = a->h_ctrl.as<unsigned long long>();
         if (st != HIBF_GPU_ERR_OVERFLOW || attempt > 8)
-            fail(st, st == HIBF_GPU_ERR_TIMEOUT ? "device wait limit expired" :
-                     st == HIBF_GPU_ERR_CYCLE   ? "merged bins form a cycle (descent deeper than the hierarchy)" :
-                                                  "batch capacity exceeded");
+            fail(st, st == HIBF_GPU_ERR_TIMEOUT     ? "device wait limit expired" :
+                     st == HIBF_GPU_ERR_CYCLE       ? "merged bins form a cycle (descent deeper than the hierarchy)" :
+                     st == HIBF_GPU_ERR_INVALID_ARG ? "a claim-order entry is not a query index of the batch" :
+                     st == HIBF_GPU_ERR_LOGIC       ? "a tuned kernel variant met an IBF it does not handle" :
+                                                      "batch capacity exceeded");
         if (c[C_ERROR] & E_OVERFLOW_TASK)
             tasks *= 4;
         if (c[C_ERROR] & E_OVERFLOW_REC)
@@ -824,6 +849,60 @@ extern "C"
             });
     }
 
+    int hibf_gpu_agent_set_order_d(hibf_gpu_agent * a, uint32_t const * d_order, uint64_t n_queries)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                a->order = n_queries ? d_order : nullptr;
+                a->order_n = a->order ? n_queries : 0;
+                if (a->graph)
+                {
+                    HG_CUDA(cudaGraphExecDestroy(a->graph));
+                    a->graph = nullptr;
+                }
+            });
+    }
+
+    int hibf_gpu_agent_set_work_out_d(hibf_gpu_agent * a, uint64_t * d_work, uint64_t n_queries)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                a->qwork = n_queries ? reinterpret_cast<unsigned long long *>(d_work) : nullptr;
+                a->qwork_n = a->qwork ? n_queries : 0;
+                if (a->graph)
+                {
+                    HG_CUDA(cudaGraphExecDestroy(a->graph));
+                    a->graph = nullptr;
+                }
+            });
+    }
+
+    int hibf_gpu_agent_query_features_d(hibf_gpu_agent * a, uint64_t const * d_values,
+                                        uint64_t const * d_query_offsets, uint64_t n_queries,
+                                        uint64_t const * d_thresholds, uint32_t probe, float * d_features)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !d_query_offsets || !d_thresholds || (n_queries && !d_features) || probe == 0)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                if (!n_queries)
+                    return;
+                query_params p = base_params(a, d_values, d_query_offsets, d_thresholds, n_queries, ~0ull);
+                uint64_t const want = (n_queries + 7) / 8;
+                unsigned const grid = static_cast<unsigned>(
+                    std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(sm_count()) * 8u)));
+                features_kernel(a->h->hash_count)<<<grid, 256, query_smem(a->h), a->stream>>>(p, probe, d_features);
+                HG_CUDA(cudaGetLastError());
+            });
+    }
+
     int hibf_gpu_agent_get_tuning(hibf_gpu_agent * a, hibf_gpu_tuning * t)
     {
         if (!a || !t)
@@ -1051,6 +1130,9 @@ extern "C"
                         HG_CUDA(cudaFuncSetAttribute(query_kernel(h->hash_count, v),
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      static_cast<int>(std::max<size_t>(smem, 48 * 1024))));
+                    HG_CUDA(cudaFuncSetAttribute(features_kernel(h->hash_count),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(std::max<size_t>(smem, 48 * 1024))));
                 }
                 catch (...)
                 {

@@ -53,6 +53,7 @@ constexpr unsigned long long E_OVERFLOW_TASK = 2ull;
 constexpr unsigned long long E_TIMEOUT = 4ull;
 constexpr unsigned long long E_CYCLE = 8ull;
 constexpr unsigned long long E_VARIANT = 16ull; // a tuned variant met a row of more than 4 words (host rejects this)
+constexpr unsigned long long E_ORDER = 32ull;   // a claim-order entry was not a query index (skipped)
 
 // Tuning variants of the counting loop (compile-time), one kernel each:
 //   UM  values hashed per lane per pass, as a multiple of max(1, 4 / lanes-per-row): more row loads in flight
@@ -99,6 +100,10 @@ struct query_params
     uint32_t ee_step;
     uint32_t ee_stages;
     uint32_t ee_min;
+    // optional: root tasks are claimed in this order of queries (a permutation of 0..n_queries-1), and the executed
+    // value visits of every query are added to qwork[query + q_base]
+    uint32_t const * order;
+    unsigned long long * qwork;
 };
 
 using query_kernel_t = void (*)(query_params);
@@ -262,6 +267,8 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
     {
         if (lane == 0)
         {
+            if (p.qwork)
+                atomicAdd(p.qwork + q + p.q_base, static_cast<unsigned long long>(done));
             __threadfence();
             atomicAdd(p.ctrl + C_PENDING, ~0ull); // retires without results or children
             ++n_tasks;
@@ -366,6 +373,8 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
     __syncwarp();
     if (lane == 0)
     {
+        if (p.qwork)
+            atomicAdd(p.qwork + q + p.q_base, static_cast<unsigned long long>(done));
         __threadfence();
         atomicAdd(p.ctrl + C_PENDING, ~0ull); // this task retires
         ++n_tasks;
@@ -407,7 +416,18 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
         unsigned long long task;
         if (idx < p.n_queries)
         {
-            task = make_task(idx, 0u, 0u);
+            uint64_t const q = p.order ? p.order[idx] : idx;
+            if (q >= p.n_queries)
+            {
+                if (lane == 0)
+                {
+                    atomicOr(p.ctrl + C_ERROR, E_ORDER);
+                    __threadfence();
+                    atomicAdd(p.ctrl + C_PENDING, ~0ull);
+                }
+                continue;
+            }
+            task = make_task(q, 0u, 0u);
         }
         else
         {
@@ -428,6 +448,95 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
         atomicAdd(p.stats + 0, n_tasks);
         atomicAdd(p.stats + 1, n_visits);
         atomicAdd(p.stats + 2, n_executed);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Features of the learned scheduler (cost_model.cu): cheap per-query inputs from which it predicts a query's work.
+// One warp per query counts the query's first `probe` values in the root IBF, then summarises the root's segments:
+//   f0 = log2(1 + n) / 16          f1 = min(t / n, 2)               f2 = best segment count / probe values
+//   f3 = min(#segments reaching t/n of the probe, 8) / 8               f4 = the same for merged bins only
+//   f5 = probe values / probe
+// ---------------------------------------------------------------------------------------------------------------
+constexpr int kCostFeatures = 6;
+using features_kernel_t = void (*)(query_params, uint32_t, float *);
+
+template <int H>
+__global__ void __launch_bounds__(256) k_query_features(query_params p, uint32_t probe, float * __restrict__ out)
+{
+    extern __shared__ uint32_t s_counts[];
+    int const lane = threadIdx.x & 31;
+    uint32_t * counts = s_counts + (threadIdx.x >> 5) * p.counters_per_warp;
+    uint64_t const warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
+    uint64_t const nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+    dev_node const nd = p.nodes[0];
+    row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
+    uint32_t const ncount = nd.bin_words > 32 ? 64u * nd.bin_words : (64u << nd.lpv_log2);
+    uint2 const * d = p.descs + nd.desc_offset;
+    for (uint64_t q = warp; q < p.n_queries; q += nwarps)
+    {
+        uint64_t const b0 = p.qoff[q];
+        uint64_t const n = p.qoff[q + 1] - b0;
+        uint64_t const m = n < probe ? n : probe;
+        for (uint32_t i = lane; i < ncount; i += 32)
+            counts[i] = 0;
+        __syncwarp();
+        if (m)
+            count_variant<H, 0>(rp, nd.lpv_log2, p.values + b0, m, counts, lane);
+        __syncwarp();
+        double const rate = n ? static_cast<double>(p.thr[q]) / static_cast<double>(n) : 0.0;
+        unsigned long long const need = static_cast<unsigned long long>(ceil(rate * static_cast<double>(m)));
+        unsigned long long best = 0;
+        uint32_t pass_seg = 0, pass_merged = 0;
+        unsigned long long carry = 0;
+        for (uint32_t c = 0; c < nd.bins; c += 32)
+        {
+            uint32_t const b = c + lane;
+            bool const valid = b < nd.bins;
+            uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
+            unsigned long long x = valid ? static_cast<unsigned long long>(counts[b]) : 0ull;
+            bool f = valid && (ds.y & F_HEAD);
+            if (lane == 0 && !f)
+                x += carry;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
+                int const fy = __shfl_up_sync(kFullMask, static_cast<int>(f), o);
+                if (lane >= o)
+                {
+                    if (!f)
+                        x += y;
+                    f = f || fy;
+                }
+            }
+            bool const ends = valid && (ds.y & (F_RUN_END | F_MERGED));
+            bool const pass = ends && m && x >= need;
+            if (ends && x > best)
+                best = x;
+            pass_seg += __popc(__ballot_sync(kFullMask, pass));
+            pass_merged += __popc(__ballot_sync(kFullMask, pass && (ds.y & F_MERGED)));
+            unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
+            uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
+            carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            unsigned long long const y = __shfl_xor_sync(kFullMask, best, o);
+            best = y > best ? y : best;
+        }
+        if (lane == 0)
+        {
+            float * f = out + q * kCostFeatures;
+            f[0] = log2f(1.0f + static_cast<float>(n)) / 16.0f;
+            f[1] = static_cast<float>(rate < 2.0 ? rate : 2.0);
+            f[2] = m ? static_cast<float>(best) / static_cast<float>(m) : 0.0f;
+            f[3] = static_cast<float>(pass_seg < 8u ? pass_seg : 8u) / 8.0f;
+            f[4] = static_cast<float>(pass_merged < 8u ? pass_merged : 8u) / 8.0f;
+            f[5] = probe ? static_cast<float>(m) / static_cast<float>(probe) : 0.0f;
+        }
+        __syncwarp();
     }
 }
 
@@ -466,6 +575,28 @@ query_kernel_t query_kernel_h2(int v);
 query_kernel_t query_kernel_h3(int v);
 query_kernel_t query_kernel_h4(int v);
 query_kernel_t query_kernel_h5(int v);
+features_kernel_t features_kernel_h1();
+features_kernel_t features_kernel_h2();
+features_kernel_t features_kernel_h3();
+features_kernel_t features_kernel_h4();
+features_kernel_t features_kernel_h5();
+
+inline features_kernel_t features_kernel(uint32_t h)
+{
+    switch (h)
+    {
+    case 1:
+        return features_kernel_h1();
+    case 2:
+        return features_kernel_h2();
+    case 3:
+        return features_kernel_h3();
+    case 4:
+        return features_kernel_h4();
+    default:
+        return features_kernel_h5();
+    }
+}
 
 inline query_kernel_t query_kernel(uint32_t h, int v)
 {

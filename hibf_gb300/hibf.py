@@ -223,6 +223,22 @@ class _agent_base:
         N.call("hibf_gpu_agent_kernel_ms", self._a, ctypes.byref(ms))
         return float(ms.value)
 
+    def set_order(self, d_order: int | None, n_queries: int = 0) -> None:
+        """Claim order of root tasks for later batches of exactly n_queries queries (device uint32 permutation;
+        None: query order)."""
+        N.call("hibf_gpu_agent_set_order_d", self._a, d_order, n_queries if d_order else 0)
+
+    def set_work_out(self, d_work: int | None, n_queries: int = 0) -> None:
+        """Record each query's executed value visits into a device uint64 array of n_queries entries during later
+        batches (None: off)."""
+        N.call("hibf_gpu_agent_set_work_out_d", self._a, d_work, n_queries if d_work else 0)
+
+    def query_features(self, d_values: int, d_query_offsets: int, n_queries: int, d_thresholds: int, probe: int,
+                       d_features: int) -> None:
+        """The learned scheduler's per-query features (float32, 6 per query), asynchronous on the agent's stream."""
+        N.call("hibf_gpu_agent_query_features_d", self._a, d_values, d_query_offsets, n_queries, d_thresholds,
+               probe, d_features)
+
     @property
     def tuning(self) -> dict:
         """The persistent kernel's schedule (hibf_gpu_tuning fields)."""

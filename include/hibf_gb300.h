@@ -320,6 +320,51 @@ int hibf_gpu_agent_autotune(hibf_gpu_agent * a, int mode, uint64_t const * d_val
                             hibf_gpu_tune_trial * trials, uint64_t cap, uint64_t * n_trials);
 
 /* ============================================================================================================ */
+/* Learned scheduler (no counterpart in the reference): a small MLP predicts each query's work from cheap features  */
+/* and the persistent kernel claims root tasks largest-first.  Only the order of tasks changes; results are exact.  */
+/* ============================================================================================================ */
+#define HIBF_GPU_COST_FEATURES 6
+#define HIBF_GPU_COST_PARAMS 1313
+/* Claim order of the root tasks for the agent's later batches: a device permutation of 0..n_queries-1 (NULL or
+ * n_queries == 0: query order).  Later batches must have exactly n_queries queries (else INVALID_ARG); an entry that
+ * is not a query index is skipped and reported as INVALID_ARG by the batch status.  The pointer is used as given by
+ * every later batch (a captured graph is dropped: capture again).  Ignored by the plain form. */
+int hibf_gpu_agent_set_order_d(hibf_gpu_agent * a, uint32_t const * d_order, uint64_t n_queries);
+/* Records each query's executed value visits (summed over its tasks) into d_work[0..n) during later batches of at
+ * most n_queries queries (zeroed at each batch start; NULL: off).  The training target of the cost model. */
+int hibf_gpu_agent_set_work_out_d(hibf_gpu_agent * a, uint64_t * d_work, uint64_t n_queries);
+/* Features of each query, HIBF_GPU_COST_FEATURES floats per query: log2(1+n)/16, min(t/n, 2), and from the root
+ * IBF's counts over the first `probe` values: the best segment's count / probe values, the number of segments and
+ * of merged bins that reach t/n of the probe (/ 8, at most 1), probe values / probe.  Asynchronous on the agent's
+ * stream. */
+int hibf_gpu_agent_query_features_d(hibf_gpu_agent * a, uint64_t const * d_values, uint64_t const * d_query_offsets,
+                                    uint64_t n_queries, uint64_t const * d_thresholds, uint32_t probe,
+                                    float * d_features);
+typedef struct hibf_gpu_cost_model hibf_gpu_cost_model;
+/* 6 -> 32 -> 32 -> 1 ReLU network, He-uniform initial weights from a seeded splitmix64 stream. */
+int hibf_gpu_cost_model_create(uint64_t seed, hibf_gpu_cost_model ** out);
+int hibf_gpu_cost_model_destroy(hibf_gpu_cost_model * m);
+/* HIBF_GPU_COST_PARAMS floats: W1[32][6], b1[32], W2[32][32], b2[32], w3[32], b3 (set resets the optimiser). */
+int hibf_gpu_cost_model_get_params(hibf_gpu_cost_model * m, float * out);
+int hibf_gpu_cost_model_set_params(hibf_gpu_cost_model * m, float const * in);
+/* Mean squared error of the prediction against log(1 + d_work[i]) over n samples and its gradient (host array of
+ * HIBF_GPU_COST_PARAMS floats, may be NULL), computed by the device's backward kernel.  Synchronous. */
+int hibf_gpu_cost_model_loss_grad_d(hibf_gpu_cost_model * m, float const * d_features, uint64_t const * d_work,
+                                    uint64_t n, float * grads, double * loss);
+/* `steps` full-batch Adam steps (learning rate lr) on the device; *loss = the final mean squared error. */
+int hibf_gpu_cost_model_train_d(hibf_gpu_cost_model * m, float const * d_features, uint64_t const * d_work,
+                                uint64_t n, uint32_t steps, float lr, double * loss);
+/* Predicted log(1 + work) per query. */
+int hibf_gpu_cost_model_predict_d(hibf_gpu_cost_model * m, float const * d_features, uint64_t n, float * d_pred,
+                                  void * stream);
+/* Claim order by predicted work, largest first (ties in query order): predict, then a stable descending sort. */
+int hibf_gpu_cost_model_order_d(hibf_gpu_cost_model * m, float const * d_features, uint64_t n, uint32_t * d_order,
+                                void * stream);
+/* The same stable descending sort for caller-supplied keys (e.g. a heuristic's), using the model's scratch. */
+int hibf_gpu_sort_desc_d(hibf_gpu_cost_model * m, float const * d_keys, uint64_t n, uint32_t * d_order,
+                         void * stream);
+
+/* ============================================================================================================ */
 /* Continuous-batching server over a resident HIBF (no counterpart in the reference, whose agents answer one query   */
 /* per call).  A loop thread owns n_slots agents with their own streams; waiting requests are coalesced oldest-first */
 /* into one batch per free slot, bounded by the slot capacity (queries, values) and by admission_bytes, the device   */

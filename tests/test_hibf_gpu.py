@@ -209,3 +209,50 @@ def test_autotune_keeps_the_fastest_and_the_results(gpu_lib, name):
     offs, ids, _ = a.query_batch(qv, qo, t)
     for i, (g, e) in enumerate(zip(_split(offs, ids), G.mem_lists(d, "mem_sorted"))):
         np.testing.assert_array_equal(g, e, err_msg=f"query {i}")
+
+
+def test_claim_order_work_counters_and_features(gpu_lib):
+    """A permuted claim order gives the same results; per-query work sums to the batch's executed visits; the
+    scheduler's features are well-formed."""
+    import torch
+
+    d = G.hibf_case("synth600")
+    H = _gpu_hibf(d)
+    a = H.membership_agent()
+    qv, qo, t = d["q_values"], d["q_offsets"], d["mem_t"]
+    nq = qo.size - 1
+    dv = torch.from_numpy(qv.view(np.int64)).cuda()
+    dq = torch.from_numpy(qo.view(np.int64)).cuda()
+    dt = torch.from_numpy(t.astype(np.uint64).view(np.int64)).cuda()
+    perm = np.random.default_rng(1).permutation(nq).astype(np.uint32)
+    dperm = torch.from_numpy(perm.view(np.int32)).cuda()
+    work = torch.zeros(nq, dtype=torch.int64, device="cuda")
+    a.set_work_out(work.data_ptr(), nq)
+    a.set_order(dperm.data_ptr(), nq)
+    offs, ids, _ = a.query_batch(qv, qo, t)
+    for i, (g, e) in enumerate(zip(_split(offs, ids), G.mem_lists(d, "mem_sorted"))):
+        np.testing.assert_array_equal(g, e, err_msg=f"query {i}")
+    w = work.cpu().numpy().view(np.uint64)
+    assert int(w.sum()) == a.last_work_executed()
+    assert np.all(w >= np.minimum(np.diff(qo), 1))  # every query reads at least one value at the root (if any)
+    bad = perm.copy()
+    bad[5] = nq + 7
+    dbad = torch.from_numpy(bad.view(np.int32)).cuda()
+    a.set_order(dbad.data_ptr(), nq)
+    with pytest.raises(hg.InvalidArgument):
+        a.query_batch(qv, qo, t)
+    a.set_order(dperm.data_ptr(), nq - 1)
+    with pytest.raises(hg.InvalidArgument, match="different length"):
+        a.query_batch(qv, qo, t)
+    a.set_order(None)
+    a.set_work_out(None)
+    offs, ids, _ = a.query_batch(qv, qo, t)
+    assert np.array_equal(_split(offs, ids)[-1], G.mem_lists(d, "mem_sorted")[-1])
+    feats = torch.zeros(nq * 6, dtype=torch.float32, device="cuda")
+    a.query_features(dv.data_ptr(), dq.data_ptr(), nq, dt.data_ptr(), 16, feats.data_ptr())
+    torch.cuda.synchronize()
+    f = feats.cpu().numpy().reshape(nq, 6)
+    n = np.diff(qo).astype(np.float64)
+    np.testing.assert_allclose(f[:, 0], np.log2(1 + n) / 16, rtol=1e-6)
+    np.testing.assert_allclose(f[:, 5], np.minimum(n, 16) / 16, rtol=1e-6)
+    assert np.all((f[:, 2] >= 0) & (f[:, 2] <= 1)) and np.all((f[:, 3] >= 0) & (f[:, 3] <= 1))
