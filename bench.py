@@ -58,7 +58,7 @@ def parse_args():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel schedule")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned scheduler measurement")
-    ap.add_argument("--sched-queries", type=int, default=65536, help="batch size of the learned scheduler test")
+    ap.add_argument("--sched-queries", type=int, default=20000, help="batch size of the learned scheduler test")
     ap.add_argument("--tune-queries", type=int, default=200_000, help="sample batch of the autotuner")
     ap.add_argument("--l2-fetch", type=int, default=-1,
                     help="set the context's L2 fetch granularity hint (bytes) before the run; -1 leaves it")
@@ -210,7 +210,7 @@ def learned_scheduler(hibf, tuning, d_v, d_qo, d_thr, qo, nq, n, stream):
         v, q, t = sub(first)
         f = torch.zeros(n * 6, dtype=torch.float32, device="cuda")
         w = torch.zeros(n, dtype=torch.int64, device="cuda")
-        a.query_features(v, q, n, t, 16, f.data_ptr())
+        a.query_features(v, q, n, t, 32, f.data_ptr())
         a.set_work_out(w.data_ptr(), n)
         a.query_batch_device(v, q, n, t)
         stream.synchronize()

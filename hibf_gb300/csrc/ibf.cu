@@ -160,10 +160,104 @@ __global__ void k_bulk_contains(row_params rp, uint64_t const * __restrict__ val
     }
 }
 
+// bulk_contains for rows of up to 32 words with H hash functions: the same work mapping as the counting loop
+// (count.cuh) -- LPV lanes per row, lanes hash U values each, the H row words of four sub-steps are loaded together
+// (4 * H loads per lane in flight) -- and each lane stores its word of the AND.
+template <int LPV, int H>
+__global__ void __launch_bounds__(256) k_bulk_contains_h(row_params rp, uint64_t const * __restrict__ values,
+                                                         uint64_t n, uint64_t * __restrict__ out)
+{
+    constexpr int G = 32 / LPV;
+    constexpr int U = LPV >= 4 ? 1 : 4 / LPV;
+    constexpr int STEPS = U * LPV;
+    constexpr int BLOCK = 32 * U;
+    int const lane = threadIdx.x & 31;
+    int const g = lane / LPV;
+    int const j = lane % LPV;
+    bool const wj = static_cast<uint32_t>(j) < rp.bin_words;
+    uint64_t const bw = rp.bin_words;
+    uint64_t const * __restrict__ words = rp.words + j;
+    uint64_t const warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
+    uint64_t const nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t base = warp * BLOCK; base < n; base += nwarps * BLOCK)
+    {
+        uint64_t off[U][H];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+        {
+            uint64_t const idx = base + static_cast<uint64_t>(u * 32 + lane);
+            uint64_t const v = idx < n ? values[idx] : 0u;
+#pragma unroll
+            for (int i = 0; i < H; ++i)
+                off[u][i] = hash_row(v, c_hash_seeds[i], rp.hash_shift, rp.bin_size) * rp.row_words;
+        }
+#pragma unroll 1
+        for (int s = 0; s < STEPS; s += 4)
+        {
+            uint64_t w[4][H];
+            uint64_t idx[4];
+            bool ok[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+            {
+                int const step = s + t;
+                int const u = U == 1 ? 0 : step / LPV;
+                int const src = (step % LPV) * G + g;
+                idx[t] = base + static_cast<uint64_t>(u * 32 + src);
+                ok[t] = wj && idx[t] < n;
+#pragma unroll
+                for (int i = 0; i < H; ++i)
+                {
+                    uint64_t o = off[u][i];
+                    if constexpr (LPV > 1)
+                        o = __shfl_sync(kFullMask, o, src);
+                    w[t][i] = ok[t] ? __ldg(words + o) : 0ull;
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+            {
+                uint64_t x = w[t][0];
+#pragma unroll
+                for (int i = 1; i < H; ++i)
+                    x &= w[t][i];
+                if (ok[t])
+                    out[idx[t] * bw + j] = x;
+            }
+        }
+    }
+}
+
+template <int H>
+void launch_contains_h(row_params const & rp, uint32_t lpv_log2, uint64_t const * d_values, uint64_t n,
+                       uint64_t * d_out, unsigned grid, cudaStream_t s)
+{
+    switch (lpv_log2)
+    {
+    case 0:
+        k_bulk_contains_h<1, H><<<grid, 256, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    case 1:
+        k_bulk_contains_h<2, H><<<grid, 256, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    case 2:
+        k_bulk_contains_h<4, H><<<grid, 256, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    case 3:
+        k_bulk_contains_h<8, H><<<grid, 256, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    case 4:
+        k_bulk_contains_h<16, H><<<grid, 256, 0, s>>>(rp, d_values, n, d_out);
+        break;
+    default:
+        k_bulk_contains_h<32, H><<<grid, 256, 0, s>>>(rp, d_values, n, d_out);
+    }
+}
+
 // bulk_count over n values into one counting vector: every warp counts a contiguous chunk into the block's shared
 // counters, the block adds them to 64-bit global totals.
 template <int H>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, 2)
     k_bulk_count(row_params rp, uint32_t lpv_log2, uint64_t const * __restrict__ values, uint64_t n, uint64_t chunk,
                  unsigned long long * __restrict__ totals, uint32_t n_counters)
 {
@@ -341,28 +435,32 @@ void launch_contains(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, ui
         return;
     unsigned const block = 256;
     uint32_t const l = f->lpv_log2();
-    uint64_t const lanes = n << l;
-    unsigned const grid = grid_for(lanes, block);
     row_params const rp = f->rp();
-    switch (l)
+    if (f->bin_words > 32)
     {
-    case 0:
-        k_bulk_contains<1><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
-        break;
-    case 1:
-        k_bulk_contains<2><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
-        break;
-    case 2:
-        k_bulk_contains<4><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
-        break;
-    case 3:
-        k_bulk_contains<8><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
-        break;
-    case 4:
-        k_bulk_contains<16><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
-        break;
-    default:
-        k_bulk_contains<32><<<grid, block, 0, s>>>(rp, d_values, n, d_out);
+        // rows wider than a warp: lanes stride over the words
+        k_bulk_contains<32><<<grid_for(n << 5, block), block, 0, s>>>(rp, d_values, n, d_out);
+    }
+    else
+    {
+        unsigned const grid = grid_for(n, block);
+        switch (f->hash_funs)
+        {
+        case 1:
+            launch_contains_h<1>(rp, l, d_values, n, d_out, grid, s);
+            break;
+        case 2:
+            launch_contains_h<2>(rp, l, d_values, n, d_out, grid, s);
+            break;
+        case 3:
+            launch_contains_h<3>(rp, l, d_values, n, d_out, grid, s);
+            break;
+        case 4:
+            launch_contains_h<4>(rp, l, d_values, n, d_out, grid, s);
+            break;
+        default:
+            launch_contains_h<5>(rp, l, d_values, n, d_out, grid, s);
+        }
     }
     HG_CUDA(cudaGetLastError());
 }
