@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel schedule")
+    ap.add_argument("--tuning", type=str, default="",
+                    help="fixed kernel schedule 'values_per_lane,fetch_bytes,counter_bits' (skips the autotuner)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned scheduler measurement")
     ap.add_argument("--sched-queries", type=int, default=20000, help="batch size of the learned scheduler test")
     ap.add_argument("--tune-queries", type=int, default=200_000, help="sample batch of the autotuner")
@@ -292,7 +294,11 @@ def run_ours(args, wl, rank, world, local):
     agent.set_stream(stream.cuda_stream)
     # autotune the kernel schedule on the batch's first queries (results are checked identical across schedules)
     tune = None
-    if not args.no_autotune:
+    if args.tuning:
+        vpl, fb, cb = (int(x) for x in args.tuning.split(","))
+        agent.tuning = dict(agent.tuning, values_per_lane=vpl, fetch_bytes=fb, counter_bits=cb)
+        tune = {"fixed": agent.tuning}
+    elif not args.no_autotune:
         ns = min(nq, args.tune_queries)
         t0 = time.perf_counter()
         trials = agent.autotune(d_v.data_ptr(), d_qo.data_ptr(), ns, d_thr.data_ptr(), reps=2)
@@ -532,6 +538,17 @@ def ibf_cpu_sample(O, w, budget_s, threads):
         n = min(w["n_queries"], n * 4)
 
 
+def ibf_workload(scale=1.0):
+    """The 1,024-bin IBF workload; scale < 1 shrinks the bin size, values per bin and query values together (for
+    profiling captures that must stay small)."""
+    w = dict(IBF1024)
+    if scale != 1.0:
+        w["bin_size"] = max(1 << 12, int(w["bin_size"] * scale))
+        w["values_per_bin"] = max(1, int(w["values_per_bin"] * scale))
+        w["n_queries"] = max(1 << 16, int(w["n_queries"] * scale))
+    return w
+
+
 def build_ibf1024(w, stream):
     import torch
 
@@ -559,7 +576,7 @@ def run_ibf_ours(args, rank, world, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    w = dict(IBF1024)
+    w = ibf_workload(args.scale)
     nq = args.queries or w["n_queries"]
     stream = torch.cuda.Stream()
     ibf, build_ms = build_ibf1024(w, stream)
@@ -663,7 +680,8 @@ def run_ibf_ours(args, rank, world, local):
             "value": value, "unit": "values/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic: seeded splitmix64 bins and query values (include/hibf_gb300_synthetic.h)",
-            "config": {"workload": WORKLOAD_DESC["ibf1024"], "name": "ibf1024", "bins": w["bins"],
+            "config": {"workload": WORKLOAD_DESC["ibf1024"], "name": "ibf1024", "size_scale": args.scale,
+                       "bins": w["bins"],
                        "bin_size": w["bin_size"], "hash_functions": w["h"], "query_values_per_step": nq,
                        "index_bytes": w["bins"] // 64 * 8 * w["bin_size"], "parallelism": f"replicas x{world}",
                        "l2": "index (8 GiB) and outputs (2 GiB) larger than L2; no flush",
@@ -700,7 +718,7 @@ def run_ibf_reference(args, rank, world, local):
     import torch
 
     torch.cuda.set_device(local)
-    w = dict(IBF1024)
+    w = ibf_workload(args.scale)
     stream = torch.cuda.Stream()
     ibf, _ = build_ibf1024(w, stream)
     O = ibf_oracle_from_device(ibf, w)

@@ -256,8 +256,10 @@ void launch_contains_h(row_params const & rp, uint32_t lpv_log2, uint64_t const 
 
 // bulk_count over n values into one counting vector: every warp counts a contiguous chunk into the block's shared
 // counters, the block adds them to 64-bit global totals.
+// Four blocks per SM (64 registers, some spilled for h >= 3) measured faster than two blocks without spills (1.53 vs
+// 2.16 ms for 2^24 values on 1,024 bins, h = 3): more warps keep more row loads in flight.
 template <int H>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, 4)
     k_bulk_count(row_params rp, uint32_t lpv_log2, uint64_t const * __restrict__ values, uint64_t n, uint64_t chunk,
                  unsigned long long * __restrict__ totals, uint32_t n_counters)
 {
