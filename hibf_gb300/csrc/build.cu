@@ -553,6 +553,37 @@ struct hibf_gpu_sink
 extern "C"
 {
 
+    int hibf_gpu_hll_sketch(uint64_t const * values, uint64_t n, uint32_t bits, uint8_t * registers)
+    {
+        return guarded(
+            [&]
+            {
+                if ((n && !values) || !registers)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (bits < 5 || bits > 32)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "sketch bits must be in [5, 32]");
+                hll h(bits);
+                for (uint64_t i = 0; i < n; ++i)
+                    h.add(values[i]);
+                std::copy(h.reg.begin(), h.reg.end(), registers);
+            });
+    }
+
+    int hibf_gpu_hll_estimate(uint8_t const * registers, uint32_t bits, double * estimate)
+    {
+        return guarded(
+            [&]
+            {
+                if (!registers || !estimate)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (bits < 5 || bits > 32)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "sketch bits must be in [5, 32]");
+                hll h(bits);
+                std::copy(registers, registers + h.size, h.reg.begin());
+                *estimate = h.estimate();
+            });
+    }
+
     int hibf_gpu_sink_push(hibf_gpu_sink * sink, uint64_t const * values, uint64_t n)
     {
         return guarded(

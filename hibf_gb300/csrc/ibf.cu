@@ -415,7 +415,10 @@ void launch_count(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int w
     if (n)
     {
         unsigned const block = 256;
-        uint64_t const chunk = 2048;
+        // one contiguous chunk per warp of a full wave (4 blocks of 8 warps per SM), at least 512 values: fewer,
+        // larger chunks left SMs idle on small calls (128 blocks for 2^21 values with fixed 2,048-value chunks)
+        uint64_t const wave = static_cast<uint64_t>(sm_count()) * 4u * 8u;
+        uint64_t const chunk = std::max<uint64_t>(512, ((n + wave - 1) / wave + 127) / 128 * 128);
         uint64_t const warps = (n + chunk - 1) / chunk;
         unsigned const grid = static_cast<unsigned>(
             std::max<uint64_t>(1, std::min<uint64_t>((warps + 7) / 8, static_cast<uint64_t>(sm_count()) * 4u)));

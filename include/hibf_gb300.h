@@ -197,6 +197,16 @@ int hibf_gpu_ibf_build(hibf_gpu_build_config const * cfg, uint64_t max_bin_eleme
 /* The host part of that constructor alone (no device): the bin size in bits and the user bin it was taken from. */
 int hibf_gpu_ibf_plan(hibf_gpu_build_config const * cfg, uint64_t max_bin_elements, uint32_t sketch_bits,
                       hibf_gpu_input_fn input_fn, void * user, uint64_t * bin_size, uint64_t * biggest_user_bin);
+/* HyperLogLog sketches (seqan::hibf::sketch::hyperloglog, src/sketch/hyperloglog.cpp): registers of 2^bits bytes.
+ * Host: hyperloglog(bits) + add(values[i]) for i < n (hyperloglog.cpp:55-70); estimate() (hyperloglog.cpp:72-128).
+ * Device: compute_sketches (src/sketch/compute_sketches.cpp:27-43) for n_user_bins user bins at once, user bin u =
+ * d_values[offsets[u] .. offsets[u+1]) (host offsets), or, when d_values is NULL, those positions of the splitmix64
+ * stream `seed`; d_registers receives n_user_bins * 2^bits bytes, the same registers as the host.  bits in [5, 16]
+ * on the device.  Synchronous. */
+int hibf_gpu_hll_sketch(uint64_t const * values, uint64_t n, uint32_t bits, uint8_t * registers);
+int hibf_gpu_hll_estimate(uint8_t const * registers, uint32_t bits, double * estimate);
+int hibf_gpu_hll_sketch_d(uint64_t const * d_values, uint64_t seed, uint64_t const * offsets, uint64_t n_user_bins,
+                          uint32_t bits, uint8_t * d_registers, void * stream);
 /* Host-only planning for pairwise disjoint user bins of the given distinct sizes: the IBF count and total bins
  * (first call with NULL arrays), then sizes, tables and each IBF's parent (IBF, bin).  No device needed. */
 int hibf_gpu_plan_disjoint(hibf_gpu_build_config const * cfg, char const * layout_text,
