@@ -123,6 +123,7 @@ _SIGS = [
     ("hibf_gpu_hll_sketch", None, [vp, u64, ctypes.c_uint32, vp]),
     ("hibf_gpu_hll_estimate", None, [vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_hll_sketch_d", None, [vp, u64, vp, u64, ctypes.c_uint32, vp, vp]),
+    ("hibf_gpu_hibf_build_inputs", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, INPUT_FN, vp, vp, vp]),
     ("hibf_gpu_ibf_plan", None, [ctypes.POINTER(BuildConfig), u64, ctypes.c_uint32, INPUT_FN, vp, u64p, u64p]),
     ("hibf_gpu_hibf_build_synthetic", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, u64, vp,
                                              ctypes.POINTER(vp)]),

@@ -213,3 +213,22 @@ def ibf_plan(configuration: config, max_bin_elements: int = 0) -> tuple[int, int
     N.call("hibf_gpu_ibf_plan", ctypes.byref(_cfg(configuration, False)), int(max_bin_elements),
            configuration.sketch_bits, cb, None, ctypes.byref(size), ctypes.byref(best))
     return size.value, best.value
+
+
+def build_inputs(configuration: config, layout_text: str) -> tuple[np.ndarray, np.ndarray]:
+    """Host part of the build alone: (offsets, values) of every user bin's distinct values in insertion order, split
+    user bins in the reference's chunk order (chunk k of ceil(n / tbs) values -> technical bin storage + k)."""
+    configuration.validate_and_set_defaults()
+    fn = configuration.input_fn
+
+    def trampoline(_user, ub, sink):
+        fn(int(ub), insert_iterator(sink))
+
+    cb = N.INPUT_FN(trampoline)
+    c = _cfg(configuration, False)
+    offs = np.zeros(configuration.number_of_user_bins + 1, np.uint64)
+    N.call("hibf_gpu_hibf_build_inputs", ctypes.byref(c), layout_text.encode(), cb, None, offs.ctypes.data, None)
+    vals = np.zeros(int(offs[-1]), np.uint64)
+    N.call("hibf_gpu_hibf_build_inputs", ctypes.byref(c), layout_text.encode(), cb, None, offs.ctypes.data,
+           vals.ctypes.data)
+    return offs, vals

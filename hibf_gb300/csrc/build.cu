@@ -11,13 +11,15 @@
 // IBFs are numbered in depth-first pre-order with children in layout order (the reference numbers them in a
 // randomised order, HIBF.cpp:111-116; numbering does not change any bit or query result).
 //
-// Split user bins are chunked in the order their distinct values first appear (stream order).  The reference
-// chunks in the iteration order of its hash set (robin_hood::unordered_flat_set, insert_into_ibf.cpp:34-47), which
-// changes which of the split bins a value lands in, not the sizes, tables or the bins of any unsplit user bin.
+// Split user bins: the input_fn build chunks them in the reference's order (the iteration order of its hash set,
+// robin_hood::unordered_flat_set, insert_into_ibf.cpp:34-47, replayed by reference_split_orders), so its bit store
+// equals the reference's.  The synthetic build (values generated on the device, no host sets) chunks in stream
+// order: which of the split bins a value lands in differs; sizes, tables and every unsplit user bin's bins do not.
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <unordered_set>
 #include <vector>
@@ -26,6 +28,7 @@
 #include "common.hpp"
 #include "device.cuh"
 #include "hibf_internal.cuh"
+#include "rh_set.hpp"
 
 namespace hibf_gb300
 {
@@ -353,6 +356,61 @@ plan_t make_plan(hibf_gpu_build_config const & cfg, layout_t const & L, std::vec
     return P;
 }
 
+// The order in which the reference chunks every user bin it splits over several technical bins: its hash set's
+// iteration order at that moment.  hierarchical_build (src/hierarchical_interleaved_bloom_filter.cpp:39-171) keeps
+// one set per IBF for the max bin and the records (cleared, not shrunk, between records), fills it through the
+// favourite child when the max bin is merged, and adds every non-root set to its parent's; the root's other
+// children run in a shuffled order but with sets of their own, so nothing observable depends on that order.  The
+// history is replayed here on rh_set.  `sets[u]` = user bin u's distinct values in input order.
+std::vector<std::vector<uint64_t>> reference_split_orders(plan_t const & P,
+                                                          std::vector<std::vector<uint64_t>> const & sets)
+{
+    std::vector<std::vector<uint64_t>> out(sets.size());
+    std::function<void(size_t, rh_set *, bool)> build_node = [&](size_t n, rh_set * parent, bool is_root)
+    {
+        node_t const & node = P.g[n];
+        bool const max_merged = node.favourite >= 0;
+        auto add_to_parent = [&](rh_set const & k)
+        {
+            if (!is_root)
+                k.for_each([&](uint64_t v) { parent->insert(v); });
+        };
+        auto take = [&](rh_set & k, user_bin_rec const & r)
+        {
+            for (uint64_t v : sets[r.idx])
+                k.insert(v);
+            if (r.ntb > 1)
+                out[r.idx] = k.ordered();
+        };
+        rh_set kmers;
+        if (max_merged)
+            build_node(node.children[static_cast<size_t>(node.favourite)], &kmers, false);
+        else if (!node.records.empty())
+            take(kmers, node.records[0]);
+        add_to_parent(kmers); // construct_ibf
+        kmers.clear();
+        for (size_t i = 0; i < node.children.size(); ++i)
+        {
+            if (max_merged && static_cast<int64_t>(i) == node.favourite)
+                continue;
+            rh_set local;
+            build_node(node.children[i], &local, false);
+            add_to_parent(local);
+        }
+        for (size_t i = max_merged ? 0 : 1; i < node.records.size(); ++i)
+        {
+            user_bin_rec const & r = node.records[i];
+            if (is_root && r.ntb == 1)
+                continue; // inserted straight from input_fn, no set
+            take(kmers, r);
+            add_to_parent(kmers);
+            kmers.clear();
+        }
+    };
+    build_node(0, nullptr, true);
+    return out;
+}
+
 // Distinct values under each node when user bins are pairwise disjoint: sums of their sizes.
 std::vector<uint64_t> disjoint_unions(plan_t const & P, std::vector<uint64_t> const & distinct, layout_t const & L)
 {
@@ -549,6 +607,85 @@ struct hibf_gpu_sink
 {
     std::vector<uint64_t> values;
 };
+
+namespace
+{
+
+// The host part of hibf_gpu_hibf_build: reads every user bin once through input_fn (its distinct values in input
+// order: the set the reference builds with compute_kmers, src/build/compute_kmers.cpp:23-32), sizes the IBFs
+// (exact distinct counts of the unions that size merged max bins), and puts split user bins in the reference's
+// chunk order.  `sets[u]` receives user bin u's values in device insertion order.
+plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_text, hibf_gpu_input_fn input_fn,
+                   void * user, std::vector<std::vector<uint64_t>> & sets_out)
+{
+    hibf_gpu_build_config const * cfg = &cfg_ref;
+    uint64_t const nub = cfg->number_of_user_bins;
+    // Read every user bin once: its distinct values in first-appearance order (the set the reference
+    // builds with compute_kmers, src/build/compute_kmers.cpp:23-32).
+    std::vector<std::vector<uint64_t>> & sets = sets_out;
+    sets.assign(nub, {});
+    std::vector<uint64_t> distinct(nub);
+    for (uint64_t u = 0; u < nub; ++u)
+    {
+        hibf_gpu_sink sink;
+        input_fn(user, u, &sink);
+        std::unordered_set<uint64_t> seen;
+        seen.reserve(sink.values.size() * 2);
+        for (uint64_t v : sink.values)
+            if (seen.insert(v).second)
+                sets[u].push_back(v);
+        distinct[u] = sets[u].size();
+    }
+    layout_t const L = parse_layout(layout_text);
+    plan_t const P0 = make_plan(*cfg, L, distinct, [](size_t) { return uint64_t{1}; });
+    // exact distinct counts of subtree unions (merged max bins), or sums for disjoint user bins
+    std::vector<uint64_t> sums;
+    if (cfg->user_bins_disjoint)
+        sums = disjoint_unions(P0, distinct, L);
+    else
+    {
+        sums.assign(P0.g.size(), 0);
+        std::vector<std::vector<uint64_t>> members(P0.g.size());
+        for (uint64_t u = 0; u < nub; ++u)
+        {
+            size_t n = P0.order[P0.ub_leaf[u]];
+            while (true)
+            {
+                members[n].push_back(u);
+                if (P0.g[n].parent == SIZE_MAX)
+                    break;
+                n = P0.g[n].parent;
+            }
+        }
+        for (size_t n = 0; n < P0.g.size(); ++n)
+        {
+            // only favourite children are sized by their union
+            bool needed = false;
+            if (P0.g[n].parent != SIZE_MAX)
+            {
+                node_t const & p = P0.g[P0.g[n].parent];
+                needed = p.favourite >= 0 && p.children[static_cast<size_t>(p.favourite)] == n;
+            }
+            if (!needed)
+                continue;
+            std::unordered_set<uint64_t> un;
+            for (uint64_t u : members[n])
+                un.insert(sets[u].begin(), sets[u].end());
+            sums[n] = un.size();
+        }
+    }
+    plan_t const P = make_plan(*cfg, L, distinct, [&](size_t node) { return sums[node]; });
+    // split user bins in the reference's chunk order
+    {
+        std::vector<std::vector<uint64_t>> split = reference_split_orders(P, sets);
+        for (uint64_t u = 0; u < nub; ++u)
+            if (P.ub_rec[u].ntb > 1)
+                sets[u] = std::move(split[u]);
+    }
+    return P;
+}
+
+} // namespace
 
 extern "C"
 {
@@ -781,60 +918,8 @@ extern "C"
                     fail(HIBF_GPU_ERR_INVALID_ARG, "null argument (config::input_fn is required)");
                 *out = nullptr;
                 uint64_t const nub = cfg->number_of_user_bins;
-                // Read every user bin once: its distinct values in first-appearance order (the set the reference
-                // builds with compute_kmers, src/build/compute_kmers.cpp:23-32).
-                std::vector<std::vector<uint64_t>> sets(nub);
-                std::vector<uint64_t> distinct(nub);
-                for (uint64_t u = 0; u < nub; ++u)
-                {
-                    hibf_gpu_sink sink;
-                    input_fn(user, u, &sink);
-                    std::unordered_set<uint64_t> seen;
-                    seen.reserve(sink.values.size() * 2);
-                    for (uint64_t v : sink.values)
-                        if (seen.insert(v).second)
-                            sets[u].push_back(v);
-                    distinct[u] = sets[u].size();
-                }
-                layout_t const L = parse_layout(layout_text);
-                plan_t const P0 = make_plan(*cfg, L, distinct, [](size_t) { return uint64_t{1}; });
-                // exact distinct counts of subtree unions (merged max bins), or sums for disjoint user bins
-                std::vector<uint64_t> sums;
-                if (cfg->user_bins_disjoint)
-                    sums = disjoint_unions(P0, distinct, L);
-                else
-                {
-                    sums.assign(P0.g.size(), 0);
-                    std::vector<std::vector<uint64_t>> members(P0.g.size());
-                    for (uint64_t u = 0; u < nub; ++u)
-                    {
-                        size_t n = P0.order[P0.ub_leaf[u]];
-                        while (true)
-                        {
-                            members[n].push_back(u);
-                            if (P0.g[n].parent == SIZE_MAX)
-                                break;
-                            n = P0.g[n].parent;
-                        }
-                    }
-                    for (size_t n = 0; n < P0.g.size(); ++n)
-                    {
-                        // only favourite children are sized by their union
-                        bool needed = false;
-                        if (P0.g[n].parent != SIZE_MAX)
-                        {
-                            node_t const & p = P0.g[P0.g[n].parent];
-                            needed = p.favourite >= 0 && p.children[static_cast<size_t>(p.favourite)] == n;
-                        }
-                        if (!needed)
-                            continue;
-                        std::unordered_set<uint64_t> un;
-                        for (uint64_t u : members[n])
-                            un.insert(sets[u].begin(), sets[u].end());
-                        sums[n] = un.size();
-                    }
-                }
-                plan_t const P = make_plan(*cfg, L, distinct, [&](size_t node) { return sums[node]; });
+                std::vector<std::vector<uint64_t>> sets;
+                plan_t const P = plan_inputs(*cfg, layout_text, input_fn, user, sets);
                 hibf_gpu_hibf * h = create_from_plan(P, nub);
                 try
                 {
@@ -870,6 +955,27 @@ extern "C"
                     throw;
                 }
                 *out = h;
+            });
+    }
+
+    int hibf_gpu_hibf_build_inputs(hibf_gpu_build_config const * cfg, char const * layout_text,
+                                   hibf_gpu_input_fn input_fn, void * user, uint64_t * offsets, uint64_t * values)
+    {
+        return guarded(
+            [&]
+            {
+                validate(cfg);
+                if (!input_fn || !offsets)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::vector<std::vector<uint64_t>> sets;
+                plan_inputs(*cfg, layout_text, input_fn, user, sets);
+                offsets[0] = 0;
+                for (size_t u = 0; u < sets.size(); ++u)
+                {
+                    offsets[u + 1] = offsets[u] + sets[u].size();
+                    if (values)
+                        std::copy(sets[u].begin(), sets[u].end(), values + offsets[u]);
+                }
             });
     }
 

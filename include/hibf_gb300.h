@@ -207,6 +207,13 @@ int hibf_gpu_hll_sketch(uint64_t const * values, uint64_t n, uint32_t bits, uint
 int hibf_gpu_hll_estimate(uint8_t const * registers, uint32_t bits, double * estimate);
 int hibf_gpu_hll_sketch_d(uint64_t const * d_values, uint64_t seed, uint64_t const * offsets, uint64_t n_user_bins,
                           uint32_t bits, uint8_t * d_registers, void * stream);
+/* Host part of hibf_gpu_hibf_build alone (no device): every user bin's distinct values in the order the build
+ * inserts them, user bin u = values[offsets[u] .. offsets[u+1]).  Split user bins come in the reference's chunk
+ * order (its hash set's iteration order, src/build/insert_into_ibf.cpp:28-47, replayed through the history of
+ * hierarchical_build, src/hierarchical_interleaved_bloom_filter.cpp:39-171); chunk k of ceil(n / tbs) values goes
+ * to technical bin storage + k.  First call with values == NULL for the offsets (n_user_bins + 1 entries). */
+int hibf_gpu_hibf_build_inputs(hibf_gpu_build_config const * cfg, char const * layout_text,
+                               hibf_gpu_input_fn input_fn, void * user, uint64_t * offsets, uint64_t * values);
 /* Host-only planning for pairwise disjoint user bins of the given distinct sizes: the IBF count and total bins
  * (first call with NULL arrays), then sizes, tables and each IBF's parent (IBF, bin).  No device needed. */
 int hibf_gpu_plan_disjoint(hibf_gpu_build_config const * cfg, char const * layout_text,

@@ -353,6 +353,18 @@ class Reference:
         return RefIBF(self, self.lib.ref_ibf_from_config(ctypes.byref(cfg), _ptr(v), _ptr(o), max_bin_elements))
 
     # -- layout / HIBF -----------------------------------------------------------------------------------
+    def hll(self, values, bits):
+        """The reference's hyperloglog over `values`: (registers, estimate)."""
+        L = self.lib
+        L.ref_hll.restype = ctypes.c_int
+        L.ref_hll.argtypes = [vp, u64, ctypes.c_uint32, vp, ctypes.POINTER(ctypes.c_double)]
+        v = _u64(values)
+        regs = np.zeros(1 << bits, np.uint8)
+        e = ctypes.c_double(0)
+        if L.ref_hll(_ptr(v), v.size, bits, _ptr(regs), ctypes.byref(e)) != 0:
+            raise RuntimeError("reference hyperloglog failed")
+        return regs, e.value
+
     def layout(self, cfg: RefCfg, values=None, offsets=None, seed=0, synthetic=False) -> str:
         v = None if values is None else _u64(values)
         o = _u64(offsets)

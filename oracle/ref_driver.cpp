@@ -296,6 +296,31 @@ extern "C"
     // ---------------------------------------------------------------------------------------------------------
     // The same steps as hierarchical_interleaved_bloom_filter(config&) (HIBF.cpp:211-245) up to the layout, which
     // is returned in the reference's layout-file format (layout.cpp write_to).  Free with ref_free.
+    // hyperloglog(bits) + add(values[i]) (src/sketch/hyperloglog.cpp:55-70): the registers, read back through
+    // hyperloglog::store (one byte of bits, then 2^bits register bytes), and estimate() (hyperloglog.cpp:72-128).
+    int ref_hll(uint64_t const * values, uint64_t n, uint32_t bits, uint8_t * registers, double * estimate)
+    {
+        try
+        {
+            hibf::sketch::hyperloglog h(static_cast<uint8_t>(bits));
+            for (uint64_t i = 0; i < n; ++i)
+                h.add(values[i]);
+            std::ostringstream os;
+            h.store(os);
+            std::string const raw = os.str();
+            uint64_t const size = uint64_t{1} << bits;
+            if (raw.size() != 1 + size)
+                return 1;
+            std::memcpy(registers, raw.data() + 1, size);
+            *estimate = h.estimate();
+            return 0;
+        }
+        catch (...)
+        {
+            return 1;
+        }
+    }
+
     char * ref_layout(ref_cfg const * c, uint64_t const * values, uint64_t const * offsets, uint64_t seed, int synthetic)
     {
         try

@@ -271,6 +271,23 @@ def make_ibf_config(R: Reference):
     np.savez_compressed(OUT / "ibf_config.npz", **out)
 
 
+def make_hll(R: Reference):
+    """hyperloglog registers and estimates for a few value sets and widths (src/sketch/hyperloglog.cpp)."""
+    out = {}
+    rng = np.random.default_rng(21)
+    cases = [(S.stream_range(3, 0, 1000), 12), (S.stream_range(4, 0, 200000), 12), (S.stream_range(5, 0, 5), 5),
+             (rng.integers(0, 1 << 63, 30000, dtype=np.uint64), 8), (np.zeros(0, np.uint64), 12),
+             (np.arange(100000, dtype=np.uint64), 14), (S.stream_range(6, 0, 50000), 16)]
+    for i, (v, bits) in enumerate(cases):
+        regs, est = R.hll(v, bits)
+        out[f"c{i}_values"] = np.asarray(v, np.uint64)
+        out[f"c{i}_bits"] = np.array([bits], np.uint64)
+        out[f"c{i}_registers"] = regs
+        out[f"c{i}_estimate"] = np.array([est], np.float64)
+    out["n_cases"] = np.array([len(cases)], np.uint64)
+    np.savez_compressed(OUT / "hll_cases.npz", **out)
+
+
 def make_c1(R: Reference):
     """The 64-user-bin workload at full size: everything except the bit words (which are 2.9 MB)."""
     sizes = S.user_bin_sizes(1, 64, S.SIZES_LOG_UNIFORM, 0, 0, 1000, 100000)
@@ -313,9 +330,11 @@ def make_c4_layout(R: Reference):
 def main(argv):
     build_reference()
     R = Reference()
-    which = set(argv) or {"ibf", "ibfcfg", "hibf", "hibfwide", "c1", "c3"}
+    which = set(argv) or {"ibf", "ibfcfg", "hll", "hibf", "hibfwide", "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
+    if "hll" in which:
+        make_hll(R)
     if "hibfwide" in which:
         make_hibf_wide_cases(R)
     if "ibfcfg" in which:

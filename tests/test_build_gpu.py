@@ -26,7 +26,9 @@ def _cfg(d, input_fn=None):
                     relaxed_fpr=rfpr)
 
 
-def _compare_with_reference(H, d):
+def _compare_with_reference(H, d, every_ibf=False):
+    """Same IBFs (matched by path of merged bins), sizes and tables; bit stores equal for every IBF holding no split
+    user bin, or for every IBF (`every_ibf`: builds that chunk split user bins in the reference's order)."""
     ref_t = G.tables(d)
     ref = canonical(ref_t)
     got = canonical(H.tables())
@@ -35,7 +37,7 @@ def _compare_with_reference(H, d):
     for path, (bins, size, row, k_ref) in ref.items():
         gb, gs, grow, k_got = got[path]
         assert (bins, size, row) == (gb, gs, grow), path
-        if split_free(ref_t, k_ref):
+        if every_ibf or split_free(ref_t, k_ref):
             assert S.digest(H.words(k_got).tolist()) == int(d["digests"][k_ref]), path
             n_exact += 1
     return n_exact
@@ -67,16 +69,24 @@ def test_build_synthetic_matches_reference(gpu_lib, oracle, name):
         assert int(ca.bulk_count(v, 1)[ub]) >= v.size
 
 
-@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "similar", "same"])
+@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "same", "synth64",
+                                  "synth600", "synth_t128", "synth_t256"])
 def test_build_input_fn_matches_reference(gpu_lib, oracle, name):
+    """hierarchical_interleaved_bloom_filter(config&, layout) through input_fn: every IBF's bit store equals the
+    reference's, split user bins included."""
     d = G.hibf_case(name)
-    vals, offs = d["ub_values"], d["ub_offsets"]
+    if "ub_values" in d:
+        vals, offs = d["ub_values"], d["ub_offsets"]
+        ubs = [vals[offs[u]:offs[u + 1]] for u in range(d["n_ub"])]
+    else:
+        seed = int(d["synthetic_seed"][0])
+        ubs = [S.user_bin_values(seed, d["ub_offsets"], u) for u in range(d["n_ub"])]
 
     def input_fn(ub, it):
-        it.push(vals[offs[ub]:offs[ub + 1]])
+        it.push(ubs[ub])
 
     H = hg.hierarchical_interleaved_bloom_filter(_cfg(d, input_fn), d["layout_text"])
-    _compare_with_reference(H, d)
+    assert _compare_with_reference(H, d, every_ibf=True) == len(d["bins"])
     _queries_vs_oracle(H, oracle, d)
 
 

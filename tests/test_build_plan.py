@@ -85,3 +85,58 @@ def test_ibf_plan_matches_reference(case):
     cfg = B.config(input_fn=lambda ub, it: it.push(ubs[ub]), **case["config"])
     size, _biggest = B.ibf_plan(cfg, case["max_bin_elements"])
     assert size == int(case["params"][1])
+
+
+def _ub_values(d):
+    if "ub_values" in d:
+        v, o = d["ub_values"], d["ub_offsets"].astype(np.int64)
+        return [v[o[u]:o[u + 1]] for u in range(o.size - 1)]
+    seed = int(d["synthetic_seed"][0])
+    return [S.user_bin_values(seed, d["ub_offsets"], u) for u in range(d["n_ub"])]
+
+
+@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "same", "synth64",
+                                  "synth600", "synth_t128", "synth_t256"])
+def test_insertion_order_reproduces_reference_bits(oracle, name):
+    """Every IBF's bit store, split user bins included, rebuilt on the CPU oracle from the builder's insertion order
+    (split user bins in the replayed hash-set order) and the reference's own tables, equals the reference's words."""
+    d = G.hibf_case(name)
+    ubs = _ub_values(d)
+    h = int(d["hash_funs"][0])
+    fpr, rfpr, _, _ = (float(x) for x in d["fpr"])
+    cfg = B.config(input_fn=lambda u, it: it.push(ubs[u]), number_of_user_bins=d["n_ub"],
+                   number_of_hash_functions=h, maximum_fpr=fpr, relaxed_fpr=rfpr)
+    offs, vals = B.build_inputs(cfg, d["layout_text"])
+    T = G.tables(d)
+    bins = T["bins"].astype(np.int64)
+    tb_off = np.concatenate([[0], np.cumsum(bins)])
+    nxt, ub = T["next_ibf"], T["user_bin"]
+    ibfs = [oracle.ibf(int(bins[k]), int(T["bin_size"][k]), h) for k in range(bins.size)]
+    # parent (IBF, merged bin) of every non-root IBF
+    parent = {}
+    for k in range(bins.size):
+        for tb in range(int(bins[k])):
+            c = int(nxt[tb_off[k] + tb])
+            if ub[tb_off[k] + tb] == np.uint64(2**64 - 1) and c != k:  # merged bin -> child IBF
+                parent[c] = (k, tb)
+    leaf = {}
+    for k in range(bins.size):
+        for tb in range(int(bins[k])):
+            u = int(ub[tb_off[k] + tb])
+            if u < d["n_ub"]:
+                leaf.setdefault(u, (k, []))[1].append(tb)
+    for u in range(d["n_ub"]):
+        v = vals[offs[u]:offs[u + 1]]
+        k, tbs = leaf[u]
+        first, ntb = min(tbs), len(tbs)
+        chunk = -(-v.size // ntb) if v.size else 1
+        for c in range(ntb):
+            part = v[c * chunk:(c + 1) * chunk]
+            if part.size:
+                ibfs[k].emplace(part, first + c)
+        while k in parent:
+            k, tb = parent[k]
+            if v.size:
+                ibfs[k].emplace(v, tb)
+    for k in range(bins.size):
+        assert S.digest(ibfs[k].words().tolist()) == int(d["digests"][k]), f"IBF {k}"
