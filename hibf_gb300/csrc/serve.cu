@@ -1,10 +1,11 @@
 // serve.cu -- continuous-batching query server over a resident HIBF, and an open-loop load driver.
 //
 // The server keeps the HIBF on the device and owns `slots` agents, each with its own stream and buffers.  Requests
-// (CSR batches of queries from callers) wait in a FIFO.  A loop thread admits them: whenever a slot is free it
+// (CSR batches of queries from callers) wait in a FIFO.  Each slot has its own thread: whenever it is free it
 // coalesces waiting requests, oldest first, into one batch bounded by the slot's capacity and by the device-memory
-// admission cap (inputs, task queue, records and result lists of all batches in flight).  Batches on different
-// slots overlap on the device; a request that arrives while others run joins the next batch a free slot takes.
+// admission cap (inputs, task queue, records and result lists of all batches in flight), stages and launches it,
+// waits for it and splits the results.  Batches on different slots overlap on the device and their host work runs
+// in parallel; a request that arrives while others run joins the next batch a free slot takes.
 // Results are split back per request; a batch's results equal each request's results alone because queries are
 // independent.  A request that alone needs more than the admission cap is rejected (HIBF_GPU_ERR_ADMISSION).
 //
@@ -50,7 +51,7 @@ struct request
     double t_arrival{};                      // when the request counts as arrived (caller's clock, seconds)
     double t_done{};
     int status{HIBF_GPU_OK};
-    std::atomic<bool> done{false}; // set by the loop thread after the results, read by waiters
+    std::atomic<bool> done{false}; // set by a slot thread after the results, read by waiters
     bool solo{false}; // run alone (after a batch overflowed)
     std::vector<uint64_t> res_off, res_ids;
 };
@@ -60,10 +61,8 @@ struct slot
     hibf_gpu_agent * agent{};
     cudaStream_t stream{};
     cudaEvent_t ev{};
-    int phase{0}; // 0 idle, 1 kernels + offsets in flight, 2 ids in flight
     std::vector<request *> reqs;
     uint64_t nq{}, nv{}, bytes{};
-    uint64_t nr{};
     dbuf d_values, d_qoff, d_thr;
     hbuf h_values, h_qoff, h_thr, h_roff, h_ids;
     uint64_t const * d_roff{};
@@ -85,7 +84,7 @@ struct hibf_gpu_server
     std::unordered_map<uint64_t, std::unique_ptr<request>> reqs;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::thread loop;
+    std::vector<std::thread> workers; // one per slot
     std::atomic<bool> stop{false};
     uint64_t inflight_bytes{};
     uint64_t next_id{1};
@@ -104,17 +103,54 @@ uint64_t batch_bytes(uint64_t nq, uint64_t nv)
     return nv * 8 + (nq + 1) * 8 + nq * 8 + nq * 8 * 8 + nq * 16 * (4 + 4 + 8 + 8 + 8 + 8);
 }
 
-void start_batch(hibf_gpu_server * S, slot & sl)
+void finish(request * r, int status, double t)
 {
-    // gather inputs into pinned staging, offsets relative to the batch
+    r->status = status;
+    r->t_done = t;
+    r->done.store(true);
+}
+
+// Moves the oldest waiting requests that fit into one batch of `sl` (slot capacity, admission cap; a request rerun
+// alone after an overflow runs by itself).  Requests that cannot run even alone are rejected.  Caller holds S->mu.
+void take_batch(hibf_gpu_server * S, slot & sl)
+{
     uint64_t nq = 0, nv = 0;
-    for (request * r : sl.reqs)
+    while (!S->waiting.empty())
     {
+        request * r = S->waiting.front();
+        uint64_t const b = batch_bytes(nq + r->nq, nv + r->nv);
+        bool const fits_slot = nq + r->nq <= S->max_queries && nv + r->nv <= S->max_values;
+        bool const fits_cap = S->inflight_bytes + b <= S->admission_bytes;
+        bool const alone_ok = batch_bytes(r->nq, r->nv) <= S->admission_bytes;
+        if (sl.reqs.empty() && (!(r->nq <= S->max_queries && r->nv <= S->max_values) || !alone_ok))
+        {
+            S->waiting.pop_front(); // cannot run even alone in a slot
+            finish(r, HIBF_GPU_ERR_ADMISSION, now_s());
+            ++S->rejected;
+            S->cv_done.notify_all();
+            continue;
+        }
+        if (!fits_slot || !fits_cap || (r->solo && !sl.reqs.empty()))
+            break;
+        S->waiting.pop_front();
+        sl.reqs.push_back(r);
         nq += r->nq;
         nv += r->nv;
+        if (r->solo)
+            break;
     }
     sl.nq = nq;
     sl.nv = nv;
+    sl.bytes = sl.reqs.empty() ? 0 : batch_bytes(nq, nv);
+    S->inflight_bytes += sl.bytes;
+}
+
+// Stages the slot's requests into pinned memory, copies them to the device and launches the batch; then waits for
+// it, fetches the result offsets and ids, and splits them per request.  Runs on the slot's own thread, so batches of
+// different slots stage, run and finish concurrently.  Returns the requests to rerun alone (after an overflow).
+std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
+{
+    uint64_t const nq = sl.nq, nv = sl.nv;
     uint64_t * hv = sl.h_values.as<uint64_t>();
     uint64_t * ho = sl.h_qoff.as<uint64_t>();
     uint64_t * ht = sl.h_thr.as<uint64_t>();
@@ -135,65 +171,51 @@ void start_batch(hibf_gpu_server * S, slot & sl)
     HG_CUDA(cudaMemcpyAsync(sl.d_qoff.p, ho, (nq + 1) * 8, cudaMemcpyHostToDevice, sl.stream));
     HG_CUDA(cudaMemcpyAsync(sl.d_thr.p, ht, std::max<uint64_t>(nq, 1) * 8, cudaMemcpyHostToDevice, sl.stream));
     void const * cnt = nullptr;
-    int const st = hibf_gpu_agent_query_batch_d(sl.agent, HIBF_GPU_QUERY_MEMBERSHIP, sl.d_values.as<uint64_t>(),
-                                                sl.d_qoff.as<uint64_t>(), nq, sl.d_thr.as<uint64_t>(), 2, &sl.d_roff,
-                                                &sl.d_ids, &cnt);
+    int st = hibf_gpu_agent_query_batch_d(sl.agent, HIBF_GPU_QUERY_MEMBERSHIP, sl.d_values.as<uint64_t>(),
+                                          sl.d_qoff.as<uint64_t>(), nq, sl.d_thr.as<uint64_t>(), 2, &sl.d_roff,
+                                          &sl.d_ids, &cnt);
     if (st != HIBF_GPU_OK)
         fail(st, "batch launch failed");
     HG_CUDA(cudaMemcpyAsync(sl.h_roff.p, sl.d_roff, (nq + 1) * 8, cudaMemcpyDeviceToHost, sl.stream));
-    HG_CUDA(cudaEventRecord(sl.ev, sl.stream));
-    sl.phase = 1;
-    ++S->batches;
-    S->batched_queries += nq;
-}
-
-// Advances a slot whose event has fired.  Returns true when its requests completed (or were requeued).
-bool advance_slot(hibf_gpu_server * S, slot & sl, std::vector<request *> & requeue)
-{
-    if (sl.phase == 1)
     {
-        int const st = hibf_gpu_agent_status(sl.agent);
-        if (st == HIBF_GPU_ERR_OVERFLOW)
-        {
-            // rerun every request alone; a request that overflows alone fails
-            for (request * r : sl.reqs)
-            {
-                if (sl.reqs.size() == 1 || r->solo)
-                {
-                    r->status = HIBF_GPU_ERR_OVERFLOW;
-                    r->done = true;
-                    r->t_done = now_s();
-                }
-                else
-                {
-                    r->solo = true;
-                    requeue.push_back(r);
-                }
-            }
-            return true;
-        }
-        if (st != HIBF_GPU_OK)
-        {
-            for (request * r : sl.reqs)
-            {
-                r->status = st;
-                r->done = true;
-                r->t_done = now_s();
-            }
-            return true;
-        }
-        sl.nr = sl.h_roff.as<uint64_t>()[sl.nq];
-        if (sl.nr)
-            HG_CUDA(cudaMemcpyAsync(sl.h_ids.p, sl.d_ids, sl.nr * 8, cudaMemcpyDeviceToHost, sl.stream));
-        HG_CUDA(cudaEventRecord(sl.ev, sl.stream));
-        sl.phase = 2;
-        return false;
+        std::lock_guard<std::mutex> lk(S->mu);
+        ++S->batches;
+        S->batched_queries += nq;
     }
-    // phase 2: results on the host -> split per request
+    std::vector<request *> requeue;
+    st = hibf_gpu_agent_status(sl.agent); // synchronises the slot's stream
+    if (st == HIBF_GPU_ERR_OVERFLOW)
+    {
+        // rerun every request alone; a request that overflows alone fails
+        double const t = now_s();
+        for (request * r : sl.reqs)
+        {
+            if (sl.reqs.size() == 1 || r->solo)
+                finish(r, HIBF_GPU_ERR_OVERFLOW, t);
+            else
+            {
+                r->solo = true;
+                requeue.push_back(r);
+            }
+        }
+        return requeue;
+    }
+    if (st != HIBF_GPU_OK)
+    {
+        double const t = now_s();
+        for (request * r : sl.reqs)
+            finish(r, st, t);
+        return requeue;
+    }
     uint64_t const * ro = sl.h_roff.as<uint64_t>();
+    uint64_t const nr = ro[nq];
+    if (nr)
+    {
+        HG_CUDA(cudaMemcpyAsync(sl.h_ids.p, sl.d_ids, nr * 8, cudaMemcpyDeviceToHost, sl.stream));
+        HG_CUDA(cudaStreamSynchronize(sl.stream));
+    }
     uint64_t const * ids = sl.h_ids.as<uint64_t>();
-    double const t = now_s();
-    uint64_t q = 0;
+    q = 0;
     for (request * r : sl.reqs)
     {
         uint64_t const base = ro[q];
@@ -201,147 +223,54 @@ bool advance_slot(hibf_gpu_server * S, slot & sl, std::vector<request *> & reque
         for (uint64_t i = 0; i <= r->nq; ++i)
             r->res_off[i] = ro[q + i] - base;
         r->res_ids.assign(ids + base, ids + ro[q + r->nq]);
-        r->status = HIBF_GPU_OK;
-        r->done = true;
-        r->t_done = t;
         q += r->nq;
     }
-    return true;
+    double const t = now_s();
+    for (request * r : sl.reqs)
+        finish(r, HIBF_GPU_OK, t);
+    return requeue;
 }
 
-void server_loop(hibf_gpu_server * S)
+// One thread per slot: take the oldest waiting requests that fit, run them as one batch, complete them, repeat.
+void slot_loop(hibf_gpu_server * S, slot * sl)
 {
     cudaSetDevice(S->device);
-    std::vector<request *> requeue;
-    while (!S->stop.load())
+    while (true)
     {
-        bool progressed = false;
-        // completions
-        for (auto & slp : S->slots)
         {
-            slot & sl = *slp;
-            if (sl.phase == 0)
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv_work.wait(lk, [&] { return S->stop.load() || !S->waiting.empty(); });
+            if (S->stop.load())
+                return;
+            take_batch(S, *sl);
+            if (sl->reqs.empty())
+            {
+                // the admission cap is taken by batches in flight: wait for one to finish
+                S->cv_work.wait_for(lk, std::chrono::microseconds(200));
                 continue;
-            cudaError_t const e = cudaEventQuery(sl.ev);
-            if (e == cudaErrorNotReady)
-                continue;
-            if (e != cudaSuccess)
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                S->loop_error = cudaGetErrorString(e);
-                for (request * r : sl.reqs)
-                {
-                    r->status = HIBF_GPU_ERR_CUDA;
-                    r->done = true;
-                }
-                sl.reqs.clear();
-                sl.phase = 0;
-                S->cv_done.notify_all();
-                continue;
-            }
-            bool finished = false;
-            try
-            {
-                finished = advance_slot(S, sl, requeue);
-            }
-            catch (status_error const & err)
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                S->loop_error = err.what();
-                for (request * r : sl.reqs)
-                {
-                    r->status = err.status;
-                    r->done = true;
-                }
-                finished = true;
-            }
-            progressed = true;
-            if (finished)
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                S->inflight_bytes -= sl.bytes;
-                for (auto it = requeue.rbegin(); it != requeue.rend(); ++it)
-                    S->waiting.push_front(*it);
-                requeue.clear();
-                sl.reqs.clear();
-                sl.phase = 0;
-                S->cv_done.notify_all();
             }
         }
-        // admission: fill free slots with the oldest waiting requests
-        for (auto & slp : S->slots)
+        std::vector<request *> requeue;
+        try
         {
-            slot & sl = *slp;
-            if (sl.phase != 0)
-                continue;
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                uint64_t nq = 0, nv = 0;
-                while (!S->waiting.empty())
-                {
-                    request * r = S->waiting.front();
-                    uint64_t const b = batch_bytes(nq + r->nq, nv + r->nv);
-                    bool const fits_slot = nq + r->nq <= S->max_queries && nv + r->nv <= S->max_values;
-                    bool const fits_cap = S->inflight_bytes + b <= S->admission_bytes;
-                    if (sl.reqs.empty() && !fits_slot)
-                    {
-                        // cannot run even alone in a slot
-                        S->waiting.pop_front();
-                        r->status = HIBF_GPU_ERR_ADMISSION;
-                        r->done = true;
-                        r->t_done = now_s();
-                        ++S->rejected;
-                        S->cv_done.notify_all();
-                        continue;
-                    }
-                    if (!fits_slot || !fits_cap || (r->solo && !sl.reqs.empty()))
-                        break;
-                    S->waiting.pop_front();
-                    sl.reqs.push_back(r);
-                    nq += r->nq;
-                    nv += r->nv;
-                    if (r->solo)
-                        break;
-                }
-                if (sl.reqs.empty())
-                    continue;
-                sl.bytes = batch_bytes(nq, nv);
-                S->inflight_bytes += sl.bytes;
-            }
-            try
-            {
-                start_batch(S, sl);
-            }
-            catch (status_error const & err)
-            {
-                std::lock_guard<std::mutex> lk(S->mu);
-                S->loop_error = err.what();
-                for (request * r : sl.reqs)
-                {
-                    r->status = err.status;
-                    r->done = true;
-                }
-                S->inflight_bytes -= sl.bytes;
-                sl.reqs.clear();
-                sl.phase = 0;
-                S->cv_done.notify_all();
-            }
-            progressed = true;
+            requeue = run_batch(S, *sl);
         }
-        if (!progressed)
+        catch (status_error const & err)
         {
-            bool busy = false;
-            for (auto & slp : S->slots)
-                busy = busy || slp->phase != 0;
-            if (busy)
-                std::this_thread::yield();
-            else
-            {
-                std::unique_lock<std::mutex> lk(S->mu);
-                S->cv_work.wait_for(lk, std::chrono::microseconds(200),
-                                    [&] { return S->stop.load() || !S->waiting.empty(); });
-            }
+            double const t = now_s();
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->loop_error = err.what();
+            for (request * r : sl->reqs)
+                if (!r->done.load())
+                    finish(r, err.status, t);
         }
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->inflight_bytes -= sl->bytes;
+        for (auto it = requeue.rbegin(); it != requeue.rend(); ++it)
+            S->waiting.push_front(*it);
+        sl->reqs.clear();
+        S->cv_done.notify_all();
+        S->cv_work.notify_all();
     }
 }
 
@@ -391,7 +320,8 @@ extern "C"
                     S->slots.push_back(std::move(sl));
                 }
                 hibf_gpu_server * raw = S.release();
-                raw->loop = std::thread(server_loop, raw);
+                for (auto & sl : raw->slots)
+                    raw->workers.emplace_back(slot_loop, raw, sl.get());
                 *out = raw;
             });
     }
@@ -403,10 +333,14 @@ extern "C"
             {
                 if (!S)
                     return;
-                S->stop.store(true);
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    S->stop.store(true);
+                }
                 S->cv_work.notify_all();
-                if (S->loop.joinable())
-                    S->loop.join();
+                for (auto & w : S->workers)
+                    if (w.joinable())
+                        w.join();
                 for (auto & sl : S->slots)
                 {
                     cudaStreamSynchronize(sl->stream);
