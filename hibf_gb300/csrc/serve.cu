@@ -52,7 +52,8 @@ struct request
     double t_done{};
     int status{HIBF_GPU_OK};
     std::atomic<bool> done{false}; // set by a slot thread after the results, read by waiters
-    bool solo{false}; // run alone (after a batch overflowed)
+    bool solo{false};   // run alone (after a batch overflowed)
+    bool pinned{false}; // values are in page-locked host memory: copied to the device directly, not staged
     std::vector<uint64_t> res_off, res_ids;
 };
 
@@ -156,9 +157,28 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     uint64_t * ht = sl.h_thr.as<uint64_t>();
     uint64_t q = 0, v = 0;
     ho[0] = 0;
+    uint64_t staged_from = 0; // start of the current run of staged requests
+    auto flush_staged = [&](uint64_t to)
+    {
+        if (to > staged_from)
+            HG_CUDA(cudaMemcpyAsync(sl.d_values.as<uint64_t>() + staged_from, hv + staged_from,
+                                    (to - staged_from) * 8, cudaMemcpyHostToDevice, sl.stream));
+    };
     for (request * r : sl.reqs)
     {
-        std::memcpy(hv + v, r->values, r->nv * 8);
+        if (r->pinned)
+        {
+            // page-locked caller memory: one DMA straight into the batch's input, no host copy
+            flush_staged(v);
+            if (r->nv)
+                HG_CUDA(cudaMemcpyAsync(sl.d_values.as<uint64_t>() + v, r->values, r->nv * 8, cudaMemcpyHostToDevice,
+                                        sl.stream));
+            staged_from = v + r->nv;
+        }
+        else
+        {
+            std::memcpy(hv + v, r->values, r->nv * 8);
+        }
         for (uint64_t i = 0; i < r->nq; ++i)
         {
             ho[q + i + 1] = v + r->qoff[i + 1];
@@ -167,7 +187,7 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
         q += r->nq;
         v += r->nv;
     }
-    HG_CUDA(cudaMemcpyAsync(sl.d_values.p, hv, std::max<uint64_t>(nv, 1) * 8, cudaMemcpyHostToDevice, sl.stream));
+    flush_staged(v);
     HG_CUDA(cudaMemcpyAsync(sl.d_qoff.p, ho, (nq + 1) * 8, cudaMemcpyHostToDevice, sl.stream));
     HG_CUDA(cudaMemcpyAsync(sl.d_thr.p, ht, std::max<uint64_t>(nq, 1) * 8, cudaMemcpyHostToDevice, sl.stream));
     void const * cnt = nullptr;
@@ -394,6 +414,14 @@ extern "C"
                     r->values = values;
                     r->qoff = query_offsets;
                     r->thr = thresholds;
+                    if (r->nv)
+                    {
+                        cudaPointerAttributes a{};
+                        if (cudaPointerGetAttributes(&a, values) == cudaSuccess)
+                            r->pinned = a.type == cudaMemoryTypeHost;
+                        else
+                            cudaGetLastError(); // plain pageable memory: not an error
+                    }
                 }
                 r->t_arrival = arrival_s >= 0 ? arrival_s : now_s();
                 std::lock_guard<std::mutex> lk(S->mu);
@@ -513,19 +541,48 @@ extern "C"
                     plans.push_back(plan{t, q % pool_queries, nq, thr_lo + (thr_hi - thr_lo) * U(rng)});
                     q += nq;
                 }
-                // build request payloads ahead of time (contiguous pool slices, wrapping)
+                // Requests borrow contiguous slices of the pool (a request that would wrap starts at query 0).  The
+                // pool is page-locked for the run, as a client that registers its receive buffers would have it, so
+                // the server copies request values to the device without staging them.
+                bool registered = false;
+                uint64_t const pool_bytes = pool_offsets[pool_queries] * 8;
+                if (pool_bytes)
+                {
+                    cudaPointerAttributes a{};
+                    bool const already = cudaPointerGetAttributes(&a, pool_values) == cudaSuccess &&
+                                         a.type == cudaMemoryTypeHost;
+                    cudaGetLastError();
+                    if (!already)
+                    {
+                        HG_CUDA(cudaHostRegister(const_cast<uint64_t *>(pool_values), pool_bytes,
+                                                 cudaHostRegisterDefault));
+                        registered = true;
+                    }
+                }
+                struct unregister_guard
+                {
+                    void * p;
+                    ~unregister_guard()
+                    {
+                        if (p)
+                            cudaHostUnregister(p);
+                    }
+                } guard{registered ? const_cast<uint64_t *>(pool_values) : nullptr};
                 std::vector<std::vector<uint64_t>> offs(plans.size()), thrs(plans.size());
-                std::vector<std::vector<uint64_t>> vals(plans.size());
+                std::vector<uint64_t const *> vals(plans.size());
                 for (size_t i = 0; i < plans.size(); ++i)
                 {
                     auto & p = plans[i];
+                    if (p.q0 + p.nq > pool_queries)
+                        p.q0 = 0;
+                    uint64_t const base = pool_offsets[p.q0];
+                    vals[i] = pool_values + base;
                     offs[i].push_back(0);
                     for (uint64_t k = 0; k < p.nq; ++k)
                     {
-                        uint64_t const qi = (p.q0 + k) % pool_queries;
+                        uint64_t const qi = p.q0 + k;
                         uint64_t const b = pool_offsets[qi], e = pool_offsets[qi + 1];
-                        vals[i].insert(vals[i].end(), pool_values + b, pool_values + e);
-                        offs[i].push_back(vals[i].size());
+                        offs[i].push_back(e - base);
                         thrs[i].push_back(static_cast<uint64_t>(std::ceil(p.f * static_cast<double>(e - b))));
                     }
                 }
@@ -536,8 +593,8 @@ extern "C"
                     double const ta = t0 + plans[i].t;
                     while (now_s() < ta)
                         ;
-                    int const st = hibf_gpu_server_submit(S, vals[i].data(), offs[i].data(), plans[i].nq,
-                                                          thrs[i].data(), ta, 0, &ids[i]);
+                    int const st = hibf_gpu_server_submit(S, vals[i], offs[i].data(), plans[i].nq, thrs[i].data(), ta,
+                                                          0, &ids[i]);
                     if (st != HIBF_GPU_OK)
                         fail(st, "submit failed");
                 }

@@ -50,6 +50,15 @@ class server:
                t.ctypes.data if t.size else None, arrival_s, 1, ctypes.byref(rid))
         return rid.value
 
+    def submit_borrowed(self, values_ptr: int, query_offsets, thresholds, arrival_s: float = -1.0) -> int:
+        """Submits without copying: the server reads `values_ptr` (host memory; page-locked memory is copied to the
+        device directly) and the offsets/thresholds arrays until release().  Keep all three alive until then."""
+        qo, t = _u64(query_offsets), _u64(thresholds)
+        rid = ctypes.c_uint64(0)
+        N.call("hibf_gpu_server_submit", self._s, values_ptr, qo.ctypes.data, qo.size - 1,
+               t.ctypes.data if t.size else None, arrival_s, 0, ctypes.byref(rid))
+        return rid.value
+
     def wait(self, rid: int, timeout_ms: float = -1.0):
         """(status, offsets pointer, ids pointer, latency_s); the pointers stay valid until release(rid)."""
         st = ctypes.c_int(0)

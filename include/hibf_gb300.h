@@ -393,7 +393,9 @@ typedef struct hibf_gpu_server hibf_gpu_server;
 int hibf_gpu_server_create(hibf_gpu_hibf * h, int n_slots, uint64_t max_batch_queries, uint64_t max_batch_values,
                            uint64_t admission_bytes, hibf_gpu_server ** out);
 int hibf_gpu_server_destroy(hibf_gpu_server * s);
-/* copy != 0: inputs copied; copy == 0: the caller keeps them alive until hibf_gpu_server_release (offsets from 0).
+/* copy != 0: inputs copied; copy == 0: the caller keeps them alive until hibf_gpu_server_release (offsets from 0);
+ * borrowed values in page-locked host memory (cudaHostAlloc / cudaHostRegister) are copied to the device directly,
+ * other memory is staged through the slot's pinned buffer.
  * arrival_s: arrival time on hibf_gpu_server_now's clock (< 0: now); latencies are measured from it. */
 int hibf_gpu_server_submit(hibf_gpu_server * s, uint64_t const * values, uint64_t const * query_offsets,
                            uint64_t n_queries, uint64_t const * thresholds, double arrival_s, int copy, uint64_t * id);

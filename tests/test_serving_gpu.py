@@ -111,3 +111,29 @@ def test_allocation_failure_is_a_status(gpu_lib):
     ibf = hg.interleaved_bloom_filter(hg.bin_count(64), hg.bin_size(1024), hg.hash_function_count(2))
     ibf.emplace(5, hg.bin_index(3))
     assert ibf.counting_agent().bulk_count([5])[3] == 1
+
+
+def test_pinned_borrowed_requests_match(gpu_lib):
+    """Requests whose values sit in page-locked memory go to the device without staging; mixed with staged ones in
+    the same batches, every result equals the query answered alone."""
+    import torch
+
+    H, d = _hibf()
+    reqs = _requests(d, 40, seed=5)
+    agent = H.membership_agent()
+    expect = [agent.query_batch(v, qo, t)[:2] for v, qo, t in reqs]
+    srv = server(H, slots=2, max_batch_queries=4096, max_batch_values=1 << 22, admission_bytes=1 << 30)
+    keep, ids = [], []
+    for i, (v, qo, t) in enumerate(reqs):
+        if i % 2 == 0:
+            pv = torch.from_numpy(v.view(np.int64)).pin_memory()
+            keep.append((pv, qo, t))
+            ids.append(srv.submit_borrowed(pv.data_ptr(), qo, t))
+        else:
+            ids.append(srv.submit(v, qo, t))
+    for rid, (v, qo, t), (eo, ei) in zip(ids, reqs, expect):
+        st, offs, res, _ = srv.wait_result(rid, qo.size - 1)
+        assert st == 0
+        np.testing.assert_array_equal(offs, eo)
+        np.testing.assert_array_equal(res, ei)
+    srv.close()
