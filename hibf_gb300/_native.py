@@ -177,6 +177,8 @@ _SIGS = [
     ("hibf_gpu_server_wait", None, [vp, u64, ctypes.c_double, ctypes.POINTER(ci), ctypes.POINTER(u64p),
                                     ctypes.POINTER(u64p), ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_server_release", None, [vp, u64]),
+    ("hibf_gpu_server_register_host", None, [vp, vp, u64, ci]),
+    ("hibf_gpu_server_unregister_host", None, [vp, vp]),
     ("hibf_gpu_server_now", ctypes.c_double, []),
     ("hibf_gpu_server_stats", None, [vp, u64p]),
     ("hibf_gpu_server_open_loop", None, [vp, vp, vp, u64, ctypes.c_double, ctypes.c_double, u64, ctypes.c_double,

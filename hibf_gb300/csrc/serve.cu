@@ -93,6 +93,13 @@ struct hibf_gpu_server
     std::string loop_error;
     // counters
     uint64_t batches{}, batched_queries{}, rejected{};
+    // page-locked host ranges [begin, end) registered with the server, and whether the server pinned them
+    struct host_range
+    {
+        uintptr_t begin, end;
+        bool pinned_here;
+    };
+    std::vector<host_range> host_ranges;
 };
 
 namespace
@@ -361,6 +368,9 @@ extern "C"
                 for (auto & w : S->workers)
                     if (w.joinable())
                         w.join();
+                for (auto const & hr : S->host_ranges)
+                    if (hr.pinned_here)
+                        cudaHostUnregister(reinterpret_cast<void *>(hr.begin));
                 for (auto & sl : S->slots)
                 {
                     cudaStreamSynchronize(sl->stream);
@@ -369,6 +379,44 @@ extern "C"
                     cudaStreamDestroy(sl->stream);
                 }
                 delete S;
+            });
+    }
+
+    int hibf_gpu_server_register_host(hibf_gpu_server * S, void const * ptr, uint64_t bytes, int already_pinned)
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !ptr || bytes == 0)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                if (!already_pinned)
+                    HG_CUDA(cudaHostRegister(const_cast<void *>(ptr), bytes, cudaHostRegisterDefault));
+                uintptr_t const b = reinterpret_cast<uintptr_t>(ptr);
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->host_ranges.push_back(hibf_gpu_server::host_range{b, b + bytes, !already_pinned});
+            });
+    }
+
+    int hibf_gpu_server_unregister_host(hibf_gpu_server * S, void const * ptr)
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !ptr)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
+                uintptr_t const b = reinterpret_cast<uintptr_t>(ptr);
+                bool pinned_here = false;
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    auto it = std::find_if(S->host_ranges.begin(), S->host_ranges.end(),
+                                           [&](auto const & hr) { return hr.begin == b; });
+                    if (it == S->host_ranges.end())
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "range not registered");
+                    pinned_here = it->pinned_here;
+                    S->host_ranges.erase(it);
+                }
+                if (pinned_here)
+                    HG_CUDA(cudaHostUnregister(const_cast<void *>(ptr)));
             });
     }
 
@@ -414,14 +462,14 @@ extern "C"
                     r->values = values;
                     r->qoff = query_offsets;
                     r->thr = thresholds;
-                    if (r->nv)
-                    {
-                        cudaPointerAttributes a{};
-                        if (cudaPointerGetAttributes(&a, values) == cudaSuccess)
-                            r->pinned = a.type == cudaMemoryTypeHost;
-                        else
-                            cudaGetLastError(); // plain pageable memory: not an error
-                    }
+                    // registered page-locked memory is copied to the device without staging (a host-side range
+                    // check: no CUDA call on the submitting thread)
+                    uintptr_t const b = reinterpret_cast<uintptr_t>(values);
+                    uintptr_t const e = b + r->nv * 8;
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    for (auto const & hr : S->host_ranges)
+                        if (r->nv && b >= hr.begin && e <= hr.end)
+                            r->pinned = true;
                 }
                 r->t_arrival = arrival_s >= 0 ? arrival_s : now_s();
                 std::lock_guard<std::mutex> lk(S->mu);
@@ -542,32 +590,21 @@ extern "C"
                     q += nq;
                 }
                 // Requests borrow contiguous slices of the pool (a request that would wrap starts at query 0).  The
-                // pool is page-locked for the run, as a client that registers its receive buffers would have it, so
-                // the server copies request values to the device without staging them.
-                bool registered = false;
+                // pool is registered with the server for the run, as a client that registers its receive buffers
+                // would have it, so the server copies request values to the device without staging them.
                 uint64_t const pool_bytes = pool_offsets[pool_queries] * 8;
-                if (pool_bytes)
-                {
-                    cudaPointerAttributes a{};
-                    bool const already = cudaPointerGetAttributes(&a, pool_values) == cudaSuccess &&
-                                         a.type == cudaMemoryTypeHost;
-                    cudaGetLastError();
-                    if (!already)
-                    {
-                        HG_CUDA(cudaHostRegister(const_cast<uint64_t *>(pool_values), pool_bytes,
-                                                 cudaHostRegisterDefault));
-                        registered = true;
-                    }
-                }
+                bool const registered =
+                    pool_bytes && hibf_gpu_server_register_host(S, pool_values, pool_bytes, 0) == HIBF_GPU_OK;
                 struct unregister_guard
                 {
-                    void * p;
+                    hibf_gpu_server * s;
+                    void const * p;
                     ~unregister_guard()
                     {
                         if (p)
-                            cudaHostUnregister(p);
+                            hibf_gpu_server_unregister_host(s, p);
                     }
-                } guard{registered ? const_cast<uint64_t *>(pool_values) : nullptr};
+                } guard{S, registered ? pool_values : nullptr};
                 std::vector<std::vector<uint64_t>> offs(plans.size()), thrs(plans.size());
                 std::vector<uint64_t const *> vals(plans.size());
                 for (size_t i = 0; i < plans.size(); ++i)

@@ -50,9 +50,16 @@ class server:
                t.ctypes.data if t.size else None, arrival_s, 1, ctypes.byref(rid))
         return rid.value
 
+    def register_host(self, ptr: int, nbytes: int, already_pinned: bool = False) -> None:
+        """Registers host memory for borrowed requests: their values are then copied to the device without staging."""
+        N.call("hibf_gpu_server_register_host", self._s, ptr, nbytes, int(already_pinned))
+
+    def unregister_host(self, ptr: int) -> None:
+        N.call("hibf_gpu_server_unregister_host", self._s, ptr)
+
     def submit_borrowed(self, values_ptr: int, query_offsets, thresholds, arrival_s: float = -1.0) -> int:
-        """Submits without copying: the server reads `values_ptr` (host memory; page-locked memory is copied to the
-        device directly) and the offsets/thresholds arrays until release().  Keep all three alive until then."""
+        """Submits without copying: the server reads `values_ptr` (values inside a registered range go to the device
+        directly) and the offsets/thresholds arrays until release().  Keep all three alive until then."""
         qo, t = _u64(query_offsets), _u64(thresholds)
         rid = ctypes.c_uint64(0)
         N.call("hibf_gpu_server_submit", self._s, values_ptr, qo.ctypes.data, qo.size - 1,

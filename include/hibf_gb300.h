@@ -394,11 +394,16 @@ int hibf_gpu_server_create(hibf_gpu_hibf * h, int n_slots, uint64_t max_batch_qu
                            uint64_t admission_bytes, hibf_gpu_server ** out);
 int hibf_gpu_server_destroy(hibf_gpu_server * s);
 /* copy != 0: inputs copied; copy == 0: the caller keeps them alive until hibf_gpu_server_release (offsets from 0);
- * borrowed values in page-locked host memory (cudaHostAlloc / cudaHostRegister) are copied to the device directly,
+ * borrowed values inside a range registered with hibf_gpu_server_register_host are copied to the device directly,
  * other memory is staged through the slot's pinned buffer.
  * arrival_s: arrival time on hibf_gpu_server_now's clock (< 0: now); latencies are measured from it. */
 int hibf_gpu_server_submit(hibf_gpu_server * s, uint64_t const * values, uint64_t const * query_offsets,
                            uint64_t n_queries, uint64_t const * thresholds, double arrival_s, int copy, uint64_t * id);
+/* Registers [ptr, ptr + bytes) as page-locked request memory: borrowed requests whose values lie inside a registered
+ * range are copied to the device directly (no staging).  already_pinned == 0: the server page-locks the range
+ * (cudaHostRegister) and unlocks it on unregister or destroy; != 0: the caller allocated it page-locked. */
+int hibf_gpu_server_register_host(hibf_gpu_server * s, void const * ptr, uint64_t bytes, int already_pinned);
+int hibf_gpu_server_unregister_host(hibf_gpu_server * s, void const * ptr);
 /* Waits up to timeout_ms (< 0: forever); *status is the request's status; results valid until release. */
 int hibf_gpu_server_wait(hibf_gpu_server * s, uint64_t id, double timeout_ms, int * status,
                          uint64_t const ** result_offsets, uint64_t const ** result_ids, double * latency_s);

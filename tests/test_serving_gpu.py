@@ -127,6 +127,7 @@ def test_pinned_borrowed_requests_match(gpu_lib):
     for i, (v, qo, t) in enumerate(reqs):
         if i % 2 == 0:
             pv = torch.from_numpy(v.view(np.int64)).pin_memory()
+            srv.register_host(pv.data_ptr(), max(8, pv.numel() * 8), already_pinned=True)
             keep.append((pv, qo, t))
             ids.append(srv.submit_borrowed(pv.data_ptr(), qo, t))
         else:
