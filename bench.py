@@ -402,11 +402,13 @@ def run_ours(args, wl, rank, world, local):
 
         pool_q = min(nq, 100_000)
         pool_v = hv[:int(qo[pool_q])]
-        srv = server(hibf, slots=4, max_batch_queries=65536, max_batch_values=1 << 27, admission_bytes=4 << 30)
-        for load, dur in ((1e4, 2.0), (1e5, 1.0), (1e6, 1.0)):
-            serving.append(srv.open_loop(pool_v, qo[:pool_q + 1], offered_qps=load, duration_s=dur,
-                                         max_request_queries=4096, thr_lo=0.5, thr_hi=0.9, seed=int(load)))
-        srv.close()
+        for load, dur in ((1e4, 3.0), (1e5, 2.0), (1e6, 2.0)):
+            srv = server(hibf, slots=4, max_batch_queries=65536, max_batch_values=1 << 27, admission_bytes=4 << 30)
+            r = srv.open_loop(pool_v, qo[:pool_q + 1], offered_qps=load, duration_s=dur, max_request_queries=4096,
+                              thr_lo=0.5, thr_hi=0.9, seed=int(load))
+            r["mean_batch_phases_ms"] = srv.phase_times()
+            serving.append(r)
+            srv.close()
 
     learned = None
     if not args.no_learned and nq >= 2 * args.sched_queries:

@@ -181,6 +181,7 @@ _SIGS = [
     ("hibf_gpu_server_unregister_host", None, [vp, vp]),
     ("hibf_gpu_server_now", ctypes.c_double, []),
     ("hibf_gpu_server_stats", None, [vp, u64p]),
+    ("hibf_gpu_server_phase_times", None, [vp, ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_server_open_loop", None, [vp, vp, vp, u64, ctypes.c_double, ctypes.c_double, u64, ctypes.c_double,
                                          ctypes.c_double, u64, ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_probe_random_reads", None, [u64, u64, ctypes.POINTER(ctypes.c_double)]),

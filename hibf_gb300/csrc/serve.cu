@@ -93,6 +93,9 @@ struct hibf_gpu_server
     std::string loop_error;
     // counters
     uint64_t batches{}, batched_queries{}, rejected{};
+    // summed seconds per batch phase: queueing of the batch's oldest request, staging + launch, until the batch's
+    // device work is done, result fetch, per-request split
+    double t_queue{}, t_stage{}, t_device{}, t_fetch{}, t_split{};
     // page-locked host ranges [begin, end) registered with the server, and whether the server pinned them
     struct host_range
     {
@@ -159,6 +162,10 @@ void take_batch(hibf_gpu_server * S, slot & sl)
 std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
 {
     uint64_t const nq = sl.nq, nv = sl.nv;
+    double const t_start = now_s();
+    double t_oldest = t_start;
+    for (request * r : sl.reqs)
+        t_oldest = std::min(t_oldest, r->t_arrival);
     uint64_t * hv = sl.h_values.as<uint64_t>();
     uint64_t * ho = sl.h_qoff.as<uint64_t>();
     uint64_t * ht = sl.h_thr.as<uint64_t>();
@@ -204,13 +211,10 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     if (st != HIBF_GPU_OK)
         fail(st, "batch launch failed");
     HG_CUDA(cudaMemcpyAsync(sl.h_roff.p, sl.d_roff, (nq + 1) * 8, cudaMemcpyDeviceToHost, sl.stream));
-    {
-        std::lock_guard<std::mutex> lk(S->mu);
-        ++S->batches;
-        S->batched_queries += nq;
-    }
+    double const t_launched = now_s();
     std::vector<request *> requeue;
     st = hibf_gpu_agent_status(sl.agent); // synchronises the slot's stream
+    double const t_device_done = now_s();
     if (st == HIBF_GPU_ERR_OVERFLOW)
     {
         // rerun every request alone; a request that overflows alone fails
@@ -242,6 +246,7 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
         HG_CUDA(cudaStreamSynchronize(sl.stream));
     }
     uint64_t const * ids = sl.h_ids.as<uint64_t>();
+    double const t_fetched = now_s();
     q = 0;
     for (request * r : sl.reqs)
     {
@@ -255,6 +260,14 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     double const t = now_s();
     for (request * r : sl.reqs)
         finish(r, HIBF_GPU_OK, t);
+    std::lock_guard<std::mutex> lk(S->mu);
+    ++S->batches;
+    S->batched_queries += nq;
+    S->t_queue += std::max(0.0, t_start - t_oldest);
+    S->t_stage += t_launched - t_start;
+    S->t_device += t_device_done - t_launched;
+    S->t_fetch += t_fetched - t_device_done;
+    S->t_split += t - t_fetched;
     return requeue;
 }
 
@@ -529,6 +542,24 @@ extern "C"
     double hibf_gpu_server_now(void)
     {
         return now_s();
+    }
+
+    // out: mean seconds per batch of queueing (its oldest request), staging + launch, device work, result fetch, split
+    int hibf_gpu_server_phase_times(hibf_gpu_server * S, double out[5])
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(S->mu);
+                double const n = S->batches ? static_cast<double>(S->batches) : 1.0;
+                out[0] = S->t_queue / n;
+                out[1] = S->t_stage / n;
+                out[2] = S->t_device / n;
+                out[3] = S->t_fetch / n;
+                out[4] = S->t_split / n;
+            });
     }
 
     // out: batches, batched queries, rejected requests, bytes in flight

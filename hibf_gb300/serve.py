@@ -94,6 +94,12 @@ class server:
         N.call("hibf_gpu_server_stats", self._s, out)
         return dict(batches=out[0], batched_queries=out[1], rejected=out[2], inflight_bytes=out[3])
 
+    def phase_times(self) -> dict:
+        """Mean milliseconds per batch: queueing, staging + launch, device work, result fetch, split."""
+        out = (ctypes.c_double * 5)()
+        N.call("hibf_gpu_server_phase_times", self._s, out)
+        return dict(zip(("queue_ms", "stage_ms", "device_ms", "fetch_ms", "split_ms"), (x * 1e3 for x in out)))
+
     def open_loop(self, pool_values, pool_offsets, offered_qps: float, duration_s: float = 1.0,
                   max_request_queries: int = 4096, thr_lo: float = 0.5, thr_hi: float = 0.9, seed: int = 1) -> dict:
         v, qo = _u64(pool_values), _u64(pool_offsets)

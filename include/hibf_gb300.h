@@ -410,6 +410,9 @@ int hibf_gpu_server_wait(hibf_gpu_server * s, uint64_t id, double timeout_ms, in
 int hibf_gpu_server_release(hibf_gpu_server * s, uint64_t id);
 double hibf_gpu_server_now(void);
 /* out: batches launched, queries in them, requests rejected, device bytes admitted in flight. */
+/* Mean seconds per batch since creation: queueing of the batch's oldest request, staging + launch, device work,
+ * result fetch, per-request split. */
+int hibf_gpu_server_phase_times(hibf_gpu_server * s, double out[5]);
 int hibf_gpu_server_stats(hibf_gpu_server * s, uint64_t out[4]);
 /* Open-loop Poisson load from a pool of queries (host CSR): request sizes log-uniform in [1, max_request_queries],
  * per-request thresholds ceil(f * length), f uniform in [thr_lo, thr_hi].  out: achieved queries/s, p50, p99, p99.9
