@@ -64,7 +64,7 @@ class Tuning(ctypes.Structure):
 
     _fields_ = [(n, ctypes.c_uint32) for n in ("values_per_lane", "fetch_bytes", "counter_bits", "blocks_per_sm",
                                                  "early_exit_first", "early_exit_step", "early_exit_stages",
-                                                 "early_exit_min")]
+                                                 "early_exit_min", "block_queries")]
 
     def as_dict(self) -> dict:
         return {n: int(getattr(self, n)) for n, _ in self._fields_}

@@ -334,6 +334,7 @@ struct hibf_gpu_agent
     hibf_gpu_tuning tune{};                // schedule of the persistent kernel
     int variant{0};                        // kernel variant of `tune`
     int max_blocks[kQueryVariants]{};      // resident 256-thread blocks per SM of each variant
+    int max_blocks_blk{};                  // and of the block-per-task kernel
     uint32_t const * order{};              // claim order of the root tasks (device; null = query order)
     uint64_t order_n{};                    // its length: batches must have exactly this many queries
     unsigned long long * qwork{};          // executed value visits per query (device; null = not recorded)
@@ -487,10 +488,11 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
     if (nq)
     {
         query_params p = base_params(a, d_values, d_qoff, d_thr, nq, mask_for(mode, width));
-        int const fit = a->max_blocks[a->variant];
+        bool const blk = nq <= a->tune.block_queries;
+        int const fit = blk ? a->max_blocks_blk : a->max_blocks[a->variant];
         int const per_sm = a->tune.blocks_per_sm ? std::min<int>(fit, static_cast<int>(a->tune.blocks_per_sm)) : fit;
         uint64_t const full = static_cast<uint64_t>(sm_count()) * static_cast<uint64_t>(per_sm);
-        uint64_t const want = (nq + 7) / 8;
+        uint64_t const want = blk ? nq * 4 : (nq + 7) / 8; // block mode: room for the children of every query
         unsigned const grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min(full, want)));
         // inside a stream capture an event record only orders work unless it is marked external; external records
         // become event-record nodes of the graph, so replays time the kernel too
@@ -498,7 +500,8 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         HG_CUDA(cudaStreamIsCapturing(s, &cap));
         unsigned const rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
-        query_kernel(h->hash_count, a->variant)<<<grid, 256, query_smem(h), s>>>(p);
+        (blk ? query_block_kernel(h->hash_count) : query_kernel(h->hash_count, a->variant))<<<grid, 256,
+                                                                                           query_smem(h), s>>>(p);
         HG_CUDA(cudaGetLastError());
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k1, s, rec_flags));
     }
@@ -527,7 +530,8 @@ void launch_plain(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         p.self_init = 1;
         HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u) * 8, s));
         p.task_cap = std::min<uint64_t>(a->cap_tasks, 64u * h->n_ibfs + 64u);
-        query_kernel(h->hash_count, a->variant)<<<1, 256, query_smem(h), s>>>(p);
+        (a->tune.block_queries ? query_block_kernel(h->hash_count) : query_kernel(h->hash_count, a->variant))<<<
+            1, 256, query_smem(h), s>>>(p);
         HG_CUDA(cudaGetLastError());
     }
     launch_postprocess(a, nq, mode, width);
@@ -829,6 +833,7 @@ extern "C"
         t->early_exit_step = 10;
         t->early_exit_stages = 7;
         t->early_exit_min = 256;
+        t->block_queries = 512;
     }
 
     int hibf_gpu_agent_set_tuning(hibf_gpu_agent * a, hibf_gpu_tuning const * t)
@@ -1133,6 +1138,9 @@ extern "C"
                     HG_CUDA(cudaFuncSetAttribute(features_kernel(h->hash_count),
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  static_cast<int>(std::max<size_t>(smem, 48 * 1024))));
+                    HG_CUDA(cudaFuncSetAttribute(query_block_kernel(h->hash_count),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(std::max<size_t>(smem, 48 * 1024))));
                 }
                 catch (...)
                 {
@@ -1311,6 +1319,12 @@ extern "C"
                         HG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, query_kernel(h->hash_count, v), 256,
                                                                               query_smem(h)));
                         a->max_blocks[v] = std::max(1, nb);
+                    }
+                    {
+                        int nb = 0;
+                        HG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, query_block_kernel(h->hash_count),
+                                                                              256, query_smem(h)));
+                        a->max_blocks_blk = std::max(1, nb);
                     }
                     hibf_gpu_tuning_default(&a->tune);
                     ensure_capacity(a, 1024, 4096, 4096);

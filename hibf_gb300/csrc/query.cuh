@@ -209,75 +209,13 @@ __device__ __forceinline__ void count_variant(row_params const & rp, uint32_t lp
     }
 }
 
-template <int H, int V>
-__device__ void process_task(query_params const & p, unsigned long long task, uint32_t * counts, int lane,
-                             unsigned long long & n_tasks, unsigned long long & n_visits,
-                             unsigned long long & n_executed)
+// The bin scan of a counted task: report user bins and queue child IBFs whose summation segment reaches the
+// threshold, then retire the task (one warp; `counts` = the task's per-bin counts).
+__device__ inline void emit_task(query_params const & p, dev_node const & nd, uint32_t const * counts, uint64_t q,
+                                 uint32_t depth, uint64_t n, uint64_t done, uint64_t thr, int lane,
+                                 unsigned long long & n_tasks, unsigned long long & n_visits,
+                                 unsigned long long & n_executed)
 {
-    uint64_t const q = task >> 32;
-    uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
-    uint32_t const k = static_cast<uint32_t>(task) & kNodeMask;
-    dev_node const nd = p.nodes[k];
-    uint64_t const b0 = p.qoff[q];
-    uint64_t const n = p.qoff[q + 1] - b0;
-    uint64_t const thr = p.thr[q];
-
-    if (V != 0 && nd.lpv_log2 > 2)
-    {
-        if (lane == 0)
-        {
-            atomicOr(p.ctrl + C_ERROR, E_VARIANT);
-            __threadfence();
-            atomicAdd(p.ctrl + C_PENDING, ~0ull);
-        }
-        return;
-    }
-    uint32_t const ncount = nd.bin_words > 32 ? 64u * nd.bin_words : (64u << nd.lpv_log2);
-    for (uint32_t i = lane; i < ncount; i += 32)
-        counts[i] = 0;
-    __syncwarp();
-    row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
-    // Count in stages; after each stage stop if no segment can reach the threshold any more (exact: see above).
-    uint64_t done = 0;
-    bool hopeless = !any_segment_reachable(p, nd, counts, n, thr, lane);
-    if (!hopeless && n >= p.ee_min)
-    {
-        for (uint32_t s = 0; s < p.ee_stages; ++s)
-        {
-            uint64_t const stop = n * (p.ee_first + s * p.ee_step) / 100u;
-            if (stop <= done)
-                continue;
-            count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
-            done = stop;
-            __syncwarp();
-            if (!any_segment_reachable(p, nd, counts, n - done, thr, lane))
-            {
-                hopeless = true;
-                break;
-            }
-        }
-    }
-    if (!hopeless)
-    {
-        count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, n - done, counts, lane);
-        done = n;
-    }
-    __syncwarp();
-    if (hopeless)
-    {
-        if (lane == 0)
-        {
-            if (p.qwork)
-                atomicAdd(p.qwork + q + p.q_base, static_cast<unsigned long long>(done));
-            __threadfence();
-            atomicAdd(p.ctrl + C_PENDING, ~0ull); // retires without results or children
-            ++n_tasks;
-            n_visits += n;
-            n_executed += done;
-        }
-        return;
-    }
-
     uint2 const * d = p.descs + nd.desc_offset;
     unsigned long long carry = 0;
     unsigned const lt_mask = (1u << lane) - 1u;
@@ -383,6 +321,79 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
     }
 }
 
+
+template <int H, int V>
+__device__ void process_task(query_params const & p, unsigned long long task, uint32_t * counts, int lane,
+                             unsigned long long & n_tasks, unsigned long long & n_visits,
+                             unsigned long long & n_executed)
+{
+    uint64_t const q = task >> 32;
+    uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
+    uint32_t const k = static_cast<uint32_t>(task) & kNodeMask;
+    dev_node const nd = p.nodes[k];
+    uint64_t const b0 = p.qoff[q];
+    uint64_t const n = p.qoff[q + 1] - b0;
+    uint64_t const thr = p.thr[q];
+
+    if (V != 0 && nd.lpv_log2 > 2)
+    {
+        if (lane == 0)
+        {
+            atomicOr(p.ctrl + C_ERROR, E_VARIANT);
+            __threadfence();
+            atomicAdd(p.ctrl + C_PENDING, ~0ull);
+        }
+        return;
+    }
+    uint32_t const ncount = nd.bin_words > 32 ? 64u * nd.bin_words : (64u << nd.lpv_log2);
+    for (uint32_t i = lane; i < ncount; i += 32)
+        counts[i] = 0;
+    __syncwarp();
+    row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
+    // Count in stages; after each stage stop if no segment can reach the threshold any more (exact: see above).
+    uint64_t done = 0;
+    bool hopeless = !any_segment_reachable(p, nd, counts, n, thr, lane);
+    if (!hopeless && n >= p.ee_min)
+    {
+        for (uint32_t s = 0; s < p.ee_stages; ++s)
+        {
+            uint64_t const stop = n * (p.ee_first + s * p.ee_step) / 100u;
+            if (stop <= done)
+                continue;
+            count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
+            done = stop;
+            __syncwarp();
+            if (!any_segment_reachable(p, nd, counts, n - done, thr, lane))
+            {
+                hopeless = true;
+                break;
+            }
+        }
+    }
+    if (!hopeless)
+    {
+        count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, n - done, counts, lane);
+        done = n;
+    }
+    __syncwarp();
+    if (hopeless)
+    {
+        if (lane == 0)
+        {
+            if (p.qwork)
+                atomicAdd(p.qwork + q + p.q_base, static_cast<unsigned long long>(done));
+            __threadfence();
+            atomicAdd(p.ctrl + C_PENDING, ~0ull); // retires without results or children
+            ++n_tasks;
+            n_visits += n;
+            n_executed += done;
+        }
+        return;
+    }
+
+    emit_task(p, nd, counts, q, depth, n, done, thr, lane, n_tasks, n_visits, n_executed);
+}
+
 // H = the hierarchy's hash function count (one value for all IBFs, as in the reference's build).
 // HIBF_QUERY_MIN_BLOCKS blocks of eight warps per SM bound the register budget (2: 128 registers per thread,
 // measured fastest: the kernel is limited by the memory system's random-access rate, not by occupancy).
@@ -444,6 +455,106 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
         process_task<H, V>(p, task, counts, lane, n_tasks, n_visits, n_executed);
     }
     if (lane == 0 && n_tasks)
+    {
+        atomicAdd(p.stats + 0, n_tasks);
+        atomicAdd(p.stats + 1, n_visits);
+        atomicAdd(p.stats + 2, n_executed);
+    }
+}
+
+// Latency mode: a whole block (eight warps) works on one task.  Warp w counts its eighth of the task's values into
+// its own shared counters, the block adds the eight count arrays, warp 0 scans and emits.  A task then takes about an
+// eighth of the time, which shortens a batch whose tasks are fewer than the GPU's warps (the chain root -> child ->
+// grandchild of its slowest query bounds it).  No early exit: a slice's counts do not bound the task's.
+constexpr unsigned long long kSkipTask = kEmpty - 1u; // an order entry that was not a query index
+
+template <int H>
+__global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query_blk(query_params p)
+{
+    extern __shared__ uint32_t s_counts[];
+    __shared__ unsigned long long s_task;
+    int const lane = threadIdx.x & 31;
+    int const warp = threadIdx.x >> 5;
+    int const nwarps = blockDim.x >> 5;
+    uint32_t * counts = s_counts + warp * p.counters_per_warp;
+    if (p.self_init)
+    {
+        if (threadIdx.x == 0)
+        {
+            p.ctrl[C_HEAD] = 0;
+            p.ctrl[C_TAIL] = 0;
+            p.ctrl[C_PENDING] = p.n_queries;
+            __threadfence();
+        }
+        __syncthreads();
+    }
+    unsigned long long n_tasks = 0, n_visits = 0, n_executed = 0;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+        {
+            unsigned long long const idx = atomicAdd(p.ctrl + C_HEAD, 1ull);
+            unsigned long long task;
+            if (idx < p.n_queries)
+            {
+                uint64_t const q = p.order ? p.order[idx] : idx;
+                if (q >= p.n_queries)
+                {
+                    atomicOr(p.ctrl + C_ERROR, E_ORDER);
+                    __threadfence();
+                    atomicAdd(p.ctrl + C_PENDING, ~0ull);
+                    task = kSkipTask;
+                }
+                else
+                {
+                    task = make_task(q, 0u, 0u);
+                }
+            }
+            else
+            {
+                unsigned long long const slot = idx - p.n_queries;
+                task = slot >= p.task_cap ? kEmpty : wait_for_task(p, slot);
+            }
+            s_task = task;
+        }
+        __syncthreads();
+        unsigned long long const task = s_task;
+        if (task == kEmpty)
+            break;
+        if (task == kSkipTask)
+        {
+            __syncthreads();
+            continue;
+        }
+        uint64_t const q = task >> 32;
+        uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
+        dev_node const nd = p.nodes[static_cast<uint32_t>(task) & kNodeMask];
+        uint64_t const b0 = p.qoff[q];
+        uint64_t const n = p.qoff[q + 1] - b0;
+        uint32_t const ncount = nd.bin_words > 32 ? 64u * nd.bin_words : (64u << nd.lpv_log2);
+        for (uint32_t i = lane; i < ncount; i += 32)
+            counts[i] = 0;
+        __syncwarp();
+        row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
+        uint64_t const per = (n + nwarps - 1) / nwarps;
+        uint64_t const lo = min(n, static_cast<uint64_t>(warp) * per);
+        uint64_t const hi = min(n, lo + per);
+        if (hi > lo)
+            count_variant<H, 0>(rp, nd.lpv_log2, p.values + b0 + lo, hi - lo, counts, lane);
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < ncount; i += blockDim.x)
+        {
+            uint32_t sum = s_counts[i];
+            for (int w = 1; w < nwarps; ++w)
+                sum += s_counts[w * p.counters_per_warp + i];
+            s_counts[i] = sum;
+        }
+        __syncthreads();
+        if (warp == 0)
+            emit_task(p, nd, s_counts, q, depth, n, n, p.thr[q], lane, n_tasks, n_visits, n_executed);
+        __syncthreads(); // the counters and s_task are reused by the next task
+    }
+    if (threadIdx.x == 0 && n_tasks)
     {
         atomicAdd(p.stats + 0, n_tasks);
         atomicAdd(p.stats + 1, n_visits);
@@ -575,11 +686,33 @@ query_kernel_t query_kernel_h2(int v);
 query_kernel_t query_kernel_h3(int v);
 query_kernel_t query_kernel_h4(int v);
 query_kernel_t query_kernel_h5(int v);
+query_kernel_t query_block_kernel_h1();
+query_kernel_t query_block_kernel_h2();
+query_kernel_t query_block_kernel_h3();
+query_kernel_t query_block_kernel_h4();
+query_kernel_t query_block_kernel_h5();
 features_kernel_t features_kernel_h1();
 features_kernel_t features_kernel_h2();
 features_kernel_t features_kernel_h3();
 features_kernel_t features_kernel_h4();
 features_kernel_t features_kernel_h5();
+
+inline query_kernel_t query_block_kernel(uint32_t h)
+{
+    switch (h)
+    {
+    case 1:
+        return query_block_kernel_h1();
+    case 2:
+        return query_block_kernel_h2();
+    case 3:
+        return query_block_kernel_h3();
+    case 4:
+        return query_block_kernel_h4();
+    default:
+        return query_block_kernel_h5();
+    }
+}
 
 inline features_kernel_t features_kernel(uint32_t h)
 {

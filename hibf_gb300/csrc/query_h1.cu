@@ -9,6 +9,10 @@ query_kernel_t query_kernel_h1(int v)
 {
     return query_kernel_variant<1>(v);
 }
+query_kernel_t query_block_kernel_h1()
+{
+    return k_query_blk<1>;
+}
 features_kernel_t features_kernel_h1()
 {
     return k_query_features<1>;

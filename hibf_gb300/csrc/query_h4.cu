@@ -9,6 +9,10 @@ query_kernel_t query_kernel_h4(int v)
 {
     return query_kernel_variant<4>(v);
 }
+query_kernel_t query_block_kernel_h4()
+{
+    return k_query_blk<4>;
+}
 features_kernel_t features_kernel_h4()
 {
     return k_query_features<4>;

@@ -309,6 +309,8 @@ typedef struct hibf_gpu_tuning
     uint32_t early_exit_step;   /* percent between later checks */
     uint32_t early_exit_stages; /* number of checks (0: none; first + (stages - 1) * step must stay below 100) */
     uint32_t early_exit_min;    /* tasks with fewer values are counted in one stage */
+    uint32_t block_queries;     /* batches of at most this many queries run one task per block of 8 warps (latency
+                                   mode: each task's values split over the warps, no early exit); 0: never */
 } hibf_gpu_tuning;
 /* (values_per_lane, fetch_bytes, counter_bits) in {(1,8,7) (2,8,7) (1,8,5) (2,8,5) (1,16,7) (1,16,5)}; hierarchies
  * with more than 3 hash functions or rows of more than 4 words (over 256 technical bins) take (1,8,7) only. */

@@ -29,13 +29,16 @@ def _split(offs, ids):
     return [ids[offs[i]:offs[i + 1]] for i in range(offs.size - 1)]
 
 
+@pytest.mark.parametrize("mode", ["warp", "block"])
 @pytest.mark.parametrize("name", G.HIBF_CASES)
-def test_hibf_batch_matches_reference(gpu_lib, name):
+def test_hibf_batch_matches_reference(gpu_lib, name, mode):
+    """Every golden HIBF's queries, one task per warp and one task per block of eight warps (latency mode)."""
     d = G.hibf_case(name)
     H = _gpu_hibf(d)
     for k, w in enumerate(G.tables(d)["words"]):
         np.testing.assert_array_equal(H.words(k), w)
     agent = H.membership_agent()
+    agent.tuning = dict(agent.tuning, block_queries=0 if mode == "warp" else 1 << 30)
     qv, qo = d["q_values"], d["q_offsets"]
     offs, ids, _ = agent.query_batch(qv, qo, d["mem_t"], mode=N.QUERY_MEMBERSHIP)
     got = _split(offs, ids)
@@ -167,7 +170,8 @@ def test_every_schedule_gives_the_reference_results(gpu_lib, name):
     for vpl, fb, cb in KERNELS:
         for ee in EARLY_EXIT:
             for bps in (0, 1):
-                a.tuning = dict(values_per_lane=vpl, fetch_bytes=fb, counter_bits=cb, blocks_per_sm=bps, **ee)
+                a.tuning = dict(values_per_lane=vpl, fetch_bytes=fb, counter_bits=cb, blocks_per_sm=bps,
+                                block_queries=0, **ee)
                 offs, ids, _ = a.query_batch(qv, qo, d["mem_t"])
                 got = _split(offs, ids)
                 for i, (g, e) in enumerate(zip(got, exp)):
