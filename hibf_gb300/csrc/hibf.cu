@@ -492,7 +492,8 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         int const fit = blk ? a->max_blocks_blk : a->max_blocks[a->variant];
         int const per_sm = a->tune.blocks_per_sm ? std::min<int>(fit, static_cast<int>(a->tune.blocks_per_sm)) : fit;
         uint64_t const full = static_cast<uint64_t>(sm_count()) * static_cast<uint64_t>(per_sm);
-        uint64_t const want = blk ? nq * 4 : (nq + 7) / 8; // block mode: room for the children of every query
+        // block mode: one block per query at most, so that concurrent batches (a server's slots) find room
+        uint64_t const want = blk ? nq : (nq + 7) / 8;
         unsigned const grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min(full, want)));
         // inside a stream capture an event record only orders work unless it is marked external; external records
         // become event-record nodes of the graph, so replays time the kernel too
@@ -833,7 +834,7 @@ extern "C"
         t->early_exit_step = 10;
         t->early_exit_stages = 7;
         t->early_exit_min = 256;
-        t->block_queries = 512;
+        t->block_queries = 8192;
     }
 
     int hibf_gpu_agent_set_tuning(hibf_gpu_agent * a, hibf_gpu_tuning const * t)

@@ -26,7 +26,7 @@ def test_default_schedule():
     t = N.Tuning()
     N.lib().hibf_gpu_tuning_default(ctypes.byref(t))
     assert t.as_dict() == dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, blocks_per_sm=0, early_exit_first=30,
-                               early_exit_step=10, early_exit_stages=7, early_exit_min=256, block_queries=512)
+                               early_exit_step=10, early_exit_stages=7, early_exit_min=256, block_queries=8192)
 
 
 def cost(t):
