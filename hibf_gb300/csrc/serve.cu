@@ -359,6 +359,42 @@ extern "C"
                     sl->h_ids.ensure((mq * 16 + 4096) * 8);
                     S->slots.push_back(std::move(sl));
                 }
+                // warm every slot: one single-value query in latency mode and one in throughput mode, so that the
+                // first requests do not pay for loading kernels or first-touching buffers
+                for (auto & sl : S->slots)
+                {
+                    uint64_t * hv = sl->h_values.as<uint64_t>();
+                    uint64_t * ho = sl->h_qoff.as<uint64_t>();
+                    uint64_t * ht = sl->h_thr.as<uint64_t>();
+                    hv[0] = 0;
+                    ho[0] = 0;
+                    ho[1] = 1;
+                    ht[0] = 1;
+                    HG_CUDA(cudaMemcpyAsync(sl->d_values.p, hv, 8, cudaMemcpyHostToDevice, sl->stream));
+                    HG_CUDA(cudaMemcpyAsync(sl->d_qoff.p, ho, 16, cudaMemcpyHostToDevice, sl->stream));
+                    HG_CUDA(cudaMemcpyAsync(sl->d_thr.p, ht, 8, cudaMemcpyHostToDevice, sl->stream));
+                    hibf_gpu_tuning t{}, warm{};
+                    hibf_gpu_agent_get_tuning(sl->agent, &t);
+                    for (uint32_t bq : {t.block_queries, 0u})
+                    {
+                        warm = t;
+                        warm.block_queries = bq;
+                        int st = hibf_gpu_agent_set_tuning(sl->agent, &warm);
+                        uint64_t const *ro = nullptr, *ri = nullptr;
+                        void const * rc = nullptr;
+                        if (st == HIBF_GPU_OK)
+                            st = hibf_gpu_agent_query_batch_d(sl->agent, HIBF_GPU_QUERY_MEMBERSHIP, sl->d_values.as<uint64_t>(),
+                                                              sl->d_qoff.as<uint64_t>(), 1, sl->d_thr.as<uint64_t>(), 2,
+                                                              &ro, &ri, &rc);
+                        if (st == HIBF_GPU_OK)
+                            st = hibf_gpu_agent_status(sl->agent);
+                        if (st != HIBF_GPU_OK)
+                            fail(st, "slot warm-up failed");
+                    }
+                    int const st = hibf_gpu_agent_set_tuning(sl->agent, &t);
+                    if (st != HIBF_GPU_OK)
+                        fail(st, "agent tuning");
+                }
                 hibf_gpu_server * raw = S.release();
                 for (auto & sl : raw->slots)
                     raw->workers.emplace_back(slot_loop, raw, sl.get());
