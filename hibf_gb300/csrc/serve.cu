@@ -660,8 +660,17 @@ extern "C"
                 // pool is registered with the server for the run, as a client that registers its receive buffers
                 // would have it, so the server copies request values to the device without staging them.
                 uint64_t const pool_bytes = pool_offsets[pool_queries] * 8;
-                bool const registered =
-                    pool_bytes && hibf_gpu_server_register_host(S, pool_values, pool_bytes, 0) == HIBF_GPU_OK;
+                bool registered = false;
+                if (pool_bytes)
+                {
+                    // a pool that is already page-locked (cudaHostAlloc) is registered as such
+                    cudaPointerAttributes a{};
+                    bool const pinned =
+                        cudaPointerGetAttributes(&a, pool_values) == cudaSuccess && a.type == cudaMemoryTypeHost;
+                    cudaGetLastError();
+                    registered = hibf_gpu_server_register_host(S, pool_values, pool_bytes, pinned ? 1 : 0) ==
+                                 HIBF_GPU_OK;
+                }
                 struct unregister_guard
                 {
                     hibf_gpu_server * s;
