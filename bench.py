@@ -34,6 +34,9 @@ METRIC = "HIBF query values/s on 1 GB300, batched vs plain (bit-exact); p99 serv
 WORKLOAD_DESC = {
     "hibf8192": "HIBF 8,192 user bins (log-normal median 2e5 sigma 1.5, [1e3,5e7]), h=2, fpr 0.05, tmax 64; "
                 "1e6 queries len U[20,2000] (70% from 1-3 UBs, 2% noise), t=ceil(0.7 len); membership_for",
+    "hibf65536": "HIBF 65,536 user bins (log-normal median 1e5 sigma 2.0, [500,2e8]), h=3, fpr 0.02, tmax 256; "
+                 "1e6 of 1e7 queries per step, len U[50,5000] (70% from 1-3 UBs, 2% noise), t=ceil(0.6 len); "
+                 "membership_for",
     "hibf64": "HIBF 64 user bins (log-uniform [1e3,1e5]), h=2, fpr 0.05, tmax 64; 10,000 queries of 250 values "
               "(half from one UB), t=125; membership_for",
 }
@@ -49,7 +52,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["hibf8192", "hibf64", "ibf1024"], default="hibf8192")
+    ap.add_argument("--workload", choices=["hibf8192", "hibf64", "hibf65536", "ibf1024"], default="hibf8192")
     ap.add_argument("--queries", type=int, default=0, help="override the number of queries per step")
     ap.add_argument("--plain-queries", type=int, default=2000, help="queries timed in the plain form")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
@@ -124,13 +127,14 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_value_visit():
+def traffic_per_value_visit(workload="hibf8192"):
     """DRAM bytes per (value, IBF) visit of the query kernel from the committed ncu summary, if present."""
     p = ROOT / "profiles" / "traffic.txt"
     if not p.exists():
         return None
+    key = "k_query_bytes_per_value_visit" + ("" if workload == "hibf8192" else "_" + workload) + "="
     for line in p.read_text().splitlines():
-        if line.startswith("k_query_bytes_per_value_visit="):
+        if line.startswith(key):
             return float(line.split("=", 1)[1])
     return None
 
@@ -168,6 +172,30 @@ def oracle_from_device(hibf):
         addr, n = OH.data_ptr(k)
         N.call("hibf_gpu_hibf_download_words", hibf._h, k, addr, n)
     return OH
+
+
+def host_ram_bytes():
+    try:
+        return os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    except (ValueError, OSError):
+        return 1 << 40
+
+
+def cpu_baseline_scaled(args, wl, scale):
+    """CPU baseline and oracle parity on the same layout with every user bin scaled by `scale`."""
+    hibf, offs, _ = build_index(wl, scale)
+    OH = oracle_from_device(hibf)
+    threads = os.cpu_count() or 1
+    s = cpu_sample(OH, wl, offs, args.cpu_seconds, threads)
+    cpu = {"value": s["values"] / s["seconds"], "unit": "values/s", "cores": threads, "kind": "port",
+           "sample": f"{s['queries']} queries ({s['values']} values) on the same layout with user bins at {scale} of "
+                     f"their size (the full index does not fit host memory for the oracle), membership_for + "
+                     f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads"}
+    o_off, o_ids = OH.membership_batch(s["v"], s["qo"], s["thr"], threads=threads)
+    g_off, g_ids, _ = hibf.membership_agent().query_batch(s["v"], s["qo"], s["thr"])
+    n = s["queries"]
+    return cpu, {"oracle_sample_queries": n, "oracle_sample_index_scale": scale,
+                 "oracle_sample_equal": bool(np.array_equal(o_off, g_off) and np.array_equal(o_ids, g_ids))}
 
 
 def cpu_sample(OH, wl, offs, budget_s, threads, first=0):
@@ -278,7 +306,7 @@ def run_ours(args, wl, rank, world, local):
 
         dist.init_process_group("nccl")
     hibf, offs, build_s = build_index(wl, args.scale)
-    nq = args.queries or wl.n_queries
+    nq = args.queries or min(wl.n_queries, 1_000_000)
     qo, thr = wl.query_offsets(0, nq)
     nv = int(qo[-1])
     d_ub = torch.from_numpy(offs.view(np.int64)).cuda()
@@ -397,7 +425,7 @@ def run_ours(args, wl, rank, world, local):
 
     # serving: open-loop Poisson arrivals against the resident index (continuous batching, 4 slots, 4 GiB cap)
     serving = []
-    if not args.no_serve:
+    if not args.no_serve and wl.name == "hibf8192":  # the serving workload runs on the 8,192-user-bin index
         from hibf_gb300.serve import server
 
         pool_q = min(nq, 100_000)
@@ -420,10 +448,15 @@ def run_ours(args, wl, rank, world, local):
         bytes_per_visit = wl.h * 1 * 32  # h rows of ceil(64/256) = 1 sector each (all IBFs have 64 bins)
         # bytes the executed work needs: a task stops reading values once its IBF can no longer report (exact)
         achieved = executed * bytes_per_visit / (kernel_ms / 1e3) / 1e9
-        tpv = traffic_per_value_visit()
+        tpv = traffic_per_value_visit(wl.name)
         cpu = None
         parity = {"plain_equals_batch": plain_equal, "e2e_equals_batch": e2e_equal}
-        if not args.no_cpu:
+        if not args.no_cpu and int(hibf.info()["device_bytes"]) > host_ram_bytes() // 4:
+            # the oracle holds the whole index in host memory: on an index this large it runs on the same layout at
+            # 1/50 of every user bin's size, against the device answering the same queries on that index
+            cpu, small = cpu_baseline_scaled(args, wl, 0.02)
+            parity.update(small)
+        elif not args.no_cpu:
             OH = oracle_from_device(hibf)
             threads = os.cpu_count() or 1
             s = cpu_sample(OH, wl, offs, args.cpu_seconds, threads)
@@ -484,6 +517,12 @@ def run_reference(args, wl, rank, world, local):
 
     torch.cuda.set_device(local)
     hibf, offs, _ = build_index(wl, args.scale)
+    scale_note = ""
+    if int(hibf.info()["device_bytes"]) > host_ram_bytes() // 4:
+        # the oracle needs the index in host memory: the same layout with user bins at 1/50 of their size
+        del hibf
+        hibf, offs, _ = build_index(wl, 0.02)
+        scale_note = "; index at 0.02 of every user bin's size (the full one does not fit host memory)"
     OH = oracle_from_device(hibf)
     del hibf
     threads = os.cpu_count() or 1
@@ -501,7 +540,7 @@ def run_reference(args, wl, rank, world, local):
         nqs += s["queries"]
     value = vals / secs
     sample = (f"{args.steps} steps of ~{per_step:.1f} s, {nqs} queries ({vals} values) in total, membership_for + "
-              f"sort_results")
+              f"sort_results" + scale_note)
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "values/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",

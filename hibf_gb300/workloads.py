@@ -2,6 +2,9 @@
 
 hibf64     64 user bins, sizes log-uniform in [1e3, 1e5], h=2, fpr 0.05, tmax 64; 10,000 queries of 250 values, half
            from one user bin, half uniform; threshold 125.
+hibf65536  65,536 user bins, sizes log-normal (median 1e5, sigma 2.0) clipped to [500, 2e8] (4.8e10 values), h=3,
+           fpr 0.02, tmax 256, layout from the reference's DP; 10,000,000 queries of length U[50, 5000], composition
+           as above; threshold ceil(0.6 * length).
 hibf8192   8,192 user bins, sizes log-normal (median 2e5, sigma 1.5) clipped to [1e3, 5e7], h=2, fpr 0.05, tmax 64,
            layout from the reference's DP over HyperLogLog sketches (sketch_bits 12); 1,000,000 queries of length
            U[20, 2000], 70% drawn from 1-3 user bins with 2% noise, 30% uniform; threshold ceil(0.7 * length).
@@ -79,4 +82,7 @@ HIBF64 = workload("hibf64", 64, S.SIZES_LOG_UNIFORM, 0.0, 0.0, 1000, 100000, 2, 
 HIBF8192 = workload("hibf8192", 8192, S.SIZES_LOG_NORMAL, 200000.0, 1.5, 1000, 50000000, 2, 0.05, 64, 1000000,
                     S.query_spec(1, S.QUERIES_MIXED, 20, 2000, 70, 2, 7, 10, 8192), "c3_layout.txt")
 
-WORKLOADS = {w.name: w for w in (HIBF64, HIBF8192)}
+HIBF65536 = workload("hibf65536", 65536, S.SIZES_LOG_NORMAL, 100000.0, 2.0, 500, 200000000, 3, 0.02, 256, 10000000,
+                     S.query_spec(1, S.QUERIES_MIXED, 50, 5000, 70, 2, 6, 10, 65536), "c4_layout.txt")
+
+WORKLOADS = {w.name: w for w in (HIBF64, HIBF8192, HIBF65536)}
