@@ -488,6 +488,7 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
     if (nq)
     {
         query_params p = base_params(a, d_values, d_qoff, d_thr, nq, mask_for(mode, width));
+        p.decide = mode == HIBF_GPU_QUERY_MEMBERSHIP;
         bool const blk = nq <= a->tune.block_queries;
         int const fit = blk ? a->max_blocks_blk : a->max_blocks[a->variant];
         int const per_sm = a->tune.blocks_per_sm ? std::min<int>(fit, static_cast<int>(a->tune.blocks_per_sm)) : fit;
@@ -526,6 +527,7 @@ void launch_plain(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
     {
         (void)h_qoff;
         query_params p = base_params(a, d_values, d_qoff + q, d_thr + q, 1, mask);
+        p.decide = mode == HIBF_GPU_QUERY_MEMBERSHIP;
         p.q_base = q;
         p.order = nullptr;
         p.self_init = 1;

@@ -104,6 +104,8 @@ struct query_params
     // value visits of every query are added to qwork[query + q_base]
     uint32_t const * order;
     unsigned long long * qwork;
+    // membership mode: a task may also stop once every segment's report/descend decision is final (segment_state)
+    uint32_t decide;
 };
 
 using query_kernel_t = void (*)(query_params);
@@ -139,21 +141,31 @@ __device__ inline unsigned long long wait_for_task(query_params const & p, unsig
     }
 }
 
-// Whether some summation segment of IBF `nd` can still report or descend: its counts so far plus `remaining` for each
-// of its bins (a value adds at most one to every bin) reach the threshold, or could exceed the counter range (then
-// the wrapped sum is not bounded).  When no segment can, the task's outcome is already fixed -- nothing reported,
-// nothing descended -- exactly as if every value had been counted.
-__device__ inline bool any_segment_reachable(query_params const & p, dev_node const & nd, uint32_t const * counts,
-                                             uint64_t remaining, uint64_t thr, int lane)
+// The state of a task after counting all but `remaining` of its values, from each summation segment's sum so far x
+// (a value adds at most one to every bin, so the final sum lies in [x, x + remaining]):
+//   kHopeless  no segment can reach the threshold (x + remaining < t for all): nothing is reported or descended;
+//   kDecided   (membership only, `decide`) every segment either has reached the threshold for good (x >= t and no
+//              wrap possible: x + remaining <= counter mask) or can no longer reach it: the reports and descents are
+//              final, and the bin scan on the partial counts makes exactly them;
+//   kOpen      otherwise.
+// A sum that could exceed the counter range is never decided (its wrapped value is not bounded).  Either early state
+// gives the same outcome as counting every value.
+constexpr int kOpen = 0;
+constexpr int kHopeless = 1;
+constexpr int kDecided = 2;
+
+__device__ inline int segment_state(query_params const & p, dev_node const & nd, uint32_t const * counts,
+                                    uint64_t remaining, uint64_t thr, int lane)
 {
     uint2 const * d = p.descs + nd.desc_offset;
     unsigned long long carry = 0;
+    bool any_reachable = false, any_open = false;
     for (uint32_t c = 0; c < nd.bins; c += 32)
     {
         uint32_t const b = c + lane;
         bool const valid = b < nd.bins;
         uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
-        unsigned long long x = valid ? static_cast<unsigned long long>(counts[b]) + remaining : 0ull;
+        unsigned long long x = valid ? static_cast<unsigned long long>(counts[b]) : 0ull;
         bool f = valid && (ds.y & F_HEAD);
         if (lane == 0 && !f)
             x += carry;
@@ -170,13 +182,20 @@ __device__ inline bool any_segment_reachable(query_params const & p, dev_node co
             }
         }
         bool const ends = valid && (ds.y & (F_RUN_END | F_MERGED));
-        if (__any_sync(kFullMask, ends && (x >= thr || x > p.count_mask)))
-            return true;
+        unsigned long long const top = x + remaining;
+        bool const reachable = ends && (top >= thr || top > p.count_mask);
+        bool const passed = x >= thr && top <= p.count_mask;
+        any_reachable = __any_sync(kFullMask, reachable) || any_reachable;
+        any_open = __any_sync(kFullMask, reachable && !passed) || any_open;
         unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
         uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
         carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
+        if (any_reachable && !p.decide)
+            return kOpen; // only hopelessness is of interest: one reachable segment settles it
     }
-    return false;
+    if (!any_reachable)
+        return kHopeless;
+    return (p.decide && !any_open) ? kDecided : kOpen;
 }
 
 // Counting with variant V.  Variant 0 handles every row width; the tuned variants only rows of up to 4 words (the
@@ -350,10 +369,10 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
         counts[i] = 0;
     __syncwarp();
     row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
-    // Count in stages; after each stage stop if no segment can reach the threshold any more (exact: see above).
+    // Count in stages; after each stage stop if the outcome is already fixed (segment_state: exact).
     uint64_t done = 0;
-    bool hopeless = !any_segment_reachable(p, nd, counts, n, thr, lane);
-    if (!hopeless && n >= p.ee_min)
+    int state = segment_state(p, nd, counts, n, thr, lane);
+    if (state == kOpen && n >= p.ee_min)
     {
         for (uint32_t s = 0; s < p.ee_stages; ++s)
         {
@@ -363,20 +382,18 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
             count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
             done = stop;
             __syncwarp();
-            if (!any_segment_reachable(p, nd, counts, n - done, thr, lane))
-            {
-                hopeless = true;
+            state = segment_state(p, nd, counts, n - done, thr, lane);
+            if (state != kOpen)
                 break;
-            }
         }
     }
-    if (!hopeless)
+    if (state == kOpen)
     {
         count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, n - done, counts, lane);
         done = n;
     }
     __syncwarp();
-    if (hopeless)
+    if (state == kHopeless)
     {
         if (lane == 0)
         {
