@@ -260,3 +260,24 @@ def test_claim_order_work_counters_and_features(gpu_lib):
     np.testing.assert_allclose(f[:, 0], np.log2(1 + n) / 16, rtol=1e-6)
     np.testing.assert_allclose(f[:, 5], np.minimum(n, 16) / 16, rtol=1e-6)
     assert np.all((f[:, 2] >= 0) & (f[:, 2] <= 1)) and np.all((f[:, 3] >= 0) & (f[:, 3] <= 1))
+
+
+@pytest.mark.parametrize("name", G.HIBF_CASES)
+def test_early_decisions_on_every_case(gpu_lib, name):
+    """Checkpoints after every 10% of every task's values (no minimum length): the hopeless and the decided exits
+    fire as often as they can, and membership lists and counts stay the reference's."""
+    d = G.hibf_case(name)
+    H = _gpu_hibf(d)
+    a = H.membership_agent()
+    a.tuning = dict(a.tuning, block_queries=0, early_exit_first=10, early_exit_step=10, early_exit_stages=9,
+                    early_exit_min=1)
+    qv, qo = d["q_values"], d["q_offsets"]
+    offs, ids, _ = a.query_batch(qv, qo, d["mem_t"])
+    for i, (g, e) in enumerate(zip(_split(offs, ids), G.mem_lists(d, "mem_sorted"))):
+        np.testing.assert_array_equal(g, e, err_msg=f"query {i}")
+    w = 2 if "count2" in d else 8
+    offs, ids, cnts = a.query_batch(qv, qo, d["cnt_t"], mode=N.QUERY_COUNT, width=w)
+    dense = np.zeros_like(d[f"count{w}"])
+    for i in range(offs.size - 1):
+        dense[i, ids[offs[i]:offs[i + 1]].astype(np.int64)] = cnts[offs[i]:offs[i + 1]]
+    np.testing.assert_array_equal(dense, d[f"count{w}"])
