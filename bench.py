@@ -446,8 +446,10 @@ def run_ours(args, wl, rank, world, local):
     if rank == 0:
         hbm, peak_kind = peaks()
         bytes_per_visit = wl.h * 1 * 32  # h rows of ceil(64/256) = 1 sector each (all IBFs have 64 bins)
-        # bytes the executed work needs: a task stops reading values once its IBF can no longer report (exact)
-        achieved = executed * bytes_per_visit / (kernel_ms / 1e3) / 1e9
+        # algorithmic bytes: h sectors for every (value, IBF) visit the reference's traversal implies; the kernel
+        # reads fewer (a task stops once its outcome is fixed), reported beside as achieved_executed
+        achieved = visits * bytes_per_visit / (kernel_ms / 1e3) / 1e9
+        achieved_executed = executed * bytes_per_visit / (kernel_ms / 1e3) / 1e9
         tpv = traffic_per_value_visit(wl.name)
         cpu = None
         parity = {"plain_equals_batch": plain_equal, "e2e_equals_batch": e2e_equal}
@@ -488,7 +490,8 @@ def run_ours(args, wl, rank, world, local):
             "batched_vs_plain": value / world / plain_vps,
             "gpu_launches": launches_per_step * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "peak_kind": peak_kind,
+                         "peak_kind": peak_kind, "achieved_executed": achieved_executed,
+                         "frac_executed": achieved_executed / hbm,
                          "traffic": (tpv * executed) if tpv is not None else None,
                          "kernel": "k_query", "kernel_ms": kernel_ms, "value_visits": visits,
                          "value_visits_executed": executed, "tasks": tasks,
