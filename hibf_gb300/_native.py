@@ -120,6 +120,11 @@ _SIGS = [
     ("hibf_gpu_hibf_build", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, INPUT_FN, vp, ctypes.POINTER(vp)]),
     ("hibf_gpu_ibf_build", None, [ctypes.POINTER(BuildConfig), u64, ctypes.c_uint32, ci, INPUT_FN, vp,
                                   ctypes.POINTER(vp)]),
+    ("hibf_gpu_hibf_set_prev", None, [vp, vp, vp]),
+    ("hibf_gpu_ibf_save", None, [vp, ctypes.c_char_p]),
+    ("hibf_gpu_ibf_load", None, [ctypes.c_char_p, ctypes.POINTER(vp)]),
+    ("hibf_gpu_hibf_save", None, [vp, ctypes.c_char_p]),
+    ("hibf_gpu_hibf_load", None, [ctypes.c_char_p, ctypes.POINTER(vp)]),
     ("hibf_gpu_hll_sketch", None, [vp, u64, ctypes.c_uint32, vp]),
     ("hibf_gpu_hll_estimate", None, [vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_hll_sketch_d", None, [vp, u64, vp, u64, ctypes.c_uint32, vp, vp]),

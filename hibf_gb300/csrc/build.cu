@@ -514,10 +514,31 @@ void run_jobs(hibf_gpu_hibf * h, std::vector<insert_job> const & jobs, uint64_t 
 hibf_gpu_hibf * create_from_plan(plan_t const & P, uint64_t n_user_bins)
 {
     hibf_gpu_hibf * h = nullptr;
-    int const st = hibf_gpu_hibf_create(n_user_bins, P.bins.size(), P.bins.data(), P.bin_size.data(),
-                                        P.hash_funs.data(), P.next_ibf.data(), P.user_bin.data(), &h);
+    int st = hibf_gpu_hibf_create(n_user_bins, P.bins.size(), P.bins.data(), P.bin_size.data(), P.hash_funs.data(),
+                                  P.next_ibf.data(), P.user_bin.data(), &h);
     if (st != HIBF_GPU_OK)
         fail(st, "hibf_gpu_hibf_create failed");
+    // prev_ibf_id as the reference's build leaves it (src/hierarchical_interleaved_bloom_filter.cpp:130): set for
+    // the children it builds in its loop over merged bins, (0, 0) for the root and for favourite children
+    std::vector<uint64_t> pi(P.bins.size(), 0), pb(P.bins.size(), 0);
+    for (size_t k = 0; k < P.order.size(); ++k)
+    {
+        size_t const n = P.order[k];
+        size_t const parent = P.g[n].parent;
+        if (parent == SIZE_MAX)
+            continue;
+        node_t const & pn = P.g[parent];
+        if (pn.favourite >= 0 && pn.children[static_cast<size_t>(pn.favourite)] == n)
+            continue;
+        pi[k] = P.ibf_of[parent];
+        pb[k] = P.g[n].parent_bin_index;
+    }
+    st = hibf_gpu_hibf_set_prev(h, pi.data(), pb.data());
+    if (st != HIBF_GPU_OK)
+    {
+        hibf_gpu_hibf_destroy(h);
+        fail(st, "prev_ibf_id");
+    }
     return h;
 }
 

@@ -19,6 +19,7 @@
 #include "device.cuh"
 #include "hibf_internal.cuh"
 #include "query.cuh"
+#include "archive.hpp"
 
 namespace hibf_gb300
 {
@@ -1090,6 +1091,23 @@ extern "C"
                     h->n_ibfs = n_ibfs;
                     h->next_ibf_id.assign(next_ibf_id, next_ibf_id + off[n_ibfs]);
                     h->user_bin_id.assign(user_bin_id, user_bin_id + off[n_ibfs]);
+                    // parents: every merged bin's child IBF gets (IBF, bin); the root keeps (0, 0)
+                    h->prev_ibf.assign(n_ibfs, 0);
+                    h->prev_bin.assign(n_ibfs, 0);
+                    for (uint64_t k = 0; k < n_ibfs; ++k)
+                        for (uint64_t b = 0; b < bins[k]; ++b)
+                        {
+                            uint64_t const i = off[k] + b;
+                            if (user_bin_id[i] == HIBF_GPU_BIN_MERGED && next_ibf_id[i] != k)
+                            {
+                                h->prev_ibf[next_ibf_id[i]] = k;
+                                h->prev_bin[next_ibf_id[i]] = b;
+                            }
+                        }
+                    h->occupancy.resize(n_ibfs);
+                    for (uint64_t k = 0; k < n_ibfs; ++k)
+                        h->occupancy[k].assign(((bins[k] + 63) / 64) * 64, 0);
+                    h->track_occupancy.assign(n_ibfs, 0);
                     h->max_depth = max_depth;
                     HG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
                     uint32_t cpw = 64;
@@ -1260,6 +1278,150 @@ extern "C"
                     h->io.as<uint64_t>(), nullptr, n, bin, h->bins[k]);
                 HG_CUDA(cudaGetLastError());
                 HG_CUDA(cudaStreamSynchronize(h->stream));
+            });
+    }
+
+    int hibf_gpu_hibf_set_prev(hibf_gpu_hibf * h, uint64_t const * prev_ibf, uint64_t const * prev_bin)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || !prev_ibf || !prev_bin)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                for (uint64_t k = 0; k < h->n_ibfs; ++k)
+                    if (prev_ibf[k] >= h->n_ibfs || prev_bin[k] >= h->bins[prev_ibf[k]])
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "prev_ibf_id out of range");
+                std::lock_guard<std::mutex> lk(h->mu);
+                h->prev_ibf.assign(prev_ibf, prev_ibf + h->n_ibfs);
+                h->prev_bin.assign(prev_bin, prev_bin + h->n_ibfs);
+            });
+    }
+
+    int hibf_gpu_hibf_save(hibf_gpu_hibf * h, char const * path)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || !path)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(h->mu);
+                HG_CUDA(cudaStreamSynchronize(h->stream));
+                file_writer w(path);
+                w.u32(kArchiveVersion);
+                w.u64(h->n_user_bins);
+                w.u64(h->n_ibfs);
+                for (uint64_t k = 0; k < h->n_ibfs; ++k)
+                {
+                    write_ibf_header(w, h->bins[k], h->bin_size[k], h->hash_funs[k]);
+                    write_rows(w, h->stores[k]->as<uint64_t>(), h->bin_size[k], h->bin_words[k], h->row_words[k],
+                               h->stream);
+                    w.u64s(h->occupancy[k]);
+                    w.u8(h->track_occupancy[k]);
+                }
+                uint64_t off = 0;
+                auto per_ibf = [&](std::vector<uint64_t> const & flat)
+                {
+                    w.u64(h->n_ibfs);
+                    off = 0;
+                    for (uint64_t k = 0; k < h->n_ibfs; ++k)
+                    {
+                        w.u64(h->bins[k]);
+                        w.raw(flat.data() + off, h->bins[k] * 8);
+                        off += h->bins[k];
+                    }
+                };
+                per_ibf(h->next_ibf_id);
+                w.u64(h->n_ibfs);
+                for (uint64_t k = 0; k < h->n_ibfs; ++k)
+                {
+                    w.u64(h->prev_ibf[k]);
+                    w.u64(h->prev_bin[k]);
+                }
+                per_ibf(h->user_bin_id);
+                w.close();
+            });
+    }
+
+    int hibf_gpu_hibf_load(char const * path, hibf_gpu_hibf ** out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!path || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *out = nullptr;
+                file_reader r(path);
+                if (r.u32() != kArchiveVersion)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "archive: unsupported hierarchical_interleaved_bloom_filter version");
+                uint64_t const nub = r.u64();
+                uint64_t const n = r.u64();
+                if (n == 0 || n > kNodeMask)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "archive: implausible number of IBFs");
+                std::vector<uint64_t> bins(n), sizes(n), funs(n);
+                std::vector<long> words_at(n);
+                std::vector<std::vector<uint64_t>> occ(n);
+                std::vector<uint8_t> track(n);
+                for (uint64_t k = 0; k < n; ++k)
+                {
+                    ibf_header const hd = read_ibf_header(r);
+                    bins[k] = hd.bins;
+                    sizes[k] = hd.bin_size;
+                    funs[k] = hd.hash_funs;
+                    words_at[k] = r.tell();
+                    r.skip(hd.bin_size * hd.bin_words * 8);
+                    occ[k] = r.u64s(hd.technical_bins);
+                    track[k] = r.u8();
+                }
+                auto per_ibf = [&]()
+                {
+                    if (r.u64() != n)
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "archive: table length differs from the IBF count");
+                    std::vector<uint64_t> flat;
+                    for (uint64_t k = 0; k < n; ++k)
+                    {
+                        std::vector<uint64_t> const v = r.u64s(bins[k]);
+                        if (v.size() != bins[k])
+                            fail(HIBF_GPU_ERR_INVALID_ARG, "archive: table row length differs from the IBF's bins");
+                        flat.insert(flat.end(), v.begin(), v.end());
+                    }
+                    return flat;
+                };
+                std::vector<uint64_t> const next = per_ibf();
+                if (r.u64() != n)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "archive: prev_ibf_id length differs from the IBF count");
+                std::vector<uint64_t> prev_ibf(n), prev_bin(n);
+                for (uint64_t k = 0; k < n; ++k)
+                {
+                    prev_ibf[k] = r.u64();
+                    prev_bin[k] = r.u64();
+                }
+                std::vector<uint64_t> const ub = per_ibf();
+                if (!r.at_end())
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "archive: trailing bytes");
+                hibf_gpu_hibf * h = nullptr;
+                int st = hibf_gpu_hibf_create(nub, n, bins.data(), sizes.data(), funs.data(), next.data(), ub.data(), &h);
+                if (st != HIBF_GPU_OK)
+                    fail(st, std::string(hibf_gpu_last_error()));
+                try
+                {
+                    for (uint64_t k = 0; k < n; ++k)
+                    {
+                        r.seek(words_at[k]);
+                        read_rows(r, h->stores[k]->as<uint64_t>(), h->bin_size[k], h->bin_words[k], h->row_words[k],
+                                  h->stream);
+                    }
+                    st = hibf_gpu_hibf_set_prev(h, prev_ibf.data(), prev_bin.data());
+                    if (st != HIBF_GPU_OK)
+                        fail(st, std::string(hibf_gpu_last_error()));
+                    h->occupancy = std::move(occ);
+                    h->track_occupancy = std::move(track);
+                }
+                catch (...)
+                {
+                    hibf_gpu_hibf_destroy(h);
+                    throw;
+                }
+                *out = h;
             });
     }
 

@@ -47,6 +47,11 @@ struct hibf_gpu_hibf
     hibf_gb300::dbuf io;
     // the tables as given (reference conventions), for hibf_gpu_hibf_get_tables
     std::vector<uint64_t> next_ibf_id, user_bin_id;
+    // prev_ibf_id (parent IBF and bin of every IBF) and each IBF's occupancy / track_occupancy, kept on the host for
+    // serialisation only (queries use neither)
+    std::vector<uint64_t> prev_ibf, prev_bin;
+    std::vector<std::vector<uint64_t>> occupancy;
+    std::vector<uint8_t> track_occupancy;
     cudaStream_t stream{};
     std::mutex mu;
 };

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/hibf_gb300_synthetic.h"
+#include "archive.hpp"
 #include "common.hpp"
 #include "count.cuh"
 #include "device.cuh"
@@ -880,6 +881,68 @@ extern "C"
                     if (counts[b] >= threshold)
                         out_ids[m++] = b;
                 *n_out = m;
+            });
+    }
+
+    int hibf_gpu_ibf_save(hibf_gpu_ibf * f, char const * path)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || !path)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(f->mu);
+                HG_CUDA(cudaStreamSynchronize(f->stream));
+                file_writer w(path);
+                write_ibf_header(w, f->bins, f->bin_size, f->hash_funs);
+                write_rows(w, f->store.as<uint64_t>(), f->bin_size, f->bin_words, f->row_words, f->stream);
+                uint64_t const tb = f->technical_bins();
+                std::vector<uint64_t> occ(tb, 0);
+                if (f->track_occupancy)
+                {
+                    HG_CUDA(cudaMemcpyAsync(occ.data(), f->occupancy.p, tb * 8, cudaMemcpyDeviceToHost, f->stream));
+                    HG_CUDA(cudaStreamSynchronize(f->stream));
+                }
+                w.u64s(occ);
+                w.u8(f->track_occupancy ? 1 : 0);
+                w.close();
+            });
+    }
+
+    int hibf_gpu_ibf_load(char const * path, hibf_gpu_ibf ** out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!path || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *out = nullptr;
+                file_reader r(path);
+                ibf_header const h = read_ibf_header(r);
+                long const words_at = r.tell();
+                r.skip(h.bin_size * h.bin_words * 8);
+                std::vector<uint64_t> const occ = r.u64s(h.technical_bins);
+                uint8_t const track = r.u8();
+                if (occ.size() != h.technical_bins || track > 1 || !r.at_end())
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "archive: malformed interleaved_bloom_filter");
+                hibf_gpu_ibf * f = nullptr;
+                int const st = hibf_gpu_ibf_create(h.bins, h.bin_size, h.hash_funs, track, &f);
+                if (st != HIBF_GPU_OK)
+                    fail(st, g_last_error);
+                try
+                {
+                    r.seek(words_at);
+                    read_rows(r, f->store.as<uint64_t>(), f->bin_size, f->bin_words, f->row_words, f->stream);
+                    HG_CUDA(cudaMemcpyAsync(f->occupancy.p, occ.data(), occ.size() * 8, cudaMemcpyHostToDevice,
+                                            f->stream));
+                    HG_CUDA(cudaStreamSynchronize(f->stream));
+                }
+                catch (...)
+                {
+                    hibf_gpu_ibf_destroy(f);
+                    throw;
+                }
+                *out = f;
             });
     }
 

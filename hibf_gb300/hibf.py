@@ -94,6 +94,26 @@ class hierarchical_interleaved_bloom_filter:
                 self.set_words(k, w)
         return self
 
+    def save(self, path) -> None:
+        """Serialises the device stores and tables in the reference's byte layout (cereal binary encoding)."""
+        N.call("hibf_gpu_hibf_save", self._h, str(path).encode())
+
+    @classmethod
+    def load(cls, path) -> "hierarchical_interleaved_bloom_filter":
+        """Reads a serialised HIBF (as the reference writes it) into new device stores."""
+        from .build import _adopt_handle
+
+        h = ctypes.c_void_p()
+        N.call("hibf_gpu_hibf_load", str(path).encode(), ctypes.byref(h))
+        info = (ctypes.c_uint64 * 4)()
+        N.call("hibf_gpu_hibf_info", h, info)
+        return _adopt_handle(h, int(info[0]))
+
+    def set_prev(self, prev_ibf, prev_bin) -> None:
+        """prev_ibf_id: parent IBF and bin of every IBF (carried through serialisation)."""
+        pi, pb = _u64(prev_ibf), _u64(prev_bin)
+        N.call("hibf_gpu_hibf_set_prev", self._h, pi.ctypes.data, pb.ctypes.data)
+
     def __del__(self):
         if getattr(self, "_h", None):
             try:

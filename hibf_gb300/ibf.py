@@ -66,6 +66,21 @@ class interleaved_bloom_filter:
         self._pending_v: list[int] = []
         self._pending_b: list[int] = []
 
+    def save(self, path) -> None:
+        """Serialises the device store in the reference's byte layout (cereal binary encoding)."""
+        self.flush()
+        N.call("hibf_gpu_ibf_save", self._h, str(path).encode())
+
+    @classmethod
+    def load(cls, path) -> "interleaved_bloom_filter":
+        """Reads a serialised IBF (as the reference writes it) into a new device store."""
+        h = ctypes.c_void_p()
+        N.call("hibf_gpu_ibf_load", str(path).encode(), ctypes.byref(h))
+        obj = cls.__new__(cls)
+        obj._h = h
+        obj._pending_v, obj._pending_b = [], []
+        return obj
+
     def __del__(self):
         if getattr(self, "_h", None):
             try:

@@ -156,6 +156,18 @@ int hibf_gpu_hibf_get_tables(hibf_gpu_hibf const * h, uint64_t * bins, uint64_t 
                              uint64_t * next_ibf_id, uint64_t * user_bin_id);
 /* Words of IBF `ibf` in the reference's bit_vector layout (for serialization or a host-built HIBF). */
 int hibf_gpu_hibf_upload_words(hibf_gpu_hibf * h, uint64_t ibf, uint64_t const * words, uint64_t n_words);
+/* prev_ibf_id (hierarchical_interleaved_bloom_filter.hpp:222-229): parent IBF and bin of every IBF.  Created
+ * hierarchies give every merged bin's child its parent and the root (0, 0); the build leaves the reference's
+ * convention ((0, 0) also for favourite children); set it to carry a host-built HIBF's table through serialisation. */
+int hibf_gpu_hibf_set_prev(hibf_gpu_hibf * h, uint64_t const * prev_ibf, uint64_t const * prev_bin);
+/* Serialisation in the reference's byte layout (cereal binary archive encoding of the serialize functions of
+ * interleaved_bloom_filter.hpp:471-485 with bit_vector.hpp:885-925, and hierarchical_interleaved_bloom_filter.hpp:
+ * 267-277): save streams the device stores to `path`, load reads one into new device stores.  Invalid or
+ * inconsistent archives fail with HIBF_GPU_ERR_INVALID_ARG. */
+int hibf_gpu_ibf_save(hibf_gpu_ibf * ibf, char const * path);
+int hibf_gpu_ibf_load(char const * path, hibf_gpu_ibf ** out);
+int hibf_gpu_hibf_save(hibf_gpu_hibf * h, char const * path);
+int hibf_gpu_hibf_load(char const * path, hibf_gpu_hibf ** out);
 int hibf_gpu_hibf_download_words(hibf_gpu_hibf * h, uint64_t ibf, uint64_t * words, uint64_t n_words);
 
 /* ------------------------------------------------------------------------------------------------------------ */

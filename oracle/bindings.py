@@ -353,6 +353,13 @@ class Reference:
         return RefIBF(self, self.lib.ref_ibf_from_config(ctypes.byref(cfg), _ptr(v), _ptr(o), max_bin_elements))
 
     # -- layout / HIBF -----------------------------------------------------------------------------------
+    def ibf_load(self, data: bytes) -> "RefIBF":
+        """The reference's load of bytes in that encoding (its serialize() with an input archive)."""
+        L = self.lib
+        L.ref_ibf_load.restype = vp
+        L.ref_ibf_load.argtypes = [ctypes.c_char_p, u64]
+        return RefIBF(self, L.ref_ibf_load(data, len(data)))
+
     def hll(self, values, bits):
         """The reference's hyperloglog over `values`: (registers, estimate)."""
         L = self.lib
@@ -393,6 +400,10 @@ class RefIBF:
         p = np.zeros(4, np.uint64)
         self.L.ref_ibf_params(h, _ptr(p))
         self.bins, self.bin_size, self.hash_funs, self.bit_size = (int(x) for x in p)
+
+    def save(self) -> bytes:
+        """The reference's serialize() through a cereal-binary-encoding byte archive (oracle/ref_driver.cpp)."""
+        return _ref_bytes(self.L, "ref_ibf_save", self.h)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -461,9 +472,26 @@ class RefIBF:
         return out[:m]
 
 
+def _ref_bytes(L, fn, h) -> bytes:
+    f = getattr(L, fn)
+    f.restype = vp
+    f.argtypes = [vp, ctypes.POINTER(u64)]
+    n = u64(0)
+    p = f(h, ctypes.byref(n))
+    if not p:
+        raise RuntimeError(f"{fn} failed")
+    out = ctypes.string_at(p, n.value)
+    L.ref_free(p)
+    return out
+
+
 class RefHIBF:
     def __init__(self, r: Reference, h, n_user_bins):
         self.r, self.L, self.h, self.n_user_bins = r, r.lib, h, n_user_bins
+
+    def save(self) -> bytes:
+        """The reference's serialize() through a cereal-binary-encoding byte archive (oracle/ref_driver.cpp)."""
+        return _ref_bytes(self.L, "ref_hibf_save", self.h)
 
     def __del__(self):
         if getattr(self, "h", None):

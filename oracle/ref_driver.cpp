@@ -16,6 +16,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <sstream>
+#include <type_traits>
+#include <stdexcept>
+#include <string_view>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -130,6 +134,121 @@ void hibf_count_into(hibf::hierarchical_interleaved_bloom_filter const & h,
 }
 
 } // namespace
+
+// ---------------------------------------------------------------------------------------------------------------
+// A byte archive with cereal's binary-archive encoding, driving the reference's own serialize/save/load functions:
+// arithmetic values as their raw little-endian bytes, binary_data as raw bytes, std::vector as a uint64 element count
+// followed by raw elements (arithmetic) or each element in turn, base_class as the base object, name-value pairs as
+// their value.  (cereal itself is not available here; this is that encoding, not cereal's code.)
+// ---------------------------------------------------------------------------------------------------------------
+template <class T>
+struct is_std_vector : std::false_type
+{};
+template <class T, class A>
+struct is_std_vector<std::vector<T, A>> : std::true_type
+{};
+template <class T>
+struct is_base_class : std::false_type
+{};
+template <class T>
+struct is_base_class<cereal::base_class<T>> : std::true_type
+{};
+
+struct byte_out_archive : cereal::detail::OutputArchiveBase
+{
+    std::string bytes;
+    template <class... T>
+    void operator()(T &&... xs)
+    {
+        (put(xs), ...);
+    }
+    void raw(void const * p, size_t n)
+    {
+        bytes.append(static_cast<char const *>(p), n);
+    }
+    template <class T>
+    void put(T const & x)
+    {
+        using U = std::remove_cv_t<std::remove_reference_t<T>>;
+        if constexpr (std::is_arithmetic_v<U>)
+            raw(&x, sizeof(U));
+        else if constexpr (std::is_same_v<U, cereal::binary_data_t>)
+            raw(x.ptr, x.size);
+        else if constexpr (is_std_vector<U>::value)
+        {
+            uint64_t const n = x.size();
+            raw(&n, 8);
+            using E = typename U::value_type;
+            if constexpr (std::is_arithmetic_v<E> && !std::is_same_v<E, bool>)
+                raw(x.data(), n * sizeof(E));
+            else
+                for (auto const & e : x)
+                    put(e);
+        }
+        else if constexpr (is_base_class<U>::value)
+            put(*x.base_ptr);
+        else if constexpr (requires(U & u, byte_out_archive & a) { u.CEREAL_SAVE_FUNCTION_NAME(a); })
+            x.CEREAL_SAVE_FUNCTION_NAME(*this);
+        else
+            const_cast<U &>(x).CEREAL_SERIALIZE_FUNCTION_NAME(*this);
+    }
+};
+
+struct byte_in_archive : cereal::detail::InputArchiveBase
+{
+    std::string_view bytes;
+    size_t pos{};
+    template <class... T>
+    void operator()(T &&... xs)
+    {
+        (get(xs), ...);
+    }
+    void raw(void * p, size_t n)
+    {
+        if (pos + n > bytes.size())
+            throw std::runtime_error("archive truncated");
+        std::memcpy(p, bytes.data() + pos, n);
+        pos += n;
+    }
+    template <class T>
+    void get(T && x)
+    {
+        using U = std::remove_cv_t<std::remove_reference_t<T>>;
+        if constexpr (std::is_arithmetic_v<U>)
+            raw(&x, sizeof(U));
+        else if constexpr (std::is_same_v<U, cereal::binary_data_t>)
+            raw(const_cast<void *>(x.ptr), x.size);
+        else if constexpr (is_std_vector<U>::value)
+        {
+            uint64_t n = 0;
+            raw(&n, 8);
+            x.resize(n);
+            using E = typename U::value_type;
+            if constexpr (std::is_arithmetic_v<E> && !std::is_same_v<E, bool>)
+                raw(x.data(), n * sizeof(E));
+            else
+                for (auto & e : x)
+                    get(e);
+        }
+        else if constexpr (is_base_class<U>::value)
+            get(*x.base_ptr);
+        else if constexpr (requires(U & u, byte_in_archive & a) { u.CEREAL_LOAD_FUNCTION_NAME(a); })
+            x.CEREAL_LOAD_FUNCTION_NAME(*this);
+        else
+            x.CEREAL_SERIALIZE_FUNCTION_NAME(*this);
+    }
+};
+
+template <class T>
+char * save_bytes(T const & obj, uint64_t * n)
+{
+    byte_out_archive ar;
+    ar(obj);
+    *n = ar.bytes.size();
+    char * out = static_cast<char *>(std::malloc(std::max<size_t>(1, ar.bytes.size())));
+    std::memcpy(out, ar.bytes.data(), ar.bytes.size());
+    return out;
+}
 
 extern "C"
 {
@@ -507,6 +626,51 @@ extern "C"
                 cnt_nnz[q] = nnz;
                 cnt_digest[q] = cd;
             }
+        }
+    }
+
+    // ---------------------------------------------------------------------------------------------------------
+    // serialisation: the reference's serialize functions through the byte archive above (free with ref_free)
+    // ---------------------------------------------------------------------------------------------------------
+    char * ref_ibf_save(void * p, uint64_t * n)
+    {
+        try
+        {
+            return save_bytes(*static_cast<hibf::interleaved_bloom_filter *>(p), n);
+        }
+        catch (...)
+        {
+            return nullptr;
+        }
+    }
+
+    void * ref_ibf_load(char const * bytes, uint64_t n)
+    {
+        try
+        {
+            auto ibf = std::make_unique<hibf::interleaved_bloom_filter>();
+            byte_in_archive ar;
+            ar.bytes = std::string_view{bytes, n};
+            ar(*ibf);
+            if (ar.pos != n)
+                return nullptr;
+            return ibf.release();
+        }
+        catch (...)
+        {
+            return nullptr;
+        }
+    }
+
+    char * ref_hibf_save(void * p, uint64_t * n)
+    {
+        try
+        {
+            return save_bytes(*static_cast<hibf::hierarchical_interleaved_bloom_filter *>(p), n);
+        }
+        catch (...)
+        {
+            return nullptr;
         }
     }
 

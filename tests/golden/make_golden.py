@@ -272,20 +272,47 @@ def make_ibf_config(R: Reference):
 
 
 def make_hll(R: Reference):
-    """hyperloglog registers and estimates for a few value sets and widths (src/sketch/hyperloglog.cpp)."""
+    """hyperloglog registers and estimates for a few value sets and widths (src/sketch/hyperloglog.cpp).  Value sets
+    are the splitmix64 stream (seed, count: regenerated by the test), 0..n-1, or stored random values."""
     out = {}
     rng = np.random.default_rng(21)
-    cases = [(S.stream_range(3, 0, 1000), 12), (S.stream_range(4, 0, 200000), 12), (S.stream_range(5, 0, 5), 5),
-             (rng.integers(0, 1 << 63, 30000, dtype=np.uint64), 8), (np.zeros(0, np.uint64), 12),
-             (np.arange(100000, dtype=np.uint64), 14), (S.stream_range(6, 0, 50000), 16)]
-    for i, (v, bits) in enumerate(cases):
+    cases = [("stream", 3, 1000, 12), ("stream", 4, 200000, 12), ("stream", 5, 5, 5), ("random", 0, 30000, 8),
+             ("stream", 0, 0, 12), ("arange", 0, 100000, 14), ("stream", 6, 50000, 16)]
+    for i, (kind, seed, n, bits) in enumerate(cases):
+        if kind == "stream":
+            v = S.stream_range(seed, 0, n)
+        elif kind == "arange":
+            v = np.arange(n, dtype=np.uint64)
+        else:
+            v = rng.integers(0, 1 << 63, n, dtype=np.uint64)
+            out[f"c{i}_values"] = v
         regs, est = R.hll(v, bits)
-        out[f"c{i}_values"] = np.asarray(v, np.uint64)
+        out[f"c{i}_source"] = np.array([("stream", "arange", "random").index(kind), seed, n], np.uint64)
         out[f"c{i}_bits"] = np.array([bits], np.uint64)
         out[f"c{i}_registers"] = regs
         out[f"c{i}_estimate"] = np.array([est], np.float64)
     out["n_cases"] = np.array([len(cases)], np.uint64)
     np.savez_compressed(OUT / "hll_cases.npz", **out)
+
+
+def make_serial(R: Reference):
+    """Serialised filters: the reference's serialize functions through cereal's binary encoding (oracle/ref_driver.cpp
+    byte archive), for an IBF with occupancy tracking and two HIBFs, with what is needed to rebuild them."""
+    # IBF: 130 bins x 1000 rows, h = 3, occupancy tracked; value i of the stream seeded 3 goes to bin i % 130
+    ibf = R.ibf(130, 1000, 3, True)
+    v = S.stream_range(3, 0, 4000)
+    ibf.emplace(v, np.arange(4000, dtype=np.uint64) % np.uint64(130))
+    (OUT / "serial_ibf.bin").write_bytes(ibf.save())
+    for name, seed in (("snippet", None), ("synth64", 7)):
+        d = np.load(OUT / f"hibf_{name}.npz")
+        cfg = ref_cfg(int(d["n_user_bins"][0]), h=int(d["config"][0]), fpr=float(d["fpr"][0]),
+                      relaxed_fpr=float(d["fpr"][1]), tmax=int(d["config"][1]), sketch_bits=int(d["config"][2]))
+        layout = bytes(d["layout"]).decode()
+        if seed is None:
+            H = R.hibf(cfg, d["ub_values"], d["ub_offsets"], layout=layout)
+        else:
+            H = R.hibf(cfg, None, d["ub_offsets"], seed=seed, synthetic=True, layout=layout)
+        (OUT / f"serial_hibf_{name}.bin").write_bytes(H.save())
 
 
 def make_c1(R: Reference):
@@ -330,9 +357,11 @@ def make_c4_layout(R: Reference):
 def main(argv):
     build_reference()
     R = Reference()
-    which = set(argv) or {"ibf", "ibfcfg", "hll", "hibf", "hibfwide", "c1", "c3"}
+    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
+    if "serial" in which:
+        make_serial(R)
     if "hll" in which:
         make_hll(R)
     if "hibfwide" in which:
