@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <cub/cub.cuh>
+
 #include "../../include/hibf_gb300_synthetic.h"
 #include "archive.hpp"
 #include "common.hpp"
@@ -84,6 +86,83 @@ __global__ void k_synth_emplace(uint64_t * __restrict__ words, uint64_t bin_size
             exists = exists && (old & bit);
         }
         if (occupancy && !exists)
+            atomicAdd(occupancy + b, 1ull);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Exact occupancy.  The reference counts a value for its bin when one of its bits was not set yet, inserting one value
+// after the other (src/interleaved_bloom_filter.cpp:119-140).  With concurrent atomicOr that depends on timing, so an
+// IBF that tracks occupancy inserts in chunks: every (value, hash) position of the chunk becomes a key row * tb + bin,
+// a stable sort groups equal positions in insertion order, and a value counts when it is the first of the chunk at a
+// position that was unset before the chunk.  Then the bits are set.
+// ---------------------------------------------------------------------------------------------------------------
+constexpr uint64_t kNoPosition = ~0ull;
+
+template <bool SYNTH>
+__global__ void k_occ_keys(uint64_t const * __restrict__ words, uint64_t bin_size, uint32_t row_words, uint32_t shift,
+                           uint32_t h, uint64_t const * __restrict__ values, uint64_t const * __restrict__ bins,
+                           uint64_t seed, uint64_t vpb, uint64_t first, uint64_t n, uint64_t bin, uint64_t n_bins,
+                           uint64_t tb, unsigned long long * __restrict__ keys, unsigned long long * __restrict__ ids,
+                           uint8_t * __restrict__ was_set, uint64_t * __restrict__ gen_values)
+{
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        uint64_t v, b;
+        if constexpr (SYNTH)
+        {
+            b = bin;
+            v = hg_ibf_bin_value(seed, vpb, bin, first + i);
+            gen_values[i] = v;
+        }
+        else
+        {
+            v = values[i];
+            b = bins ? bins[i] : bin;
+        }
+        for (uint32_t k = 0; k < h; ++k)
+        {
+            uint64_t const idx = i * h + k;
+            ids[idx] = idx;
+            if (b >= n_bins)
+            {
+                keys[idx] = kNoPosition;
+                was_set[idx] = 1;
+                continue;
+            }
+            uint64_t const r = hash_row(v, c_hash_seeds[k], shift, bin_size);
+            keys[idx] = r * tb + b;
+            was_set[idx] = static_cast<uint8_t>((words[r * row_words + (b >> 6)] >> (b & 63u)) & 1u);
+        }
+    }
+}
+
+__global__ void k_occ_first(unsigned long long const * __restrict__ keys, unsigned long long const * __restrict__ ids,
+                            uint64_t m, uint32_t h, uint8_t const * __restrict__ was_set,
+                            unsigned int * __restrict__ newly)
+{
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t j = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; j < m; j += stride)
+    {
+        if (keys[j] == kNoPosition || (j > 0 && keys[j] == keys[j - 1]))
+            continue;
+        uint64_t const idx = ids[j];
+        if (!was_set[idx])
+            newly[idx / h] = 1u;
+    }
+}
+
+template <bool SYNTH>
+__global__ void k_occ_count(unsigned int const * __restrict__ newly, uint64_t const * __restrict__ bins, uint64_t vpb,
+                            uint64_t first, uint64_t n, uint64_t bin, uint64_t n_bins,
+                            unsigned long long * __restrict__ occupancy)
+{
+    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        uint64_t const b = SYNTH ? bin : (bins ? bins[i] : bin);
+        if (newly[i] && b < n_bins)
             atomicAdd(occupancy + b, 1ull);
     }
 }
@@ -395,16 +474,77 @@ cudaStream_t pick(hibf_gpu_ibf * f, void * s)
     return s ? static_cast<cudaStream_t>(s) : f->stream;
 }
 
+// Occupancy in insertion order, chunk by chunk, then each chunk's bits; chunks run one after the other, so each sees
+// the bits of the chunks before it.  SYNTH: the n values are the generated values of bin `bin` (vpb per bin).
+template <bool SYNTH>
+void emplace_exact(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t const * d_bins, uint64_t n, uint64_t bin,
+                   uint64_t seed, uint64_t vpb, cudaStream_t s)
+{
+    constexpr uint64_t kChunk = 1u << 20;
+    unsigned const block = 256;
+    uint32_t const h = static_cast<uint32_t>(f->hash_funs);
+    uint64_t const m_max = std::min(n, kChunk) * h;
+    dbuf keys, keys2, ids, ids2, was_set, newly, gen, tmp;
+    keys.ensure(m_max * 8);
+    keys2.ensure(m_max * 8);
+    ids.ensure(m_max * 8);
+    ids2.ensure(m_max * 8);
+    was_set.ensure(m_max);
+    newly.ensure(std::min(n, kChunk) * 4);
+    if (SYNTH)
+        gen.ensure(std::min(n, kChunk) * 8);
+    size_t tmp_bytes = 0;
+    HG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.as<unsigned long long>(),
+                                            keys2.as<unsigned long long>(), ids.as<unsigned long long>(),
+                                            ids2.as<unsigned long long>(), static_cast<int>(m_max), 0, 64, s));
+    tmp.ensure(std::max<size_t>(tmp_bytes, 16));
+    uint64_t const tb = f->technical_bins();
+    for (uint64_t c0 = 0; c0 < n; c0 += kChunk)
+    {
+        uint64_t const c = std::min(kChunk, n - c0);
+        uint64_t const m = c * h;
+        uint64_t const * vals = SYNTH ? gen.as<uint64_t>() : d_values + c0;
+        uint64_t const * bins = (SYNTH || !d_bins) ? nullptr : d_bins + c0;
+        k_occ_keys<SYNTH><<<grid_for(c, block), block, 0, s>>>(
+            f->store.as<uint64_t>(), f->bin_size, static_cast<uint32_t>(f->row_words), f->shift, h,
+            SYNTH ? nullptr : vals, bins, seed, vpb, c0, c, bin, f->bins, tb, keys.as<unsigned long long>(),
+            ids.as<unsigned long long>(), was_set.as<uint8_t>(), SYNTH ? gen.as<uint64_t>() : nullptr);
+        HG_CUDA(cudaGetLastError());
+        size_t bytes = tmp_bytes;
+        HG_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, bytes, keys.as<unsigned long long>(),
+                                                keys2.as<unsigned long long>(), ids.as<unsigned long long>(),
+                                                ids2.as<unsigned long long>(), static_cast<int>(m), 0, 64, s));
+        HG_CUDA(cudaMemsetAsync(newly.p, 0, c * 4, s));
+        k_occ_first<<<grid_for(m, block), block, 0, s>>>(keys2.as<unsigned long long>(), ids2.as<unsigned long long>(),
+                                                         m, h, was_set.as<uint8_t>(), newly.as<unsigned int>());
+        HG_CUDA(cudaGetLastError());
+        k_occ_count<SYNTH><<<grid_for(c, block), block, 0, s>>>(newly.as<unsigned int>(), bins, vpb, c0, c, bin,
+                                                               f->bins, f->occupancy.as<unsigned long long>());
+        HG_CUDA(cudaGetLastError());
+        k_emplace<<<grid_for(c, block), block, 0, s>>>(f->store.as<uint64_t>(), f->bin_size,
+                                                       static_cast<uint32_t>(f->row_words), f->shift, h, vals,
+                                                       SYNTH ? nullptr : bins, c, bin, f->bins, nullptr,
+                                                       f->flag.as<int>());
+        HG_CUDA(cudaGetLastError());
+    }
+    HG_CUDA(cudaStreamSynchronize(s)); // the scratch buffers are freed on return
+}
+
 void launch_emplace(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t const * d_bins, uint64_t n, uint64_t bin,
                     cudaStream_t s)
 {
     if (n == 0)
         return;
+    if (f->track_occupancy)
+    {
+        emplace_exact<false>(f, d_values, d_bins, n, bin, 0, 1, s);
+        return;
+    }
     unsigned const block = 256;
-    k_emplace<<<grid_for(n, block), block, 0, s>>>(
-        f->store.as<uint64_t>(), f->bin_size, static_cast<uint32_t>(f->row_words), f->shift,
-        static_cast<uint32_t>(f->hash_funs), d_values, d_bins, n, bin, f->bins,
-        f->track_occupancy ? f->occupancy.as<unsigned long long>() : nullptr, f->flag.as<int>());
+    k_emplace<<<grid_for(n, block), block, 0, s>>>(f->store.as<uint64_t>(), f->bin_size,
+                                                   static_cast<uint32_t>(f->row_words), f->shift,
+                                                   static_cast<uint32_t>(f->hash_funs), d_values, d_bins, n, bin,
+                                                   f->bins, nullptr, f->flag.as<int>());
     HG_CUDA(cudaGetLastError());
 }
 
@@ -641,6 +781,13 @@ extern "C"
                 uint64_t const n = n_bins * values_per_bin;
                 if (!n)
                     return;
+                if (f->track_occupancy)
+                {
+                    for (uint64_t b = first_bin; b < first_bin + n_bins; ++b)
+                        emplace_exact<true>(f, nullptr, nullptr, values_per_bin, b, seed, values_per_bin,
+                                            pick(f, stream));
+                    return;
+                }
                 unsigned const block = 256;
                 k_synth_emplace<<<grid_for(n, block), block, 0, pick(f, stream)>>>(
                     f->store.as<uint64_t>(), f->bin_size, static_cast<uint32_t>(f->row_words), f->shift,

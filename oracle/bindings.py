@@ -158,6 +158,12 @@ class OracleIBF:
             raise MemoryError
         self.bins = n
 
+    def occupancy(self) -> np.ndarray:
+        L = self.L
+        L.orc_ibf_occupancy.restype = ctypes.POINTER(u64)
+        L.orc_ibf_occupancy.argtypes = [vp]
+        return np.ctypeslib.as_array(L.orc_ibf_occupancy(self.h), shape=((self.bins + 63) // 64 * 64,)).copy()
+
     def data_ptr(self) -> tuple[int, int]:
         """(address, words) of the bit store, to fill it in place (e.g. from a device download)."""
         return ctypes.cast(self.L.orc_ibf_data(self.h), ctypes.c_void_p).value, self.L.orc_ibf_nwords(self.h)

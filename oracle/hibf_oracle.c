@@ -97,6 +97,12 @@ uint64_t orc_ibf_nwords(orc_ibf const * ibf)
     return ibf->nwords;
 }
 
+/* occupancy counters, technical_bins of them (IBF.cpp:123-139: counted in insertion order) */
+uint64_t const * orc_ibf_occupancy(orc_ibf const * ibf)
+{
+    return ibf->occupancy;
+}
+
 /* IBF.cpp:119-140: set bit hash_and_fit(value, seed_i) + bin for every hash function; with occupancy tracking,
  * count the bin once if any of the bits was newly set. */
 void orc_ibf_emplace(orc_ibf * ibf, uint64_t value, uint64_t bin)

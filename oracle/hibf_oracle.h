@@ -58,6 +58,7 @@ orc_ibf * orc_ibf_new(uint64_t bins, uint64_t bin_size, uint64_t hash_funs, int 
 void orc_ibf_delete(orc_ibf * ibf);
 uint64_t * orc_ibf_data(orc_ibf * ibf);
 uint64_t orc_ibf_nwords(orc_ibf const * ibf);
+uint64_t const * orc_ibf_occupancy(orc_ibf const * ibf);
 
 void orc_ibf_emplace(orc_ibf * ibf, uint64_t value, uint64_t bin);
 void orc_ibf_emplace_many(orc_ibf * ibf, uint64_t const * values, uint64_t const * bins, uint64_t n);

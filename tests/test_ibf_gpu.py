@@ -126,3 +126,24 @@ def test_ibf_empty_and_ragged_inputs(gpu_lib, oracle):
         ibf.emplace_many(v, n % 100)
         o.emplace(v, np.full(n, n % 100, np.uint64))
         np.testing.assert_array_equal(ibf.counting_agent().bulk_count(v), o.bulk_count(v, 2))
+
+
+@pytest.mark.parametrize("binned", [False, True])
+def test_occupancy_in_insertion_order(gpu_lib, oracle, binned):
+    """track_occupancy counts a value when one of its bits was not set yet, in insertion order (the reference's
+    sequential emplace); a small filter makes values of a bin share bits, and a 3e6-value call spans chunks."""
+    rng = np.random.default_rng(12)
+    bins, size = 70, 64
+    ibf = _ibf(bins, size, 3, True)
+    O = oracle.ibf(bins, size, 3, True)
+    for n in (5, 1000, 3_000_000):
+        v = rng.integers(0, 1 << 62, n, dtype=np.uint64)
+        if binned:
+            b = rng.integers(0, bins, n).astype(np.uint64)
+            ibf.emplace_many(v, b)
+            O.emplace(v, b)
+        else:
+            ibf.emplace_many(v, np.full(n, 7, np.uint64))
+            O.emplace(v, 7)
+        np.testing.assert_array_equal(ibf.occupancy, O.occupancy())
+    np.testing.assert_array_equal(ibf.words(), O.words())
