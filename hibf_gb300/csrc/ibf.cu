@@ -337,28 +337,41 @@ void launch_contains_h(row_params const & rp, uint32_t lpv_log2, uint64_t const 
 // bulk_count over n values into one counting vector: every warp counts a contiguous chunk into the block's shared
 // counters, the block adds them to 64-bit global totals.
 // Four blocks per SM (64 registers, some spilled for h >= 3) measured faster than two blocks without spills (1.53 vs
-// 2.16 ms for 2^24 values on 1,024 bins, h = 3): more warps keep more row loads in flight.
-template <int H>
+// 2.16 ms for 2^24 values on 1,024 bins, h = 3): more warps keep more row loads in flight.  PRIVATE: every warp
+// flushes into counters of its own (no shared-memory atomics), summed by the block at the end; otherwise the block's
+// warps share one set of counters.
+template <int H, bool PRIVATE>
 __global__ void __launch_bounds__(256, 4)
     k_bulk_count(row_params rp, uint32_t lpv_log2, uint64_t const * __restrict__ values, uint64_t n, uint64_t chunk,
                  unsigned long long * __restrict__ totals, uint32_t n_counters)
 {
     extern __shared__ uint32_t s_counts[];
-    for (uint32_t i = threadIdx.x; i < n_counters; i += blockDim.x)
+    int const nwarps_block = blockDim.x >> 5;
+    uint32_t const n_smem = PRIVATE ? n_counters * nwarps_block : n_counters;
+    for (uint32_t i = threadIdx.x; i < n_smem; i += blockDim.x)
         s_counts[i] = 0;
     __syncthreads();
     int const lane = threadIdx.x & 31;
+    uint32_t * counts = PRIVATE ? s_counts + (threadIdx.x >> 5) * n_counters : s_counts;
     uint64_t const warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
     uint64_t const nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
     for (uint64_t start = warp * chunk; start < n; start += nwarps * chunk)
     {
         uint64_t const len = (n - start) < chunk ? (n - start) : chunk;
-        warp_count_h<H, true>(rp, lpv_log2, values + start, len, s_counts, lane);
+        if (PRIVATE && rp.bin_words <= 32)
+            warp_count_lpv<H, false>(rp, lpv_log2, values + start, len, counts, lane);
+        else
+            warp_count_h<H, true>(rp, lpv_log2, values + start, len, counts, lane);
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < n_counters; i += blockDim.x)
-        if (s_counts[i])
-            atomicAdd(totals + i, static_cast<unsigned long long>(s_counts[i]));
+    {
+        uint64_t sum = 0;
+        for (int w = 0; w < (PRIVATE ? nwarps_block : 1); ++w)
+            sum += s_counts[w * n_counters + i];
+        if (sum)
+            atomicAdd(totals + i, static_cast<unsigned long long>(sum));
+    }
 }
 
 // Reduce exact totals modulo the counter width (the reference's counting_vector wraps).
@@ -388,20 +401,23 @@ __global__ void k_store_counts(unsigned long long const * __restrict__ totals, u
 using bulk_count_kernel_t = void (*)(row_params, uint32_t, uint64_t const *, uint64_t, uint64_t,
                                      unsigned long long *, uint32_t);
 
-bulk_count_kernel_t bulk_count_kernel(uint64_t h)
+// Warp-private counters when eight sets fit in 96 KiB of shared memory (up to 3,072 technical bins).
+constexpr uint32_t kPrivateCountersMax = 3072;
+
+bulk_count_kernel_t bulk_count_kernel(uint64_t h, bool priv)
 {
     switch (h)
     {
     case 1:
-        return k_bulk_count<1>;
+        return priv ? k_bulk_count<1, true> : k_bulk_count<1, false>;
     case 2:
-        return k_bulk_count<2>;
+        return priv ? k_bulk_count<2, true> : k_bulk_count<2, false>;
     case 3:
-        return k_bulk_count<3>;
+        return priv ? k_bulk_count<3, true> : k_bulk_count<3, false>;
     case 4:
-        return k_bulk_count<4>;
+        return priv ? k_bulk_count<4, true> : k_bulk_count<4, false>;
     default:
-        return k_bulk_count<5>;
+        return priv ? k_bulk_count<5, true> : k_bulk_count<5, false>;
     }
 }
 
@@ -563,12 +579,14 @@ void launch_count(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int w
         uint64_t const warps = (n + chunk - 1) / chunk;
         unsigned const grid = static_cast<unsigned>(
             std::max<uint64_t>(1, std::min<uint64_t>((warps + 7) / 8, static_cast<uint64_t>(sm_count()) * 4u)));
-        size_t const smem = nc * sizeof(uint32_t);
+        bool const priv = nc <= kPrivateCountersMax;
+        size_t const smem = nc * sizeof(uint32_t) * (priv ? block / 32 : 1);
         if (smem > 48 * 1024)
-            HG_CUDA(cudaFuncSetAttribute(bulk_count_kernel(f->hash_funs), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem)));
-        bulk_count_kernel(f->hash_funs)<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk,
-                                               f->totals.as<unsigned long long>(), static_cast<uint32_t>(nc));
+            HG_CUDA(cudaFuncSetAttribute(bulk_count_kernel(f->hash_funs, priv),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        bulk_count_kernel(f->hash_funs, priv)<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk,
+                                                                        f->totals.as<unsigned long long>(),
+                                                                        static_cast<uint32_t>(nc));
         HG_CUDA(cudaGetLastError());
     }
     k_store_counts<<<grid_for(f->bins, 256), 256, 0, s>>>(f->totals.as<unsigned long long>(), f->bins, width, d_out);
@@ -1191,9 +1209,9 @@ extern "C"
                         1, std::min<uint64_t>((warps + 7) / 8, static_cast<uint64_t>(sm_count()) * 4u)));
                     size_t const smem = nc * sizeof(uint32_t);
                     if (smem > 48 * 1024)
-                        HG_CUDA(cudaFuncSetAttribute(bulk_count_kernel(f->hash_funs), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        HG_CUDA(cudaFuncSetAttribute(bulk_count_kernel(f->hash_funs, false), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      static_cast<int>(smem)));
-                    bulk_count_kernel(f->hash_funs)<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk, totals,
+                    bulk_count_kernel(f->hash_funs, false)<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk, totals,
                                                            static_cast<uint32_t>(nc));
                     HG_CUDA(cudaGetLastError());
                 }
