@@ -1,0 +1,526 @@
+// hibf_gb300.hpp -- C++20 facade over the C ABI (hibf_gb300.h) with the shape of seqan::hibf's public classes, so a
+// seqan::hibf user switches by namespace: strong types bin_count / bin_size / hash_function_count / bin_index
+// (include/hibf/interleaved_bloom_filter.hpp:51-81), interleaved_bloom_filter with containment / counting /
+// membership agents (interleaved_bloom_filter.hpp:225-391, 552-770), config with input_fn and insert_iterator
+// (include/hibf/config.hpp:75-413, include/hibf/misc/insert_iterator.hpp:24-111), and
+// hierarchical_interleaved_bloom_filter built from a layout with its membership and counting agents
+// (include/hibf/hierarchical_interleaved_bloom_filter.hpp:197-247, 322-566).
+//
+// Errors follow the reference: construction logic errors throw std::logic_error, invalid arguments
+// std::invalid_argument, other failures std::runtime_error.  Agents own their result buffers, valid until their next
+// call, as in the reference.  Every computation runs on the device; nothing here falls back to the CPU.
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <exception>
+#include <functional>
+#include <limits>
+#include <ranges>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "hibf_gb300.h"
+
+namespace hibf_gb300
+{
+
+inline void check(int status)
+{
+    if (status == HIBF_GPU_OK)
+        return;
+    std::string const msg = hibf_gpu_last_error();
+    if (status == HIBF_GPU_ERR_LOGIC)
+        throw std::logic_error{msg};
+    if (status == HIBF_GPU_ERR_INVALID_ARG)
+        throw std::invalid_argument{msg};
+    throw std::runtime_error{msg};
+}
+
+struct bin_count
+{
+    uint64_t value;
+};
+struct bin_size
+{
+    uint64_t value;
+};
+struct hash_function_count
+{
+    uint64_t value;
+};
+struct bin_index
+{
+    uint64_t value;
+};
+
+namespace detail
+{
+template <std::ranges::input_range values_t>
+std::vector<uint64_t> to_vector(values_t && values)
+{
+    std::vector<uint64_t> v;
+    if constexpr (std::ranges::sized_range<values_t>)
+        v.reserve(std::ranges::size(values));
+    for (auto && x : values)
+        v.push_back(static_cast<uint64_t>(x));
+    return v;
+}
+
+template <typename T>
+constexpr int width_of()
+{
+    static_assert(std::is_integral_v<T> && std::is_unsigned_v<T> && sizeof(T) <= 8, "unsigned counter types");
+    return static_cast<int>(sizeof(T));
+}
+} // namespace detail
+
+// The result of bulk_contains: one bit per bin (the reference's bit_vector, read-only here).
+class bit_vector
+{
+public:
+    bit_vector() = default;
+    bit_vector(std::vector<uint64_t> words, uint64_t bits) : words_{std::move(words)}, bits_{bits}
+    {}
+    bool operator[](uint64_t i) const
+    {
+        return (words_[i / 64] >> (i % 64)) & 1u;
+    }
+    uint64_t size() const
+    {
+        return bits_;
+    }
+    std::vector<uint64_t> const & data() const
+    {
+        return words_;
+    }
+    bool operator==(std::vector<bool> const & other) const
+    {
+        if (other.size() != bits_)
+            return false;
+        for (uint64_t i = 0; i < bits_; ++i)
+            if ((*this)[i] != other[i])
+                return false;
+        return true;
+    }
+
+private:
+    std::vector<uint64_t> words_;
+    uint64_t bits_{};
+};
+
+class interleaved_bloom_filter
+{
+public:
+    interleaved_bloom_filter(hibf_gb300::bin_count bins, hibf_gb300::bin_size size,
+                             hibf_gb300::hash_function_count funs = {2},
+                             bool track_occupancy = false)
+    {
+        check(hibf_gpu_ibf_create(bins.value, size.value, funs.value, track_occupancy ? 1 : 0, &f_));
+    }
+    explicit interleaved_bloom_filter(hibf_gpu_ibf * adopted) : f_{adopted}
+    {}
+    interleaved_bloom_filter(interleaved_bloom_filter const &) = delete;
+    interleaved_bloom_filter & operator=(interleaved_bloom_filter const &) = delete;
+    interleaved_bloom_filter(interleaved_bloom_filter && o) noexcept : f_{std::exchange(o.f_, nullptr)}
+    {}
+    ~interleaved_bloom_filter()
+    {
+        if (f_)
+            hibf_gpu_ibf_destroy(f_);
+    }
+
+    void emplace(uint64_t value, bin_index bin)
+    {
+        check(hibf_gpu_ibf_emplace(f_, &value, 1, bin.value));
+    }
+    // Many values into one bin in one device call (the insert_iterator loop of the reference, batched).
+    template <std::ranges::input_range values_t>
+    void emplace(values_t && values, bin_index bin)
+    {
+        auto const v = detail::to_vector(values);
+        check(hibf_gpu_ibf_emplace(f_, v.data(), v.size(), bin.value));
+    }
+    void clear(bin_index bin)
+    {
+        check(hibf_gpu_ibf_clear(f_, bin.value));
+    }
+    template <std::ranges::forward_range bins_t>
+        requires std::same_as<std::ranges::range_value_t<bins_t>, bin_index>
+    void clear(bins_t && bins)
+    {
+        std::vector<uint64_t> b;
+        for (bin_index x : bins)
+            b.push_back(x.value);
+        check(hibf_gpu_ibf_clear_range(f_, b.data(), b.size()));
+    }
+    bool try_increase_bin_number_to(hibf_gb300::bin_count new_bins)
+    {
+        int ok = 0;
+        check(hibf_gpu_ibf_try_increase_bin_number_to(f_, new_bins.value, &ok));
+        return ok != 0;
+    }
+    void increase_bin_number_to(hibf_gb300::bin_count new_bins)
+    {
+        check(hibf_gpu_ibf_increase_bin_number_to(f_, new_bins.value));
+    }
+
+    uint64_t bin_count() const
+    {
+        return info()[0];
+    }
+    uint64_t bin_size() const
+    {
+        return info()[1];
+    }
+    uint64_t hash_function_count() const
+    {
+        return info()[2];
+    }
+    uint64_t bit_size() const
+    {
+        return info()[3];
+    }
+
+    class containment_agent_type
+    {
+    public:
+        explicit containment_agent_type(interleaved_bloom_filter const & ibf) : ibf_{&ibf}
+        {}
+        bit_vector const & bulk_contains(uint64_t value) & noexcept
+        {
+            uint64_t const words = (ibf_->bin_count() + 63) / 64;
+            std::vector<uint64_t> w(words);
+            if (hibf_gpu_ibf_bulk_contains(ibf_->f_, &value, 1, w.data()) != HIBF_GPU_OK)
+                std::terminate(); // queries are noexcept in the reference
+            result_ = bit_vector{std::move(w), ibf_->bin_count()};
+            return result_;
+        }
+
+    private:
+        interleaved_bloom_filter const * ibf_;
+        bit_vector result_;
+    };
+
+    template <typename value_t = uint16_t>
+    class counting_agent_type
+    {
+    public:
+        explicit counting_agent_type(interleaved_bloom_filter const & ibf) : ibf_{&ibf}
+        {}
+        template <std::ranges::input_range values_t>
+        std::vector<value_t> const & bulk_count(values_t && values) & noexcept
+        {
+            auto const v = detail::to_vector(values);
+            result_.assign(ibf_->bin_count(), 0);
+            if (hibf_gpu_ibf_bulk_count(ibf_->f_, v.data(), v.size(), detail::width_of<value_t>(), result_.data()) !=
+                HIBF_GPU_OK)
+                std::terminate();
+            return result_;
+        }
+
+    private:
+        interleaved_bloom_filter const * ibf_;
+        std::vector<value_t> result_;
+    };
+
+    class membership_agent_type
+    {
+    public:
+        explicit membership_agent_type(interleaved_bloom_filter const & ibf) : ibf_{&ibf}
+        {}
+        template <std::ranges::input_range values_t>
+        std::vector<uint64_t> const & membership_for(values_t && values, uint16_t threshold) & noexcept
+        {
+            auto const v = detail::to_vector(values);
+            result_.resize(ibf_->bin_count());
+            uint64_t n = 0;
+            if (hibf_gpu_ibf_membership_for(ibf_->f_, v.data(), v.size(), threshold, result_.data(), &n) !=
+                HIBF_GPU_OK)
+                std::terminate();
+            result_.resize(n);
+            return result_;
+        }
+
+    private:
+        interleaved_bloom_filter const * ibf_;
+        std::vector<uint64_t> result_;
+    };
+
+    containment_agent_type containment_agent() const
+    {
+        return containment_agent_type{*this};
+    }
+    template <typename value_t = uint16_t>
+    counting_agent_type<value_t> counting_agent() const
+    {
+        return counting_agent_type<value_t>{*this};
+    }
+    membership_agent_type membership_agent() const
+    {
+        return membership_agent_type{*this};
+    }
+
+    void save(std::string const & path) const
+    {
+        check(hibf_gpu_ibf_save(f_, path.c_str()));
+    }
+    static interleaved_bloom_filter load(std::string const & path)
+    {
+        hibf_gpu_ibf * f = nullptr;
+        check(hibf_gpu_ibf_load(path.c_str(), &f));
+        return interleaved_bloom_filter{f};
+    }
+    hibf_gpu_ibf * handle() const
+    {
+        return f_;
+    }
+
+private:
+    std::vector<uint64_t> info() const
+    {
+        std::vector<uint64_t> out(5);
+        check(hibf_gpu_ibf_info(f_, out.data()));
+        return out;
+    }
+    hibf_gpu_ibf * f_{};
+};
+
+// What config::input_fn receives: `it = value` inserts one value (insert_iterator.hpp:24-111).
+class insert_iterator
+{
+public:
+    explicit insert_iterator(hibf_gpu_sink * sink) : sink_{sink}
+    {}
+    insert_iterator & operator=(uint64_t value)
+    {
+        check(hibf_gpu_sink_push(sink_, &value, 1));
+        return *this;
+    }
+    insert_iterator & operator*()
+    {
+        return *this;
+    }
+    insert_iterator & operator++()
+    {
+        return *this;
+    }
+    insert_iterator & operator++(int)
+    {
+        return *this;
+    }
+    // Many values in one call.
+    void push(std::vector<uint64_t> const & values)
+    {
+        check(hibf_gpu_sink_push(sink_, values.data(), values.size()));
+    }
+
+private:
+    hibf_gpu_sink * sink_;
+};
+
+// The fields of seqan::hibf::config the device build uses (config.hpp:75-413).
+struct config
+{
+    std::function<void(size_t const, insert_iterator &&)> input_fn;
+    size_t number_of_user_bins{};
+    size_t number_of_hash_functions{2};
+    double maximum_fpr{0.05};
+    double relaxed_fpr{0.3};
+    size_t threads{1};
+};
+
+class hierarchical_interleaved_bloom_filter
+{
+public:
+    // hierarchical_interleaved_bloom_filter(config&, layout const&) with the reference's layout file text.
+    hierarchical_interleaved_bloom_filter(config & configuration, std::string const & layout_text)
+    {
+        if (!configuration.input_fn)
+            throw std::invalid_argument{"[HIBF CONFIG ERROR] You did not set the required config::input_fn."};
+        hibf_gpu_build_config c{configuration.number_of_user_bins, configuration.number_of_hash_functions,
+                                configuration.maximum_fpr, configuration.relaxed_fpr, configuration.threads, 0};
+        check(hibf_gpu_hibf_build(&c, layout_text.c_str(), &trampoline, &configuration, &h_));
+        load_tables();
+    }
+    explicit hierarchical_interleaved_bloom_filter(hibf_gpu_hibf * adopted) : h_{adopted}
+    {
+        load_tables();
+    }
+    hierarchical_interleaved_bloom_filter(hierarchical_interleaved_bloom_filter const &) = delete;
+    hierarchical_interleaved_bloom_filter & operator=(hierarchical_interleaved_bloom_filter const &) = delete;
+    hierarchical_interleaved_bloom_filter(hierarchical_interleaved_bloom_filter && o) noexcept :
+        number_of_user_bins{o.number_of_user_bins},
+        h_{std::exchange(o.h_, nullptr)},
+        rank_{std::move(o.rank_)}
+    {}
+    ~hierarchical_interleaved_bloom_filter()
+    {
+        if (h_)
+            hibf_gpu_hibf_destroy(h_);
+    }
+
+    size_t number_of_user_bins{};
+
+    class membership_agent_type
+    {
+    public:
+        explicit membership_agent_type(hierarchical_interleaved_bloom_filter const & h) : h_{&h}
+        {
+            check(hibf_gpu_agent_create(h.h_, &a_));
+        }
+        membership_agent_type(membership_agent_type && o) noexcept :
+            h_{o.h_},
+            a_{std::exchange(o.a_, nullptr)},
+            result_{std::move(o.result_)}
+        {}
+        ~membership_agent_type()
+        {
+            if (a_)
+                hibf_gpu_agent_destroy(a_);
+        }
+        // User bins whose summed counts reach the threshold, in the reference's traversal order
+        // (hierarchical_interleaved_bloom_filter.hpp:322-355, 424-439).
+        template <std::ranges::input_range values_t>
+        std::vector<uint64_t> const & membership_for(values_t && values, uint16_t threshold) & noexcept
+        {
+            auto const v = detail::to_vector(values);
+            uint64_t const * ids = nullptr;
+            uint64_t n = 0;
+            if (hibf_gpu_agent_membership_for(a_, v.data(), v.size(), threshold, &ids, &n) != HIBF_GPU_OK)
+                std::terminate();
+            result_.assign(ids, ids + n);
+            std::ranges::sort(result_, [&](uint64_t x, uint64_t y) { return h_->rank_[x] < h_->rank_[y]; });
+            return result_;
+        }
+        // hierarchical_interleaved_bloom_filter.hpp:380-383
+        void sort_results()
+        {
+            std::ranges::sort(result_);
+        }
+
+    private:
+        hierarchical_interleaved_bloom_filter const * h_;
+        hibf_gpu_agent * a_{};
+        std::vector<uint64_t> result_;
+    };
+
+    template <typename value_t = uint16_t>
+    class counting_agent_type
+    {
+    public:
+        explicit counting_agent_type(hierarchical_interleaved_bloom_filter const & h) : h_{&h}
+        {
+            check(hibf_gpu_agent_create(h.h_, &a_));
+        }
+        counting_agent_type(counting_agent_type && o) noexcept :
+            h_{o.h_},
+            a_{std::exchange(o.a_, nullptr)},
+            result_{std::move(o.result_)}
+        {}
+        ~counting_agent_type()
+        {
+            if (a_)
+                hibf_gpu_agent_destroy(a_);
+        }
+        // hierarchical_interleaved_bloom_filter.hpp:463-566: per user bin the summed count if it reaches t, else 0.
+        template <std::ranges::input_range values_t>
+        std::vector<value_t> const & bulk_count(values_t && values, size_t threshold) & noexcept
+        {
+            auto const v = detail::to_vector(values);
+            void const * counts = nullptr;
+            if (hibf_gpu_agent_bulk_count(a_, v.data(), v.size(), threshold, detail::width_of<value_t>(), &counts) !=
+                HIBF_GPU_OK)
+                std::terminate();
+            auto const * c = static_cast<value_t const *>(counts);
+            result_.assign(c, c + h_->number_of_user_bins);
+            return result_;
+        }
+
+    private:
+        hierarchical_interleaved_bloom_filter const * h_;
+        hibf_gpu_agent * a_{};
+        std::vector<value_t> result_;
+    };
+
+    membership_agent_type membership_agent() const
+    {
+        return membership_agent_type{*this};
+    }
+    template <typename value_t = uint16_t>
+    counting_agent_type<value_t> counting_agent() const
+    {
+        return counting_agent_type<value_t>{*this};
+    }
+
+    void save(std::string const & path) const
+    {
+        check(hibf_gpu_hibf_save(h_, path.c_str()));
+    }
+    static hierarchical_interleaved_bloom_filter load(std::string const & path)
+    {
+        hibf_gpu_hibf * h = nullptr;
+        check(hibf_gpu_hibf_load(path.c_str(), &h));
+        return hierarchical_interleaved_bloom_filter{h};
+    }
+    hibf_gpu_hibf * handle() const
+    {
+        return h_;
+    }
+
+private:
+    static void trampoline(void * user, uint64_t user_bin, hibf_gpu_sink * sink)
+    {
+        auto & c = *static_cast<config *>(user);
+        c.input_fn(static_cast<size_t>(user_bin), insert_iterator{sink});
+    }
+
+    // Position of every user bin in the order membership_for reports it: bins scanned in order, merged bins
+    // descended in place (a user bin occurs in one place).
+    void load_tables()
+    {
+        uint64_t info[4];
+        check(hibf_gpu_hibf_info(h_, info));
+        number_of_user_bins = info[0];
+        uint64_t const n_ibfs = info[1];
+        std::vector<uint64_t> bins(n_ibfs);
+        check(hibf_gpu_hibf_get_tables(h_, bins.data(), nullptr, nullptr, nullptr, nullptr));
+        std::vector<uint64_t> off(n_ibfs + 1, 0);
+        for (uint64_t k = 0; k < n_ibfs; ++k)
+            off[k + 1] = off[k] + bins[k];
+        std::vector<uint64_t> next(off[n_ibfs]), ub(off[n_ibfs]);
+        check(hibf_gpu_hibf_get_tables(h_, nullptr, nullptr, nullptr, next.data(), ub.data()));
+        rank_.assign(number_of_user_bins, std::numeric_limits<uint64_t>::max());
+        uint64_t r = 0;
+        std::vector<std::pair<uint64_t, uint64_t>> stack{{0, 0}};
+        uint64_t steps = 0;
+        while (!stack.empty() && steps++ <= 4 * (off[n_ibfs] + 1))
+        {
+            auto [k, b] = stack.back();
+            stack.pop_back();
+            if (b >= bins[k])
+                continue;
+            stack.emplace_back(k, b + 1);
+            uint64_t const i = off[k] + b;
+            uint64_t const u = ub[i];
+            if (u == HIBF_GPU_BIN_MERGED)
+            {
+                if (next[i] != k)
+                    stack.emplace_back(next[i], 0);
+            }
+            else if (u != HIBF_GPU_BIN_DELETED && (b + 1 == bins[k] || ub[i + 1] != u) && u < number_of_user_bins &&
+                     rank_[u] == std::numeric_limits<uint64_t>::max())
+            {
+                rank_[u] = r++;
+            }
+        }
+    }
+
+    hibf_gpu_hibf * h_{};
+    std::vector<uint64_t> rank_;
+};
+
+} // namespace hibf_gb300

@@ -1,0 +1,216 @@
+// The C++ facade (include/hibf_gb300.hpp) exercised like the reference's own unit tests
+// (test/unit/hibf/interleaved_bloom_filter_test.cpp, test/unit/hibf/hierarchical_interleaved_bloom_filter_test.cpp,
+// test/snippet/readme.cpp), with the expectations those tests state.  Usage: test_facade <dir with layout files>.
+// Exits 0 when every check holds.
+#include <cstdio>
+#include <fstream>
+#include <numeric>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "hibf_gb300.hpp"
+
+namespace h = hibf_gb300;
+
+static int failures = 0;
+
+#define CHECK(cond)                                                                                                     \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        if (!(cond))                                                                                                   \
+        {                                                                                                              \
+            std::fprintf(stderr, "%s:%d: CHECK failed: %s\n", __FILE__, __LINE__, #cond);                              \
+            ++failures;                                                                                                \
+        }                                                                                                              \
+    } while (0)
+
+template <typename F, typename E>
+bool throws(F && f)
+{
+    try
+    {
+        f();
+    }
+    catch (E const &)
+    {
+        return true;
+    }
+    catch (...)
+    {
+        return false;
+    }
+    return false;
+}
+
+static std::string read_file(std::string const & path)
+{
+    std::ifstream in{path};
+    std::stringstream ss;
+    ss << in.rdbuf();
+    return ss.str();
+}
+
+static std::vector<uint64_t> iota(uint64_t n)
+{
+    std::vector<uint64_t> v(n);
+    std::iota(v.begin(), v.end(), 0u);
+    return v;
+}
+
+// interleaved_bloom_filter_test.cpp: construction
+static void ibf_construction()
+{
+    CHECK((throws<void (*)(), std::logic_error>(+[] { h::interleaved_bloom_filter{h::bin_count{64}, h::bin_size{0}}; })));
+    CHECK((throws<void (*)(), std::logic_error>(+[] { h::interleaved_bloom_filter{h::bin_count{0}, h::bin_size{32}}; })));
+    h::interleaved_bloom_filter ibf{h::bin_count{64}, h::bin_size{1024}};
+    CHECK(ibf.bin_count() == 64 && ibf.bin_size() == 1024 && ibf.hash_function_count() == 2);
+}
+
+// interleaved_bloom_filter_test.cpp: bulk_contains on an empty filter, then after emplace
+static void ibf_contains()
+{
+    h::interleaved_bloom_filter ibf{h::bin_count{64}, h::bin_size{1024}};
+    auto agent = ibf.containment_agent();
+    for (uint64_t v = 0; v < 64; ++v)
+        CHECK(agent.bulk_contains(v) == std::vector<bool>(64, false));
+    for (uint64_t b = 0; b < 64; ++b)
+        ibf.emplace(b, h::bin_index{b});
+    for (uint64_t v = 0; v < 64; ++v)
+        CHECK(agent.bulk_contains(v)[v]);
+}
+
+// interleaved_bloom_filter_test.cpp: counting (every bin holds 0..127, so every count is 128)
+static void ibf_counting()
+{
+    h::interleaved_bloom_filter ibf{h::bin_count{128}, h::bin_size{1024}, h::hash_function_count{2}};
+    for (uint64_t b = 0; b < 128; ++b)
+        ibf.emplace(iota(128), h::bin_index{b});
+    auto agent = ibf.counting_agent<uint64_t>();
+    CHECK(agent.bulk_count(iota(128)) == std::vector<uint64_t>(128, 128));
+    auto agent8 = ibf.counting_agent<uint8_t>(); // 128 * 3 wraps modulo 256
+    std::vector<uint64_t> thrice = iota(128);
+    thrice.insert(thrice.end(), thrice.begin(), thrice.end());
+    thrice.insert(thrice.end(), thrice.begin(), thrice.begin() + 128);
+    CHECK(agent8.bulk_count(thrice) == std::vector<uint8_t>(128, static_cast<uint8_t>(384 % 256)));
+}
+
+// interleaved_bloom_filter_test.cpp: clear and clear(range)
+static void ibf_clear()
+{
+    h::interleaved_bloom_filter ibf{h::bin_count{64}, h::bin_size{1024}};
+    for (uint64_t b = 0; b < 64; ++b)
+        ibf.emplace(iota(50), h::bin_index{b});
+    ibf.clear(h::bin_index{17});
+    std::vector<h::bin_index> r{h::bin_index{3}, h::bin_index{40}};
+    ibf.clear(r);
+    auto agent = ibf.counting_agent<uint16_t>(); // agents are lvalues, as in the reference (rvalue calls deleted)
+    auto const & counts = agent.bulk_count(iota(50));
+    for (uint64_t b = 0; b < 64; ++b)
+        CHECK(counts[b] == ((b == 17 || b == 3 || b == 40) ? 0 : 50));
+}
+
+// interleaved_bloom_filter_test.cpp: membership_for (user bins {1..10}, {1..5}; query 1..5, threshold 2)
+static void ibf_membership()
+{
+    h::interleaved_bloom_filter ibf{h::bin_count{2}, h::bin_size{1024}};
+    for (uint64_t v = 1; v <= 10; ++v)
+        ibf.emplace(v, h::bin_index{0});
+    for (uint64_t v = 1; v <= 5; ++v)
+        ibf.emplace(v, h::bin_index{1});
+    auto agent = ibf.membership_agent();
+    std::vector<uint64_t> const query{1, 2, 3, 4, 5};
+    CHECK(agent.membership_for(query, 2) == (std::vector<uint64_t>{0, 1}));
+    CHECK(agent.membership_for(std::vector<uint64_t>{6, 7, 8}, 2) == (std::vector<uint64_t>{0}));
+}
+
+// interleaved_bloom_filter_test.cpp: increase_bin_number_to keeps the content
+static void ibf_increase()
+{
+    h::interleaved_bloom_filter ibf{h::bin_count{73}, h::bin_size{1024}};
+    ibf.emplace(iota(30), h::bin_index{72});
+    CHECK(ibf.try_increase_bin_number_to(h::bin_count{128}));
+    CHECK(ibf.bin_count() == 128);
+    CHECK(!ibf.try_increase_bin_number_to(h::bin_count{129}) || ibf.bin_count() == 129);
+    auto agent = ibf.counting_agent<uint16_t>();
+    auto const & counts = agent.bulk_count(iota(30));
+    CHECK(counts[72] == 30);
+    CHECK((throws<void (*)(), std::invalid_argument>(+[] {
+        h::interleaved_bloom_filter f{h::bin_count{64}, h::bin_size{8}};
+        f.increase_bin_number_to(h::bin_count{32});
+    })));
+}
+
+// hierarchical_interleaved_bloom_filter_test.cpp small example and test/snippet/readme.cpp, with the layouts the
+// reference computes for them.
+static void hibf_small(std::string const & dir)
+{
+    std::vector<std::vector<uint64_t>> hashes{{1, 2, 3, 4, 5, 6, 7, 8, 9, 10}, {1, 2, 3, 4, 5}};
+    h::config config{.input_fn =
+                         [&](size_t const num, h::insert_iterator && it)
+                     {
+                         for (auto const hash : hashes[num])
+                             it = hash;
+                     },
+                     .number_of_user_bins = 2};
+    h::hierarchical_interleaved_bloom_filter hibf{config, read_file(dir + "/layout_snippet.txt")};
+    auto agent = hibf.membership_agent();
+    std::vector<uint64_t> const query{1, 2, 3, 4, 5};
+    auto & result = agent.membership_for(query, 2);
+    agent.sort_results();
+    CHECK(result == (std::vector<uint64_t>{0, 1}));
+    CHECK(hibf.number_of_user_bins == 2);
+    // copy_agents: counting {5, 5} at threshold 1 and {0, 0} at threshold 6
+    auto counter = hibf.counting_agent<uint16_t>();
+    CHECK(counter.bulk_count(query, 1) == (std::vector<uint16_t>{5, 5}));
+    CHECK(counter.bulk_count(query, 6) == (std::vector<uint16_t>{0, 0}));
+}
+
+static void hibf_readme(std::string const & dir)
+{
+    std::vector<std::vector<uint64_t>> hashes{{1, 2, 3, 4, 5, 6, 7, 8, 9, 10}, {1, 2, 3, 4, 5}, {3, 9, 11}};
+    h::config config{.input_fn =
+                         [&](size_t const num, h::insert_iterator && it)
+                     {
+                         for (auto const hash : hashes[num])
+                             it = hash;
+                     },
+                     .number_of_user_bins = 3};
+    h::hierarchical_interleaved_bloom_filter hibf{config, read_file(dir + "/layout_readme.txt")};
+    auto agent = hibf.membership_agent();
+    // test/snippet/readme.out: "2 0" unsorted, then "0 1" for 0..14 at threshold 5 after sort_results()
+    CHECK(agent.membership_for(std::vector<uint64_t>{3, 9, 12, 14}, 2) == (std::vector<uint64_t>{2, 0}));
+    auto & r = agent.membership_for(iota(15), 5);
+    agent.sort_results();
+    CHECK(r == (std::vector<uint64_t>{0, 1}));
+    // save and load keep the answers
+    hibf.save(dir + "/readme.hibf");
+    auto loaded = h::hierarchical_interleaved_bloom_filter::load(dir + "/readme.hibf");
+    auto agent2 = loaded.membership_agent();
+    CHECK(agent2.membership_for(std::vector<uint64_t>{3, 9, 12, 14}, 2) == (std::vector<uint64_t>{2, 0}));
+}
+
+int main(int argc, char ** argv)
+{
+    if (argc < 2)
+    {
+        std::fprintf(stderr, "usage: test_facade <dir with layout_snippet.txt and layout_readme.txt>\n");
+        return 2;
+    }
+    std::string const dir = argv[1];
+    ibf_construction();
+    ibf_contains();
+    ibf_counting();
+    ibf_clear();
+    ibf_membership();
+    ibf_increase();
+    hibf_small(dir);
+    hibf_readme(dir);
+    if (failures)
+    {
+        std::fprintf(stderr, "%d check(s) failed\n", failures);
+        return 1;
+    }
+    std::printf("all facade checks passed\n");
+    return 0;
+}
