@@ -404,6 +404,34 @@ def run_ours(args, wl, rank, world, local):
                        np.array_equal(plain_ids, res_ids[:int(res_offs[P])]))
     plain_vps = float(qo[P]) / plain_s
 
+    # counting_agent<uint16>::bulk_count over the same batch: the same traversal with the counts kept (no decided
+    # exit: every count must be exact); its user bins must be the membership lists
+    ca = hibf.counting_agent(2)
+    ca.tuning = agent.tuning
+    ca.reserve(nq, nv, nq * 8 + 65536, nq * 8 + 65536)
+    ca.set_stream(stream.cuda_stream)
+    ca.capture_batch_device(d_v.data_ptr(), d_qo.data_ptr(), nq, d_thr.data_ptr(), mode=N.QUERY_COUNT, width=2)
+    for _ in range(3):
+        ca.replay()
+    stream.synchronize()
+    ca.status()
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    count_steps = max(1, min(args.steps, 5))
+    c0.record(stream)
+    for _ in range(count_steps):
+        ca.replay()
+    c1.record(stream)
+    c1.synchronize()
+    ca.status()
+    count_ms = c0.elapsed_time(c1) / count_steps
+    c_offs, c_ids, c_cnt = ca.fetch_results(nq, mode=N.QUERY_COUNT, width=2)
+    c_thr_ok = bool(np.all(c_cnt.astype(np.uint64) >= np.repeat(thr, np.diff(c_offs).astype(np.int64))))
+    count = {"values_per_s": world * nv / (count_ms / 1e3), "ms_per_step": count_ms, "steps": count_steps,
+             "form": "one persistent launch per batch, CUDA-graph replay, uint16 counts",
+             "user_bins_equal_membership": bool(np.array_equal(c_offs, res_offs) and np.array_equal(c_ids, res_ids)),
+             "counts_at_least_threshold": c_thr_ok}
+    del ca
+
     # end to end through the C ABI host call: pinned host inputs -> H2D -> batch -> D2H results
     h_v = torch.empty(max(nv, 1), dtype=torch.int64, pin_memory=True)
     h_v.copy_(d_v)
@@ -445,7 +473,7 @@ def run_ours(args, wl, rank, world, local):
     out = None
     if rank == 0:
         hbm, peak_kind = peaks()
-        bytes_per_visit = wl.h * 1 * 32  # h rows of ceil(64/256) = 1 sector each (all IBFs have 64 bins)
+        bytes_per_visit = wl.h * 1 * 32  # h rows of ceil(tb/256) = 1 sector each (every IBF has tb <= tmax <= 256)
         # algorithmic bytes: h sectors for every (value, IBF) visit the reference's traversal implies; the kernel
         # reads fewer (a task stops once its outcome is fixed), reported beside as achieved_executed
         achieved = visits * bytes_per_visit / (kernel_ms / 1e3) / 1e9
@@ -487,6 +515,7 @@ def run_ours(args, wl, rank, world, local):
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
                     "call": "hibf_gpu_agent_query_batch (host buffers, pinned)"},
             "plain": {"values_per_s": plain_vps, "queries": P, "form": "one launch per query"},
+            "bulk_count": count,
             "batched_vs_plain": value / world / plain_vps,
             "gpu_launches": launches_per_step * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
