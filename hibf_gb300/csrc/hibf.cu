@@ -7,6 +7,8 @@
 // The query kernel itself (semantics, work queue, tuning variants) is in query.cuh; this file holds the stores, the
 // result compaction passes, agents, the autotuner and their C-ABI entry points.
 
+#include <cuda.h> // driver types of cuStreamWriteValue32, reached through the runtime's entry-point query
+
 #include <algorithm>
 #include <cstring>
 #include <memory>
@@ -344,6 +346,15 @@ struct hibf_gpu_agent
     dbuf ctrl, stats, tasks, rec_q, rec_ub, rec_cnt, qcount, cursor, roff, bsum, out_ids, out_cnt, out_cntw, large;
     // host-call staging
     dbuf in_values, in_qoff, in_thr;
+    // streamed host batches: value chunks copied on copy_stream while the kernel answers the arrived ones
+    cudaStream_t copy_stream{};
+    cudaEvent_t ev_ready{}, ev_copied{};
+    dbuf arrived, arrive_first;
+    hbuf h_arrive_first;
+    unsigned int const * arrive{};  // set for the duration of one streamed host batch
+    uint32_t arrive_chunks{};
+    uint64_t arrive_limit_ns{};
+    uint32_t last_chunks{}; // chunks of the last host batch (0: not streamed)
     hbuf h_roff, h_ids, h_cnt, h_ctrl, h_stats;
     std::vector<uint64_t> single_ids;
     std::vector<uint8_t> dense;
@@ -413,6 +424,10 @@ query_params base_params(hibf_gpu_agent * a, uint64_t const * d_values, uint64_t
     p.ee_min = a->tune.early_exit_min;
     p.order = a->order;
     p.qwork = a->qwork;
+    p.arrived = a->arrive;
+    p.arrive_first = a->arrive ? a->arrive_first.as<uint64_t>() : nullptr;
+    p.arrive_chunks = a->arrive_chunks;
+    p.arrive_limit_ns = a->arrive_limit_ns;
     return p;
 }
 
@@ -581,7 +596,58 @@ void check_mode(int mode, int width, uint64_t const * thr, uint64_t nq)
         }
 }
 
-// Host-pointer batch with automatic growth on overflow.  Results land in the agent's pinned host buffers.
+using stream_write_fn = CUresult (*)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+
+// cuStreamWriteValue32 (a write executed by the stream itself, after the stream's earlier work and behind a memory
+// fence), or null when the driver does not offer it.
+stream_write_fn stream_write_value32()
+{
+    static stream_write_fn const fn = []
+    {
+        void * f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+        {
+            cudaGetLastError();
+            return static_cast<stream_write_fn>(nullptr);
+        }
+        return reinterpret_cast<stream_write_fn>(f);
+    }();
+    return fn;
+}
+
+constexpr uint64_t kStreamMinBytes = 64ull << 20;    // smaller host batches are copied whole before the launch
+constexpr uint64_t kStreamChunkBytes = 16ull << 20;  // smallest target chunk: up to 64 chunks of at least this
+constexpr uint32_t kStreamMaxChunks = 64;
+
+// Chunk boundaries of a streamed host batch: query indices q_0 = 0 < q_1 < ... < q_K = nq, each q_k (0 < k < K) a
+// query whose first value starts a 32-byte sector (qoff[q_k] % 4 == 0), so that no sector of the device copy holds
+// values of two chunks.  Fewer than two chunks: the batch is not streamed.
+std::vector<uint64_t> stream_chunks(uint64_t const * qoff, uint64_t nq)
+{
+    uint64_t const nv = qoff[nq];
+    uint64_t want = std::min<uint64_t>(kStreamMaxChunks, std::max<uint64_t>(2, nv * 8 / kStreamChunkBytes));
+    want = std::min(want, nq);
+    std::vector<uint64_t> qb{0};
+    for (uint64_t k = 1; k < want; ++k)
+    {
+        uint64_t q = std::max(qb.back() + 1, k * nq / want);
+        uint64_t const stop = std::min(nq, q + nq / want);
+        while (q < stop && (qoff[q] & 3u) != 0)
+            ++q;
+        if (q < stop && qoff[q] > qoff[qb.back()])
+            qb.push_back(q);
+    }
+    qb.push_back(nq);
+    return qb;
+}
+
+// Host-pointer batch with automatic growth on overflow.  Results land in the agent's pinned host buffers.  Large
+// batches are streamed: the offsets and thresholds go first, then the values in chunks on a second stream, each
+// followed by a write of the chunk counter that the kernel's root claims wait for, so the kernel answers the
+// queries of arrived chunks while later chunks are still being copied.
 void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t const * qoff, uint64_t nq,
                 uint64_t const * thr, int width, bool plain)
 {
@@ -593,13 +659,75 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
     a->in_values.ensure(nv * 8);
     a->in_qoff.ensure((nq + 1) * 8);
     a->in_thr.ensure(std::max<uint64_t>(nq, 1) * 8);
-    if (nv)
-        HG_CUDA(cudaMemcpyAsync(a->in_values.p, values, nv * 8, cudaMemcpyHostToDevice, a->stream));
+    std::vector<uint64_t> qb;
+    stream_write_fn const write_value = stream_write_value32();
+    if (!plain && !a->order && nv * 8 >= kStreamMinBytes && write_value)
+        qb = stream_chunks(qoff, nq);
+    bool const streamed = qb.size() > 2;
+    a->last_chunks = streamed ? static_cast<uint32_t>(qb.size() - 1) : 0u;
+    uint64_t tasks = std::max<uint64_t>(a->cap_tasks, nq * 4 + 1024);
+    uint64_t results = std::max<uint64_t>(a->cap_results, nq * 4 + 1024);
+    ensure_capacity(a, std::max<uint64_t>(nq, 1), tasks, results); // allocations synchronise: before any copy
     HG_CUDA(cudaMemcpyAsync(a->in_qoff.p, qoff, (nq + 1) * 8, cudaMemcpyHostToDevice, a->stream));
     if (nq)
         HG_CUDA(cudaMemcpyAsync(a->in_thr.p, thr, nq * 8, cudaMemcpyHostToDevice, a->stream));
-    uint64_t tasks = std::max<uint64_t>(a->cap_tasks, nq * 4 + 1024);
-    uint64_t results = std::max<uint64_t>(a->cap_results, nq * 4 + 1024);
+    struct arrive_reset
+    {
+        hibf_gpu_agent * a;
+        ~arrive_reset()
+        {
+            if (a->arrive)
+                cudaStreamSynchronize(a->copy_stream); // an error left copies in flight: finish them first
+            a->arrive = nullptr;
+        }
+    } const reset{a};
+    if (streamed)
+    {
+        if (!a->copy_stream)
+        {
+            HG_CUDA(cudaStreamCreateWithFlags(&a->copy_stream, cudaStreamNonBlocking));
+            HG_CUDA(cudaEventCreateWithFlags(&a->ev_ready, cudaEventDisableTiming));
+            HG_CUDA(cudaEventCreateWithFlags(&a->ev_copied, cudaEventDisableTiming));
+        }
+        uint32_t const chunks = static_cast<uint32_t>(qb.size() - 1);
+        a->arrived.ensure(4);
+        a->arrive_first.ensure(qb.size() * 8);
+        a->h_arrive_first.ensure(qb.size() * 8);
+        std::memcpy(a->h_arrive_first.p, qb.data(), qb.size() * 8);
+        HG_CUDA(cudaMemcpyAsync(a->arrive_first.p, a->h_arrive_first.p, qb.size() * 8, cudaMemcpyHostToDevice,
+                                a->stream));
+        HG_CUDA(cudaMemsetAsync(a->arrived.p, 0, 4, a->stream));
+        HG_CUDA(cudaEventRecord(a->ev_ready, a->stream));
+        HG_CUDA(cudaStreamWaitEvent(a->copy_stream, a->ev_ready, 0));
+        try
+        {
+            for (uint32_t k = 0; k < chunks; ++k)
+            {
+                uint64_t const v0 = qoff[qb[k]], v1 = qoff[qb[k + 1]];
+                if (v1 > v0)
+                    HG_CUDA(cudaMemcpyAsync(a->in_values.as<uint64_t>() + v0, values + v0, (v1 - v0) * 8,
+                                            cudaMemcpyHostToDevice, a->copy_stream));
+                CUresult const r = write_value(reinterpret_cast<CUstream>(a->copy_stream),
+                                               reinterpret_cast<CUdeviceptr>(a->arrived.p), k + 1u,
+                                               CU_STREAM_WRITE_VALUE_DEFAULT);
+                if (r != CUDA_SUCCESS)
+                    fail(HIBF_GPU_ERR_CUDA, "cuStreamWriteValue32 failed (" + std::to_string(static_cast<int>(r)) + ")");
+            }
+            HG_CUDA(cudaEventRecord(a->ev_copied, a->copy_stream));
+        }
+        catch (...)
+        {
+            cudaStreamSynchronize(a->copy_stream);
+            throw;
+        }
+        a->arrive = a->arrived.as<unsigned int>();
+        a->arrive_chunks = chunks;
+        a->arrive_limit_ns = 10ull * 1000 * 1000 * 1000 + nv * 8 / 2; // 10 s + the copy at 2 GB/s
+    }
+    else if (nv)
+    {
+        HG_CUDA(cudaMemcpyAsync(a->in_values.p, values, nv * 8, cudaMemcpyHostToDevice, a->stream));
+    }
     for (int attempt = 0;; ++attempt)
     {
         ensure_capacity(a, std::max<uint64_t>(nq, 1), tasks, results);
@@ -609,6 +737,8 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
         else
             launch_batch(a, mode, a->in_values.as<uint64_t>(), a->in_qoff.as<uint64_t>(), a->in_thr.as<uint64_t>(),
                          nq, width);
+        if (streamed && attempt == 0)
+            HG_CUDA(cudaStreamWaitEvent(a->stream, a->ev_copied, 0)); // later work on the stream follows the copies
         int const st = read_status(a);
         if (st == HIBF_GPU_OK)
             break;
@@ -1517,6 +1647,13 @@ extern "C"
                     cudaGraphExecDestroy(a->graph);
                 cudaEventDestroy(a->ev_k0);
                 cudaEventDestroy(a->ev_k1);
+                if (a->copy_stream)
+                {
+                    cudaStreamSynchronize(a->copy_stream);
+                    cudaEventDestroy(a->ev_ready);
+                    cudaEventDestroy(a->ev_copied);
+                    cudaStreamDestroy(a->copy_stream);
+                }
                 cudaStreamDestroy(a->own);
                 delete a;
             });
@@ -1757,6 +1894,17 @@ extern "C"
                     fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
                 HG_CUDA(cudaEventSynchronize(a->ev_k1));
                 HG_CUDA(cudaEventElapsedTime(ms, a->ev_k0, a->ev_k1));
+            });
+    }
+
+    int hibf_gpu_agent_input_chunks(hibf_gpu_agent const * a, uint32_t * chunks)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !chunks)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *chunks = a->last_chunks;
             });
     }
 

@@ -106,6 +106,12 @@ struct query_params
     unsigned long long * qwork;
     // membership mode: a task may also stop once every segment's report/descend decision is final (segment_state)
     uint32_t decide;
+    // streamed inputs (host batches): the values of queries [arrive_first[k], arrive_first[k + 1]) are on the device
+    // once *arrived > k (a stream write behind chunk k's copy); null = all inputs are resident
+    unsigned int const * arrived;
+    uint64_t const * arrive_first;
+    uint32_t arrive_chunks;
+    uint64_t arrive_limit_ns;
 };
 
 using query_kernel_t = void (*)(query_params);
@@ -138,6 +144,42 @@ __device__ inline unsigned long long wait_for_task(query_params const & p, unsig
             return kEmpty;
         }
         __nanosleep(256);
+    }
+}
+
+// Streamed inputs: waits (bounded) until the chunk holding query q's values has been copied.  The copy stream
+// writes the chunk counter behind the chunk's copy with a memory fence, and chunks start on 32-byte sector
+// boundaries, so no sector holding values of an unarrived chunk was cached before.  False (and E_TIMEOUT) when the
+// limit expires.
+__device__ inline bool wait_arrival(query_params const & p, uint64_t q)
+{
+    uint32_t lo = 0, hi = p.arrive_chunks - 1u; // the last chunk k with arrive_first[k] <= q
+    while (lo < hi)
+    {
+        uint32_t const mid = (lo + hi + 1u) >> 1;
+        if (p.arrive_first[mid] <= q)
+            lo = mid;
+        else
+            hi = mid - 1u;
+    }
+    unsigned int const need = lo + 1u;
+    volatile unsigned int const * f = p.arrived;
+    uint64_t start = 0;
+    for (uint32_t it = 0;; ++it)
+    {
+        if (*f >= need)
+        {
+            __threadfence();
+            return true;
+        }
+        if (it == 0)
+            start = globaltimer_ns();
+        else if ((it & 15u) == 0 && globaltimer_ns() - start > p.arrive_limit_ns)
+        {
+            atomicOr(p.ctrl + C_ERROR, E_TIMEOUT);
+            return false;
+        }
+        __nanosleep(512);
     }
 }
 
@@ -455,6 +497,14 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
                 }
                 continue;
             }
+            if (p.arrived)
+            {
+                int ok = 1;
+                if (lane == 0)
+                    ok = wait_arrival(p, q);
+                if (!__shfl_sync(kFullMask, ok, 0))
+                    break;
+            }
             task = make_task(q, 0u, 0u);
         }
         else
@@ -524,7 +574,7 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query_blk(query_
                 }
                 else
                 {
-                    task = make_task(q, 0u, 0u);
+                    task = !p.arrived || wait_arrival(p, q) ? make_task(q, 0u, 0u) : kEmpty;
                 }
             }
             else

@@ -243,6 +243,12 @@ class _agent_base:
         N.call("hibf_gpu_agent_kernel_ms", self._a, ctypes.byref(ms))
         return float(ms.value)
 
+    def input_chunks(self) -> int:
+        """Chunks in which the last host batch streamed its values (0: copied whole before the launch)."""
+        n = ctypes.c_uint32(0)
+        N.call("hibf_gpu_agent_input_chunks", self._a, ctypes.byref(n))
+        return int(n.value)
+
     def set_order(self, d_order: int | None, n_queries: int = 0) -> None:
         """Claim order of root tasks for later batches of exactly n_queries queries (device uint32 permutation;
         None: query order)."""

@@ -262,7 +262,9 @@ int hibf_gpu_agent_bulk_count(hibf_gpu_agent * a, uint64_t const * values, uint6
  * HIBF_GPU_QUERY_COUNT the size_t thresholds of bulk_count with counters of `width` bytes (thresholds > 0).
  * Results are CSR per query, ascending user-bin ids, and for COUNT the count of each listed user bin (the
  * dense counting vector's non-zero entries; every other entry is 0).  Host form: *result_offsets (n_queries+1),
- * *result_ids and *result_counts (width bytes each; NULL for MEMBERSHIP) point into agent-owned host memory. */
+ * *result_ids and *result_counts (width bytes each; NULL for MEMBERSHIP) point into agent-owned host memory.
+ * A host batch of at least 64 MiB of values is streamed: its values are copied in chunks on a second stream while
+ * the kernel answers the queries of chunks already copied (results are the same either way). */
 #define HIBF_GPU_QUERY_MEMBERSHIP 1
 #define HIBF_GPU_QUERY_COUNT 2
 int hibf_gpu_agent_query_batch(hibf_gpu_agent * a, int mode, uint64_t const * values,
@@ -300,6 +302,8 @@ int hibf_gpu_agent_capture_batch_d(hibf_gpu_agent * a, int mode, uint64_t const 
 int hibf_gpu_agent_replay(hibf_gpu_agent * a);
 /* Device time of the persistent query kernel of the agent's last batch (CUDA events on the agent's stream). */
 int hibf_gpu_agent_kernel_ms(hibf_gpu_agent * a, float * ms);
+/* Number of chunks in which the agent's last host batch streamed its values (0: copied whole before the launch). */
+int hibf_gpu_agent_input_chunks(hibf_gpu_agent const * a, uint32_t * chunks);
 /* Number of (query, IBF) tasks the last batch processed and the number of query values they covered
  * (sum over tasks of the query length): the work the roofline is computed from. */
 int hibf_gpu_agent_last_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits);

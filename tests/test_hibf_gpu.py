@@ -281,3 +281,90 @@ def test_early_decisions_on_every_case(gpu_lib, name):
     for i in range(offs.size - 1):
         dense[i, ids[offs[i]:offs[i + 1]].astype(np.int64)] = cnts[offs[i]:offs[i + 1]]
     np.testing.assert_array_equal(dense, d[f"count{w}"])
+
+
+def _long_batch(d, n_queries, rng, odd=True):
+    """n_queries queries cut from the golden queries' values, lengths in [301, 799] (odd lengths when `odd`)."""
+    qs = [q for q in G.queries(d) if q.size]
+    lens = rng.integers(150, 400, n_queries) * 2 + (1 if odd else 0)
+    parts = []
+    for i, n in enumerate(lens):
+        q = qs[i % len(qs)]
+        parts.append(np.resize(q, int(n)))
+    qo = np.zeros(n_queries + 1, np.uint64)
+    np.cumsum(lens, out=qo[1:])
+    thr = np.floor(lens * rng.uniform(0.3, 0.8, n_queries)).astype(np.uint64)
+    return np.concatenate(parts).astype(np.uint64), qo, thr
+
+
+def test_streamed_host_batch_equals_resident_batch(gpu_lib, oracle):
+    """A host batch of at least 64 MiB of values is copied in chunks while the kernel answers the chunks already
+    copied.  Its results equal the device-resident batch's and the oracle's, for odd query lengths (chunks start only
+    where a query's first value starts a 32-byte sector) and for counts as well as membership."""
+    import torch
+
+    d = G.hibf_case("synth600")
+    H = _gpu_hibf(d)
+    rng = np.random.default_rng(11)
+    vals, qo, thr = _long_batch(d, 24000, rng)
+    assert vals.size * 8 >= 64 << 20
+    a = H.membership_agent()
+    offs, ids, _ = a.query_batch(vals, qo, thr)
+    assert a.input_chunks() > 2
+    dv = torch.from_numpy(vals.view(np.int64)).cuda()
+    dq = torch.from_numpy(qo.view(np.int64)).cuda()
+    dt = torch.from_numpy(thr.view(np.int64)).cuda()
+    r = H.membership_agent()
+    nq = qo.size - 1
+    r.reserve(nq, vals.size, nq * 8 + 65536, nq * 16 + 65536)
+    r.query_batch_device(dv.data_ptr(), dq.data_ptr(), nq, dt.data_ptr())
+    offs_r, ids_r, _ = r.fetch_results(nq)
+    np.testing.assert_array_equal(offs, offs_r)
+    np.testing.assert_array_equal(ids, ids_r)
+    O = oracle.hibf(G.tables(d))
+    o_off, o_ids = O.membership_batch(vals, qo, thr, threads=8)
+    np.testing.assert_array_equal(offs, o_off)
+    np.testing.assert_array_equal(ids, o_ids)
+    c = H.counting_agent(2)
+    cthr = np.maximum(thr, 1)
+    c_offs, c_ids, c_cnt = c.query_batch(vals, qo, cthr, mode=N.QUERY_COUNT, width=2)
+    assert c.input_chunks() > 2
+    c.reserve(nq, vals.size, nq * 8 + 65536, nq * 16 + 65536)
+    c.query_batch_device(dv.data_ptr(), dq.data_ptr(), qo.size - 1,
+                         torch.from_numpy(cthr.view(np.int64)).cuda().data_ptr(), mode=N.QUERY_COUNT, width=2)
+    r_offs, r_ids, r_cnt = c.fetch_results(qo.size - 1, mode=N.QUERY_COUNT, width=2)
+    np.testing.assert_array_equal(c_offs, r_offs)
+    np.testing.assert_array_equal(c_ids, r_ids)
+    np.testing.assert_array_equal(c_cnt, r_cnt)
+
+
+def test_host_batch_without_sector_aligned_query_starts_is_copied_whole(gpu_lib):
+    """Query offsets that never start a 32-byte sector after the first query: no chunk boundary exists, the batch is
+    copied whole before the launch, with the same results."""
+    import torch
+
+    d = G.hibf_case("synth600")
+    H = _gpu_hibf(d)
+    rng = np.random.default_rng(12)
+    vals, qo, thr = _long_batch(d, 18000, rng, odd=False)
+    lens = np.diff(qo)
+    lens = lens - lens % 4  # every length a multiple of 4 ...
+    lens[0] = 1             # ... after a first query of one value: every later query starts at 1 mod 4
+    qo = np.zeros(lens.size + 1, np.uint64)
+    np.cumsum(lens, out=qo[1:])
+    vals = vals[:int(qo[-1])]
+    thr = np.minimum(thr, lens)
+    assert vals.size * 8 >= 64 << 20 and np.all(qo[1:] % 4 == 1)
+    a = H.membership_agent()
+    offs, ids, _ = a.query_batch(vals, qo, thr)
+    assert a.input_chunks() == 0
+    dv = torch.from_numpy(vals.view(np.int64)).cuda()
+    dq = torch.from_numpy(qo.view(np.int64)).cuda()
+    dt = torch.from_numpy(thr.view(np.int64)).cuda()
+    r = H.membership_agent()
+    nq = qo.size - 1
+    r.reserve(nq, vals.size, nq * 8 + 65536, nq * 16 + 65536)
+    r.query_batch_device(dv.data_ptr(), dq.data_ptr(), nq, dt.data_ptr())
+    offs_r, ids_r, _ = r.fetch_results(nq)
+    np.testing.assert_array_equal(offs, offs_r)
+    np.testing.assert_array_equal(ids, ids_r)
