@@ -45,6 +45,7 @@ enum : int
     C_NREC = 3,
     C_ERROR = 4,
     C_NLARGE = 5,
+    C_CHILD = 6, // streamed inputs: claims of child slots (roots and children are then claimed separately)
     C_WORDS = 8
 };
 // error bits
@@ -147,11 +148,10 @@ __device__ inline unsigned long long wait_for_task(query_params const & p, unsig
     }
 }
 
-// Streamed inputs: waits (bounded) until the chunk holding query q's values has been copied.  The copy stream
-// writes the chunk counter behind the chunk's copy with a memory fence, and chunks start on 32-byte sector
-// boundaries, so no sector holding values of an unarrived chunk was cached before.  False (and E_TIMEOUT) when the
-// limit expires.
-__device__ inline bool wait_arrival(query_params const & p, uint64_t q)
+// Streamed inputs: the chunk counter value at which query q's values are on the device (its chunk index + 1).  The
+// copy stream writes the counter behind each chunk's copy with a memory fence, and chunks start on 32-byte sector
+// boundaries, so no sector holding values of an unarrived chunk was cached before.
+__device__ inline unsigned int arrival_needed(query_params const & p, uint64_t q)
 {
     uint32_t lo = 0, hi = p.arrive_chunks - 1u; // the last chunk k with arrive_first[k] <= q
     while (lo < hi)
@@ -162,7 +162,27 @@ __device__ inline bool wait_arrival(query_params const & p, uint64_t q)
         else
             hi = mid - 1u;
     }
-    unsigned int const need = lo + 1u;
+    return lo + 1u;
+}
+
+// Streamed inputs: claims the oldest queued child slot (lane 0) when at least `reserve` reserved slots are unclaimed,
+// else kEmpty.  With reserve = the grid's warp count no claim can pass the reserved slots (fewer warps than that claim
+// at the same time), so a claimed slot is written soon by its producer; a plain atomicAdd does the claim, since
+// compare-and-swap retries of thousands of warps on one word stall its L2 slice.
+__device__ inline unsigned long long try_claim_child(query_params const & p, unsigned long long reserve)
+{
+    volatile unsigned long long * c = p.ctrl;
+    unsigned long long const h = c[C_CHILD];
+    if (c[C_TAIL] < h + reserve)
+        return kEmpty;
+    unsigned long long const s = atomicAdd(p.ctrl + C_CHILD, 1ull);
+    return s < p.task_cap ? s : kEmpty;
+}
+
+// Waits (bounded) until query q's chunk has arrived.  False (and E_TIMEOUT) when the limit expires.
+__device__ inline bool wait_arrival(query_params const & p, uint64_t q)
+{
+    unsigned int const need = arrival_needed(p, q);
     volatile unsigned int const * f = p.arrived;
     uint64_t start = 0;
     for (uint32_t it = 0;; ++it)
@@ -477,47 +497,141 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
         __syncthreads();
     }
     unsigned long long n_tasks = 0, n_visits = 0, n_executed = 0;
+    // Streamed inputs: roots are claimed through C_HEAD and children through C_CHILD, children first whenever more
+    // than a grid's worth of warps of them are queued.  The copy paces the roots, so children run as they appear
+    // instead of piling up behind the last chunk; a warp whose claimed root (`held`) has not arrived yet runs queued
+    // children meanwhile.
+    unsigned long long const reserve = static_cast<unsigned long long>(gridDim.x) * (blockDim.x >> 5);
+    unsigned long long held = kEmpty;
+    unsigned int held_need = 0;
+    uint64_t held_since = 0;
+    // idle polls of a held root back off from 1 to 16 us and read the shared queue words only every 4th time: thousands
+    // of warps polling one L2 line would stall that L2 slice, and with it every warp's row reads that map there
+    unsigned int backoff = 0, polls = 0;
     for (;;)
     {
-        unsigned long long idx = 0;
-        if (lane == 0)
-            idx = atomicAdd(p.ctrl + C_HEAD, 1ull);
-        idx = __shfl_sync(kFullMask, idx, 0);
-        unsigned long long task;
-        if (idx < p.n_queries)
+        unsigned long long task = kEmpty;
+        if (held != kEmpty)
         {
-            uint64_t const q = p.order ? p.order[idx] : idx;
-            if (q >= p.n_queries)
+            int action = 0; // 0 wait, 1 run the held root, 2 run a stolen child, 3 give up
+            unsigned long long slot = 0;
+            if (lane == 0)
             {
-                if (lane == 0)
+                if (*reinterpret_cast<volatile unsigned int const *>(p.arrived) >= held_need)
                 {
-                    atomicOr(p.ctrl + C_ERROR, E_ORDER);
                     __threadfence();
-                    atomicAdd(p.ctrl + C_PENDING, ~0ull);
+                    action = 1;
                 }
-                continue;
+                else
+                {
+                    slot = (polls++ & 3u) == 0 ? try_claim_child(p, reserve) : kEmpty;
+                    if (slot != kEmpty)
+                    {
+                        action = 2;
+                    }
+                    else if (held_since == 0)
+                    {
+                        held_since = globaltimer_ns();
+                    }
+                    else if (globaltimer_ns() - held_since > p.arrive_limit_ns)
+                    {
+                        atomicOr(p.ctrl + C_ERROR, E_TIMEOUT);
+                        action = 3;
+                    }
+                    if (action == 0)
+                    {
+                        backoff = backoff ? min(2u * backoff, 16384u) : 1024u;
+                        __nanosleep(backoff);
+                    }
+                    else
+                    {
+                        backoff = 0;
+                        polls = 0;
+                    }
+                }
             }
-            if (p.arrived)
+            action = __shfl_sync(kFullMask, action, 0);
+            if (action == 3)
+                break;
+            if (action == 0)
+                continue;
+            if (action == 1)
             {
-                int ok = 1;
+                task = held;
+                held = kEmpty;
+            }
+            else
+            {
                 if (lane == 0)
-                    ok = wait_arrival(p, q);
-                if (!__shfl_sync(kFullMask, ok, 0))
+                    task = wait_for_task(p, slot); // a reserved slot: its writer is storing it
+                task = __shfl_sync(kFullMask, task, 0);
+                if (task == kEmpty)
                     break;
             }
-            task = make_task(q, 0u, 0u);
         }
         else
         {
-            unsigned long long const slot = idx - p.n_queries;
-            if (slot >= p.task_cap)
-                break;
-            task = 0;
+            if (p.arrived)
+            {
+                unsigned long long slot = kEmpty;
+                if (lane == 0)
+                    slot = try_claim_child(p, reserve);
+                slot = __shfl_sync(kFullMask, slot, 0);
+                if (slot != kEmpty)
+                {
+                    if (lane == 0)
+                        task = wait_for_task(p, slot);
+                    task = __shfl_sync(kFullMask, task, 0);
+                    if (task == kEmpty)
+                        break;
+                }
+            }
+        }
+        if (task == kEmpty && held == kEmpty)
+        {
+            unsigned long long idx = 0;
             if (lane == 0)
-                task = wait_for_task(p, slot);
-            task = __shfl_sync(kFullMask, task, 0);
-            if (task == kEmpty)
-                break;
+                idx = atomicAdd(p.ctrl + C_HEAD, 1ull);
+            idx = __shfl_sync(kFullMask, idx, 0);
+            if (idx < p.n_queries)
+            {
+                uint64_t const q = p.order ? p.order[idx] : idx;
+                if (q >= p.n_queries)
+                {
+                    if (lane == 0)
+                    {
+                        atomicOr(p.ctrl + C_ERROR, E_ORDER);
+                        __threadfence();
+                        atomicAdd(p.ctrl + C_PENDING, ~0ull);
+                    }
+                    continue;
+                }
+                if (p.arrived)
+                {
+                    held = make_task(q, 0u, 0u);
+                    held_need = arrival_needed(p, q);
+                    held_since = 0;
+                    continue;
+                }
+                task = make_task(q, 0u, 0u);
+            }
+            else
+            {
+                unsigned long long slot = idx - p.n_queries;
+                if (p.arrived)
+                {
+                    if (lane == 0)
+                        slot = atomicAdd(p.ctrl + C_CHILD, 1ull);
+                    slot = __shfl_sync(kFullMask, slot, 0);
+                }
+                if (slot >= p.task_cap)
+                    break;
+                if (lane == 0)
+                    task = wait_for_task(p, slot);
+                task = __shfl_sync(kFullMask, task, 0);
+                if (task == kEmpty)
+                    break;
+            }
         }
         process_task<H, V>(p, task, counts, lane, n_tasks, n_visits, n_executed);
     }
