@@ -34,9 +34,9 @@ METRIC = "HIBF query values/s on 1 GB300, batched vs plain (bit-exact); p99 serv
 WORKLOAD_DESC = {
     "hibf8192": "HIBF 8,192 user bins (log-normal median 2e5 sigma 1.5, [1e3,5e7]), h=2, fpr 0.05, tmax 64; "
                 "1e6 queries len U[20,2000] (70% from 1-3 UBs, 2% noise), t=ceil(0.7 len); membership_for",
-    "hibf65536": "HIBF 65,536 user bins (log-normal median 1e5 sigma 2.0, [500,2e8]), h=3, fpr 0.02, tmax 256; "
-                 "1e6 of 1e7 queries per step, len U[50,5000] (70% from 1-3 UBs, 2% noise), t=ceil(0.6 len); "
-                 "membership_for",
+    "hibf65536": "HIBF 65,536 user bins (log-normal median 1e5 sigma 2.0, [500,2e8]), h=3, fpr 0.02, tmax 256, "
+                 "layout from the reference's DP with summed sizes; 1e6 of 1e7 queries per step, len U[50,5000] "
+                 "(70% from 1-3 UBs, 2% noise), t=ceil(0.6 len); membership_for",
     "hibf64": "HIBF 64 user bins (log-uniform [1e3,1e5]), h=2, fpr 0.05, tmax 64; 10,000 queries of 250 values "
               "(half from one UB), t=125; membership_for",
 }

@@ -3,8 +3,10 @@
 hibf64     64 user bins, sizes log-uniform in [1e3, 1e5], h=2, fpr 0.05, tmax 64; 10,000 queries of 250 values, half
            from one user bin, half uniform; threshold 125.
 hibf65536  65,536 user bins, sizes log-normal (median 1e5, sigma 2.0) clipped to [500, 2e8] (4.8e10 values), h=3,
-           fpr 0.02, tmax 256, layout from the reference's DP; 10,000,000 queries of length U[50, 5000], composition
-           as above; threshold ceil(0.6 * length).
+           fpr 0.02, tmax 256, layout from the reference's DP with summed user bin sizes (disable_estimate_union,
+           which also disables rearrangement; the union-estimating DP needs ~2e9 HyperLogLog union estimates at
+           this many user bins); 10,000,000 queries of length U[50, 5000], composition as above; threshold
+           ceil(0.6 * length).
 hibf8192   8,192 user bins, sizes log-normal (median 2e5, sigma 1.5) clipped to [1e3, 5e7], h=2, fpr 0.05, tmax 64,
            layout from the reference's DP over HyperLogLog sketches (sketch_bits 12); 1,000,000 queries of length
            U[20, 2000], 70% drawn from 1-3 user bins with 2% noise, 30% uniform; threshold ceil(0.7 * length).
@@ -83,6 +85,6 @@ HIBF8192 = workload("hibf8192", 8192, S.SIZES_LOG_NORMAL, 200000.0, 1.5, 1000, 5
                     S.query_spec(1, S.QUERIES_MIXED, 20, 2000, 70, 2, 7, 10, 8192), "c3_layout.txt")
 
 HIBF65536 = workload("hibf65536", 65536, S.SIZES_LOG_NORMAL, 100000.0, 2.0, 500, 200000000, 3, 0.02, 256, 10000000,
-                     S.query_spec(1, S.QUERIES_MIXED, 50, 5000, 70, 2, 6, 10, 65536), "c4_layout.txt")
+                     S.query_spec(1, S.QUERIES_MIXED, 50, 5000, 70, 2, 6, 10, 65536), "c4_layout_sum.txt")
 
 WORKLOADS = {w.name: w for w in (HIBF64, HIBF8192, HIBF65536)}

@@ -346,7 +346,8 @@ def make_c4_layout(R: Reference, estimate_union=True):
     """The 65,536-user-bin layout (h=3, fpr 0.02, tmax 256): reference DP over HyperLogLog sketches of the
     synthetic user bins, streamed from the generator (about 4.8e10 values; no value is materialised).  With
     estimate_union=False the DP sums user bin sizes instead of estimating unions (config::disable_estimate_union,
-    which also disables rearrangement): minutes instead of hours of CPU."""
+    which also disables rearrangement): about an hour of one core.  The union-estimating DP merges sketches for
+    every (column, earlier column) pair, ~2e9 union estimates at this size, and does not finish in hours."""
     sizes = S.user_bin_sizes(1, 65536, S.SIZES_LOG_NORMAL, 100000.0, 2.0, 500, 200000000)
     offs = S.offsets_of(sizes)
     cfg = ref_cfg(65536, h=3, fpr=0.02, tmax=256, threads=8, sketch_bits=12,
@@ -378,7 +379,7 @@ def main(argv):
         make_c1(R)
     if "c3" in which:
         make_c3_layout(R)
-    if "c4" in which:  # not in the default set: hours of CPU
+    if "c4" in which:  # not in the default set: far more than hours of CPU
         make_c4_layout(R)
     if "c4sum" in which:  # not in the default set
         make_c4_layout(R, estimate_union=False)
