@@ -7,8 +7,6 @@
 // The query kernel itself (semantics, work queue, tuning variants) is in query.cuh; this file holds the stores, the
 // result compaction passes, agents, the autotuner and their C-ABI entry points.
 
-#include <cuda.h> // driver types of cuStreamWriteValue32, reached through the runtime's entry-point query
-
 #include <algorithm>
 #include <cstring>
 #include <memory>
@@ -350,7 +348,7 @@ struct hibf_gpu_agent
     cudaStream_t copy_stream{};
     cudaEvent_t ev_ready{}, ev_copied{};
     dbuf arrived, arrive_first;
-    hbuf h_arrive_first;
+    hbuf h_arrive_first, h_arrive_counts;
     unsigned int const * arrive{};  // set for the duration of one streamed host batch
     uint32_t arrive_chunks{};
     uint64_t arrive_limit_ns{};
@@ -596,28 +594,6 @@ void check_mode(int mode, int width, uint64_t const * thr, uint64_t nq)
         }
 }
 
-using stream_write_fn = CUresult (*)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
-
-// cuStreamWriteValue32 (a write executed by the stream itself, after the stream's earlier work and behind a memory
-// fence), or null when the driver does not offer it.
-stream_write_fn stream_write_value32()
-{
-    static stream_write_fn const fn = []
-    {
-        void * f = nullptr;
-        cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &f, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-        {
-            cudaGetLastError();
-            return static_cast<stream_write_fn>(nullptr);
-        }
-        return reinterpret_cast<stream_write_fn>(f);
-    }();
-    return fn;
-}
-
 constexpr uint64_t kStreamMinBytes = 64ull << 20;    // smaller host batches are copied whole before the launch
 constexpr uint64_t kStreamChunkBytes = 16ull << 20;  // smallest target chunk: up to 64 chunks of at least this
 constexpr uint32_t kStreamMaxChunks = 64;
@@ -646,8 +622,8 @@ std::vector<uint64_t> stream_chunks(uint64_t const * qoff, uint64_t nq)
 
 // Host-pointer batch with automatic growth on overflow.  Results land in the agent's pinned host buffers.  Large
 // batches are streamed: the offsets and thresholds go first, then the values in chunks on a second stream, each
-// followed by a write of the chunk counter that the kernel's root claims wait for, so the kernel answers the
-// queries of arrived chunks while later chunks are still being copied.
+// followed by a copy of the chunk counter (its replicas) that the kernel's root claims wait for, so the kernel
+// answers the queries of arrived chunks while later chunks are still being copied.
 void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t const * qoff, uint64_t nq,
                 uint64_t const * thr, int width, bool plain)
 {
@@ -660,8 +636,7 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
     a->in_qoff.ensure((nq + 1) * 8);
     a->in_thr.ensure(std::max<uint64_t>(nq, 1) * 8);
     std::vector<uint64_t> qb;
-    stream_write_fn const write_value = stream_write_value32();
-    if (!plain && !a->order && nv * 8 >= kStreamMinBytes && write_value)
+    if (!plain && !a->order && nv * 8 >= kStreamMinBytes)
         qb = stream_chunks(qoff, nq);
     bool const streamed = qb.size() > 2;
     a->last_chunks = streamed ? static_cast<uint32_t>(qb.size() - 1) : 0u;
@@ -690,13 +665,20 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
             HG_CUDA(cudaEventCreateWithFlags(&a->ev_copied, cudaEventDisableTiming));
         }
         uint32_t const chunks = static_cast<uint32_t>(qb.size() - 1);
-        a->arrived.ensure(4);
+        size_t const counter_bytes = kArrivalReplicas * kArrivalStride * 4;
+        a->arrived.ensure(counter_bytes);
         a->arrive_first.ensure(qb.size() * 8);
         a->h_arrive_first.ensure(qb.size() * 8);
+        a->h_arrive_counts.ensure(chunks * counter_bytes); // chunk k's source holds k + 1 in every replica
         std::memcpy(a->h_arrive_first.p, qb.data(), qb.size() * 8);
+        unsigned int * counts = a->h_arrive_counts.as<unsigned int>();
+        std::memset(counts, 0, chunks * counter_bytes);
+        for (uint32_t k = 0; k < chunks; ++k)
+            for (uint32_t r = 0; r < kArrivalReplicas; ++r)
+                counts[(static_cast<size_t>(k) * kArrivalReplicas + r) * kArrivalStride] = k + 1u;
         HG_CUDA(cudaMemcpyAsync(a->arrive_first.p, a->h_arrive_first.p, qb.size() * 8, cudaMemcpyHostToDevice,
                                 a->stream));
-        HG_CUDA(cudaMemsetAsync(a->arrived.p, 0, 4, a->stream));
+        HG_CUDA(cudaMemsetAsync(a->arrived.p, 0, counter_bytes, a->stream));
         HG_CUDA(cudaEventRecord(a->ev_ready, a->stream));
         HG_CUDA(cudaStreamWaitEvent(a->copy_stream, a->ev_ready, 0));
         try
@@ -707,11 +689,8 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
                 if (v1 > v0)
                     HG_CUDA(cudaMemcpyAsync(a->in_values.as<uint64_t>() + v0, values + v0, (v1 - v0) * 8,
                                             cudaMemcpyHostToDevice, a->copy_stream));
-                CUresult const r = write_value(reinterpret_cast<CUstream>(a->copy_stream),
-                                               reinterpret_cast<CUdeviceptr>(a->arrived.p), k + 1u,
-                                               CU_STREAM_WRITE_VALUE_DEFAULT);
-                if (r != CUDA_SUCCESS)
-                    fail(HIBF_GPU_ERR_CUDA, "cuStreamWriteValue32 failed (" + std::to_string(static_cast<int>(r)) + ")");
+                unsigned int const * src = counts + static_cast<size_t>(k) * kArrivalReplicas * kArrivalStride;
+                HG_CUDA(cudaMemcpyAsync(a->arrived.p, src, counter_bytes, cudaMemcpyHostToDevice, a->copy_stream));
             }
             HG_CUDA(cudaEventRecord(a->ev_copied, a->copy_stream));
         }

@@ -108,7 +108,9 @@ struct query_params
     // membership mode: a task may also stop once every segment's report/descend decision is final (segment_state)
     uint32_t decide;
     // streamed inputs (host batches): the values of queries [arrive_first[k], arrive_first[k + 1]) are on the device
-    // once *arrived > k (a stream write behind chunk k's copy); null = all inputs are resident
+    // once the chunk counter exceeds k (copied behind chunk k's values on the same stream); the counter is replicated
+    // kArrivalReplicas times, kArrivalStride words apart, and block b polls replica b % kArrivalReplicas; null = all
+    // inputs are resident
     unsigned int const * arrived;
     uint64_t const * arrive_first;
     uint32_t arrive_chunks;
@@ -116,6 +118,17 @@ struct query_params
 };
 
 using query_kernel_t = void (*)(query_params);
+
+// One 128-byte line per replica of the chunk counter: thousands of warps polling a single line starve the copy
+// stream's write of it (and with it the copies queued behind), so blocks spread their polls over 64 lines.
+constexpr uint32_t kArrivalReplicas = 64;
+constexpr uint32_t kArrivalStride = 32;
+
+__device__ __forceinline__ unsigned int arrival_count(query_params const & p)
+{
+    return *(reinterpret_cast<volatile unsigned int const *>(p.arrived) +
+             (blockIdx.x % kArrivalReplicas) * kArrivalStride);
+}
 
 __device__ __forceinline__ unsigned long long make_task(uint64_t q, uint32_t depth, uint32_t node)
 {
@@ -149,8 +162,8 @@ __device__ inline unsigned long long wait_for_task(query_params const & p, unsig
 }
 
 // Streamed inputs: the chunk counter value at which query q's values are on the device (its chunk index + 1).  The
-// copy stream writes the counter behind each chunk's copy with a memory fence, and chunks start on 32-byte sector
-// boundaries, so no sector holding values of an unarrived chunk was cached before.
+// copy stream copies the counter behind each chunk's values (stream order: after they are written), and chunks start
+// on 32-byte sector boundaries, so no sector holding values of an unarrived chunk was cached before.
 __device__ inline unsigned int arrival_needed(query_params const & p, uint64_t q)
 {
     uint32_t lo = 0, hi = p.arrive_chunks - 1u; // the last chunk k with arrive_first[k] <= q
@@ -183,11 +196,10 @@ __device__ inline unsigned long long try_claim_child(query_params const & p, uns
 __device__ inline bool wait_arrival(query_params const & p, uint64_t q)
 {
     unsigned int const need = arrival_needed(p, q);
-    volatile unsigned int const * f = p.arrived;
     uint64_t start = 0;
     for (uint32_t it = 0;; ++it)
     {
-        if (*f >= need)
+        if (arrival_count(p) >= need)
         {
             __threadfence();
             return true;
@@ -517,7 +529,7 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
             unsigned long long slot = 0;
             if (lane == 0)
             {
-                if (*reinterpret_cast<volatile unsigned int const *>(p.arrived) >= held_need)
+                if (arrival_count(p) >= held_need)
                 {
                     __threadfence();
                     action = 1;
