@@ -513,56 +513,66 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
     // than a grid's worth of warps of them are queued.  The copy paces the roots, so children run as they appear
     // instead of piling up behind the last chunk; a warp whose claimed root (`held`) has not arrived yet runs queued
     // children meanwhile.
-    unsigned long long const reserve = static_cast<unsigned long long>(gridDim.x) * (blockDim.x >> 5);
-    unsigned long long held = kEmpty;
-    unsigned int held_need = 0;
-    uint64_t held_since = 0;
-    // idle polls of a held root back off from 1 to 16 us and read the shared queue words only every 4th time: thousands
-    // of warps polling one L2 line would stall that L2 slice, and with it every warp's row reads that map there
-    unsigned int backoff = 0, polls = 0;
+    // The streamed-mode state of each warp lives in shared memory, off the registers of the counting code.
+    __shared__ unsigned long long s_held[8], s_held_since[8];
+    __shared__ unsigned int s_held_need[8], s_backoff[8], s_polls[8];
+    int const w = threadIdx.x >> 5;
+    if (lane == 0)
+    {
+        s_held[w] = kEmpty;
+        s_held_since[w] = 0;
+        s_held_need[w] = s_backoff[w] = s_polls[w] = 0;
+    }
+    __syncwarp();
     for (;;)
     {
         unsigned long long task = kEmpty;
+        unsigned long long held = s_held[w];
         if (held != kEmpty)
         {
             int action = 0; // 0 wait, 1 run the held root, 2 run a stolen child, 3 give up
             unsigned long long slot = 0;
             if (lane == 0)
             {
-                if (arrival_count(p) >= held_need)
+                if (arrival_count(p) >= s_held_need[w])
                 {
                     __threadfence();
                     action = 1;
                 }
                 else
                 {
-                    slot = (polls++ & 3u) == 0 ? try_claim_child(p, reserve) : kEmpty;
+                    unsigned long long const reserve = static_cast<unsigned long long>(gridDim.x) * (blockDim.x >> 5);
+                    slot = (s_polls[w]++ & 3u) == 0 ? try_claim_child(p, reserve) : kEmpty;
                     if (slot != kEmpty)
                     {
                         action = 2;
                     }
-                    else if (held_since == 0)
+                    else if (s_held_since[w] == 0)
                     {
-                        held_since = globaltimer_ns();
+                        s_held_since[w] = globaltimer_ns();
                     }
-                    else if (globaltimer_ns() - held_since > p.arrive_limit_ns)
+                    else if (globaltimer_ns() - s_held_since[w] > p.arrive_limit_ns)
                     {
                         atomicOr(p.ctrl + C_ERROR, E_TIMEOUT);
                         action = 3;
                     }
                     if (action == 0)
                     {
-                        backoff = backoff ? min(2u * backoff, 16384u) : 1024u;
-                        __nanosleep(backoff);
+                        unsigned int const b = s_backoff[w];
+                        s_backoff[w] = b ? min(2u * b, 16384u) : 1024u;
+                        __nanosleep(s_backoff[w]);
                     }
                     else
                     {
-                        backoff = 0;
-                        polls = 0;
+                        s_backoff[w] = 0;
+                        s_polls[w] = 0;
                     }
                 }
+                if (action == 1)
+                    s_held[w] = kEmpty;
             }
             action = __shfl_sync(kFullMask, action, 0);
+            __syncwarp();
             if (action == 3)
                 break;
             if (action == 0)
@@ -587,7 +597,7 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
             {
                 unsigned long long slot = kEmpty;
                 if (lane == 0)
-                    slot = try_claim_child(p, reserve);
+                    slot = try_claim_child(p, static_cast<unsigned long long>(gridDim.x) * (blockDim.x >> 5));
                 slot = __shfl_sync(kFullMask, slot, 0);
                 if (slot != kEmpty)
                 {
@@ -620,9 +630,13 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
                 }
                 if (p.arrived)
                 {
-                    held = make_task(q, 0u, 0u);
-                    held_need = arrival_needed(p, q);
-                    held_since = 0;
+                    if (lane == 0)
+                    {
+                        s_held[w] = make_task(q, 0u, 0u);
+                        s_held_need[w] = arrival_needed(p, q);
+                        s_held_since[w] = 0;
+                    }
+                    __syncwarp();
                     continue;
                 }
                 task = make_task(q, 0u, 0u);
