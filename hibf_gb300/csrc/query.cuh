@@ -443,28 +443,34 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
         counts[i] = 0;
     __syncwarp();
     row_params const rp{nd.words, nd.bin_size, nd.row_words, nd.bin_words, nd.hash_shift, nd.hash_funs};
-    // Count in stages; after each stage stop if the outcome is already fixed (segment_state: exact).
+    // Count in stages; after each stage stop if the outcome is already fixed (segment_state: exact).  One call site
+    // of the counting code for the stages and the rest: each call site inlines every row width's counting path, and a
+    // hierarchy of mixed widths runs them all at once, so a second copy would double the instruction footprint.
     uint64_t done = 0;
     int state = segment_state(p, nd, counts, n, thr, lane);
-    if (state == kOpen && n >= p.ee_min)
+    uint32_t const stages = state == kOpen && n >= p.ee_min ? p.ee_stages : 0u;
+    uint32_t s = 0;
+#pragma unroll 1
+    while (state == kOpen && done < n)
     {
-        for (uint32_t s = 0; s < p.ee_stages; ++s)
+        uint64_t stop = n; // the next checkpoint past `done` (checkpoints are below 100%, so below n), else the end
+        for (; s < stages; ++s)
         {
-            uint64_t const stop = n * (p.ee_first + s * p.ee_step) / 100u;
-            if (stop <= done)
-                continue;
-            count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
-            done = stop;
+            uint64_t const c = n * (p.ee_first + s * p.ee_step) / 100u;
+            if (c > done)
+            {
+                stop = c;
+                ++s;
+                break;
+            }
+        }
+        count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
+        done = stop;
+        if (done < n)
+        {
             __syncwarp();
             state = segment_state(p, nd, counts, n - done, thr, lane);
-            if (state != kOpen)
-                break;
         }
-    }
-    if (state == kOpen)
-    {
-        count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, n - done, counts, lane);
-        done = n;
     }
     __syncwarp();
     if (state == kHopeless)
