@@ -195,7 +195,44 @@ def cpu_baseline_scaled(args, wl, scale):
     g_off, g_ids, _ = hibf.membership_agent().query_batch(s["v"], s["qo"], s["thr"])
     n = s["queries"]
     return cpu, {"oracle_sample_queries": n, "oracle_sample_index_scale": scale,
-                 "oracle_sample_equal": bool(np.array_equal(o_off, g_off) and np.array_equal(o_ids, g_ids))}
+                 "oracle_sample_equal": bool(np.array_equal(o_off, g_off) and np.array_equal(o_ids, g_ids)),
+                 **count_parity(OH, hibf, s, threads)}
+
+
+def _mix64(z):
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def _digest_step(h, x):
+    return _mix64(h ^ _mix64(x + np.uint64(0x9E3779B97F4A7C15)))
+
+
+def count_digests(offs, ids, cnts):
+    """Per query the digest of its non-zero (user bin, count) pairs in ascending user bin order, as the oracle's
+    orc_hibf_query_batch forms it (hg_digest_step over ub then count, include/hibf_gb300_synthetic.h)."""
+    nq = offs.size - 1
+    d = np.full(nq, 0x6A09E667F3BCC908, np.uint64)
+    lens = np.diff(offs).astype(np.int64)
+    with np.errstate(over="ignore"):
+        for j in range(int(lens.max()) if nq else 0):
+            sel = np.nonzero(lens > j)[0]
+            pos = offs[sel].astype(np.int64) + j
+            d[sel] = _digest_step(_digest_step(d[sel], ids[pos]), cnts[pos].astype(np.uint64))
+    return d, lens.astype(np.uint64)
+
+
+def count_parity(OH, hibf, s, threads, n_max=50_000):
+    """counting_agent<uint16>::bulk_count of the device against the oracle on the sample's first queries."""
+    n = min(s["queries"], n_max)
+    qo = s["qo"][:n + 1]
+    v, thr = s["v"][:int(qo[-1])], s["thr"][:n]
+    o = OH.query_batch(v, qo, thr, thr, threads=threads)
+    g_off, g_ids, g_cnt = hibf.counting_agent(2).query_batch(v, qo, thr)
+    dg, nnz = count_digests(g_off, g_ids, g_cnt)
+    return {"oracle_count_sample_queries": n,
+            "oracle_count_sample_equal": bool(np.array_equal(dg, o["cnt_digest"]) and np.array_equal(nnz, o["cnt_nnz"]))}
 
 
 def cpu_sample(OH, wl, offs, budget_s, threads, first=0):
@@ -498,6 +535,7 @@ def run_ours(args, wl, rank, world, local):
             parity["oracle_sample_queries"] = n
             parity["oracle_sample_equal"] = bool(np.array_equal(o_off, res_offs[:n + 1]) and
                                                  np.array_equal(o_ids, res_ids[:int(res_offs[n])]))
+            parity.update(count_parity(OH, hibf, s, threads))
         value = world * nv / (ms / 1e3)
         out = {
             "metric": METRIC, "value": value, "unit": "values/s", "n_gpus": world, "steps": args.steps,
