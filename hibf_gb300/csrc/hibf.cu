@@ -623,7 +623,9 @@ std::vector<uint64_t> stream_chunks(uint64_t const * qoff, uint64_t nq)
 // Host-pointer batch with automatic growth on overflow.  Results land in the agent's pinned host buffers.  Large
 // batches are streamed: the offsets and thresholds go first, then the values in chunks on a second stream, each
 // followed by a copy of the chunk counter (its replicas) that the kernel's root claims wait for, so the kernel
-// answers the queries of arrived chunks while later chunks are still being copied.
+// answers the queries of arrived chunks while later chunks are still being copied.  Every copy is issued before the
+// kernel launch: a host call after the launch can block until the kernel ends (the first launch of a lazily loaded
+// kernel waits for the device's running work), and the kernel would then wait for chunks nobody issued.
 void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t const * qoff, uint64_t nq,
                 uint64_t const * thr, int width, bool plain)
 {
