@@ -17,10 +17,14 @@
 // order: which of the split bins a value lands in differs; sizes, tables and every unsplit user bin's bins do not.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <functional>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <unordered_set>
 #include <vector>
 
@@ -383,19 +387,62 @@ std::vector<std::vector<uint64_t>> reference_split_orders(plan_t const & P,
                 out[r.idx] = k.ordered();
         };
         rh_set kmers;
-        if (max_merged)
-            build_node(node.children[static_cast<size_t>(node.favourite)], &kmers, false);
-        else if (!node.records.empty())
-            take(kmers, node.records[0]);
-        add_to_parent(kmers); // construct_ibf
-        kmers.clear();
-        for (size_t i = 0; i < node.children.size(); ++i)
+        if (is_root)
         {
-            if (max_merged && static_cast<int64_t>(i) == node.favourite)
-                continue;
-            rh_set local;
-            build_node(node.children[i], &local, false);
-            add_to_parent(local);
+            // The root's child subtrees are independent: the favourite fills the root's set, every other child a
+            // set of its own that the root drops (it has no parent).  Replay them on all host threads.
+            std::vector<size_t> jobs(node.children.size());
+            for (size_t i = 0; i < jobs.size(); ++i)
+                jobs[i] = i;
+            std::atomic<size_t> next{0};
+            std::exception_ptr error;
+            std::mutex error_lock;
+            auto worker = [&]
+            {
+                for (size_t j; (j = next.fetch_add(1)) < jobs.size();)
+                {
+                    try
+                    {
+                        bool const fav = max_merged && static_cast<int64_t>(j) == node.favourite;
+                        rh_set local;
+                        build_node(node.children[j], fav ? &kmers : &local, false);
+                    }
+                    catch (...)
+                    {
+                        std::lock_guard<std::mutex> g(error_lock);
+                        error = std::current_exception();
+                    }
+                }
+            };
+            size_t const nt = std::min<size_t>(jobs.size(), std::max(1u, std::thread::hardware_concurrency()));
+            std::vector<std::thread> pool;
+            for (size_t t = 1; t < nt; ++t)
+                pool.emplace_back(worker);
+            worker();
+            for (std::thread & t : pool)
+                t.join();
+            if (error)
+                std::rethrow_exception(error);
+            if (!max_merged && !node.records.empty())
+                take(kmers, node.records[0]);
+            kmers.clear();
+        }
+        else
+        {
+            if (max_merged)
+                build_node(node.children[static_cast<size_t>(node.favourite)], &kmers, false);
+            else if (!node.records.empty())
+                take(kmers, node.records[0]);
+            add_to_parent(kmers); // construct_ibf
+            kmers.clear();
+            for (size_t i = 0; i < node.children.size(); ++i)
+            {
+                if (max_merged && static_cast<int64_t>(i) == node.favourite)
+                    continue;
+                rh_set local;
+                build_node(node.children[i], &local, false);
+                add_to_parent(local);
+            }
         }
         for (size_t i = max_merged ? 0 : 1; i < node.records.size(); ++i)
         {
@@ -629,34 +676,61 @@ struct hibf_gpu_sink
     std::vector<uint64_t> values;
 };
 
+namespace hibf_gb300
+{
+// sets.cu: the set materialisation on the device
+bool device_present();
+void distinct_sets_device(uint64_t const * values, std::vector<uint64_t> const & offsets,
+                          std::vector<std::vector<uint64_t>> & sets);
+uint64_t union_size_device(std::vector<std::vector<uint64_t>> const & sets, std::vector<uint64_t> const & members);
+} // namespace hibf_gb300
+
 namespace
 {
 
 // The host part of hibf_gpu_hibf_build: reads every user bin once through input_fn (its distinct values in input
 // order: the set the reference builds with compute_kmers, src/build/compute_kmers.cpp:23-32), sizes the IBFs
 // (exact distinct counts of the unions that size merged max bins), and puts split user bins in the reference's
-// chunk order.  `sets[u]` receives user bin u's values in device insertion order.
+// chunk order.  `sets[u]` receives user bin u's values in device insertion order.  With a device present the distinct
+// sets and the union sizes are sorts on the device (sets.cu); without one (planning only) host hash sets.
 plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_text, hibf_gpu_input_fn input_fn,
                    void * user, std::vector<std::vector<uint64_t>> & sets_out)
 {
     hibf_gpu_build_config const * cfg = &cfg_ref;
     uint64_t const nub = cfg->number_of_user_bins;
+    bool const device = device_present();
     // Read every user bin once: its distinct values in first-appearance order (the set the reference
     // builds with compute_kmers, src/build/compute_kmers.cpp:23-32).
     std::vector<std::vector<uint64_t>> & sets = sets_out;
     sets.assign(nub, {});
     std::vector<uint64_t> distinct(nub);
-    for (uint64_t u = 0; u < nub; ++u)
+    if (device)
     {
-        hibf_gpu_sink sink;
-        input_fn(user, u, &sink);
-        std::unordered_set<uint64_t> seen;
-        seen.reserve(sink.values.size() * 2);
-        for (uint64_t v : sink.values)
-            if (seen.insert(v).second)
-                sets[u].push_back(v);
-        distinct[u] = sets[u].size();
+        std::vector<uint64_t> all, off(nub + 1, 0);
+        for (uint64_t u = 0; u < nub; ++u)
+        {
+            hibf_gpu_sink sink;
+            input_fn(user, u, &sink);
+            all.insert(all.end(), sink.values.begin(), sink.values.end());
+            off[u + 1] = all.size();
+        }
+        distinct_sets_device(all.data(), off, sets);
     }
+    else
+    {
+        for (uint64_t u = 0; u < nub; ++u)
+        {
+            hibf_gpu_sink sink;
+            input_fn(user, u, &sink);
+            std::unordered_set<uint64_t> seen;
+            seen.reserve(sink.values.size() * 2);
+            for (uint64_t v : sink.values)
+                if (seen.insert(v).second)
+                    sets[u].push_back(v);
+        }
+    }
+    for (uint64_t u = 0; u < nub; ++u)
+        distinct[u] = sets[u].size();
     layout_t const L = parse_layout(layout_text);
     plan_t const P0 = make_plan(*cfg, L, distinct, [](size_t) { return uint64_t{1}; });
     // exact distinct counts of subtree unions (merged max bins), or sums for disjoint user bins
@@ -689,6 +763,11 @@ plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_te
             }
             if (!needed)
                 continue;
+            if (device)
+            {
+                sums[n] = union_size_device(sets, members[n]);
+                continue;
+            }
             std::unordered_set<uint64_t> un;
             for (uint64_t u : members[n])
                 un.insert(sets[u].begin(), sets[u].end());

@@ -215,6 +215,23 @@ def make_hibf_cases(R: Reference):
     hibf_case(R, "synth600", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=11)
 
 
+def make_dups_case(R: Reference):
+    """User bins read with repeated values (drawn with replacement from a per-bin pool plus a pool shared by all):
+    the builder's distinct sets in first-appearance order and the split bins' hash-set order both see duplicates."""
+    rng = np.random.default_rng(21)
+    shared = rng.integers(0, 2**63, 64, dtype=np.uint64)
+    sizes = np.clip(np.exp(rng.normal(np.log(300.0), 1.3, 200)).astype(np.int64), 5, 20000)
+    ubs = []
+    for n in sizes:
+        pool = np.concatenate([rng.integers(0, 2**63, max(1, int(n) // 3), dtype=np.uint64), shared[:8]])
+        ubs.append(rng.choice(pool, int(n), replace=True))
+    v, o = csr(ubs)
+    qs = [np.resize(ubs[u], 60) for u in range(0, 200, 7)] + [rng.integers(0, 2**63, 60, dtype=np.uint64)]
+    thr = [20] * len(qs)
+    cfg = ref_cfg(200, h=2, fpr=0.05, tmax=64)
+    hibf_case(R, "dups", cfg, v, o, csr(qs), thr, thr, widths=(2,))
+
+
 def make_hibf_wide_cases(R: Reference):
     """Hierarchies whose IBFs have rows of 2 and 4 words (tmax 128 and 256), for the 16-byte-fetch kernels."""
     # the 65,536-user-bin workload's shape at reduced sizes: h=3, fpr 0.02, tmax 256, log-normal sizes (sigma 2)
@@ -362,7 +379,7 @@ def make_c4_layout(R: Reference, estimate_union=True):
 def main(argv):
     build_reference()
     R = Reference()
-    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "c1", "c3"}
+    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "dups", "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
     if "serial" in which:
@@ -371,6 +388,8 @@ def main(argv):
         make_hll(R)
     if "hibfwide" in which:
         make_hibf_wide_cases(R)
+    if "dups" in which:
+        make_dups_case(R)
     if "ibfcfg" in which:
         make_ibf_config(R)
     if "hibf" in which:

@@ -145,3 +145,14 @@ def test_ibf_from_config_membership_for(gpu_lib):
     ibf = B.ibf_from_config(B.config(input_fn=lambda ub, it: it.push(ubs[ub]), number_of_user_bins=2))
     got = ibf.membership_agent().membership_for(np.arange(1, 6, dtype=np.uint64), 2)
     assert got.tolist() == [0, 1]
+
+
+@pytest.mark.parametrize("name", ["three_level", "uneven", "similar", "same", "synth600", "synth_t256", "dups"])
+def test_device_set_materialisation_reproduces_reference_bits(gpu_lib, oracle, name):
+    """With a device present the builder's front end materialises every user bin's distinct set (first-appearance
+    order) and sizes the merged-bin unions by sorts on the device; the insertion order it returns must rebuild every
+    IBF of the reference bit-exactly, split user bins and repeated values included (the same check the CPU test makes
+    of the host front end)."""
+    from tests.test_build_plan import test_insertion_order_reproduces_reference_bits as check
+
+    check(oracle, name)
