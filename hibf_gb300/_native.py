@@ -30,6 +30,7 @@ ERR_CYCLE = 9
 
 QUERY_MEMBERSHIP = 1
 QUERY_COUNT = 2
+EARLY_EXIT_ADAPTIVE = 0xFFFFFFFF  # hibf_gpu_tuning.early_exit_stages: checks where the outcome can first change
 
 BIN_MERGED = (1 << 64) - 1
 BIN_DELETED = (1 << 64) - 2

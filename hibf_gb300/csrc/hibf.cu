@@ -786,7 +786,12 @@ void check_tuning(hibf_gpu_tuning const & t, hibf_gpu_hibf const * h)
                                        "words; this hierarchy takes the default (1, 8, 7)");
     if (t.blocks_per_sm > 32)
         fail(HIBF_GPU_ERR_INVALID_ARG, "blocks_per_sm must be in [0, 32]");
-    if (t.early_exit_stages)
+    if (t.early_exit_stages == HIBF_GPU_EARLY_EXIT_ADAPTIVE)
+    {
+        if (t.early_exit_step == 0)
+            fail(HIBF_GPU_ERR_INVALID_ARG, "the adaptive early exit needs early_exit_step >= 1 values between checks");
+    }
+    else if (t.early_exit_stages)
     {
         uint64_t const last = t.early_exit_first + static_cast<uint64_t>(t.early_exit_stages - 1) * t.early_exit_step;
         if (t.early_exit_first == 0 || last >= 100 || (t.early_exit_stages > 1 && t.early_exit_step == 0))
@@ -802,14 +807,23 @@ hibf_gpu_tuning with_schedule(hibf_gpu_tuning t, uint32_t first, uint32_t step)
     return t;
 }
 
+hibf_gpu_tuning with_adaptive(hibf_gpu_tuning t, uint32_t min_values)
+{
+    t.early_exit_first = 0;
+    t.early_exit_step = min_values;
+    t.early_exit_stages = HIBF_GPU_EARLY_EXIT_ADAPTIVE;
+    return t;
+}
+
 bool same_schedule(hibf_gpu_tuning const & a, hibf_gpu_tuning const & b)
 {
     return a.early_exit_stages == b.early_exit_stages &&
            (a.early_exit_stages == 0 || (a.early_exit_first == b.early_exit_first && a.early_exit_step == b.early_exit_step));
 }
 
-// Stage 1: every kernel variant at 1 block per SM and at as many as fit; stage 2: the early-exit checkpoints with
-// the fastest kernel; stage 3: the minimum task length for early exit.
+// Stage 1: every kernel variant at 1 block per SM and at as many as fit; stage 2: the early-exit checkpoints (fixed
+// schedules, then the adaptive one at two minimum step sizes) with the fastest kernel; stage 3: the minimum task
+// length for early exit.
 void tune_search(uint32_t hash_count, uint64_t max_row_words, hibf_gpu_tune_measure_fn measure, void * user,
                  std::vector<hibf_gpu_tune_trial> & trials, hibf_gpu_tuning & best)
 {
@@ -848,10 +862,17 @@ void tune_search(uint32_t hash_count, uint64_t max_row_words, hibf_gpu_tune_meas
         }
     }
     hibf_gpu_tuning const k = best;
-    static constexpr uint32_t schedules[][2] = {{0, 0}, {10, 10}, {20, 10}, {30, 10}, {50, 10}, {30, 20}, {50, 20}};
+    static constexpr uint32_t schedules[][2] = {{0, 0},   {10, 10}, {20, 10}, {30, 10}, {50, 10},
+                                                {30, 20}, {50, 20}, {40, 5},  {50, 5},  {60, 5}};
     for (auto const & sch : schedules)
     {
         hibf_gpu_tuning const t = with_schedule(k, sch[0], sch[1]);
+        if (!same_schedule(t, k))
+            run(t);
+    }
+    for (uint32_t m : {32u, 128u})
+    {
+        hibf_gpu_tuning const t = with_adaptive(k, m);
         if (!same_schedule(t, k))
             run(t);
     }

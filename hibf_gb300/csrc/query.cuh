@@ -25,6 +25,10 @@
 namespace hibf_gb300
 {
 
+// query_params::ee_stages value of the adaptive early exit (checks where the outcome can first change, ee_step
+// values apart at least); the same as HIBF_GPU_EARLY_EXIT_ADAPTIVE of the C interface.
+constexpr uint32_t kEarlyExitAdaptive = 0xFFFFFFFFu;
+
 constexpr uint32_t F_MERGED = 1u;
 constexpr uint32_t F_DELETED = 2u;
 constexpr uint32_t F_RUN_END = 4u;
@@ -216,60 +220,117 @@ __device__ inline bool wait_arrival(query_params const & p, uint64_t q)
 }
 
 // The state of a task after counting all but `remaining` of its values, from each summation segment's sum so far x
-// (a value adds at most one to every bin, so the final sum lies in [x, x + remaining]):
-//   kHopeless  no segment can reach the threshold (x + remaining < t for all): nothing is reported or descended;
+// and its number of bins w (every bin of a segment adds its count, and a value adds at most one to every bin, so the
+// final sum lies in [x, top] with top = x + w * remaining):
+//   kHopeless  no segment can reach the threshold (top < t for all): nothing is reported or descended;
 //   kDecided   (membership only, `decide`) every segment either has reached the threshold for good (x >= t and no
-//              wrap possible: x + remaining <= counter mask) or can no longer reach it: the reports and descents are
-//              final, and the bin scan on the partial counts makes exactly them;
+//              wrap possible: top <= counter mask) or can no longer reach it: the reports and descents are final,
+//              and the bin scan on the partial counts makes exactly them;
 //   kOpen      otherwise.
 // A sum that could exceed the counter range is never decided (its wrapped value is not bounded).  Either early state
 // gives the same outcome as counting every value.
+//
+// `next` (if given) receives how many more values must be counted before the state can change at all (top falls by
+// at most w and x grows by at most w per value): an open segment passes for good no sooner than after
+// ceil((t - x) / w) values (and ceil((top - mask) / w) for a sum that could wrap), and turns unreachable no sooner
+// than after ceil((top - t + 1) / w); a task turns hopeless only once every reachable segment can be unreachable, and
+// (membership) decided once every open segment can be settled.  kNever: no later change is possible (a segment that
+// reached the threshold keeps a bulk count open).
 constexpr int kOpen = 0;
 constexpr int kHopeless = 1;
 constexpr int kDecided = 2;
+constexpr unsigned int kNever = 0xFFFFFFFFu;
+
+__device__ __forceinline__ unsigned long long ceil_div(unsigned long long a, unsigned long long w)
+{
+    return (a + w - 1u) / w;
+}
 
 __device__ inline int segment_state(query_params const & p, dev_node const & nd, uint32_t const * counts,
-                                    uint64_t remaining, uint64_t thr, int lane)
+                                    uint64_t remaining, uint64_t thr, int lane, unsigned int * next = nullptr)
 {
     uint2 const * d = p.descs + nd.desc_offset;
-    unsigned long long carry = 0;
+    unsigned long long carry = 0, carry_w = 0;
     bool any_reachable = false, any_open = false;
+    unsigned int wait = 0; // per lane: the largest earliest-change distance of its segments
+    bool never = false;
+    unsigned long long const mask = p.count_mask;
     for (uint32_t c = 0; c < nd.bins; c += 32)
     {
         uint32_t const b = c + lane;
         bool const valid = b < nd.bins;
         uint2 const ds = valid ? d[b] : make_uint2(0u, 0u);
         unsigned long long x = valid ? static_cast<unsigned long long>(counts[b]) : 0ull;
+        unsigned long long w = valid ? 1ull : 0ull;
         bool f = valid && (ds.y & F_HEAD);
         if (lane == 0 && !f)
+        {
             x += carry;
+            w += carry_w;
+        }
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1)
         {
             unsigned long long const y = __shfl_up_sync(kFullMask, x, o);
+            unsigned long long const yw = __shfl_up_sync(kFullMask, w, o);
             int const fy = __shfl_up_sync(kFullMask, static_cast<int>(f), o);
             if (lane >= o)
             {
                 if (!f)
+                {
                     x += y;
+                    w += yw;
+                }
                 f = f || fy;
             }
         }
         bool const ends = valid && (ds.y & (F_RUN_END | F_MERGED));
-        unsigned long long const top = x + remaining;
-        bool const reachable = ends && (top >= thr || top > p.count_mask);
-        bool const passed = x >= thr && top <= p.count_mask;
+        // x + w * remaining, saturated (the product cannot overflow for the sizes a batch admits, but stay safe)
+        unsigned long long const top =
+            remaining > (~0ull - x) / (w ? w : 1ull) ? ~0ull : x + w * static_cast<unsigned long long>(remaining);
+        bool const reachable = ends && (top >= thr || top > mask);
+        bool const passed = x >= thr && top <= mask;
         any_reachable = __any_sync(kFullMask, reachable) || any_reachable;
         any_open = __any_sync(kFullMask, reachable && !passed) || any_open;
         unsigned long long const lastx = __shfl_sync(kFullMask, x, 31);
+        unsigned long long const lastw = __shfl_sync(kFullMask, w, 31);
         uint32_t const lastf = __shfl_sync(kFullMask, ds.y, 31);
-        carry = (lastf & (F_MERGED | F_RUN_END)) ? 0ull : lastx;
-        if (any_reachable && !p.decide)
+        bool const cut = (lastf & (F_MERGED | F_RUN_END)) != 0;
+        carry = cut ? 0ull : lastx;
+        carry_w = cut ? 0ull : lastw;
+        if (next)
+        {
+            if (reachable)
+            {
+                unsigned long long const unreach = ceil_div(top >= thr ? top - thr + 1u : top - mask, w);
+                unsigned long long k = 0;
+                if (p.decide)
+                {
+                    if (!passed)
+                        k = min(unreach, max(x < thr ? ceil_div(thr - x, w) : 0ull,
+                                             top > mask ? ceil_div(top - mask, w) : 0ull));
+                }
+                else if (x >= thr)
+                    never = true; // a reached segment stays reachable: the bulk count never turns hopeless
+                else
+                    k = unreach;
+                wait = max(wait, static_cast<unsigned int>(min(k, 0xFFFFFFFEull)));
+            }
+        }
+        else if (any_reachable && !p.decide)
             return kOpen; // only hopelessness is of interest: one reachable segment settles it
+    }
+    if (next)
+    {
+        bool const nv = __any_sync(kFullMask, never);
+        unsigned int const wmax = __reduce_max_sync(kFullMask, wait);
+        *next = nv ? kNever : max(wmax, 1u);
     }
     if (!any_reachable)
         return kHopeless;
-    return (p.decide && !any_open) ? kDecided : kOpen;
+    if (!p.decide)
+        return kOpen;
+    return any_open ? kOpen : kDecided;
 }
 
 // Counting with variant V.  Variant 0 handles every row width; the tuned variants only rows of up to 4 words (the
@@ -447,21 +508,32 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
     // of the counting code for the stages and the rest: each call site inlines every row width's counting path, and a
     // hierarchy of mixed widths runs them all at once, so a second copy would double the instruction footprint.
     uint64_t done = 0;
-    int state = segment_state(p, nd, counts, n, thr, lane);
-    uint32_t const stages = state == kOpen && n >= p.ee_min ? p.ee_stages : 0u;
+    bool const adaptive = p.ee_stages == kEarlyExitAdaptive && n >= p.ee_min;
+    unsigned int next = kNever;
+    int state = segment_state(p, nd, counts, n, thr, lane, adaptive ? &next : nullptr);
+    uint32_t const stages = !adaptive && state == kOpen && n >= p.ee_min ? p.ee_stages : 0u;
     uint32_t s = 0;
 #pragma unroll 1
     while (state == kOpen && done < n)
     {
         uint64_t stop = n; // the next checkpoint past `done` (checkpoints are below 100%, so below n), else the end
-        for (; s < stages; ++s)
+        if (adaptive)
         {
-            uint64_t const c = n * (p.ee_first + s * p.ee_step) / 100u;
-            if (c > done)
+            // the earliest position where the outcome can change, at least ee_step values on
+            if (next != kNever)
+                stop = min(n, done + static_cast<uint64_t>(max(next, p.ee_step)));
+        }
+        else
+        {
+            for (; s < stages; ++s)
             {
-                stop = c;
-                ++s;
-                break;
+                uint64_t const c = n * (p.ee_first + s * p.ee_step) / 100u;
+                if (c > done)
+                {
+                    stop = c;
+                    ++s;
+                    break;
+                }
             }
         }
         count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
@@ -469,7 +541,7 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
         if (done < n)
         {
             __syncwarp();
-            state = segment_state(p, nd, counts, n - done, thr, lane);
+            state = segment_state(p, nd, counts, n - done, thr, lane, adaptive ? &next : nullptr);
         }
     }
     __syncwarp();

@@ -315,6 +315,7 @@ int hibf_gpu_agent_last_work_executed(hibf_gpu_agent * a, uint64_t * value_visit
 /* Schedule of the persistent query kernel and its autotuner (no counterpart in the reference).  Every schedule     */
 /* computes the same exact counts, so results do not depend on it; only the time does.                              */
 /* ============================================================================================================ */
+#define HIBF_GPU_EARLY_EXIT_ADAPTIVE 0xFFFFFFFFu
 typedef struct hibf_gpu_tuning
 {
     uint32_t values_per_lane;   /* 1 or 2: values each lane hashes per pass, times max(1, 4 / lanes per row) */
@@ -322,8 +323,10 @@ typedef struct hibf_gpu_tuning
     uint32_t counter_bits;      /* 5 or 7: width of the per-lane bit-sliced counters between shared-memory flushes */
     uint32_t blocks_per_sm;     /* persistent blocks of 256 threads per SM; 0 = as many as fit */
     uint32_t early_exit_first;  /* percent of a task's values counted before its first early-exit check */
-    uint32_t early_exit_step;   /* percent between later checks */
-    uint32_t early_exit_stages; /* number of checks (0: none; first + (stages - 1) * step must stay below 100) */
+    uint32_t early_exit_step;   /* percent between later checks (adaptive: the fewest values between checks) */
+    uint32_t early_exit_stages; /* number of checks (0: none; first + (stages - 1) * step must stay below 100), or
+                                   HIBF_GPU_EARLY_EXIT_ADAPTIVE: check where the outcome can first change, computed
+                                   from the bin sums at every check (early_exit_first unused) */
     uint32_t early_exit_min;    /* tasks with fewer values are counted in one stage */
     uint32_t block_queries;     /* batches of at most this many queries run one task per block of 8 warps (latency
                                    mode: each task's values split over the warps, no early exit); 0: never */

@@ -368,3 +368,39 @@ def test_host_batch_without_sector_aligned_query_starts_is_copied_whole(gpu_lib)
     offs_r, ids_r, _ = r.fetch_results(nq)
     np.testing.assert_array_equal(offs, offs_r)
     np.testing.assert_array_equal(ids, ids_r)
+
+
+@pytest.mark.parametrize("schedule", ["fixed", "adaptive"])
+def test_early_exit_bounds_a_split_user_bins_sum_by_its_bin_count(gpu_lib, oracle, schedule):
+    """A user bin split over w technical bins sums w counts, so one value can add up to w to its sum: the early exit
+    must bound the final sum by x + w * remaining, not x + remaining.  All-ones rows make every value count in every
+    bin: user bin 0 (4 bins) sums 4 per value and reaches a threshold of 3 x the query length; the others sum 1."""
+    tb = 64
+    user_bin = np.array([0, 0, 0, 0] + list(range(1, tb - 3)), np.uint64)
+    t = dict(n_user_bins=int(user_bin.max()) + 1, bins=np.array([tb], np.uint64), bin_size=np.array([1024], np.uint64),
+             hash_funs=np.array([2], np.uint64), next_ibf=np.zeros(tb, np.uint64), user_bin=user_bin)
+    words = np.full(1024 * (tb // 64), np.uint64(~np.uint64(0)), np.uint64)
+    H = hg.hierarchical_interleaved_bloom_filter.from_tables(t["n_user_bins"], t["bins"], t["bin_size"],
+                                                             t["hash_funs"], t["next_ibf"], t["user_bin"],
+                                                             words=[words])
+    O = oracle.hibf(dict(t, words=[words]))
+    rng = np.random.default_rng(3)
+    lens = [1000, 2000, 700, 3000]
+    vals = rng.integers(0, 2**63, sum(lens), dtype=np.uint64)
+    qo = np.zeros(len(lens) + 1, np.uint64)
+    np.cumsum(lens, out=qo[1:])
+    thr = np.array([3 * n for n in lens], np.uint64)
+    a = H.membership_agent()
+    tune = dict(a.tuning, early_exit_min=64)
+    if schedule == "adaptive":
+        tune.update(early_exit_stages=N.EARLY_EXIT_ADAPTIVE, early_exit_step=32)
+    a.tuning = tune
+    offs, ids, _ = a.query_batch(vals, qo, thr)
+    o_off, o_ids = O.membership_batch(vals, qo, thr, threads=2)
+    np.testing.assert_array_equal(offs, o_off)
+    np.testing.assert_array_equal(ids, o_ids)
+    assert list(ids) == [0] * len(lens)
+    c = H.counting_agent(2)
+    c.tuning = tune
+    c_offs, c_ids, c_cnt = c.query_batch(vals, qo, thr, mode=N.QUERY_COUNT, width=2)
+    assert list(c_ids) == [0] * len(lens) and list(c_cnt) == [4 * n for n in lens]

@@ -46,9 +46,10 @@ def test_search_finds_the_minimum_over_all_stages():
     assert (best["early_exit_first"], best["early_exit_step"], best["early_exit_min"]) == (20, 10, 128)
     assert best["early_exit_stages"] == 8  # checkpoints 20, 30, ..., 90 percent
     assert min(tr["kernel_ms"] for tr in trials) == pytest.approx(cost(best))
-    # stage 1: all six kernels at two occupancies; stage 2: six other checkpoint schedules; stage 3: four minimums
+    # stage 1: all six kernels at two occupancies; stage 2: nine other checkpoint schedules and two adaptive ones;
+    # stage 3: four minimums
     assert {kernel(tr) for tr in trials[:12]} == VARIANTS
-    assert len(trials) == 12 + 6 + 4
+    assert len(trials) == 12 + 11 + 4
     assert trials[0] == dict(best | dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, early_exit_first=30,
                                          early_exit_stages=7, early_exit_min=256), kernel_ms=trials[0]["kernel_ms"])
 
@@ -59,13 +60,13 @@ def test_search_respects_what_the_hierarchy_admits():
     for h, words in ((4, 1), (5, 4), (2, 8), (3, 16)):  # more hashes or wider rows: the default kernel only
         _, trials = tune_search(h, words, cost)
         assert {kernel(tr) for tr in trials} == {(1, 8, 7)}
-        assert len(trials) == 2 + 6 + 4
+        assert len(trials) == 2 + 11 + 4
 
 
 def test_search_without_early_exit_skips_its_minimum():
     best, trials = tune_search(3, 4, lambda t: 1.0 if t["early_exit_stages"] == 0 else 2.0)
     assert best["early_exit_stages"] == 0
-    assert len(trials) == 12 + 6  # no minimum-length stage when early exit is off
+    assert len(trials) == 12 + 11  # no minimum-length stage when early exit is off
 
 
 def test_search_reports_measurement_failures():
