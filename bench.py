@@ -61,7 +61,8 @@ def parse_args():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel schedule")
     ap.add_argument("--tuning", type=str, default="",
-                    help="fixed kernel schedule 'values_per_lane,fetch_bytes,counter_bits' (skips the autotuner)")
+                    help="fixed kernel schedule 'values_per_lane,fetch_bytes,counter_bits[,adaptive_step,ee_min]' "
+                         "(skips the autotuner; the two optional fields select the adaptive early exit)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned scheduler measurement")
     ap.add_argument("--sched-queries", type=int, default=20000, help="batch size of the learned scheduler test")
     ap.add_argument("--tune-queries", type=int, default=200_000, help="sample batch of the autotuner")
@@ -360,8 +361,12 @@ def run_ours(args, wl, rank, world, local):
     # autotune the kernel schedule on the batch's first queries (results are checked identical across schedules)
     tune = None
     if args.tuning:
-        vpl, fb, cb = (int(x) for x in args.tuning.split(","))
-        agent.tuning = dict(agent.tuning, values_per_lane=vpl, fetch_bytes=fb, counter_bits=cb)
+        f = [int(x) for x in args.tuning.split(",")]
+        t = dict(agent.tuning, values_per_lane=f[0], fetch_bytes=f[1], counter_bits=f[2])
+        if len(f) >= 5:
+            t.update(early_exit_first=0, early_exit_step=f[3], early_exit_stages=N.EARLY_EXIT_ADAPTIVE,
+                     early_exit_min=f[4])
+        agent.tuning = t
         tune = {"fixed": agent.tuning}
     elif not args.no_autotune:
         ns = min(nq, args.tune_queries)
