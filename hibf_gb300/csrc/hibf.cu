@@ -965,9 +965,9 @@ extern "C"
         t->fetch_bytes = 8;
         t->counter_bits = 7;
         t->blocks_per_sm = 0;
-        t->early_exit_first = 30;
-        t->early_exit_step = 10;
-        t->early_exit_stages = 7;
+        t->early_exit_first = 0;
+        t->early_exit_step = 32; // adaptive: checks where the outcome can first change, at least 32 values apart
+        t->early_exit_stages = HIBF_GPU_EARLY_EXIT_ADAPTIVE;
         t->early_exit_min = 256;
         t->block_queries = 8192;
     }

@@ -155,7 +155,9 @@ def test_work_counters(gpu_lib):
 KERNELS = [(1, 8, 7), (2, 8, 7), (1, 8, 5), (2, 8, 5), (1, 16, 7), (1, 16, 5)]
 EARLY_EXIT = [dict(early_exit_first=30, early_exit_step=10, early_exit_stages=7, early_exit_min=256),
               dict(early_exit_stages=0),
-              dict(early_exit_first=10, early_exit_step=10, early_exit_stages=9, early_exit_min=16)]
+              dict(early_exit_first=10, early_exit_step=10, early_exit_stages=9, early_exit_min=16),
+              dict(early_exit_first=0, early_exit_step=32, early_exit_stages=N.EARLY_EXIT_ADAPTIVE, early_exit_min=16),
+              dict(early_exit_first=0, early_exit_step=1, early_exit_stages=N.EARLY_EXIT_ADAPTIVE, early_exit_min=1)]
 
 
 @pytest.mark.parametrize("name", ["synth600", "synth_t128", "synth_t256"])
@@ -263,14 +265,20 @@ def test_claim_order_work_counters_and_features(gpu_lib):
 
 
 @pytest.mark.parametrize("name", G.HIBF_CASES)
-def test_early_decisions_on_every_case(gpu_lib, name):
-    """Checkpoints after every 10% of every task's values (no minimum length): the hopeless and the decided exits
-    fire as often as they can, and membership lists and counts stay the reference's."""
+@pytest.mark.parametrize("schedule", ["fixed", "adaptive"])
+def test_early_decisions_on_every_case(gpu_lib, name, schedule):
+    """Checkpoints after every 10% of every task's values, or adaptive checks at most one value apart (no minimum
+    length): the hopeless and the decided exits fire as often as they can, and membership lists and counts stay the
+    reference's."""
     d = G.hibf_case(name)
     H = _gpu_hibf(d)
     a = H.membership_agent()
-    a.tuning = dict(a.tuning, block_queries=0, early_exit_first=10, early_exit_step=10, early_exit_stages=9,
-                    early_exit_min=1)
+    if schedule == "fixed":
+        a.tuning = dict(a.tuning, block_queries=0, early_exit_first=10, early_exit_step=10, early_exit_stages=9,
+                        early_exit_min=1)
+    else:
+        a.tuning = dict(a.tuning, block_queries=0, early_exit_first=0, early_exit_step=1,
+                        early_exit_stages=N.EARLY_EXIT_ADAPTIVE, early_exit_min=1)
     qv, qo = d["q_values"], d["q_offsets"]
     offs, ids, _ = a.query_batch(qv, qo, d["mem_t"])
     for i, (g, e) in enumerate(zip(_split(offs, ids), G.mem_lists(d, "mem_sorted"))):

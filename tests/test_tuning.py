@@ -25,8 +25,9 @@ def kernel(t):
 def test_default_schedule():
     t = N.Tuning()
     N.lib().hibf_gpu_tuning_default(ctypes.byref(t))
-    assert t.as_dict() == dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, blocks_per_sm=0, early_exit_first=30,
-                               early_exit_step=10, early_exit_stages=7, early_exit_min=256, block_queries=8192)
+    assert t.as_dict() == dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, blocks_per_sm=0, early_exit_first=0,
+                               early_exit_step=32, early_exit_stages=N.EARLY_EXIT_ADAPTIVE, early_exit_min=256,
+                               block_queries=8192)
 
 
 def cost(t):
@@ -46,12 +47,13 @@ def test_search_finds_the_minimum_over_all_stages():
     assert (best["early_exit_first"], best["early_exit_step"], best["early_exit_min"]) == (20, 10, 128)
     assert best["early_exit_stages"] == 8  # checkpoints 20, 30, ..., 90 percent
     assert min(tr["kernel_ms"] for tr in trials) == pytest.approx(cost(best))
-    # stage 1: all six kernels at two occupancies; stage 2: nine other checkpoint schedules and two adaptive ones;
-    # stage 3: four minimums
+    # stage 1: all six kernels at two occupancies (the default adaptive schedule); stage 2: ten fixed checkpoint
+    # schedules and the other adaptive step; stage 3: four minimums
     assert {kernel(tr) for tr in trials[:12]} == VARIANTS
     assert len(trials) == 12 + 11 + 4
-    assert trials[0] == dict(best | dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, early_exit_first=30,
-                                         early_exit_stages=7, early_exit_min=256), kernel_ms=trials[0]["kernel_ms"])
+    assert trials[0] == dict(best | dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, early_exit_first=0,
+                                         early_exit_step=32, early_exit_stages=N.EARLY_EXIT_ADAPTIVE,
+                                         early_exit_min=256), kernel_ms=trials[0]["kernel_ms"])
 
 
 def test_search_respects_what_the_hierarchy_admits():
