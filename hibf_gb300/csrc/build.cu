@@ -593,7 +593,7 @@ void validate(hibf_gpu_build_config const * cfg)
 {
     if (!cfg)
         fail(HIBF_GPU_ERR_INVALID_ARG, "null config");
-    // config::validate_and_set_defaults (src/config.cpp:64-130), the fields this build uses
+    // config::validate_and_set_defaults (src/config.cpp:64-130), the fields the builder reads
     if (cfg->number_of_user_bins == 0)
         fail(HIBF_GPU_ERR_INVALID_ARG, "[HIBF CONFIG ERROR] You did not set the required config::number_of_user_bins.");
     if (cfg->number_of_hash_functions == 0 || cfg->number_of_hash_functions > 5)
