@@ -412,3 +412,43 @@ def test_early_exit_bounds_a_split_user_bins_sum_by_its_bin_count(gpu_lib, oracl
     c.tuning = tune
     c_offs, c_ids, c_cnt = c.query_batch(vals, qo, thr, mode=N.QUERY_COUNT, width=2)
     assert list(c_ids) == [0] * len(lens) and list(c_cnt) == [4 * n for n in lens]
+
+
+def test_streamed_host_batch_with_empty_queries_and_zero_thresholds(gpu_lib):
+    """Streamed host batch whose queries include empty ones (some at chunk boundaries, since a chunk may start at any
+    query whose first value starts a sector) and zero thresholds (every segment reached, every merged bin descended):
+    the same results as the device-resident batch."""
+    import torch
+
+    d = G.hibf_case("synth600")
+    H = _gpu_hibf(d)
+    rng = np.random.default_rng(13)
+    vals, qo, thr = _long_batch(d, 20000, rng)
+    lens = np.diff(qo).astype(np.int64)
+    lens[rng.random(lens.size) < 0.2] = 0  # a fifth of the queries empty
+    lens[:3] = 0
+    lens[-3:] = 0
+    keep = np.concatenate([np.arange(qo[i], qo[i] + lens[i]) for i in range(lens.size)]).astype(np.int64)
+    vals = vals[keep]
+    qo = np.zeros(lens.size + 1, np.uint64)
+    np.cumsum(lens, out=qo[1:])
+    thr = np.minimum(thr, np.maximum(lens, 1).astype(np.uint64))  # empty queries: threshold 1, no result
+    thr[rng.random(thr.size) < 0.01] = 0  # threshold 0: every user bin, every merged bin descended
+    assert vals.size * 8 >= 64 << 20
+    a = H.membership_agent()
+    offs, ids, _ = a.query_batch(vals, qo, thr)
+    assert a.input_chunks() > 2
+    nq = qo.size - 1
+    r = H.membership_agent()
+    r.reserve(nq, vals.size, nq * 16 + 65536, nq * 128 + 65536)
+    dv = torch.from_numpy(vals.view(np.int64)).cuda()
+    dq = torch.from_numpy(qo.view(np.int64)).cuda()
+    dt = torch.from_numpy(thr.view(np.int64)).cuda()
+    r.query_batch_device(dv.data_ptr(), dq.data_ptr(), nq, dt.data_ptr())
+    offs_r, ids_r, _ = r.fetch_results(nq)
+    np.testing.assert_array_equal(offs, offs_r)
+    np.testing.assert_array_equal(ids, ids_r)
+    empty = (lens == 0) & (thr > 0)
+    assert empty.sum() > 1000 and np.all(np.diff(offs)[empty] == 0)
+    zero = thr == 0
+    assert zero.sum() > 50 and np.all(np.diff(offs)[zero] == d["n_ub"])
