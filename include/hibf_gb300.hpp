@@ -402,10 +402,36 @@ public:
             std::ranges::sort(result_);
         }
 
+        // Many queries in one persistent launch (no counterpart in the reference): query q is
+        // values[offsets[q] .. offsets[q + 1]) with threshold thresholds[q]; its user bins are
+        // ids[result_offsets[q] .. result_offsets[q + 1]), ascending (membership_for + sort_results).  Batches of at
+        // least 64 MiB of values are streamed to the device.  Failures throw (std::invalid_argument, ...).
+        struct batch_result
+        {
+            std::vector<uint64_t> offsets;
+            std::vector<uint64_t> ids;
+        };
+        batch_result const & membership_for_batch(std::vector<uint64_t> const & values,
+                                                  std::vector<uint64_t> const & offsets,
+                                                  std::vector<uint16_t> const & thresholds) &
+        {
+            if (offsets.empty() || thresholds.size() + 1 != offsets.size() || offsets.back() > values.size())
+                throw std::invalid_argument{"membership_for_batch: offsets must have one entry per query plus one"};
+            std::vector<uint64_t> const t(thresholds.begin(), thresholds.end());
+            uint64_t const nq = thresholds.size();
+            uint64_t const *ro = nullptr, *ri = nullptr;
+            check(hibf_gpu_agent_query_batch(a_, HIBF_GPU_QUERY_MEMBERSHIP, values.data(), offsets.data(), nq,
+                                             t.data(), 2, &ro, &ri, nullptr));
+            batch_.offsets.assign(ro, ro + nq + 1);
+            batch_.ids.assign(ri, ri + batch_.offsets.back());
+            return batch_;
+        }
+
     private:
         hierarchical_interleaved_bloom_filter const * h_;
         hibf_gpu_agent * a_{};
         std::vector<uint64_t> result_;
+        batch_result batch_;
     };
 
     template <typename value_t = uint16_t>
@@ -440,10 +466,38 @@ public:
             return result_;
         }
 
+        // Many queries in one persistent launch (no counterpart in the reference): query q's counting vector as
+        // bulk_count(values[offsets[q] .. offsets[q + 1]), thresholds[q]) returns it, stored sparsely: its non-zero
+        // entries are counts[result_offsets[q] ..] for the ascending user bins ids[result_offsets[q] ..].
+        struct batch_result
+        {
+            std::vector<uint64_t> offsets;
+            std::vector<uint64_t> ids;
+            std::vector<value_t> counts;
+        };
+        batch_result const & bulk_count_batch(std::vector<uint64_t> const & values, std::vector<uint64_t> const & offsets,
+                                              std::vector<uint64_t> const & thresholds) &
+        {
+            if (offsets.empty() || thresholds.size() + 1 != offsets.size() || offsets.back() > values.size())
+                throw std::invalid_argument{"bulk_count_batch: offsets must have one entry per query plus one"};
+            uint64_t const nq = thresholds.size();
+            uint64_t const *ro = nullptr, *ri = nullptr;
+            void const * rc = nullptr;
+            check(hibf_gpu_agent_query_batch(a_, HIBF_GPU_QUERY_COUNT, values.data(), offsets.data(), nq,
+                                             thresholds.data(), detail::width_of<value_t>(), &ro, &ri, &rc));
+            batch_.offsets.assign(ro, ro + nq + 1);
+            uint64_t const nr = batch_.offsets.back();
+            batch_.ids.assign(ri, ri + nr);
+            auto const * c = static_cast<value_t const *>(rc);
+            batch_.counts.assign(c, c + nr);
+            return batch_;
+        }
+
     private:
         hierarchical_interleaved_bloom_filter const * h_;
         hibf_gpu_agent * a_{};
         std::vector<value_t> result_;
+        batch_result batch_;
     };
 
     membership_agent_type membership_agent() const

@@ -4,6 +4,7 @@
 // Exits 0 when every check holds.
 #include <cstdio>
 #include <fstream>
+#include <functional>
 #include <numeric>
 #include <sstream>
 #include <string>
@@ -190,6 +191,52 @@ static void hibf_readme(std::string const & dir)
     CHECK(agent2.membership_for(std::vector<uint64_t>{3, 9, 12, 14}, 2) == (std::vector<uint64_t>{2, 0}));
 }
 
+// The batched calls (no counterpart in the reference) give, per query, what the one-query agents give.
+static void hibf_batch(std::string const & dir)
+{
+    std::vector<std::vector<uint64_t>> hashes{{1, 2, 3, 4, 5, 6, 7, 8, 9, 10}, {1, 2, 3, 4, 5}, {3, 9, 11}};
+    h::config config{.input_fn =
+                         [&](size_t const num, h::insert_iterator && it)
+                     {
+                         for (auto const hash : hashes[num])
+                             it = hash;
+                     },
+                     .number_of_user_bins = 3};
+    h::hierarchical_interleaved_bloom_filter hibf{config, read_file(dir + "/layout_readme.txt")};
+    std::vector<std::vector<uint64_t>> queries{{3, 9, 12, 14}, iota(15), {}, {1, 2, 3}, {11, 11, 9}};
+    std::vector<uint16_t> thr{2, 5, 1, 3, 2};
+    std::vector<uint64_t> values, offsets{0};
+    for (auto const & q : queries)
+    {
+        values.insert(values.end(), q.begin(), q.end());
+        offsets.push_back(values.size());
+    }
+    auto agent = hibf.membership_agent();
+    auto single = hibf.membership_agent();
+    auto const & b = agent.membership_for_batch(values, offsets, thr);
+    CHECK(b.offsets.size() == queries.size() + 1);
+    for (size_t q = 0; q < queries.size(); ++q)
+    {
+        auto & r = single.membership_for(queries[q], thr[q]);
+        single.sort_results();
+        CHECK(std::vector<uint64_t>(b.ids.begin() + b.offsets[q], b.ids.begin() + b.offsets[q + 1]) == r);
+    }
+    auto counter = hibf.counting_agent<uint16_t>();
+    auto one = hibf.counting_agent<uint16_t>();
+    std::vector<uint64_t> const cthr{1, 5, 1, 2, 1};
+    auto const & c = counter.bulk_count_batch(values, offsets, cthr);
+    for (size_t q = 0; q < queries.size(); ++q)
+    {
+        std::vector<uint16_t> dense(hibf.number_of_user_bins, 0);
+        for (uint64_t i = c.offsets[q]; i < c.offsets[q + 1]; ++i)
+            dense[c.ids[i]] = c.counts[i];
+        CHECK(dense == one.bulk_count(queries[q], cthr[q]));
+    }
+    bool const rejected = throws<std::function<void()>, std::invalid_argument>(
+        [&] { agent.membership_for_batch(values, std::vector<uint64_t>{0}, thr); });
+    CHECK(rejected);
+}
+
 int main(int argc, char ** argv)
 {
     if (argc < 2)
@@ -206,6 +253,7 @@ int main(int argc, char ** argv)
     ibf_increase();
     hibf_small(dir);
     hibf_readme(dir);
+    hibf_batch(dir);
     if (failures)
     {
         std::fprintf(stderr, "%d check(s) failed\n", failures);
