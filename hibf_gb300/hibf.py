@@ -202,7 +202,9 @@ class _agent_base:
 
     def query_batch(self, values, query_offsets, thresholds, mode=N.QUERY_MEMBERSHIP, width=2):
         """All queries in one persistent launch.  Returns (offsets, ids, counts) as numpy copies; ids ascending per
-        query; counts (mode COUNT) are the non-zero entries of each dense counting vector."""
+        query; counts (mode COUNT) are the non-zero entries of each dense counting vector.  Batches of at least 64 MiB
+        of values are copied to the device in chunks while the kernel answers the chunks already copied
+        (input_chunks() reports how many)."""
         v, qo = _u64(values), _u64(query_offsets)
         nq = qo.size - 1
         t = _u64(thresholds)
