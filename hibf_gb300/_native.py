@@ -159,6 +159,7 @@ _SIGS = [
     ("hibf_gpu_agent_replay", None, [vp]),
     ("hibf_gpu_agent_kernel_ms", None, [vp, ctypes.POINTER(ctypes.c_float)]),
     ("hibf_gpu_agent_input_chunks", None, [vp, ctypes.POINTER(ctypes.c_uint32)]),
+    ("hibf_gpu_stream_plan", None, [vp, u64, vp, u64, ctypes.POINTER(ctypes.c_uint64)]),
     ("hibf_gpu_tuning_default", "void", [ctypes.POINTER(Tuning)]),
     ("hibf_gpu_agent_set_tuning", None, [vp, ctypes.POINTER(Tuning)]),
     ("hibf_gpu_agent_get_tuning", None, [vp, ctypes.POINTER(Tuning)]),

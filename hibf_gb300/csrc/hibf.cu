@@ -1899,6 +1899,26 @@ extern "C"
             });
     }
 
+    int hibf_gpu_stream_plan(uint64_t const * query_offsets, uint64_t n_queries, uint64_t * first_queries,
+                             uint64_t cap, uint64_t * n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!query_offsets || !n || (cap && !first_queries))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                for (uint64_t q = 0; q < n_queries; ++q)
+                    if (query_offsets[q + 1] < query_offsets[q])
+                        fail(HIBF_GPU_ERR_INVALID_ARG, "query offsets must be non-decreasing");
+                std::vector<uint64_t> qb;
+                if (n_queries && query_offsets[n_queries] * 8 >= kStreamMinBytes)
+                    qb = stream_chunks(query_offsets, n_queries);
+                *n = qb.size();
+                std::copy(qb.begin(), qb.begin() + static_cast<std::ptrdiff_t>(std::min<uint64_t>(cap, qb.size())),
+                          first_queries);
+            });
+    }
+
     int hibf_gpu_agent_input_chunks(hibf_gpu_agent const * a, uint32_t * chunks)
     {
         return guarded(

@@ -352,6 +352,18 @@ class counting_agent_type(_agent_base):
         return super().query_batch(values, query_offsets, thresholds, mode, self.width if width is None else width)
 
 
+def stream_plan(query_offsets) -> np.ndarray:
+    """The chunk boundaries (first query of every chunk, then the query count) in which a host batch with these query
+    offsets streams its values to the device; fewer than three entries: copied whole (no device needed)."""
+    qo = _u64(query_offsets)
+    n = ctypes.c_uint64(0)
+    N.call("hibf_gpu_stream_plan", qo.ctypes.data, qo.size - 1, None, 0, ctypes.byref(n))
+    out = np.zeros(n.value, np.uint64)
+    N.call("hibf_gpu_stream_plan", qo.ctypes.data, qo.size - 1, out.ctypes.data if n.value else None, n.value,
+           ctypes.byref(n))
+    return out
+
+
 def tune_search(hash_count: int, max_row_words: int, measure) -> tuple[dict, list[dict]]:
     """The autotuner's search with a caller-supplied measure(tuning: dict) -> ms (no device involved): returns the
     fastest schedule and every trial in measurement order."""

@@ -304,6 +304,11 @@ int hibf_gpu_agent_replay(hibf_gpu_agent * a);
 int hibf_gpu_agent_kernel_ms(hibf_gpu_agent * a, float * ms);
 /* Number of chunks in which the agent's last host batch streamed its values (0: copied whole before the launch). */
 int hibf_gpu_agent_input_chunks(hibf_gpu_agent const * a, uint32_t * chunks);
+/* (diagnostic, no device needed) The chunk boundaries a host batch with these query offsets would stream in: the
+ * first query of every chunk, then n_queries; every boundary but 0 and n_queries starts a 32-byte sector
+ * (query_offsets[q] % 4 == 0).  *n receives the count (2 or fewer: not streamed); at most cap entries are written. */
+int hibf_gpu_stream_plan(uint64_t const * query_offsets, uint64_t n_queries, uint64_t * first_queries, uint64_t cap,
+                         uint64_t * n);
 /* Number of (query, IBF) tasks the last batch processed and the number of query values they covered
  * (sum over tasks of the query length): the work the roofline is computed from. */
 int hibf_gpu_agent_last_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits);
