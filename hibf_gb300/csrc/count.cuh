@@ -77,12 +77,23 @@ __device__ __forceinline__ void planes_flush_to(uint64_t (&P)[K], uint32_t * out
     }
 }
 
-template <int W>
+// A row word loaded with L2 evict-first priority: for a single-level IBF every row read is random and not read again
+// soon, and the hint measured 4% faster counting there.  (The HIBF kernels keep the default: their small lower-level
+// IBFs hit in L2, and evict-first made them slower.)
+__device__ __forceinline__ uint64_t ldg_evict_first(uint64_t const * p)
+{
+    uint64_t pol, w;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(w) : "l"(p), "l"(pol));
+    return w;
+}
+
+template <int W, bool EF = false>
 __device__ __forceinline__ void load_row_words(uint64_t const * p, uint64_t (&w)[W])
 {
     if constexpr (W == 1)
     {
-        w[0] = __ldg(p);
+        w[0] = EF ? ldg_evict_first(p) : __ldg(p);
     }
     else
     {
@@ -97,7 +108,7 @@ __device__ __forceinline__ void load_row_words(uint64_t const * p, uint64_t (&w)
 // must then be even).  Each lane hashes U values per pass and keeps their H row offsets; the row words of
 // GS = 4 * UM masks per lane are loaded together, so GS * H * W loads per lane are in flight.  K planes count up to
 // 2^K - 1 masks between flushes.
-template <int LPV, int H, int K, bool ATOMIC, int UM = 1, int W = 1>
+template <int LPV, int H, int K, bool ATOMIC, int UM = 1, int W = 1, bool EF = false>
 __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const * __restrict__ vals, uint64_t n,
                                            uint32_t * counts, int lane)
 {
@@ -152,7 +163,7 @@ __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const
                     if constexpr (LPV > 1)
                         o = __shfl_sync(kFullMask, o, src);
                     if (ok[t])
-                        load_row_words<W>(words + o, w[t][i]);
+                        load_row_words<W, EF>(words + o, w[t][i]);
                     else
 #pragma unroll
                         for (int e = 0; e < W; ++e)
@@ -236,29 +247,29 @@ __device__ __forceinline__ void warp_count_wide(row_params const & rp, uint64_t 
     }
 }
 
-template <int H, bool ATOMIC>
+template <int H, bool ATOMIC, bool EF = false>
 __device__ __forceinline__ void warp_count_lpv(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
                                                uint64_t n, uint32_t * counts, int lane)
 {
     switch (lpv_log2)
     {
     case 0:
-        warp_count<1, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count<1, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
         break;
     case 1:
-        warp_count<2, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count<2, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
         break;
     case 2:
-        warp_count<4, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count<4, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
         break;
     case 3:
-        warp_count<8, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count<8, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
         break;
     case 4:
-        warp_count<16, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count<16, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
         break;
     default:
-        warp_count<32, H, 7, ATOMIC>(rp, vals, n, counts, lane);
+        warp_count<32, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
     }
 }
 

@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256) k_bulk_contains_h(row_params rp, uint64_t
                     uint64_t o = off[u][i];
                     if constexpr (LPV > 1)
                         o = __shfl_sync(kFullMask, o, src);
-                    w[t][i] = ok[t] ? __ldg(words + o) : 0ull;
+                    w[t][i] = ok[t] ? ldg_evict_first(words + o) : 0ull;
                 }
             }
 #pragma unroll
@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(256, 4)
     {
         uint64_t const len = (n - start) < chunk ? (n - start) : chunk;
         if (PRIVATE && rp.bin_words <= 32)
-            warp_count_lpv<H, false>(rp, lpv_log2, values + start, len, counts, lane);
+            warp_count_lpv<H, false, true>(rp, lpv_log2, values + start, len, counts, lane);
         else
             warp_count_h<H, true>(rp, lpv_log2, values + start, len, counts, lane);
     }
