@@ -191,7 +191,8 @@ def cpu_baseline_scaled(args, wl, scale):
     cpu = {"value": s["values"] / s["seconds"], "unit": "values/s", "cores": threads, "kind": "port",
            "sample": f"{s['queries']} queries ({s['values']} values) on the same layout with user bins at {scale} of "
                      f"their size (the full index does not fit host memory for the oracle), membership_for + "
-                     f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads"}
+                     f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads",
+           **cpu_extra(OH, wl, offs)}
     o_off, o_ids = OH.membership_batch(s["v"], s["qo"], s["thr"], threads=threads)
     g_off, g_ids, _ = hibf.membership_agent().query_batch(s["v"], s["qo"], s["thr"])
     n = s["queries"]
@@ -234,6 +235,15 @@ def count_parity(OH, hibf, s, threads, n_max=50_000):
     dg, nnz = count_digests(g_off, g_ids, g_cnt)
     return {"oracle_count_sample_queries": n,
             "oracle_count_sample_equal": bool(np.array_equal(dg, o["cnt_digest"]) and np.array_equal(nnz, o["cnt_nnz"]))}
+
+
+def cpu_extra(OH, wl, offs):
+    """Host architecture and a one-thread figure beside the all-cores CPU baseline (a short bounded sample)."""
+    import platform
+
+    s1 = cpu_sample(OH, wl, offs, 3.0, 1)
+    return {"machine": platform.machine(), "value_1_thread": s1["values"] / s1["seconds"],
+            "sample_1_thread": f"first {s1['queries']} queries ({s1['values']} values), one thread"}
 
 
 def cpu_sample(OH, wl, offs, budget_s, threads, first=0):
@@ -534,7 +544,8 @@ def run_ours(args, wl, rank, world, local):
             s = cpu_sample(OH, wl, offs, args.cpu_seconds, threads)
             cpu = {"value": s["values"] / s["seconds"], "unit": "values/s", "cores": threads, "kind": "port",
                    "sample": f"first {s['queries']} queries ({s['values']} values) of the batch, membership_for + "
-                             f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads"}
+                             f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads",
+                   **cpu_extra(OH, wl, offs)}
             o_off, o_ids = OH.membership_batch(s["v"], s["qo"], s["thr"], threads=threads)
             n = s["queries"]
             parity["oracle_sample_queries"] = n
