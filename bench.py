@@ -17,6 +17,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -239,8 +240,6 @@ def count_parity(OH, hibf, s, threads, n_max=50_000):
 
 def cpu_extra(OH, wl, offs):
     """Host architecture and a one-thread figure beside the all-cores CPU baseline (a short bounded sample)."""
-    import platform
-
     s1 = cpu_sample(OH, wl, offs, 3.0, 1)
     return {"machine": platform.machine(), "value_1_thread": s1["values"] / s1["seconds"],
             "sample_1_thread": f"first {s1['queries']} queries ({s1['values']} values), one thread"}
@@ -633,6 +632,7 @@ def run_reference(args, wl, rank, world, local):
             "data": "synthetic: seeded splitmix64 user bins and queries (include/hibf_gb300_synthetic.h)",
             "config": {"workload": WORKLOAD_DESC[wl.name], "name": wl.name, "n_user_bins": wl.n_user_bins},
             "cpu_baseline": {"value": value, "unit": "values/s", "cores": threads, "kind": "port",
+                             "machine": platform.machine(),
                              "sample": sample + "; oracle/hibf_oracle.c (the reference's sources are not on this host)"},
             "e2e": {"value": value, "unit": "values/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -791,6 +791,7 @@ def run_ibf_ours(args, rank, world, local):
             smp = ibf_cpu_sample(O, w, args.cpu_seconds, threads)
             n = smp["values"]
             cpu = {"value": n / smp["seconds"], "unit": "values/s", "cores": threads, "kind": "port",
+                   "machine": platform.machine(),
                    "sample": f"first {n} query values, bulk_count<uint16> + bulk_contains, oracle/hibf_oracle.c with "
                              f"{threads} OpenMP threads"}
             dq = torch.from_numpy(smp["q"].view(np.int64)).cuda()
@@ -867,6 +868,7 @@ def run_ibf_reference(args, rank, world, local):
             "vs_baseline": None, "dtype": "u64", "data": "synthetic",
             "config": {"workload": WORKLOAD_DESC["ibf1024"], "name": "ibf1024"},
             "cpu_baseline": {"value": value, "unit": "values/s", "cores": threads, "kind": "port",
+                             "machine": platform.machine(),
                              "sample": f"{args.steps} samples of ~{per_step:.1f} s ({vals} values), oracle/hibf_oracle.c"},
             "e2e": {"value": value, "unit": "values/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
