@@ -4,8 +4,9 @@
 // Reference interface: seqan::hibf::hierarchical_interleaved_bloom_filter
 // (include/hibf/hierarchical_interleaved_bloom_filter.hpp, src/hierarchical_interleaved_bloom_filter.cpp).
 //
-// The query kernel itself (semantics, work queue, tuning variants) is in query.cuh; this file holds the stores, the
-// result compaction passes, agents, the autotuner and their C-ABI entry points.
+// The query kernel itself (semantics, work queue, tuning variants, early exit) is in query.cuh; this file holds the
+// stores, the result compaction passes, agents (host batches, streamed when large: see host_batch), the autotuner
+// and their C-ABI entry points.
 
 #include <algorithm>
 #include <cstring>

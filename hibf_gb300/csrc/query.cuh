@@ -2,9 +2,9 @@
 // H and on a tuning variant V (values hashed per lane, register counter width, bytes fetched per lane).
 //
 // Query semantics (membership_for_impl HIBF.hpp:322-355, bulk_count_impl HIBF.hpp:463-496): for a query and an IBF,
-// count every value per technical bin, then scan the bins in order with a running sum in the counter type:
-//   deleted  -> keep the sum;   merged -> descend if sum >= t, reset;   last bin of a user bin -> report if sum >= t,
-//   reset.  Per bin the host precomputes MERGED, DELETED, RUN_END (last bin of a user bin's run) and HEAD (first bin
+// count every value per technical bin, then scan the bins in order adding each bin's count to a running sum in the
+// counter type: deleted -> no report, no reset;   merged -> descend if sum >= t, reset;   last bin of a user bin ->
+// report if sum >= t, reset.  Per bin the host precomputes MERGED, DELETED, RUN_END (last bin of a user bin's run) and HEAD (first bin
 // of a summation segment: bin 0 or the bin after a MERGED / RUN_END bin), which turns the scan into a segmented
 // prefix sum, done 32 bins at a time by a warp.  Counter wraparound: exact sums reduced modulo 2^(8*width) before
 // the comparison equal the reference's wrapping value_t sums.
@@ -12,7 +12,9 @@
 // Work queue: task = (query, depth, IBF).  Claim indices below n_queries are the implicit root tasks; children are
 // appended behind them.  A worker that claims an index whose task is not written yet waits (bounded by a time
 // limit) until it appears or the count of unfinished tasks drops to zero.  Children are added to that count
-// before their parent retires, so zero means no task is queued or running anywhere.
+// before their parent retires, so zero means no task is queued or running anywhere.  With streamed inputs (a large
+// host batch copied while the kernel runs) roots and children are claimed through separate counters, a root only
+// once its chunk of values has arrived (k_query).
 //
 // The kernels are instantiated per H in query_h<H>.cu (one translation unit each, compiled in parallel); the host
 // side (hibf.cu) picks one through query_kernel(h, variant).
