@@ -232,6 +232,22 @@ def make_dups_case(R: Reference):
     hibf_case(R, "dups", cfg, v, o, csr(qs), thr, thr, widths=(2,))
 
 
+def make_many_hash_cases(R: Reference):
+    """HIBFs with 4 and 5 hash functions (the query kernels for h = 4 and 5 run the default variant only)."""
+    sizes = S.user_bin_sizes(19, 300, S.SIZES_LOG_NORMAL, 300.0, 1.3, 20, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(19, S.QUERIES_MIXED, 20, 400, 70, 2, 7, 10, 300)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(300, h=4, fpr=0.05, tmax=64)
+    hibf_case(R, "synth_h4", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=19)
+    sizes = S.user_bin_sizes(23, 400, S.SIZES_LOG_NORMAL, 200.0, 1.5, 10, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(23, S.QUERIES_MIXED, 20, 400, 70, 2, 6, 10, 400)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(400, h=5, fpr=0.02, tmax=128)
+    hibf_case(R, "synth_h5", cfg, None, offs, (qv, qo), thr, thr, widths=(1, 2), synthetic_seed=23)
+
+
 def make_hibf_wide_cases(R: Reference):
     """Hierarchies whose IBFs have rows of 2 and 4 words (tmax 128 and 256), for the 16-byte-fetch kernels."""
     # the 65,536-user-bin workload's shape at reduced sizes: h=3, fpr 0.02, tmax 256, log-normal sizes (sigma 2)
@@ -379,7 +395,7 @@ def make_c4_layout(R: Reference, estimate_union=True):
 def main(argv):
     build_reference()
     R = Reference()
-    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "dups", "c1", "c3"}
+    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "dups", "hashes", "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
     if "serial" in which:
@@ -390,6 +406,8 @@ def main(argv):
         make_hibf_wide_cases(R)
     if "dups" in which:
         make_dups_case(R)
+    if "hashes" in which:
+        make_many_hash_cases(R)
     if "ibfcfg" in which:
         make_ibf_config(R)
     if "hibf" in which:

@@ -147,7 +147,8 @@ def test_ibf_from_config_membership_for(gpu_lib):
     assert got.tolist() == [0, 1]
 
 
-@pytest.mark.parametrize("name", ["three_level", "uneven", "similar", "same", "synth600", "synth_t256", "dups"])
+@pytest.mark.parametrize("name", ["three_level", "uneven", "similar", "same", "synth600", "synth_t256", "dups",
+                                  "synth_h4", "synth_h5"])
 def test_device_set_materialisation_reproduces_reference_bits(gpu_lib, oracle, name):
     """With a device present the builder's front end materialises every user bin's distinct set (first-appearance
     order) and sizes the merged-bin unions by sorts on the device; the insertion order it returns must rebuild every
