@@ -233,7 +233,13 @@ def make_dups_case(R: Reference):
 
 
 def make_many_hash_cases(R: Reference):
-    """HIBFs with 4 and 5 hash functions (the query kernels for h = 4 and 5 run the default variant only)."""
+    """HIBFs with 1, 4 and 5 hash functions (the query kernels for h = 4 and 5 run the default variant only)."""
+    sizes = S.user_bin_sizes(29, 250, S.SIZES_LOG_NORMAL, 300.0, 1.3, 20, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(29, S.QUERIES_MIXED, 20, 400, 70, 2, 7, 10, 250)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(250, h=1, fpr=0.05, tmax=64)
+    hibf_case(R, "synth_h1", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=29)
     sizes = S.user_bin_sizes(19, 300, S.SIZES_LOG_NORMAL, 300.0, 1.3, 20, 20000)
     offs = S.offsets_of(sizes)
     spec = S.query_spec(19, S.QUERIES_MIXED, 20, 400, 70, 2, 7, 10, 300)

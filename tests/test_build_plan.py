@@ -96,7 +96,8 @@ def _ub_values(d):
 
 
 @pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "same", "synth64",
-                                  "synth600", "synth_t128", "synth_t256", "dups", "synth_h4", "synth_h5"])
+                                  "synth600", "synth_t128", "synth_t256", "dups", "synth_h1", "synth_h4",
+                                  "synth_h5"])
 def test_insertion_order_reproduces_reference_bits(oracle, name):
     """Every IBF's bit store, split user bins included, rebuilt on the CPU oracle from the builder's insertion order
     (split user bins in the replayed hash-set order) and the reference's own tables, equals the reference's words."""
