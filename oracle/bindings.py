@@ -293,14 +293,15 @@ class RefCfg(ctypes.Structure):
                 ("relaxed_fpr", ctypes.c_double), ("threads", u64), ("sketch_bits", u64), ("tmax", u64),
                 ("alpha", ctypes.c_double), ("max_rearrangement_ratio", ctypes.c_double),
                 ("disable_estimate_union", ctypes.c_int), ("disable_rearrangement", ctypes.c_int),
-                ("track_occupancy", ctypes.c_int)]
+                ("track_occupancy", ctypes.c_int), ("empty_bin_fraction", ctypes.c_double)]
 
 
 def ref_cfg(n_user_bins, h=2, fpr=0.05, relaxed_fpr=0.3, threads=1, sketch_bits=12, tmax=0, alpha=1.2,
             max_rearrangement_ratio=0.5, disable_estimate_union=False, disable_rearrangement=False,
-            track_occupancy=False) -> RefCfg:
+            track_occupancy=False, empty_bin_fraction=0.0) -> RefCfg:
     return RefCfg(n_user_bins, h, fpr, relaxed_fpr, threads, sketch_bits, tmax, alpha, max_rearrangement_ratio,
-                  int(disable_estimate_union), int(disable_rearrangement), int(track_occupancy))
+                  int(disable_estimate_union), int(disable_rearrangement), int(track_occupancy),
+                  float(empty_bin_fraction))
 
 
 class Reference:

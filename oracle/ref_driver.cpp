@@ -55,6 +55,7 @@ extern "C"
         int disable_estimate_union;
         int disable_rearrangement;
         int track_occupancy;
+        double empty_bin_fraction;
     };
 }
 
@@ -101,6 +102,7 @@ hibf::config make_config(ref_cfg const & c, ub_source src)
     cfg.disable_estimate_union = c.disable_estimate_union != 0;
     cfg.disable_rearrangement = c.disable_rearrangement != 0;
     cfg.track_occupancy = c.track_occupancy != 0;
+    cfg.empty_bin_fraction = c.empty_bin_fraction;
     return cfg;
 }
 

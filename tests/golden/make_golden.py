@@ -232,6 +232,17 @@ def make_dups_case(R: Reference):
     hibf_case(R, "dups", cfg, v, o, csr(qs), thr, thr, widths=(2,))
 
 
+def make_empty_bins_case(R: Reference):
+    """config::empty_bin_fraction: the layout keeps a quarter of every IBF's technical bins empty (and the reference
+    then tracks occupancy)."""
+    sizes = S.user_bin_sizes(31, 300, S.SIZES_LOG_NORMAL, 300.0, 1.3, 20, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(31, S.QUERIES_MIXED, 20, 400, 70, 2, 7, 10, 300)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(300, h=2, fpr=0.05, tmax=64, empty_bin_fraction=0.25)
+    hibf_case(R, "empty_bins", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=31)
+
+
 def make_many_hash_cases(R: Reference):
     """HIBFs with 1, 4 and 5 hash functions (the query kernels for h = 4 and 5 run the default variant only)."""
     sizes = S.user_bin_sizes(29, 250, S.SIZES_LOG_NORMAL, 300.0, 1.3, 20, 20000)
@@ -401,7 +412,7 @@ def make_c4_layout(R: Reference, estimate_union=True):
 def main(argv):
     build_reference()
     R = Reference()
-    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "dups", "hashes", "c1", "c3"}
+    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "dups", "hashes", "empty", "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
     if "serial" in which:
@@ -414,6 +425,8 @@ def main(argv):
         make_dups_case(R)
     if "hashes" in which:
         make_many_hash_cases(R)
+    if "empty" in which:
+        make_empty_bins_case(R)
     if "ibfcfg" in which:
         make_ibf_config(R)
     if "hibf" in which:
