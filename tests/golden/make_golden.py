@@ -232,6 +232,23 @@ def make_dups_case(R: Reference):
     hibf_case(R, "dups", cfg, v, o, csr(qs), thr, thr, widths=(2,))
 
 
+def make_sizing_cases(R: Reference):
+    """A non-default relaxed_fpr (the merged max bins' sizing) and rows of 8 words (tmax 512: the default kernel
+    variant)."""
+    sizes = S.user_bin_sizes(37, 300, S.SIZES_LOG_NORMAL, 400.0, 1.4, 20, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(37, S.QUERIES_MIXED, 20, 400, 70, 2, 7, 10, 300)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(300, h=3, fpr=0.01, relaxed_fpr=0.1, tmax=64)
+    hibf_case(R, "relaxed_fpr", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=37)
+    sizes = S.user_bin_sizes(41, 1500, S.SIZES_LOG_NORMAL, 80.0, 1.5, 5, 20000)
+    offs = S.offsets_of(sizes)
+    spec = S.query_spec(41, S.QUERIES_MIXED, 20, 300, 70, 2, 7, 10, 1500)
+    qv, qo, thr = S.queries(spec, offs, 0, 300)
+    cfg = ref_cfg(1500, h=2, fpr=0.05, tmax=512)
+    hibf_case(R, "synth_t512", cfg, None, offs, (qv, qo), thr, thr, widths=(2,), synthetic_seed=41)
+
+
 def make_empty_bins_case(R: Reference):
     """config::empty_bin_fraction: the layout keeps a quarter of every IBF's technical bins empty (and the reference
     then tracks occupancy)."""
@@ -412,7 +429,8 @@ def make_c4_layout(R: Reference, estimate_union=True):
 def main(argv):
     build_reference()
     R = Reference()
-    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "dups", "hashes", "empty", "c1", "c3"}
+    which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "dups", "hashes", "empty", "sizing",
+                          "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
     if "serial" in which:
@@ -427,6 +445,8 @@ def main(argv):
         make_many_hash_cases(R)
     if "empty" in which:
         make_empty_bins_case(R)
+    if "sizing" in which:
+        make_sizing_cases(R)
     if "ibfcfg" in which:
         make_ibf_config(R)
     if "hibf" in which:

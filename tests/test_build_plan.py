@@ -20,7 +20,7 @@ def _cfg(d):
 
 
 @pytest.mark.parametrize("name", ["synth64", "synth600", "synth_t128", "synth_t256", "synth_h1", "synth_h4",
-                                  "synth_h5", "empty_bins"])
+                                  "synth_h5", "empty_bins", "relaxed_fpr", "synth_t512"])
 def test_plan_matches_reference_tables(name):
     d = G.hibf_case(name)
     sizes = np.diff(d["ub_offsets"].astype(np.int64)).astype(np.uint64)
@@ -98,7 +98,7 @@ def _ub_values(d):
 
 @pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "same", "synth64",
                                   "synth600", "synth_t128", "synth_t256", "dups", "synth_h1", "synth_h4",
-                                  "synth_h5", "empty_bins"])
+                                  "synth_h5", "empty_bins", "relaxed_fpr", "synth_t512"])
 def test_insertion_order_reproduces_reference_bits(oracle, name):
     """Every IBF's bit store, split user bins included, rebuilt on the CPU oracle from the builder's insertion order
     (split user bins in the replayed hash-set order) and the reference's own tables, equals the reference's words."""
