@@ -131,12 +131,22 @@ _SIGS = [
     ("hibf_gpu_hll_sketch_d", None, [vp, u64, vp, u64, ctypes.c_uint32, vp, vp]),
     ("hibf_gpu_hibf_build_inputs", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, INPUT_FN, vp, vp, vp]),
     ("hibf_gpu_ibf_plan", None, [ctypes.POINTER(BuildConfig), u64, ctypes.c_uint32, INPUT_FN, vp, u64p, u64p]),
-    ("hibf_gpu_hibf_build_synthetic", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, u64, vp,
+    ("hibf_gpu_hibf_build_synthetic", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, u64, vp, vp,
                                              ctypes.POINTER(vp)]),
+    ("hibf_gpu_split_table_synthetic", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, u64, vp,
+                                              ctypes.POINTER(vp)]),
+    ("hibf_gpu_split_table_inputs", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, INPUT_FN, vp,
+                                           ctypes.POINTER(vp)]),
+    ("hibf_gpu_split_table_sizes", None, [vp, u64p, u64p, u64p]),
+    ("hibf_gpu_split_table_export", None, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    ("hibf_gpu_split_table_import", None, [u64, u64, u64, vp, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(vp)]),
+    ("hibf_gpu_split_table_chunks", None, [vp, u64, vp, u64, vp]),
+    ("hibf_gpu_split_table_destroy", "void", [vp]),
     ("hibf_gpu_plan_disjoint", None, [ctypes.POINTER(BuildConfig), ctypes.c_char_p, vp, u64p, u64p, vp, vp, vp,
                                       vp, vp, vp]),
     ("hibf_gpu_hibf_upload_words", None, [vp, u64, vp, u64]),
     ("hibf_gpu_hibf_download_words", None, [vp, u64, vp, u64]),
+    ("hibf_gpu_hibf_digests", None, [vp, vp, ctypes.c_uint32]),
     ("hibf_gpu_agent_create", None, [vp, ctypes.POINTER(vp)]),
     ("hibf_gpu_agent_destroy", None, [vp]),
     ("hibf_gpu_agent_set_stream", None, [vp, vp]),
@@ -159,6 +169,8 @@ _SIGS = [
     ("hibf_gpu_agent_replay", None, [vp]),
     ("hibf_gpu_agent_kernel_ms", None, [vp, ctypes.POINTER(ctypes.c_float)]),
     ("hibf_gpu_agent_input_chunks", None, [vp, ctypes.POINTER(ctypes.c_uint32)]),
+    ("hibf_gpu_agent_last_timeline", None, [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
+                                            ctypes.POINTER(ctypes.c_uint32)]),
     ("hibf_gpu_stream_plan", None, [vp, u64, vp, u64, ctypes.POINTER(ctypes.c_uint64)]),
     ("hibf_gpu_tuning_default", "void", [ctypes.POINTER(Tuning)]),
     ("hibf_gpu_agent_set_tuning", None, [vp, ctypes.POINTER(Tuning)]),

@@ -146,15 +146,84 @@ def build_from_layout(configuration: config, layout_text: str, user_bins_disjoin
     return _adopt_handle(h, configuration.number_of_user_bins)
 
 
-def build_synthetic(configuration: config, layout_text: str, seed: int, user_bin_offsets):
-    """The same build for the seeded synthetic user bins (values generated on the device)."""
+SPLIT_TABLE_FIELDS = ("user_bin", "n_values", "mult", "mask", "bnd_off", "bnd_home", "before_off", "before")
+
+
+class split_table:
+    """How the reference chunks every split user bin of one layout and one set of user bin sizes (see
+    hibf_gpu_split_table_* in include/hibf_gb300.h): computed by replaying the reference's hash-set history, or
+    imported from the arrays of an earlier export (a dict with SPLIT_TABLE_FIELDS)."""
+
+    def __init__(self, handle: ctypes.c_void_p):
+        self._h = handle
+
+    @classmethod
+    def synthetic(cls, configuration: config, layout_text: str, seed: int, user_bin_offsets) -> "split_table":
+        if configuration.input_fn is None:
+            configuration.input_fn = lambda ub, it: None
+        configuration.validate_and_set_defaults()
+        off = np.ascontiguousarray(np.asarray(user_bin_offsets, dtype=np.uint64))
+        h = ctypes.c_void_p()
+        N.call("hibf_gpu_split_table_synthetic", ctypes.byref(_cfg(configuration, True)), layout_text.encode(),
+               int(seed), off.ctypes.data, ctypes.byref(h))
+        return cls(h)
+
+    @classmethod
+    def inputs(cls, configuration: config, layout_text: str) -> "split_table":
+        """The table of build_from_layout's inputs (configuration.input_fn read once per user bin)."""
+        configuration.validate_and_set_defaults()
+        fn = configuration.input_fn
+
+        def trampoline(_user, ub, sink):
+            fn(int(ub), insert_iterator(sink))
+
+        cb = N.INPUT_FN(trampoline)
+        h = ctypes.c_void_p()
+        N.call("hibf_gpu_split_table_inputs", ctypes.byref(_cfg(configuration, False)), layout_text.encode(), cb,
+               None, ctypes.byref(h))
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, a: dict) -> "split_table":
+        arr = {k: np.ascontiguousarray(np.asarray(a[k], dtype=np.uint64)) for k in SPLIT_TABLE_FIELDS}
+        h = ctypes.c_void_p()
+        N.call("hibf_gpu_split_table_import", arr["user_bin"].size, arr["bnd_home"].size, arr["before"].size,
+               *[arr[k].ctypes.data for k in SPLIT_TABLE_FIELDS], ctypes.byref(h))
+        return cls(h)
+
+    def arrays(self) -> dict:
+        ns, nb, nv = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        N.call("hibf_gpu_split_table_sizes", self._h, ctypes.byref(ns), ctypes.byref(nb), ctypes.byref(nv))
+        n = dict(user_bin=ns.value, n_values=ns.value, mult=ns.value, mask=ns.value, bnd_off=ns.value + 1,
+                 bnd_home=nb.value, before_off=nb.value + 1, before=nv.value)
+        out = {k: np.zeros(max(n[k], 1), np.uint64) for k in SPLIT_TABLE_FIELDS}
+        N.call("hibf_gpu_split_table_export", self._h, *[out[k].ctypes.data for k in SPLIT_TABLE_FIELDS])
+        return {k: out[k][:n[k]] for k in SPLIT_TABLE_FIELDS}
+
+    def chunks(self, user_bin: int, values) -> np.ndarray:
+        v = np.ascontiguousarray(np.asarray(values, dtype=np.uint64))
+        out = np.zeros(max(v.size, 1), np.uint64)
+        N.call("hibf_gpu_split_table_chunks", self._h, int(user_bin), v.ctypes.data, v.size, out.ctypes.data)
+        return out[:v.size]
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            N.lib().hibf_gpu_split_table_destroy(self._h)
+            self._h = None
+
+
+def build_synthetic(configuration: config, layout_text: str, seed: int, user_bin_offsets,
+                    table: split_table | None = None):
+    """The same build for the seeded synthetic user bins (values generated on the device).  Split user bins are
+    chunked in the reference's order, from `table` when given (it must belong to this layout and these offsets),
+    else from a replay of the reference's hash-set history run first on the host."""
     if configuration.input_fn is None:
         configuration.input_fn = lambda ub, it: None  # contents come from the stream, not from a callback
     configuration.validate_and_set_defaults()
     off = np.ascontiguousarray(np.asarray(user_bin_offsets, dtype=np.uint64))
     h = ctypes.c_void_p()
     N.call("hibf_gpu_hibf_build_synthetic", ctypes.byref(_cfg(configuration, True)), layout_text.encode(), int(seed),
-           off.ctypes.data, ctypes.byref(h))
+           off.ctypes.data, table._h if table is not None else None, ctypes.byref(h))
     return _adopt_handle(h, configuration.number_of_user_bins)
 
 

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <exception>
 #include <functional>
@@ -33,6 +34,12 @@
 #include "device.cuh"
 #include "hibf_internal.cuh"
 #include "rh_set.hpp"
+
+// A split table (hibf_gpu_split_table_*): flattened split_entry records, one per split user bin, ascending.
+struct hibf_gpu_split_table
+{
+    std::vector<uint64_t> user_bin, n, mult, mask, bnd_off{0}, home, before_off{0}, before;
+};
 
 namespace hibf_gb300
 {
@@ -360,102 +367,295 @@ plan_t make_plan(hibf_gpu_build_config const & cfg, layout_t const & L, std::vec
     return P;
 }
 
-// The order in which the reference chunks every user bin it splits over several technical bins: its hash set's
-// iteration order at that moment.  hierarchical_build (src/hierarchical_interleaved_bloom_filter.cpp:39-171) keeps
-// one set per IBF for the max bin and the records (cleared, not shrunk, between records), fills it through the
-// favourite child when the max bin is merged, and adds every non-root set to its parent's; the root's other
-// children run in a shuffled order but with sets of their own, so nothing observable depends on that order.  The
-// history is replayed here on rh_set.  `sets[u]` = user bin u's distinct values in input order.
+// Replays the history of the reference's build sets (hierarchical_build, src/hierarchical_interleaved_bloom_filter.cpp:
+// 39-171) on rh_set and calls on_split(user bin, technical bins, set) right after the set took a user bin that the
+// reference splits over several technical bins: the reference chunks it in that set's iteration order
+// (src/build/insert_into_ibf.cpp:34-47).  The reference keeps one set per IBF for the max bin and the records
+// (cleared, not shrunk, between records), fills it through the favourite child when the max bin is merged, and adds
+// every non-root set to its parent's; the root's other children run in a shuffled order but with sets of their own.
+// `source(u, f)` calls f(v) for user bin u's values in input order.
+//
+// Only what can be observed is replayed: a set's fills are skipped when no later fill of it takes a split user bin
+// and its contents do not flow into a set that is observed, and every subtree whose contents go nowhere (a child of
+// the root other than the favourite, or any child of such a node that does not feed its parent) runs as a job of its
+// own on the host threads.
+template <typename Source, typename OnSplit>
+void replay_split_history(plan_t const & P, Source const & source, OnSplit const & on_split, unsigned threads)
+{
+    std::mutex lock;
+    std::condition_variable wake;
+    std::vector<std::pair<size_t, bool>> queue{{0, true}};
+    size_t outstanding = 1;
+    std::exception_ptr error;
+
+    auto spawn = [&](size_t n)
+    {
+        std::lock_guard<std::mutex> g(lock);
+        queue.emplace_back(n, false);
+        ++outstanding;
+        wake.notify_one();
+    };
+    auto take = [&](rh_set & k, user_bin_rec const & r)
+    {
+        source(r.idx, [&](uint64_t v) { k.insert(v); });
+        if (r.ntb > 1)
+            on_split(r.idx, r.ntb, k);
+    };
+    auto add = [](rh_set const & from, rh_set & to) { from.for_each([&](uint64_t v) { to.insert(v); }); };
+
+    std::function<void(size_t, rh_set *, bool)> run = [&](size_t n, rh_set * parent, bool is_root)
+    {
+        node_t const & nd = P.g[n];
+        bool const max_merged = nd.favourite >= 0;
+        bool const up = parent != nullptr && !is_root; // every fill of this node's set flows into `parent`
+        size_t const start = max_merged ? 0 : 1;
+        // fill 0 is the max bin (favourite subtree or records[0]); fill f >= 1 the f-th record taken afterwards
+        int64_t last_split = (!max_merged && !nd.records.empty() && nd.records[0].ntb > 1) ? 0 : -1;
+        {
+            int64_t f = 1;
+            for (size_t i = start; i < nd.records.size(); ++i)
+            {
+                if (is_root && nd.records[i].ntb == 1)
+                    continue; // inserted straight from input_fn, no set
+                if (nd.records[i].ntb > 1)
+                    last_split = f;
+                ++f;
+            }
+        }
+        auto need = [&](int64_t f) { return up || f <= last_split; };
+        rh_set kmers;
+        if (max_merged)
+        {
+            size_t const fav = nd.children[static_cast<size_t>(nd.favourite)];
+            if (need(0))
+                run(fav, &kmers, false);
+            else
+                spawn(fav);
+        }
+        else if (!nd.records.empty() && need(0))
+        {
+            take(kmers, nd.records[0]);
+        }
+        if (up)
+            add(kmers, *parent); // construct_ibf
+        kmers.clear();
+        for (size_t i = 0; i < nd.children.size(); ++i)
+        {
+            if (max_merged && static_cast<int64_t>(i) == nd.favourite)
+                continue;
+            if (up)
+            {
+                rh_set local;
+                run(nd.children[i], &local, false);
+                add(local, *parent);
+            }
+            else
+            {
+                spawn(nd.children[i]);
+            }
+        }
+        int64_t f = 1;
+        for (size_t i = start; i < nd.records.size(); ++i)
+        {
+            user_bin_rec const & r = nd.records[i];
+            if (is_root && r.ntb == 1)
+                continue;
+            if (need(f))
+            {
+                take(kmers, r);
+                if (up)
+                    add(kmers, *parent);
+                kmers.clear();
+            }
+            ++f;
+        }
+    };
+
+    auto worker = [&]
+    {
+        while (true)
+        {
+            std::pair<size_t, bool> job;
+            {
+                std::unique_lock<std::mutex> g(lock);
+                wake.wait(g, [&] { return !queue.empty() || outstanding == 0; });
+                if (queue.empty())
+                    return;
+                job = queue.back();
+                queue.pop_back();
+            }
+            try
+            {
+                run(job.first, nullptr, job.second);
+            }
+            catch (...)
+            {
+                std::lock_guard<std::mutex> g(lock);
+                if (!error)
+                    error = std::current_exception();
+            }
+            std::lock_guard<std::mutex> g(lock);
+            if (--outstanding == 0)
+                wake.notify_all();
+        }
+    };
+    unsigned const nt = std::max(1u, threads ? threads : std::thread::hardware_concurrency());
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t)
+        pool.emplace_back(worker);
+    worker();
+    for (std::thread & t : pool)
+        t.join();
+    if (error)
+        std::rethrow_exception(error);
+}
+
+// The order in which the reference chunks every split user bin (the set's iteration order at that moment).
+// `sets[u]` = user bin u's distinct values in input order.
 std::vector<std::vector<uint64_t>> reference_split_orders(plan_t const & P,
                                                           std::vector<std::vector<uint64_t>> const & sets)
 {
     std::vector<std::vector<uint64_t>> out(sets.size());
-    std::function<void(size_t, rh_set *, bool)> build_node = [&](size_t n, rh_set * parent, bool is_root)
-    {
-        node_t const & node = P.g[n];
-        bool const max_merged = node.favourite >= 0;
-        auto add_to_parent = [&](rh_set const & k)
-        {
-            if (!is_root)
-                k.for_each([&](uint64_t v) { parent->insert(v); });
-        };
-        auto take = [&](rh_set & k, user_bin_rec const & r)
-        {
-            for (uint64_t v : sets[r.idx])
-                k.insert(v);
-            if (r.ntb > 1)
-                out[r.idx] = k.ordered();
-        };
-        rh_set kmers;
-        if (is_root)
-        {
-            // The root's child subtrees are independent: the favourite fills the root's set, every other child a
-            // set of its own that the root drops (it has no parent).  Replay them on all host threads.
-            std::vector<size_t> jobs(node.children.size());
-            for (size_t i = 0; i < jobs.size(); ++i)
-                jobs[i] = i;
-            std::atomic<size_t> next{0};
-            std::exception_ptr error;
-            std::mutex error_lock;
-            auto worker = [&]
-            {
-                for (size_t j; (j = next.fetch_add(1)) < jobs.size();)
-                {
-                    try
-                    {
-                        bool const fav = max_merged && static_cast<int64_t>(j) == node.favourite;
-                        rh_set local;
-                        build_node(node.children[j], fav ? &kmers : &local, false);
-                    }
-                    catch (...)
-                    {
-                        std::lock_guard<std::mutex> g(error_lock);
-                        error = std::current_exception();
-                    }
-                }
-            };
-            size_t const nt = std::min<size_t>(jobs.size(), std::max(1u, std::thread::hardware_concurrency()));
-            std::vector<std::thread> pool;
-            for (size_t t = 1; t < nt; ++t)
-                pool.emplace_back(worker);
-            worker();
-            for (std::thread & t : pool)
-                t.join();
-            if (error)
-                std::rethrow_exception(error);
-            if (!max_merged && !node.records.empty())
-                take(kmers, node.records[0]);
-            kmers.clear();
-        }
-        else
-        {
-            if (max_merged)
-                build_node(node.children[static_cast<size_t>(node.favourite)], &kmers, false);
-            else if (!node.records.empty())
-                take(kmers, node.records[0]);
-            add_to_parent(kmers); // construct_ibf
-            kmers.clear();
-            for (size_t i = 0; i < node.children.size(); ++i)
-            {
-                if (max_merged && static_cast<int64_t>(i) == node.favourite)
-                    continue;
-                rh_set local;
-                build_node(node.children[i], &local, false);
-                add_to_parent(local);
-            }
-        }
-        for (size_t i = max_merged ? 0 : 1; i < node.records.size(); ++i)
-        {
-            user_bin_rec const & r = node.records[i];
-            if (is_root && r.ntb == 1)
-                continue; // inserted straight from input_fn, no set
-            take(kmers, r);
-            add_to_parent(kmers);
-            kmers.clear();
-        }
-    };
-    build_node(0, nullptr, true);
+    replay_split_history(
+        P, [&](uint64_t u, auto && f) { for (uint64_t v : sets[u]) f(v); },
+        [&](uint64_t u, uint64_t, rh_set const & k) { out[u] = k.ordered(); }, 0);
     return out;
+}
+
+// A split user bin's chunking without its order.  The set's iteration order visits keys in non-decreasing home slot
+// (rh_home with the set's multiplier and mask), so a key's rank is the number of keys in lower home slots plus its
+// place among the keys of its own slot.  Chunk boundary b (rank b * ceil(n / tbs)) is therefore fixed by the home
+// slot of the key at that rank and the keys of that slot ranked before it; a key's chunk is the number of
+// boundaries it lies at or after.
+struct split_entry
+{
+    uint64_t n{};    // distinct values of the user bin
+    uint64_t mult{}; // the set's hash multiplier when it was chunked
+    uint64_t mask{}; // the set's slot mask then
+    std::vector<uint64_t> home;                // per boundary: home slot of the key at the boundary's rank
+    std::vector<std::vector<uint64_t>> before; // per boundary: keys of that home slot ranked before it
+};
+
+split_entry split_entry_of(rh_set const & k, uint64_t tbs)
+{
+    split_entry e;
+    e.n = k.size();
+    e.mult = k.multiplier();
+    e.mask = k.slot_mask();
+    uint64_t const chunk = (e.n + tbs - 1) / tbs;
+    uint64_t next = 1, rank = 0, cur = UINT64_MAX, prev = 0;
+    bool sorted = true;
+    std::vector<uint64_t> group;
+    k.for_each(
+        [&](uint64_t v)
+        {
+            uint64_t const h = rh_home(v, e.mult, e.mask);
+            if (rank > 0 && h < prev)
+                sorted = false;
+            if (h != cur)
+            {
+                group.clear();
+                cur = h;
+            }
+            if (next < tbs && next * chunk == rank)
+            {
+                e.home.push_back(h);
+                e.before.push_back(group);
+                ++next;
+            }
+            group.push_back(v);
+            prev = h;
+            ++rank;
+        });
+    if (!sorted)
+        fail(HIBF_GPU_ERR_LOGIC, "hash set iteration is not in home slot order");
+    return e;
+}
+
+// The chunk of value v of a split user bin (host form of the device's lookup).
+uint64_t split_chunk(uint64_t v, uint64_t mult, uint64_t mask, uint64_t const * home, uint64_t n_bnd,
+                     uint64_t const * before_off, uint64_t const * before)
+{
+    uint64_t const h = rh_home(v, mult, mask);
+    uint64_t c = 0;
+    while (c < n_bnd && home[c] < h)
+        ++c;
+    for (; c < n_bnd && home[c] == h; ++c)
+    {
+        bool in = false;
+        for (uint64_t j = before_off[c]; j < before_off[c + 1]; ++j)
+            in = in || before[j] == v;
+        if (in)
+            break;
+    }
+    return c;
+}
+
+// The split table of plan P: the replay with `source` giving every user bin's values in input order.
+template <typename Source>
+void compute_split_table(plan_t const & P, Source const & source, unsigned threads, hibf_gpu_split_table & t)
+{
+    size_t const nub = P.ub_rec.size();
+    std::vector<split_entry> ent(nub);
+    replay_split_history(P, source, [&](uint64_t u, uint64_t tbs, rh_set const & k) { ent[u] = split_entry_of(k, tbs); },
+                         threads);
+    t = hibf_gpu_split_table{};
+    for (size_t u = 0; u < nub; ++u)
+    {
+        if (P.ub_rec[u].ntb <= 1)
+            continue;
+        split_entry const & e = ent[u];
+        t.user_bin.push_back(u);
+        t.n.push_back(e.n);
+        t.mult.push_back(e.mult);
+        t.mask.push_back(e.mask);
+        for (size_t b = 0; b < e.home.size(); ++b)
+        {
+            t.home.push_back(e.home[b]);
+            t.before.insert(t.before.end(), e.before[b].begin(), e.before[b].end());
+            t.before_off.push_back(t.before.size());
+        }
+        t.bnd_off.push_back(t.home.size());
+    }
+}
+
+// Checks that table t belongs to plan P with user bins of `distinct` values; returns per user bin 1 + its entry
+// (0: not split).
+std::vector<uint64_t> check_split_table(plan_t const & P, hibf_gpu_split_table const & t,
+                                        std::vector<uint64_t> const & distinct)
+{
+    size_t const nub = P.ub_rec.size();
+    size_t const ns = t.user_bin.size();
+    auto bad = [](char const * what) { fail(HIBF_GPU_ERR_INVALID_ARG, std::string("split table: ") + what); };
+    if (t.n.size() != ns || t.mult.size() != ns || t.mask.size() != ns || t.bnd_off.size() != ns + 1 ||
+        t.bnd_off.back() != t.home.size() || t.before_off.size() != t.home.size() + 1 ||
+        t.before_off.back() != t.before.size())
+        bad("inconsistent array sizes");
+    std::vector<uint64_t> entry(nub, 0);
+    for (size_t i = 0; i < ns; ++i)
+    {
+        uint64_t const u = t.user_bin[i];
+        if (u >= nub || P.ub_rec[u].ntb <= 1 || entry[u] != 0)
+            bad("it lists a user bin the layout does not split, or one twice");
+        entry[u] = i + 1;
+        uint64_t const tbs = P.ub_rec[u].ntb;
+        if (t.n[i] != distinct[u])
+            bad("a user bin's size differs from the input's");
+        uint64_t const chunk = (t.n[i] + tbs - 1) / tbs;
+        uint64_t want = 0;
+        for (uint64_t b = 1; b < tbs && b * chunk < t.n[i]; ++b)
+            ++want;
+        if (t.bnd_off[i + 1] < t.bnd_off[i] || t.bnd_off[i + 1] - t.bnd_off[i] != want)
+            bad("a user bin has the wrong number of chunk boundaries");
+        for (uint64_t b = t.bnd_off[i]; b < t.bnd_off[i + 1]; ++b)
+            if (t.home[b] > t.mask[i] || (b > t.bnd_off[i] && t.home[b] < t.home[b - 1]) ||
+                t.before_off[b + 1] < t.before_off[b])
+                bad("boundaries out of order");
+    }
+    for (size_t u = 0; u < nub; ++u)
+        if (P.ub_rec[u].ntb > 1 && entry[u] == 0)
+            bad("a split user bin of the layout is missing");
+    return entry;
 }
 
 // Distinct values under each node when user bins are pairwise disjoint: sums of their sizes.
@@ -481,18 +681,67 @@ std::vector<uint64_t> disjoint_unions(plan_t const & P, std::vector<uint64_t> co
 // ---- device inserts -------------------------------------------------------------------------------------------
 struct alignas(16) insert_job
 {
-    uint64_t start;  // first value (stream position for synthetic jobs, buffer offset otherwise)
-    uint64_t n;      // number of values
-    uint64_t chunk;  // values per technical bin for split user bins; 0: all values into first_bin
+    uint64_t start; // first value (stream position for synthetic jobs, buffer offset otherwise)
+    uint64_t n;     // number of values
+    uint64_t split; // split user bins: 1 + their entry in the split table; 0: all values into first_bin
     uint32_t ibf;
     uint32_t first_bin;
 };
+
+// Device form of a split table: per split user bin its set's multiplier and mask and its boundaries; per boundary
+// the home slot and the keys of that slot ranked before it (split_entry).
+struct alignas(16) dev_split
+{
+    uint64_t mult;
+    uint64_t mask;
+    uint32_t bnd_first;
+    uint32_t bnd_count;
+    uint32_t pad[2];
+};
+
+struct alignas(16) dev_bnd
+{
+    uint64_t home;
+    uint32_t before_first;
+    uint32_t before_count;
+};
+
+// The technical bin offset of value v of a split user bin: the number of chunk boundaries it lies at or after.
+__device__ __forceinline__ uint32_t split_chunk_d(uint64_t v, dev_split const & sp, dev_bnd const * __restrict__ bnds,
+                                                  uint64_t const * __restrict__ before)
+{
+    uint64_t const h = rh_home(v, sp.mult, sp.mask);
+    uint32_t lo = 0, hi = sp.bnd_count;
+    while (lo < hi)
+    {
+        uint32_t const mid = (lo + hi) >> 1;
+        if (bnds[sp.bnd_first + mid].home < h)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    uint32_t c = lo;
+    for (; c < sp.bnd_count; ++c)
+    {
+        dev_bnd const bd = bnds[sp.bnd_first + c];
+        if (bd.home != h)
+            break;
+        bool in = false;
+        for (uint32_t j = 0; j < bd.before_count; ++j)
+            in = in || before[bd.before_first + j] == v;
+        if (in)
+            break;
+    }
+    return c;
+}
 
 // Inserts every job's values; job j covers flattened positions [end[j] - n_j, end[j]).  Values come from the
 // splitmix64 stream (values == nullptr) or from a device buffer.
 __global__ void k_insert_jobs(dev_node const * __restrict__ nodes, insert_job const * __restrict__ jobs,
                               uint64_t const * __restrict__ job_end, uint32_t n_jobs, uint64_t total,
-                              uint64_t seed, uint64_t const * __restrict__ values)
+                              uint64_t seed, uint64_t const * __restrict__ values,
+                              dev_split const * __restrict__ splits, dev_bnd const * __restrict__ bnds,
+                              uint64_t const * __restrict__ before)
 {
     uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
     uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
@@ -516,7 +765,7 @@ __global__ void k_insert_jobs(dev_node const * __restrict__ nodes, insert_job co
         insert_job const jb = jobs[j];
         uint64_t const local = i - (job_end[j] - jb.n);
         uint64_t const v = values ? values[jb.start + local] : hg_stream_at(seed, jb.start + local);
-        uint64_t const b = jb.first_bin + (jb.chunk ? local / jb.chunk : 0u);
+        uint64_t const b = jb.first_bin + (jb.split ? split_chunk_d(v, splits[jb.split - 1], bnds, before) : 0u);
         dev_node const nd = nodes[jb.ibf];
         if (b >= nd.bins)
             continue;
@@ -530,8 +779,39 @@ __global__ void k_insert_jobs(dev_node const * __restrict__ nodes, insert_job co
     }
 }
 
+// The split table on the device (uploaded once per build).
+struct dev_split_table
+{
+    dbuf splits, bnds, before;
+};
+
+void upload_split_table(hibf_gpu_split_table const & t, dev_split_table & dt, cudaStream_t s)
+{
+    size_t const ns = t.user_bin.size();
+    if (t.home.size() > UINT32_MAX || t.before.size() > UINT32_MAX)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "split table too large");
+    std::vector<dev_split> sp(ns);
+    for (size_t i = 0; i < ns; ++i)
+        sp[i] = dev_split{t.mult[i], t.mask[i], static_cast<uint32_t>(t.bnd_off[i]),
+                          static_cast<uint32_t>(t.bnd_off[i + 1] - t.bnd_off[i]), {0, 0}};
+    std::vector<dev_bnd> bd(t.home.size());
+    for (size_t b = 0; b < bd.size(); ++b)
+        bd[b] = dev_bnd{t.home[b], static_cast<uint32_t>(t.before_off[b]),
+                        static_cast<uint32_t>(t.before_off[b + 1] - t.before_off[b])};
+    dt.splits.ensure(sp.size() * sizeof(dev_split));
+    dt.bnds.ensure(bd.size() * sizeof(dev_bnd));
+    dt.before.ensure(t.before.size() * 8);
+    if (!sp.empty())
+        HG_CUDA(cudaMemcpyAsync(dt.splits.p, sp.data(), sp.size() * sizeof(dev_split), cudaMemcpyHostToDevice, s));
+    if (!bd.empty())
+        HG_CUDA(cudaMemcpyAsync(dt.bnds.p, bd.data(), bd.size() * sizeof(dev_bnd), cudaMemcpyHostToDevice, s));
+    if (!t.before.empty())
+        HG_CUDA(cudaMemcpyAsync(dt.before.p, t.before.data(), t.before.size() * 8, cudaMemcpyHostToDevice, s));
+    HG_CUDA(cudaStreamSynchronize(s)); // the host vectors may go away
+}
+
 void run_jobs(hibf_gpu_hibf * h, std::vector<insert_job> const & jobs, uint64_t seed, uint64_t const * d_values,
-              cudaStream_t s)
+              dev_split_table const * dt, cudaStream_t s)
 {
     if (jobs.empty())
         return;
@@ -553,7 +833,10 @@ void run_jobs(hibf_gpu_hibf * h, std::vector<insert_job> const & jobs, uint64_t 
     uint64_t const want = (acc + block - 1) / block;
     unsigned const grid = static_cast<unsigned>(std::min<uint64_t>(want, static_cast<uint64_t>(sm_count()) * 16));
     k_insert_jobs<<<grid, block, 0, s>>>(h->d_nodes.as<dev_node>(), dj.as<insert_job>(), de.as<uint64_t>(),
-                                         static_cast<uint32_t>(jobs.size()), acc, seed, d_values);
+                                         static_cast<uint32_t>(jobs.size()), acc, seed, d_values,
+                                         dt ? dt->splits.as<dev_split>() : nullptr,
+                                         dt ? dt->bnds.as<dev_bnd>() : nullptr,
+                                         dt ? dt->before.as<uint64_t>() : nullptr);
     HG_CUDA(cudaGetLastError());
     HG_CUDA(cudaStreamSynchronize(s));
 }
@@ -688,13 +971,33 @@ uint64_t union_size_device(std::vector<std::vector<uint64_t>> const & sets, std:
 namespace
 {
 
+// The plan of a synthetic build: pairwise distinct user bins of the given stream ranges, unions sized by sums.
+plan_t synthetic_plan(hibf_gpu_build_config const & cfg, char const * layout_text, uint64_t const * user_bin_offsets)
+{
+    uint64_t const nub = cfg.number_of_user_bins;
+    std::vector<uint64_t> distinct(nub);
+    for (uint64_t u = 0; u < nub; ++u)
+    {
+        if (user_bin_offsets[u + 1] < user_bin_offsets[u])
+            fail(HIBF_GPU_ERR_INVALID_ARG, "user bin offsets must not decrease");
+        distinct[u] = user_bin_offsets[u + 1] - user_bin_offsets[u];
+    }
+    layout_t const L = parse_layout(layout_text);
+    plan_t const P0 = make_plan(cfg, L, distinct, [](size_t) { return uint64_t{1}; });
+    std::vector<uint64_t> const sums = disjoint_unions(P0, distinct, L);
+    return make_plan(cfg, L, distinct, [&](size_t node) { return sums[node]; });
+}
+
 // The host part of hibf_gpu_hibf_build: reads every user bin once through input_fn (its distinct values in input
 // order: the set the reference builds with compute_kmers, src/build/compute_kmers.cpp:23-32), sizes the IBFs
 // (exact distinct counts of the unions that size merged max bins), and puts split user bins in the reference's
 // chunk order.  `sets[u]` receives user bin u's values in device insertion order.  With a device present the distinct
 // sets and the union sizes are sorts on the device (sets.cu); without one (planning only) host hash sets.
+//
+// With `table` the split user bins keep their input order and `table` receives their split table (the device
+// chunks them); without it they are reordered into the reference's chunk order on the host.
 plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_text, hibf_gpu_input_fn input_fn,
-                   void * user, std::vector<std::vector<uint64_t>> & sets_out)
+                   void * user, std::vector<std::vector<uint64_t>> & sets_out, hibf_gpu_split_table * table)
 {
     hibf_gpu_build_config const * cfg = &cfg_ref;
     uint64_t const nub = cfg->number_of_user_bins;
@@ -775,13 +1078,18 @@ plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_te
         }
     }
     plan_t const P = make_plan(*cfg, L, distinct, [&](size_t node) { return sums[node]; });
-    // split user bins in the reference's chunk order
+    unsigned const threads = static_cast<unsigned>(cfg->threads);
+    if (table)
     {
-        std::vector<std::vector<uint64_t>> split = reference_split_orders(P, sets);
-        for (uint64_t u = 0; u < nub; ++u)
-            if (P.ub_rec[u].ntb > 1)
-                sets[u] = std::move(split[u]);
+        compute_split_table(
+            P, [&](uint64_t u, auto && f) { for (uint64_t v : sets[u]) f(v); }, threads, *table);
+        return P;
     }
+    // split user bins in the reference's chunk order
+    std::vector<std::vector<uint64_t>> split = reference_split_orders(P, sets);
+    for (uint64_t u = 0; u < nub; ++u)
+        if (P.ub_rec[u].ntb > 1)
+            sets[u] = std::move(split[u]);
     return P;
 }
 
@@ -961,8 +1269,150 @@ extern "C"
             });
     }
 
+    int hibf_gpu_split_table_synthetic(hibf_gpu_build_config const * cfg, char const * layout_text, uint64_t seed,
+                                       uint64_t const * user_bin_offsets, hibf_gpu_split_table ** out)
+    {
+        return guarded(
+            [&]
+            {
+                validate(cfg);
+                if (!user_bin_offsets || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *out = nullptr;
+                plan_t const P = synthetic_plan(*cfg, layout_text, user_bin_offsets);
+                auto * t = new hibf_gpu_split_table;
+                try
+                {
+                    compute_split_table(
+                        P,
+                        [&](uint64_t u, auto && f)
+                        {
+                            for (uint64_t k = user_bin_offsets[u]; k < user_bin_offsets[u + 1]; ++k)
+                                f(hg_stream_at(seed, k));
+                        },
+                        static_cast<unsigned>(cfg->threads), *t);
+                }
+                catch (...)
+                {
+                    delete t;
+                    throw;
+                }
+                *out = t;
+            });
+    }
+
+    int hibf_gpu_split_table_inputs(hibf_gpu_build_config const * cfg, char const * layout_text,
+                                    hibf_gpu_input_fn input_fn, void * user, hibf_gpu_split_table ** out)
+    {
+        return guarded(
+            [&]
+            {
+                validate(cfg);
+                if (!input_fn || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument (config::input_fn is required)");
+                *out = nullptr;
+                std::vector<std::vector<uint64_t>> sets;
+                auto * t = new hibf_gpu_split_table;
+                try
+                {
+                    plan_inputs(*cfg, layout_text, input_fn, user, sets, t);
+                }
+                catch (...)
+                {
+                    delete t;
+                    throw;
+                }
+                *out = t;
+            });
+    }
+
+    int hibf_gpu_split_table_sizes(hibf_gpu_split_table const * t, uint64_t * n_split, uint64_t * n_boundaries,
+                                   uint64_t * n_before)
+    {
+        return guarded(
+            [&]
+            {
+                if (!t || !n_split || !n_boundaries || !n_before)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *n_split = t->user_bin.size();
+                *n_boundaries = t->home.size();
+                *n_before = t->before.size();
+            });
+    }
+
+    int hibf_gpu_split_table_export(hibf_gpu_split_table const * t, uint64_t * user_bin, uint64_t * n_values,
+                                    uint64_t * mult, uint64_t * mask, uint64_t * bnd_off, uint64_t * bnd_home,
+                                    uint64_t * before_off, uint64_t * before)
+    {
+        return guarded(
+            [&]
+            {
+                if (!t || !user_bin || !n_values || !mult || !mask || !bnd_off || !bnd_home || !before_off ||
+                    (!before && !t->before.empty()))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::copy(t->user_bin.begin(), t->user_bin.end(), user_bin);
+                std::copy(t->n.begin(), t->n.end(), n_values);
+                std::copy(t->mult.begin(), t->mult.end(), mult);
+                std::copy(t->mask.begin(), t->mask.end(), mask);
+                std::copy(t->bnd_off.begin(), t->bnd_off.end(), bnd_off);
+                std::copy(t->home.begin(), t->home.end(), bnd_home);
+                std::copy(t->before_off.begin(), t->before_off.end(), before_off);
+                std::copy(t->before.begin(), t->before.end(), before);
+            });
+    }
+
+    int hibf_gpu_split_table_import(uint64_t n_split, uint64_t n_boundaries, uint64_t n_before,
+                                    uint64_t const * user_bin, uint64_t const * n_values, uint64_t const * mult,
+                                    uint64_t const * mask, uint64_t const * bnd_off, uint64_t const * bnd_home,
+                                    uint64_t const * before_off, uint64_t const * before, hibf_gpu_split_table ** out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!out || (n_split && (!user_bin || !n_values || !mult || !mask)) || !bnd_off || !before_off ||
+                    (n_boundaries && !bnd_home) || (n_before && !before))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *out = nullptr;
+                auto * t = new hibf_gpu_split_table;
+                t->user_bin.assign(user_bin, user_bin + n_split);
+                t->n.assign(n_values, n_values + n_split);
+                t->mult.assign(mult, mult + n_split);
+                t->mask.assign(mask, mask + n_split);
+                t->bnd_off.assign(bnd_off, bnd_off + n_split + 1);
+                t->home.assign(bnd_home, bnd_home + n_boundaries);
+                t->before_off.assign(before_off, before_off + n_boundaries + 1);
+                t->before.assign(before, before + n_before);
+                *out = t;
+            });
+    }
+
+    int hibf_gpu_split_table_chunks(hibf_gpu_split_table const * t, uint64_t user_bin, uint64_t const * values,
+                                    uint64_t n, uint64_t * chunks)
+    {
+        return guarded(
+            [&]
+            {
+                if (!t || (n && (!values || !chunks)))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                auto const it = std::lower_bound(t->user_bin.begin(), t->user_bin.end(), user_bin);
+                if (it == t->user_bin.end() || *it != user_bin)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "the user bin is not split");
+                size_t const i = static_cast<size_t>(it - t->user_bin.begin());
+                uint64_t const b0 = t->bnd_off[i];
+                for (uint64_t j = 0; j < n; ++j)
+                    chunks[j] = split_chunk(values[j], t->mult[i], t->mask[i], t->home.data() + b0,
+                                            t->bnd_off[i + 1] - b0, t->before_off.data() + b0, t->before.data());
+            });
+    }
+
+    void hibf_gpu_split_table_destroy(hibf_gpu_split_table * t)
+    {
+        delete t;
+    }
+
     int hibf_gpu_hibf_build_synthetic(hibf_gpu_build_config const * cfg, char const * layout_text, uint64_t seed,
-                                      uint64_t const * user_bin_offsets, hibf_gpu_hibf ** out)
+                                      uint64_t const * user_bin_offsets, hibf_gpu_split_table const * table,
+                                      hibf_gpu_hibf ** out)
     {
         return guarded(
             [&]
@@ -972,31 +1422,42 @@ extern "C"
                     fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
                 *out = nullptr;
                 uint64_t const nub = cfg->number_of_user_bins;
+                plan_t const P = synthetic_plan(*cfg, layout_text, user_bin_offsets);
+                hibf_gpu_split_table computed;
+                if (!table)
+                {
+                    compute_split_table(
+                        P,
+                        [&](uint64_t u, auto && f)
+                        {
+                            for (uint64_t k = user_bin_offsets[u]; k < user_bin_offsets[u + 1]; ++k)
+                                f(hg_stream_at(seed, k));
+                        },
+                        static_cast<unsigned>(cfg->threads), computed);
+                    table = &computed;
+                }
                 std::vector<uint64_t> distinct(nub);
                 for (uint64_t u = 0; u < nub; ++u)
                     distinct[u] = user_bin_offsets[u + 1] - user_bin_offsets[u];
-                layout_t const L = parse_layout(layout_text);
-                plan_t const P0 = make_plan(*cfg, L, distinct, [](size_t) { return uint64_t{1}; });
-                std::vector<uint64_t> const sums = disjoint_unions(P0, distinct, L);
-                plan_t const P = make_plan(*cfg, L, distinct, [&](size_t node) { return sums[node]; });
+                std::vector<uint64_t> const entry = check_split_table(P, *table, distinct);
                 hibf_gpu_hibf * h = create_from_plan(P, nub);
                 try
                 {
+                    dev_split_table dt;
+                    upload_split_table(*table, dt, h->stream);
                     std::vector<insert_job> jobs;
                     for (uint64_t u = 0; u < nub; ++u)
                     {
                         uint64_t const n = distinct[u];
                         user_bin_rec const & r = P.ub_rec[u];
-                        insert_job leaf{user_bin_offsets[u], n, 0, static_cast<uint32_t>(P.ub_leaf[u]),
-                                        static_cast<uint32_t>(r.storage)};
-                        if (r.ntb > 1)
-                            leaf.chunk = (n + r.ntb - 1) / r.ntb;
-                        jobs.push_back(leaf);
+                        jobs.push_back(insert_job{user_bin_offsets[u], n, entry[u],
+                                                  static_cast<uint32_t>(P.ub_leaf[u]),
+                                                  static_cast<uint32_t>(r.storage)});
                         for (auto const & [ibf, bin] : P.ub_merged[u])
                             jobs.push_back(insert_job{user_bin_offsets[u], n, 0, static_cast<uint32_t>(ibf),
                                                       static_cast<uint32_t>(bin)});
                     }
-                    run_jobs(h, jobs, seed, nullptr, h->stream);
+                    run_jobs(h, jobs, seed, nullptr, &dt, h->stream);
                 }
                 catch (...)
                 {
@@ -1019,10 +1480,17 @@ extern "C"
                 *out = nullptr;
                 uint64_t const nub = cfg->number_of_user_bins;
                 std::vector<std::vector<uint64_t>> sets;
-                plan_t const P = plan_inputs(*cfg, layout_text, input_fn, user, sets);
+                hibf_gpu_split_table table;
+                plan_t const P = plan_inputs(*cfg, layout_text, input_fn, user, sets, &table);
+                std::vector<uint64_t> distinct(nub);
+                for (uint64_t u = 0; u < nub; ++u)
+                    distinct[u] = sets[u].size();
+                std::vector<uint64_t> const entry = check_split_table(P, table, distinct);
                 hibf_gpu_hibf * h = create_from_plan(P, nub);
                 try
                 {
+                    dev_split_table dt;
+                    upload_split_table(table, dt, h->stream);
                     // all distinct values, concatenated, uploaded once
                     std::vector<uint64_t> off(nub + 1, 0);
                     for (uint64_t u = 0; u < nub; ++u)
@@ -1038,16 +1506,13 @@ extern "C"
                     {
                         uint64_t const n = sets[u].size();
                         user_bin_rec const & r = P.ub_rec[u];
-                        insert_job leaf{off[u], n, 0, static_cast<uint32_t>(P.ub_leaf[u]),
-                                        static_cast<uint32_t>(r.storage)};
-                        if (r.ntb > 1)
-                            leaf.chunk = (n + r.ntb - 1) / r.ntb;
-                        jobs.push_back(leaf);
+                        jobs.push_back(insert_job{off[u], n, entry[u], static_cast<uint32_t>(P.ub_leaf[u]),
+                                                  static_cast<uint32_t>(r.storage)});
                         for (auto const & [ibf, bin] : P.ub_merged[u])
                             jobs.push_back(
                                 insert_job{off[u], n, 0, static_cast<uint32_t>(ibf), static_cast<uint32_t>(bin)});
                     }
-                    run_jobs(h, jobs, 0, dv.as<uint64_t>(), h->stream);
+                    run_jobs(h, jobs, 0, dv.as<uint64_t>(), &dt, h->stream);
                 }
                 catch (...)
                 {
@@ -1068,7 +1533,7 @@ extern "C"
                 if (!input_fn || !offsets)
                     fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
                 std::vector<std::vector<uint64_t>> sets;
-                plan_inputs(*cfg, layout_text, input_fn, user, sets);
+                plan_inputs(*cfg, layout_text, input_fn, user, sets, nullptr);
                 offsets[0] = 0;
                 for (size_t u = 0; u < sets.size(); ++u)
                 {

@@ -9,12 +9,16 @@
 // and their C-ABI entry points.
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <exception>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
+#include "../../include/hibf_gb300_synthetic.h"
 #include "common.hpp"
 #include "count.cuh"
 #include "device.cuh"
@@ -354,6 +358,10 @@ struct hibf_gpu_agent
     uint32_t arrive_chunks{};
     uint64_t arrive_limit_ns{};
     uint32_t last_chunks{}; // chunks of the last host batch (0: not streamed)
+    // timeline of the last host batch: its start, each value chunk's copy done, results back (timing events)
+    cudaEvent_t tl_t0{}, tl_done{};
+    std::vector<cudaEvent_t> tl_chunk;
+    uint32_t tl_n{};
     hbuf h_roff, h_ids, h_cnt, h_ctrl, h_stats;
     std::vector<uint64_t> single_ids;
     std::vector<uint8_t> dense;
@@ -646,6 +654,20 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
     uint64_t tasks = std::max<uint64_t>(a->cap_tasks, nq * 4 + 1024);
     uint64_t results = std::max<uint64_t>(a->cap_results, nq * 4 + 1024);
     ensure_capacity(a, std::max<uint64_t>(nq, 1), tasks, results); // allocations synchronise: before any copy
+    uint32_t const n_tl = streamed ? static_cast<uint32_t>(qb.size() - 1) : 1u;
+    if (!a->tl_t0)
+    {
+        HG_CUDA(cudaEventCreate(&a->tl_t0));
+        HG_CUDA(cudaEventCreate(&a->tl_done));
+    }
+    while (a->tl_chunk.size() < n_tl)
+    {
+        cudaEvent_t e{};
+        HG_CUDA(cudaEventCreate(&e));
+        a->tl_chunk.push_back(e);
+    }
+    a->tl_n = 0;
+    HG_CUDA(cudaEventRecord(a->tl_t0, a->stream));
     HG_CUDA(cudaMemcpyAsync(a->in_qoff.p, qoff, (nq + 1) * 8, cudaMemcpyHostToDevice, a->stream));
     if (nq)
         HG_CUDA(cudaMemcpyAsync(a->in_thr.p, thr, nq * 8, cudaMemcpyHostToDevice, a->stream));
@@ -694,7 +716,9 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
                                             cudaMemcpyHostToDevice, a->copy_stream));
                 unsigned int const * src = counts + static_cast<size_t>(k) * kArrivalReplicas * kArrivalStride;
                 HG_CUDA(cudaMemcpyAsync(a->arrived.p, src, counter_bytes, cudaMemcpyHostToDevice, a->copy_stream));
+                HG_CUDA(cudaEventRecord(a->tl_chunk[k], a->copy_stream));
             }
+            a->tl_n = chunks;
             HG_CUDA(cudaEventRecord(a->ev_copied, a->copy_stream));
         }
         catch (...)
@@ -706,9 +730,12 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
         a->arrive_chunks = chunks;
         a->arrive_limit_ns = 10ull * 1000 * 1000 * 1000 + nv * 8 / 2; // 10 s + the copy at 2 GB/s
     }
-    else if (nv)
+    else
     {
-        HG_CUDA(cudaMemcpyAsync(a->in_values.p, values, nv * 8, cudaMemcpyHostToDevice, a->stream));
+        if (nv)
+            HG_CUDA(cudaMemcpyAsync(a->in_values.p, values, nv * 8, cudaMemcpyHostToDevice, a->stream));
+        HG_CUDA(cudaEventRecord(a->tl_chunk[0], a->stream));
+        a->tl_n = 1;
     }
     for (int attempt = 0;; ++attempt)
     {
@@ -749,6 +776,7 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
             HG_CUDA(cudaMemcpyAsync(a->h_cnt.p, width == 8 ? a->out_cnt.p : a->out_cntw.p, nr * width,
                                     cudaMemcpyDeviceToHost, a->stream));
     }
+    HG_CUDA(cudaEventRecord(a->tl_done, a->stream));
     HG_CUDA(cudaStreamSynchronize(a->stream));
 }
 
@@ -1591,6 +1619,83 @@ extern "C"
             });
     }
 
+    int hibf_gpu_hibf_digests(hibf_gpu_hibf * h, uint64_t * out, uint32_t threads)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(h->mu);
+                HG_CUDA(cudaDeviceSynchronize());
+                int dev = 0;
+                HG_CUDA(cudaGetDevice(&dev));
+                // IBFs largest first over the host threads; each thread folds its IBF's rows in order through a
+                // pinned chunk of whole rows
+                std::vector<uint64_t> order(h->n_ibfs);
+                for (uint64_t k = 0; k < h->n_ibfs; ++k)
+                    order[k] = k;
+                std::sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b)
+                          { return h->bin_words[a] * h->bin_size[a] > h->bin_words[b] * h->bin_size[b]; });
+                std::atomic<uint64_t> next{0};
+                std::exception_ptr error;
+                std::mutex error_lock;
+                auto worker = [&]
+                {
+                    try
+                    {
+                        HG_CUDA(cudaSetDevice(dev));
+                        cudaStream_t st{};
+                        HG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+                        uint64_t const chunk_bytes = 64ull << 20;
+                        void * buf = nullptr;
+                        if (cudaHostAlloc(&buf, chunk_bytes, cudaHostAllocDefault) != cudaSuccess)
+                        {
+                            cudaStreamDestroy(st);
+                            fail(HIBF_GPU_ERR_OUT_OF_MEMORY, "pinned staging buffer");
+                        }
+                        for (uint64_t i; (i = next.fetch_add(1)) < h->n_ibfs;)
+                        {
+                            uint64_t const k = order[i];
+                            uint64_t const bw = h->bin_words[k], rows = h->bin_size[k];
+                            uint64_t const per = std::max<uint64_t>(1, chunk_bytes / (bw * 8));
+                            uint64_t d = HG_DIGEST_INIT;
+                            for (uint64_t r = 0; r < rows; r += per)
+                            {
+                                uint64_t const n = std::min(per, rows - r);
+                                auto const * src = static_cast<char const *>(h->stores[k]->p) + r * h->row_words[k] * 8;
+                                HG_CUDA(cudaMemcpy2DAsync(buf, bw * 8, src, h->row_words[k] * 8, bw * 8, n,
+                                                          cudaMemcpyDeviceToHost, st));
+                                HG_CUDA(cudaStreamSynchronize(st));
+                                auto const * w = static_cast<uint64_t const *>(buf);
+                                for (uint64_t j = 0; j < n * bw; ++j)
+                                    d = hg_digest_step(d, w[j]);
+                            }
+                            out[k] = d;
+                        }
+                        cudaFreeHost(buf);
+                        cudaStreamDestroy(st);
+                    }
+                    catch (...)
+                    {
+                        std::lock_guard<std::mutex> g(error_lock);
+                        if (!error)
+                            error = std::current_exception();
+                    }
+                };
+                unsigned const nt = static_cast<unsigned>(std::min<uint64_t>(
+                    h->n_ibfs, threads ? threads : std::max(1u, std::thread::hardware_concurrency())));
+                std::vector<std::thread> pool;
+                for (unsigned t = 1; t < nt; ++t)
+                    pool.emplace_back(worker);
+                worker();
+                for (std::thread & t : pool)
+                    t.join();
+                if (error)
+                    std::rethrow_exception(error);
+            });
+    }
+
     int hibf_gpu_agent_create(hibf_gpu_hibf * h, hibf_gpu_agent ** out)
     {
         return guarded(
@@ -1650,6 +1755,13 @@ extern "C"
                     cudaGraphExecDestroy(a->graph);
                 cudaEventDestroy(a->ev_k0);
                 cudaEventDestroy(a->ev_k1);
+                if (a->tl_t0)
+                {
+                    cudaEventDestroy(a->tl_t0);
+                    cudaEventDestroy(a->tl_done);
+                }
+                for (cudaEvent_t e : a->tl_chunk)
+                    cudaEventDestroy(e);
                 if (a->copy_stream)
                 {
                     cudaStreamSynchronize(a->copy_stream);
@@ -1917,6 +2029,33 @@ extern "C"
                 *n = qb.size();
                 std::copy(qb.begin(), qb.begin() + static_cast<std::ptrdiff_t>(std::min<uint64_t>(cap, qb.size())),
                           first_queries);
+            });
+    }
+
+    int hibf_gpu_agent_last_timeline(hibf_gpu_agent const * a, double * out_ms, uint32_t cap, uint32_t * n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !n || (cap && !out_ms))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                if (!a->tl_t0 || a->tl_n == 0)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "the agent has not answered a host batch");
+                *n = a->tl_n + 3;
+                auto since = [&](cudaEvent_t e)
+                {
+                    float ms = 0;
+                    HG_CUDA(cudaEventElapsedTime(&ms, a->tl_t0, e));
+                    return static_cast<double>(ms);
+                };
+                std::vector<double> t;
+                for (uint32_t k = 0; k < a->tl_n; ++k)
+                    t.push_back(since(a->tl_chunk[k]));
+                t.push_back(since(a->ev_k0));
+                t.push_back(since(a->ev_k1));
+                t.push_back(since(a->tl_done));
+                for (uint32_t i = 0; i < std::min<uint32_t>(cap, *n); ++i)
+                    out_ms[i] = t[i];
             });
     }
 

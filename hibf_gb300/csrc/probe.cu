@@ -8,6 +8,7 @@
 
 #include <algorithm>
 
+#include "../../include/hibf_gb300_diagnostics.h"
 #include "common.hpp"
 
 namespace hibf_gb300

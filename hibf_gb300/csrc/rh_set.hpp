@@ -19,8 +19,28 @@
 #include <stdexcept>
 #include <vector>
 
+#if defined(__CUDACC__)
+#    define RH_HD __host__ __device__ __forceinline__
+#else
+#    define RH_HD inline
+#endif
+
 namespace hibf_gb300
 {
+
+// Home slot of `key` in a table with hash multiplier `mult` and slot mask `mask` (the idx half of rh_set::slot).
+// Iteration visits keys in non-decreasing home slot order, so this slot and the table's iteration order within one
+// home slot fix a key's rank.
+RH_HD uint64_t rh_home(uint64_t key, uint64_t mult, uint64_t mask)
+{
+    uint64_t h = key;
+    h ^= h >> 33;
+    h *= 0xff51afd7ed558ccdULL;
+    h ^= h >> 33;
+    h *= mult;
+    h ^= h >> 33;
+    return (h >> 5) & mask;
+}
 
 class rh_set
 {
@@ -90,6 +110,16 @@ public:
         for (size_t i = 0; i < n; ++i)
             if (info_[i] != 0)
                 f(keys_[i]);
+    }
+
+    uint64_t multiplier() const
+    {
+        return mult_;
+    }
+
+    uint64_t slot_mask() const
+    {
+        return mask_;
     }
 
     std::vector<uint64_t> ordered() const

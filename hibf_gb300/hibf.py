@@ -144,6 +144,12 @@ class hierarchical_interleaved_bloom_filter:
         N.call("hibf_gpu_hibf_download_words", self._h, k, out.ctypes.data, out.size)
         return out
 
+    def digests(self, threads: int = 0) -> np.ndarray:
+        """Per IBF the hg_digest_step fold of its words in the reference's order (hibf_gpu_hibf_digests)."""
+        out = np.zeros(max(self.n_ibfs, 1), np.uint64)
+        N.call("hibf_gpu_hibf_digests", self._h, out.ctypes.data, int(threads))
+        return out[:self.n_ibfs]
+
     def emplace(self, k: int, values, bin: int) -> None:
         v = _u64(values)
         N.call("hibf_gpu_hibf_emplace", self._h, k, v.ctypes.data, v.size, int(bin))

@@ -59,6 +59,12 @@ def unit(x: int) -> float:
     return (x >> 11) * (1.0 / 9007199254740992.0)
 
 
+def digest_step_np(h: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """hg_digest_step elementwise."""
+    with np.errstate(over="ignore"):
+        return mix64_np(h ^ mix64_np(x + np.uint64(GAMMA)))
+
+
 def digest(values) -> int:
     h = DIGEST_INIT
     for x in values:

@@ -17,6 +17,7 @@ Layouts were computed by the reference (tests/golden/make_golden.py) and are rea
 from __future__ import annotations
 
 import ctypes
+import time
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -43,6 +44,7 @@ class workload:
     n_queries: int
     query: S.query_spec
     layout_file: str | None
+    split_table_file: str | None = None
 
     def user_bin_offsets(self) -> np.ndarray:
         off = np.zeros(self.n_user_bins + 1, np.uint64)
@@ -57,6 +59,25 @@ class workload:
         if p.suffix == ".npz":
             return bytes(np.load(p)["layout"]).decode()
         return p.read_text()
+
+    def split_table(self, offsets: np.ndarray):
+        """How the reference chunks the split user bins of this layout for user bins of `offsets`: the committed
+        table of the full-size workload when its sizes are these, else a replay of the reference's hash-set
+        history (build.split_table.synthetic)."""
+        from . import build as B
+
+        if self.split_table_file is not None and (GOLDEN / self.split_table_file).exists():
+            a = dict(np.load(GOLDEN / self.split_table_file))
+            sizes = np.diff(offsets.astype(np.uint64))
+            if a["n_values"].size and np.array_equal(sizes[a["user_bin"].astype(np.int64)], a["n_values"]):
+                return B.split_table.from_arrays(a), "committed table (tests/golden/" + self.split_table_file + ")"
+        import os
+
+        t0 = time.perf_counter()
+        c = B.config(number_of_user_bins=self.n_user_bins, number_of_hash_functions=self.h, maximum_fpr=self.fpr,
+                     threads=os.cpu_count() or 1)
+        t = B.split_table.synthetic(c, self.layout_text(), self.query.seed, offsets)
+        return t, f"replayed on the host in {time.perf_counter() - t0:.1f} s"
 
     def query_offsets(self, first: int, n: int):
         q = self.query
@@ -82,9 +103,11 @@ class workload:
 HIBF64 = workload("hibf64", 64, S.SIZES_LOG_UNIFORM, 0.0, 0.0, 1000, 100000, 2, 0.05, 64, 10000,
                   S.query_spec(1, S.QUERIES_HALF_ONE_BIN, 250, 250, 0, 0, 1, 2, 64), "c1_reference.npz")
 HIBF8192 = workload("hibf8192", 8192, S.SIZES_LOG_NORMAL, 200000.0, 1.5, 1000, 50000000, 2, 0.05, 64, 1000000,
-                    S.query_spec(1, S.QUERIES_MIXED, 20, 2000, 70, 2, 7, 10, 8192), "c3_layout.txt")
+                    S.query_spec(1, S.QUERIES_MIXED, 20, 2000, 70, 2, 7, 10, 8192), "c3_layout.txt",
+                    "c3_split_table.npz")
 
 HIBF65536 = workload("hibf65536", 65536, S.SIZES_LOG_NORMAL, 100000.0, 2.0, 500, 200000000, 3, 0.02, 256, 10000000,
-                     S.query_spec(1, S.QUERIES_MIXED, 50, 5000, 70, 2, 6, 10, 65536), "c4_layout_sum.txt")
+                     S.query_spec(1, S.QUERIES_MIXED, 50, 5000, 70, 2, 6, 10, 65536), "c4_layout_sum.txt",
+                     "c4_split_table.npz")
 
 WORKLOADS = {w.name: w for w in (HIBF64, HIBF8192, HIBF65536)}

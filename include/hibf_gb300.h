@@ -169,6 +169,11 @@ int hibf_gpu_ibf_load(char const * path, hibf_gpu_ibf ** out);
 int hibf_gpu_hibf_save(hibf_gpu_hibf * h, char const * path);
 int hibf_gpu_hibf_load(char const * path, hibf_gpu_hibf ** out);
 int hibf_gpu_hibf_download_words(hibf_gpu_hibf * h, uint64_t ibf, uint64_t * words, uint64_t n_words);
+/* Checksum of every IBF's bit store in the reference's word order (the words of ibf_vector[k]'s bit_vector,
+ * interleaved_bloom_filter.hpp:146): out[k] = fold of hg_digest_step over the words from HG_DIGEST_INIT
+ * (include/hibf_gb300_synthetic.h), for comparing a device index with a reference build without moving it.  IBFs are
+ * folded on `threads` host threads (0: all). */
+int hibf_gpu_hibf_digests(hibf_gpu_hibf * h, uint64_t * out, uint32_t threads);
 
 /* ------------------------------------------------------------------------------------------------------------ */
 /* Build from a layout (hierarchical_interleaved_bloom_filter(config&, layout::layout const&),                   */
@@ -195,10 +200,43 @@ int hibf_gpu_sink_push(hibf_gpu_sink * sink, uint64_t const * values, uint64_t n
 
 int hibf_gpu_hibf_build(hibf_gpu_build_config const * cfg, char const * layout_text, hibf_gpu_input_fn input_fn,
                         void * user, hibf_gpu_hibf ** out);
+/* Split tables.  The reference splits a user bin over k technical bins in chunks of ceil(n / k) values taken in its
+ * hash set's iteration order (src/build/insert_into_ibf.cpp:28-47; robin_hood::unordered_flat_set, whose order
+ * depends on the set's whole history in hierarchical_build, src/hierarchical_interleaved_bloom_filter.cpp:39-171).
+ * That order visits values in non-decreasing home slot of the set's table, so a split table keeps, per split user
+ * bin, only the set's hash multiplier and slot mask and, per chunk boundary, the home slot of the value at the
+ * boundary and the values of that slot ranked before it; the device places every value from it.  A table is
+ * computed by replaying the reference's set history on the host (config::threads threads; every split user bin's
+ * values and every set that can affect one are inserted, nothing else), or imported from arrays exported earlier:
+ *   user_bin[n_split] ascending, n_values[n_split], mult[n_split], mask[n_split], bnd_off[n_split + 1] (boundaries
+ *   of entry i: [bnd_off[i], bnd_off[i+1])), bnd_home[n_boundaries], before_off[n_boundaries + 1], before[n_before].
+ * A table belongs to one layout and one set of user bin sizes; builds check both. */
+typedef struct hibf_gpu_split_table hibf_gpu_split_table;
+int hibf_gpu_split_table_synthetic(hibf_gpu_build_config const * cfg, char const * layout_text, uint64_t seed,
+                                   uint64_t const * user_bin_offsets, hibf_gpu_split_table ** out);
+/* The table of an input_fn build (hibf_gpu_hibf_build's inputs: user bins read once, split user bins in input order). */
+int hibf_gpu_split_table_inputs(hibf_gpu_build_config const * cfg, char const * layout_text, hibf_gpu_input_fn input_fn,
+                                void * user, hibf_gpu_split_table ** out);
+int hibf_gpu_split_table_sizes(hibf_gpu_split_table const * t, uint64_t * n_split, uint64_t * n_boundaries,
+                               uint64_t * n_before);
+int hibf_gpu_split_table_export(hibf_gpu_split_table const * t, uint64_t * user_bin, uint64_t * n_values,
+                                uint64_t * mult, uint64_t * mask, uint64_t * bnd_off, uint64_t * bnd_home,
+                                uint64_t * before_off, uint64_t * before);
+int hibf_gpu_split_table_import(uint64_t n_split, uint64_t n_boundaries, uint64_t n_before, uint64_t const * user_bin,
+                                uint64_t const * n_values, uint64_t const * mult, uint64_t const * mask,
+                                uint64_t const * bnd_off, uint64_t const * bnd_home, uint64_t const * before_off,
+                                uint64_t const * before, hibf_gpu_split_table ** out);
+/* Host lookup: chunks[j] = the technical bin offset (from the user bin's storage bin) of values[j] of a split user bin. */
+int hibf_gpu_split_table_chunks(hibf_gpu_split_table const * t, uint64_t user_bin, uint64_t const * values, uint64_t n,
+                                uint64_t * chunks);
+void hibf_gpu_split_table_destroy(hibf_gpu_split_table * t);
 /* The same build for the seeded synthetic workloads of include/hibf_gb300_synthetic.h: user bin u holds stream
- * positions [user_bin_offsets[u], user_bin_offsets[u+1]) of the splitmix64 stream `seed`, generated on the device. */
+ * positions [user_bin_offsets[u], user_bin_offsets[u+1]) of the splitmix64 stream `seed`, generated on the device.
+ * Split user bins are chunked by `table` (NULL: computed first, as hibf_gpu_split_table_synthetic does), so every
+ * IBF's bit store is the reference's. */
 int hibf_gpu_hibf_build_synthetic(hibf_gpu_build_config const * cfg, char const * layout_text, uint64_t seed,
-                                  uint64_t const * user_bin_offsets, hibf_gpu_hibf ** out);
+                                  uint64_t const * user_bin_offsets, hibf_gpu_split_table const * table,
+                                  hibf_gpu_hibf ** out);
 /* interleaved_bloom_filter(config&, max_bin_elements) (interleaved_bloom_filter.hpp:241, src/interleaved_bloom_filter.cpp:
  * 55-117): bin count = number_of_user_bins; bin size from max_bin_elements, or -- when 0 -- from the exact distinct
  * count of the user bin with the largest HyperLogLog estimate (sketch_bits), the first such bin on ties; then user
@@ -286,10 +324,6 @@ int hibf_gpu_agent_fetch_results(hibf_gpu_agent * a, uint64_t n_queries, int mod
                                  uint64_t const ** result_offsets, uint64_t const ** result_ids,
                                  void const ** result_counts);
 int hibf_gpu_agent_status(hibf_gpu_agent * a);
-/* Hint for the L2 fetch granularity of the calling process's CUDA context (cudaLimitMaxL2FetchGranularity, bytes in
- * [0, 128]).  Random 8-32 byte row reads waste bandwidth when L2 fetches more than a sector; the limit applies to
- * every kernel of the context and ends with it. */
-int hibf_gpu_set_l2_fetch_granularity(int bytes);
 /* Failure-detection self-test of the work queue's bounded wait: runs the persistent kernel with one announced task
  * that is never pushed, so every worker's wait must expire after limit_ms and the batch must report
  * HIBF_GPU_ERR_TIMEOUT through the device status word.  Returns OK when it did; the context stays usable. */
@@ -304,6 +338,11 @@ int hibf_gpu_agent_replay(hibf_gpu_agent * a);
 int hibf_gpu_agent_kernel_ms(hibf_gpu_agent * a, float * ms);
 /* Number of chunks in which the agent's last host batch streamed its values (0: copied whole before the launch). */
 int hibf_gpu_agent_input_chunks(hibf_gpu_agent const * a, uint32_t * chunks);
+/* Timeline of the agent's last host batch (hibf_gpu_agent_query_batch), in ms from the call's first device work:
+ * the time each value chunk's copy completed (one entry when the values were copied whole), then the persistent
+ * kernel's start and end, then the time the results were back in host memory.  *n receives the entry count
+ * (chunks + 3); at most `cap` entries are written. */
+int hibf_gpu_agent_last_timeline(hibf_gpu_agent const * a, double * out_ms, uint32_t cap, uint32_t * n);
 /* (diagnostic, no device needed) The chunk boundaries a host batch with these query offsets would stream in: the
  * first query of every chunk, then n_queries; every boundary but 0 and n_queries starts a 32-byte sector
  * (query_offsets[q] % 4 == 0).  *n receives the count (2 or fewer: not streamed); at most cap entries are written. */
@@ -448,10 +487,6 @@ int hibf_gpu_server_open_loop(hibf_gpu_server * s, uint64_t const * pool_values,
                               uint64_t max_request_queries, double thr_lo, double thr_hi, uint64_t seed,
                               double out[8]);
 
-/* Diagnostic: the device's rate of independent random 8-byte reads over a buffer of footprint_bytes (region_bytes:
- * reads confined to windows of that size, 0 = the whole buffer).  The practical ceiling for the query kernels'
- * random row reads, which the copy-bandwidth peak overstates. */
-int hibf_gpu_probe_random_reads(uint64_t footprint_bytes, uint64_t region_bytes, double * reads_per_s);
 
 /* ============================================================================================================ */
 /* Seeded synthetic workloads (include/hibf_gb300_synthetic.h), for benchmarks and tests                        */

@@ -55,6 +55,13 @@ _WIDTH_DTYPE = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}
 # --------------------------------------------------------------------------------------------------------------
 # C restatement
 # --------------------------------------------------------------------------------------------------------------
+class QuerySpec(ctypes.Structure):
+    """hg_query_spec (include/hibf_gb300_synthetic.h)."""
+    _fields_ = [("seed", u64), ("law", ctypes.c_int), ("len_lo", u64), ("len_hi", u64), ("mix_pct", ctypes.c_uint32),
+                ("noise_pct", ctypes.c_uint32), ("thr_num", ctypes.c_uint32), ("thr_den", ctypes.c_uint32),
+                ("n_user_bins", u64)]
+
+
 class Oracle:
     def __init__(self, path: Path = ORACLE_SO):
         if not Path(path).exists():
@@ -93,6 +100,31 @@ class Oracle:
         L.orc_hibf_membership_batch.argtypes = [vp, vp, vp, u64, vp, ctypes.c_int, vp, vp, vp]
         L.orc_hibf_run_queries.restype = u64
         L.orc_hibf_run_queries.argtypes = [vp, vp, vp, u64, vp, vp, ctypes.c_int, ctypes.c_int, vp]
+        L.orc_hibf_fill_synthetic.restype = ctypes.c_int
+        L.orc_hibf_fill_synthetic.argtypes = [vp, u64, vp, u64, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int]
+        L.orc_hibf_digests.argtypes = [vp, vp, ctypes.c_int]
+        L.orc_synth_user_bin_offsets.argtypes = [u64, ctypes.c_int, ctypes.c_double, ctypes.c_double, u64, u64, u64,
+                                                 vp]
+        L.orc_synth_queries.argtypes = [ctypes.POINTER(QuerySpec), vp, u64, u64, vp, vp, vp, ctypes.c_int]
+
+    # -- synthetic workloads (include/hibf_gb300_synthetic.h) ---------------------------------------------
+    def synth_user_bin_offsets(self, seed, law, p0, p1, lo, hi, n) -> np.ndarray:
+        out = np.zeros(n + 1, np.uint64)
+        self.lib.orc_synth_user_bin_offsets(seed, law, p0, p1, lo, hi, n, _ptr(out))
+        return out
+
+    def synth_queries(self, spec, ub_offsets, first, n, threads=0):
+        """(values, query offsets, thresholds) of queries first .. first+n-1; `spec` has the fields of
+        hg_query_spec (hibf_gb300.synthetic.query_spec)."""
+        q = QuerySpec(spec.seed, spec.law, spec.len_lo, spec.len_hi, spec.mix_pct, spec.noise_pct, spec.thr_num,
+                      spec.thr_den, spec.n_user_bins)
+        o = _u64(ub_offsets)
+        qo, thr = np.zeros(n + 1, np.uint64), np.zeros(max(n, 1), np.uint64)
+        self.lib.orc_synth_queries(ctypes.byref(q), _ptr(o), first, n, _ptr(qo), _ptr(thr), None, 0)
+        v = np.zeros(max(int(qo[-1]), 1), np.uint64)
+        self.lib.orc_synth_queries(ctypes.byref(q), _ptr(o), first, n, _ptr(qo), _ptr(thr), _ptr(v),
+                                   threads or os.cpu_count())
+        return v[:int(qo[-1])], qo, thr[:n]
 
     # -- IBF ---------------------------------------------------------------------------------------------
     def ibf(self, bins, bin_size, hash_funs=2, track_occupancy=False) -> "OracleIBF":
@@ -237,6 +269,23 @@ class OracleHIBF:
     def emplace(self, k, values, bin_):
         v = _u64(values)
         self.L.orc_ibf_emplace_one_bin(self._ibf_ptr(k), _ptr(v), v.size, int(bin_))
+
+    def fill_synthetic(self, seed, offsets, split, threads=0):
+        """Every synthetic user bin into its technical bins (split ones chunked by the split-table arrays `split`,
+        the fields of hibf_gb300.build.SPLIT_TABLE_FIELDS) and into every ancestor's merged bin."""
+        o = _u64(offsets)
+        a = {k: _u64(split[k]) for k in ("user_bin", "mult", "mask", "bnd_off", "bnd_home", "before_off", "before")}
+        rc = self.L.orc_hibf_fill_synthetic(self.h, int(seed), _ptr(o), a["user_bin"].size,
+                                            *[_ptr(a[k]) for k in ("user_bin", "mult", "mask", "bnd_off",
+                                                                   "bnd_home", "before_off", "before")],
+                                            threads or os.cpu_count())
+        if rc != 0:
+            raise ValueError(f"orc_hibf_fill_synthetic: {rc}")
+
+    def digests(self, threads=0) -> np.ndarray:
+        out = np.zeros(max(self.n_ibfs, 1), np.uint64)
+        self.L.orc_hibf_digests(self.h, _ptr(out), threads or os.cpu_count())
+        return out[:self.n_ibfs]
 
     def membership_for(self, values, threshold, sort=True) -> np.ndarray:
         v = _u64(values)

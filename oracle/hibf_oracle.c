@@ -694,3 +694,213 @@ uint64_t orc_hibf_run_queries(orc_hibf const * h, uint64_t const * values, uint6
         *checksum = sum;
     return pairs;
 }
+
+/* ---------------------------------------------------------------------------------------------------------- */
+/* Filling an HIBF with the seeded synthetic user bins (include/hibf_gb300_synthetic.h).                       */
+/* ---------------------------------------------------------------------------------------------------------- */
+
+/* Home slot of `key` in a robin_hood::unordered_flat_set<uint64_t> table with hash multiplier `mult` and slot mask
+ * `mask` (include/hibf/contrib/robin_hood.hpp: hash_int then the keyToIdx multiply-shift). */
+static uint64_t orc_rh_home(uint64_t key, uint64_t mult, uint64_t mask)
+{
+    uint64_t h = key;
+    h ^= h >> 33;
+    h *= 0xff51afd7ed558ccdULL;
+    h ^= h >> 33;
+    h *= mult;
+    h ^= h >> 33;
+    return (h >> 5) & mask;
+}
+
+/* The chunk of value v of a split user bin: the number of chunk boundaries of its split table entry that v lies at
+ * or after.  The reference's chunks (src/build/insert_into_ibf.cpp:34-47) take its set's iteration order, which
+ * visits keys in non-decreasing home slot; a boundary is the home slot of the key at its rank and the keys of that
+ * slot ranked before it. */
+static uint64_t orc_split_chunk(uint64_t v, uint64_t mult, uint64_t mask, uint64_t const * home, uint64_t n_bnd,
+                                uint64_t const * before_off, uint64_t const * before)
+{
+    uint64_t const h = orc_rh_home(v, mult, mask);
+    uint64_t lo = 0, hi = n_bnd;
+    while (lo < hi)
+    {
+        uint64_t const mid = (lo + hi) / 2u;
+        if (home[mid] < h)
+            lo = mid + 1u;
+        else
+            hi = mid;
+    }
+    uint64_t c = lo;
+    for (; c < n_bnd && home[c] == h; ++c)
+    {
+        int in = 0;
+        for (uint64_t j = before_off[c]; j < before_off[c + 1u]; ++j)
+            in |= before[j] == v;
+        if (in)
+            break;
+    }
+    return c;
+}
+
+static void orc_ibf_emplace_atomic(orc_ibf * ibf, uint64_t value, uint64_t bin)
+{
+    for (uint64_t i = 0; i < ibf->hash_funs; ++i)
+    {
+        uint64_t const idx = orc_hash_and_fit(ibf, value, orc_seeds[i]) + bin;
+        __atomic_fetch_or(&ibf->data[idx >> 6], 1ULL << (idx & 63u), __ATOMIC_RELAXED);
+    }
+}
+
+int orc_hibf_fill_synthetic(orc_hibf * h, uint64_t seed, uint64_t const * offsets, uint64_t n_split,
+                            uint64_t const * split_user_bin, uint64_t const * split_mult,
+                            uint64_t const * split_mask, uint64_t const * bnd_off, uint64_t const * bnd_home,
+                            uint64_t const * before_off, uint64_t const * before, int threads)
+{
+    uint64_t const nub = h->n_user_bins;
+    uint64_t * leaf = malloc(nub * sizeof(uint64_t));
+    uint64_t * first = malloc(nub * sizeof(uint64_t));
+    uint64_t * ntb = calloc(nub, sizeof(uint64_t));
+    int64_t * split = malloc(nub * sizeof(int64_t));
+    uint64_t * up_ibf = malloc(h->n_ibfs * sizeof(uint64_t));
+    uint64_t * up_bin = malloc(h->n_ibfs * sizeof(uint64_t));
+    int rc = 0;
+    if (!leaf || !first || !ntb || !split || !up_ibf || !up_bin)
+    {
+        rc = -2;
+        goto done;
+    }
+    for (uint64_t k = 0; k < h->n_ibfs; ++k)
+        up_ibf[k] = UINT64_MAX;
+    for (uint64_t u = 0; u < nub; ++u)
+        split[u] = -1;
+    /* placements from the tables: a user bin's technical bins, and every child IBF's parent merged bin */
+    for (uint64_t k = 0; k < h->n_ibfs; ++k)
+        for (uint64_t b = 0; b < h->ibfs[k].bins; ++b)
+        {
+            uint64_t const i = h->tb_offsets[k] + b;
+            uint64_t const u = h->user_bin[i];
+            if (u == ORC_MERGED)
+            {
+                if (h->next_ibf[i] != k && h->next_ibf[i] < h->n_ibfs)
+                {
+                    up_ibf[h->next_ibf[i]] = k;
+                    up_bin[h->next_ibf[i]] = b;
+                }
+            }
+            else if (u < nub)
+            {
+                if (ntb[u] == 0)
+                {
+                    leaf[u] = k;
+                    first[u] = b;
+                }
+                ++ntb[u];
+            }
+        }
+    for (uint64_t i = 0; i < n_split; ++i)
+    {
+        if (split_user_bin[i] >= nub)
+        {
+            rc = -1;
+            goto done;
+        }
+        split[split_user_bin[i]] = (int64_t)i;
+    }
+    for (uint64_t u = 0; u < nub; ++u)
+        if (ntb[u] == 0 || (ntb[u] > 1 && split[u] < 0))
+        {
+            rc = -1; /* a user bin without bins, or split without a table entry */
+            goto done;
+        }
+    {
+        uint64_t const total = offsets[nub];
+        uint64_t const block = 1u << 16;
+        uint64_t const nblocks = (total + block - 1u) / block;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads > 0 ? threads : omp_get_max_threads())
+        for (uint64_t blk = 0; blk < nblocks; ++blk)
+        {
+            uint64_t p = blk * block;
+            uint64_t const end = p + block < total ? p + block : total;
+            /* the user bin holding position p: last u with offsets[u] <= p */
+            uint64_t lo = 0, hi = nub;
+            while (hi - lo > 1u)
+            {
+                uint64_t const mid = (lo + hi) / 2u;
+                if (offsets[mid] <= p)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            uint64_t u = lo;
+            for (; p < end; ++p)
+            {
+                while (offsets[u + 1u] <= p)
+                    ++u;
+                uint64_t const v = hg_stream_at(seed, p);
+                uint64_t c = 0;
+                if (split[u] >= 0)
+                {
+                    uint64_t const s = (uint64_t)split[u];
+                    c = orc_split_chunk(v, split_mult[s], split_mask[s], bnd_home + bnd_off[s],
+                                        bnd_off[s + 1u] - bnd_off[s], before_off + bnd_off[s], before);
+                }
+                uint64_t k = leaf[u];
+                orc_ibf_emplace_atomic(&h->ibfs[k], v, first[u] + c);
+                while (up_ibf[k] != UINT64_MAX)
+                {
+                    uint64_t const b = up_bin[k];
+                    k = up_ibf[k];
+                    orc_ibf_emplace_atomic(&h->ibfs[k], v, b);
+                }
+            }
+        }
+    }
+done:
+    free(leaf);
+    free(first);
+    free(ntb);
+    free(split);
+    free(up_ibf);
+    free(up_bin);
+    return rc;
+}
+
+void orc_hibf_digests(orc_hibf const * h, uint64_t * out, int threads)
+{
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads > 0 ? threads : omp_get_max_threads())
+    for (uint64_t k = 0; k < h->n_ibfs; ++k)
+    {
+        uint64_t d = HG_DIGEST_INIT;
+        for (uint64_t i = 0; i < h->ibfs[k].nwords; ++i)
+            d = hg_digest_step(d, h->ibfs[k].data[i]);
+        out[k] = d;
+    }
+}
+
+/* The seeded synthetic workloads' user bin offsets and queries (include/hibf_gb300_synthetic.h), generated on the
+ * host so that the CPU arm of the benchmark needs nothing but this file. */
+void orc_synth_user_bin_offsets(uint64_t seed, int law, double p0, double p1, uint64_t lo, uint64_t hi, uint64_t n,
+                                uint64_t * offsets)
+{
+    offsets[0] = 0;
+    for (uint64_t i = 0; i < n; ++i)
+        offsets[i + 1] = offsets[i] + hg_user_bin_size(seed, law, p0, p1, lo, hi, i);
+}
+
+void orc_synth_queries(hg_query_spec const * q, uint64_t const * ub_offsets, uint64_t first, uint64_t n,
+                       uint64_t * qoffsets, uint64_t * thresholds, uint64_t * values, int threads)
+{
+    if (!values)
+    {
+        qoffsets[0] = 0;
+        for (uint64_t i = 0; i < n; ++i)
+        {
+            uint64_t const len = hg_query_length(q, first + i);
+            qoffsets[i + 1] = qoffsets[i] + len;
+            thresholds[i] = hg_query_threshold(q, len);
+        }
+        return;
+    }
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads > 0 ? threads : omp_get_max_threads())
+    for (uint64_t i = 0; i < n; ++i)
+        hg_query_values(q, ub_offsets, first + i, values + qoffsets[i]);
+}

@@ -113,6 +113,28 @@ uint64_t orc_hibf_run_queries(orc_hibf const * h, uint64_t const * values, uint6
                               uint16_t const * mem_thresholds, uint64_t const * cnt_thresholds, int mode,
                               int threads, uint64_t * checksum);
 
+/* Fills the HIBF (tables already set) with the seeded synthetic user bins: user bin u = positions
+ * [offsets[u], offsets[u+1]) of the splitmix64 stream `seed`, inserted into its own technical bins and the merged bin
+ * of every ancestor IBF, as the reference's build inserts them (src/hierarchical_interleaved_bloom_filter.cpp:40-171,
+ * src/build/insert_into_ibf.cpp:28-84).  A user bin over several technical bins is chunked by its split-table entry
+ * (the layout of include/hibf_gb300.h, hibf_gpu_split_table_*).  0 on success, -1 when the tables and the split
+ * table do not fit together, -2 out of memory. */
+int orc_hibf_fill_synthetic(orc_hibf * h, uint64_t seed, uint64_t const * offsets, uint64_t n_split,
+                            uint64_t const * split_user_bin, uint64_t const * split_mult,
+                            uint64_t const * split_mask, uint64_t const * bnd_off, uint64_t const * bnd_home,
+                            uint64_t const * before_off, uint64_t const * before, int threads);
+/* out[k] = hg_digest_step fold over IBF k's words from HG_DIGEST_INIT. */
+void orc_hibf_digests(orc_hibf const * h, uint64_t * out, int threads);
+
+/* The synthetic workloads' generators on the host: offsets[0..n] of the user bins (hg_user_bin_size), and queries
+ * first .. first+n-1 -- with values == NULL their offsets (n + 1) and thresholds, else their values
+ * (hg_query_values). */
+struct hg_query_spec;
+void orc_synth_user_bin_offsets(uint64_t seed, int law, double p0, double p1, uint64_t lo, uint64_t hi, uint64_t n,
+                                uint64_t * offsets);
+void orc_synth_queries(struct hg_query_spec const * q, uint64_t const * ub_offsets, uint64_t first, uint64_t n,
+                       uint64_t * qoffsets, uint64_t * thresholds, uint64_t * values, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,9 @@ them through oracle/ref_driver.cpp:
                      estimate, then its exact count), bit store digest, counts, for several configs.
   c1_reference.npz   the 64-user-bin workload (log-uniform [1e3, 1e5], h=2, fpr 0.05, tmax 64): layout, per-IBF
                      digests and tables, 10,000 queries' outputs digests.
+  ref_c3_<s>.npz     the reference's build of the 8,192-user-bin workload from c3_layout.txt with every user bin at
+  ref_c4_<s>.npz     scale s (1 = full size), and of the 65,536-user-bin one from c4_layout_sum.txt: tables and
+                     per-IBF digests (targets refc3, refc3s, refc4s, refc4m; minutes each, not in the default set).
 
 Nothing here is read by the product; tests compare the oracle and the GPU path against these files.
 """
@@ -426,6 +429,30 @@ def make_c4_layout(R: Reference, estimate_union=True):
     print(f"{name}: {time.time() - t0:.0f}s")
 
 
+def make_ref_build(R: Reference, name: str, scale: float):
+    """The reference's own build of a benchmark workload from its committed layout, every user bin at `scale` of its
+    size (the same sizes as bench.py --scale), streamed from the generator: its tables (in the reference's IBF
+    numbering) and per-IBF digests of the bit words.  The device builds are compared with these by path of merged
+    bins (tests/test_build_gpu.py, bench.py).  Full size for 8,192 user bins: 4.9e9 values, 13.4 GB of bit words,
+    about 7 minutes on 8 threads."""
+    from hibf_gb300.workloads import WORKLOADS
+
+    wl = WORKLOADS[name]
+    sizes = S.user_bin_sizes(1, wl.n_user_bins, wl.size_law, wl.size_p0, wl.size_p1, wl.size_lo, wl.size_hi)
+    if scale != 1.0:
+        sizes = np.maximum(1, np.floor(sizes.astype(np.float64) * scale)).astype(np.uint64)
+    offs = S.offsets_of(sizes)
+    cfg = ref_cfg(wl.n_user_bins, h=wl.h, fpr=wl.fpr, tmax=wl.tmax, threads=8, sketch_bits=12)
+    t0 = time.time()
+    H = R.hibf(cfg, None, offs, seed=wl.query.seed, synthetic=True, layout=wl.layout_text())
+    T = H.tables(with_words=False)
+    tag = {"hibf8192": "c3", "hibf65536": "c4"}[name]
+    out = OUT / f"ref_{tag}_{scale:g}.npz"
+    np.savez_compressed(out, ub_offsets=offs, scale=np.array([scale]),
+                        **{k: T[k] for k in ("bins", "bin_size", "hash_funs", "next_ibf", "user_bin", "digests")})
+    print(f"{out.name}: {len(T['bins'])} IBFs, {int(offs[-1])} values, {time.time() - t0:.0f}s")
+
+
 def main(argv):
     build_reference()
     R = Reference()
@@ -459,6 +486,15 @@ def main(argv):
         make_c4_layout(R)
     if "c4sum" in which:  # not in the default set
         make_c4_layout(R, estimate_union=False)
+    # the reference's builds of the benchmark workloads (not in the default set: minutes each)
+    if "refc3" in which:
+        make_ref_build(R, "hibf8192", 1.0)
+    if "refc3s" in which:
+        make_ref_build(R, "hibf8192", 0.05)
+    if "refc4s" in which:
+        make_ref_build(R, "hibf65536", 0.02)
+    if "refc4m" in which:
+        make_ref_build(R, "hibf65536", 0.1)
 
 
 if __name__ == "__main__":

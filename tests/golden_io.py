@@ -74,3 +74,68 @@ def ibf_config_cases():
         d["index"] = i
         out.append(d)
     return out
+
+
+def c1_reference():
+    """The 64-user-bin workload as the reference built and queried it (make_golden.py make_c1): tables, per-IBF
+    digests and, for 10,000 queries of 250 values at threshold 125, membership_for + sort_results and
+    counting_agent<uint16_t>::bulk_count summarised per query (mem_len, mem_digest, cnt_nnz, cnt_digest)."""
+    from hibf_gb300 import synthetic as S
+
+    z = np.load(GOLDEN / "c1_reference.npz")
+    d = {k: z[k] for k in z.files}
+    d["layout_text"] = bytes(d["layout"]).decode()
+    d["n_ub"] = 64
+    spec = S.query_spec(1, S.QUERIES_HALF_ONE_BIN, 250, 250, 0, 0, 1, 2, 64)
+    d["q_values"], d["q_offsets"], thr = S.queries(spec, d["ub_offsets"], 0, 10000)
+    assert np.array_equal(thr, d["thresholds"])
+    return d
+
+
+def fold_digests(offsets, *columns):
+    """Per segment [offsets[i], offsets[i+1]) the hg_digest_step fold over its rows, each row contributing its
+    columns in order (the per-query summaries of the reference driver's ref_hibf_query_batch)."""
+    from hibf_gb300 import synthetic as S
+
+    offsets = np.asarray(offsets, dtype=np.int64)
+    n = offsets.size - 1
+    d = np.full(n, S.DIGEST_INIT, np.uint64)
+    lens = np.diff(offsets)
+    for j in range(int(lens.max()) if n else 0):
+        sel = np.nonzero(lens > j)[0]
+        pos = offsets[sel] + j
+        for c in columns:
+            d[sel] = S.digest_step_np(d[sel], np.asarray(c)[pos].astype(np.uint64))
+    return d, lens.astype(np.uint64)
+
+
+def oracle_hibf_from_inputs(oracle, t, offs, vals):
+    """The C oracle's HIBF with tables `t` (the reference's numbering) filled from the builder's insertion order
+    (user bin u = vals[offs[u]:offs[u+1]], split user bins in chunk order): each user bin into its own technical
+    bins in chunks of ceil(n / bins), and whole into the merged bin of every ancestor IBF."""
+    bins = np.asarray(t["bins"]).astype(np.int64)
+    tb_off = np.concatenate([[0], np.cumsum(bins)])
+    nxt, ub = t["next_ibf"], t["user_bin"]
+    O = oracle.hibf({k: t[k] for k in ("n_user_bins", "bins", "bin_size", "hash_funs", "next_ibf", "user_bin")})
+    parent, leaf = {}, {}
+    for k in range(bins.size):
+        for tb in range(int(bins[k])):
+            c, u = int(nxt[tb_off[k] + tb]), int(ub[tb_off[k] + tb])
+            if u == 2**64 - 1 and c != k:
+                parent[c] = (k, tb)
+            elif u < 2**64 - 2:
+                leaf.setdefault(u, (k, []))[1].append(tb)
+    for u in range(offs.size - 1):
+        v = vals[int(offs[u]):int(offs[u + 1])]
+        k, tbs = leaf[u]
+        first, ntb = min(tbs), len(tbs)
+        chunk = -(-v.size // ntb) if v.size else 1
+        for c in range(ntb):
+            part = v[c * chunk:(c + 1) * chunk]
+            if part.size:
+                O.emplace(k, part, first + c)
+        while k in parent:
+            k, tb = parent[k]
+            if v.size:
+                O.emplace(k, v, tb)
+    return O

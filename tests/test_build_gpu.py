@@ -1,10 +1,10 @@
 """GPU build from a layout (hibf_gpu_hibf_build / _build_synthetic) against the reference's own builds.
 
 For the layouts the reference computed (tests/golden), the device build must reproduce, for every IBF matched by its
-path of merged bins: the bin count, bin size and bin-to-user-bin table, and -- for IBFs that store no split user
-bin -- the exact bit words (digest).  IBFs with split user bins differ from the reference only in which split bin a
-value lands in (stream order vs the reference's hash-set order); for them every inserted value must be found in its
-user bin's bins, and query results are checked against the C oracle run on the downloaded bits.
+path of merged bins: the bin count, bin size and bin-to-user-bin table, and the exact bit words (digest), split user
+bins included (both builds chunk them in the reference's hash-set order, through a split table); query results are
+also checked against the C oracle run on the downloaded bits.  The benchmark workloads are checked the same way at
+reduced scale against the reference's own builds of them (tests/golden/ref_c3_*.npz, ref_c4_*.npz).
 """
 
 import numpy as np
@@ -59,8 +59,12 @@ def test_build_synthetic_matches_reference(gpu_lib, oracle, name):
     d = G.hibf_case(name)
     seed = int(d["synthetic_seed"][0])
     H = B.build_synthetic(_cfg(d), d["layout_text"], seed, d["ub_offsets"])
-    _compare_with_reference(H, d)
+    assert _compare_with_reference(H, d, every_ibf=True) == len(d["bins"])
     _queries_vs_oracle(H, oracle, d)
+    # the same build from an exported and re-imported split table
+    table = B.split_table.from_arrays(B.split_table.synthetic(_cfg(d), d["layout_text"], seed, d["ub_offsets"]).arrays())
+    H2 = B.build_synthetic(_cfg(d), d["layout_text"], seed, d["ub_offsets"], table)
+    np.testing.assert_array_equal(H2.digests(), H.digests())
     # no false negatives: every value of every user bin is counted in its user bin
     offs = d["ub_offsets"]
     ca = H.counting_agent(4)
@@ -104,14 +108,57 @@ def test_build_matches_reference_unit_expectations(gpu_lib):
         assert a.membership_for(np.arange(s + 5, s + 9), 4).tolist() == [ub]
 
 
-def test_build_c1_structure(gpu_lib):
-    """The 64-user-bin workload built from the reference's layout: same IBF sizes and tables as the reference."""
-    z = np.load(G.GOLDEN / "c1_reference.npz")
+def _digests_by_path(t, digests):
+    return {path: int(digests[k]) for path, (_b, _s, _r, k) in canonical(t).items()}
+
+
+def _same_index_as_reference(H, ref):
+    """Every IBF of H (tables and bit words, matched by path of merged bins) equals the reference build `ref`."""
+    rt = dict(bins=ref["bins"], bin_size=ref["bin_size"], next_ibf=ref["next_ibf"], user_bin=ref["user_bin"])
+    want, got = canonical(rt), canonical(H.tables())
+    assert {p: v[:3] for p, v in want.items()} == {p: v[:3] for p, v in got.items()}
+    assert _digests_by_path(H.tables(), H.digests()) == _digests_by_path(rt, ref["digests"])
+
+
+def test_c1_matches_reference(gpu_lib):
+    """The 64-user-bin workload (BASELINE config 1), built from the reference's layout both through input_fn and
+    from the generator: every IBF holds the reference's bits, and all 10,000 queries answer as the reference did --
+    membership_for + sort_results at t = 125 and counting_agent<uint16_t>::bulk_count at t = 125, compared per query
+    by length and digest (hierarchical_interleaved_bloom_filter.hpp:424-439, 549-566)."""
+    d = G.c1_reference()
+    offs = d["ub_offsets"]
     cfg = B.config(number_of_user_bins=64, number_of_hash_functions=2, maximum_fpr=0.05)
-    H = B.build_synthetic(cfg, bytes(z["layout"]).decode(), 1, z["ub_offsets"])
-    ref = canonical(dict(bins=z["bins"], bin_size=z["bin_size"], next_ibf=z["next_ibf"], user_bin=z["user_bin"]))
-    got = canonical(H.tables())
-    assert {p: v[:3] for p, v in ref.items()} == {p: v[:3] for p, v in got.items()}
+    ubs = [S.user_bin_values(1, offs, u) for u in range(64)]
+    H1 = hg.hierarchical_interleaved_bloom_filter(
+        B.config(input_fn=lambda u, it: it.push(ubs[u]), number_of_user_bins=64, number_of_hash_functions=2,
+                 maximum_fpr=0.05), d["layout_text"])
+    H2 = B.build_synthetic(cfg, d["layout_text"], 1, offs)
+    qv, qo, thr = d["q_values"], d["q_offsets"], d["thresholds"]
+    for H in (H1, H2):
+        _same_index_as_reference(H, d)
+        m_off, m_ids, _ = H.membership_agent().query_batch(qv, qo, thr)
+        mem_digest, mem_len = G.fold_digests(m_off, m_ids)
+        np.testing.assert_array_equal(mem_len, d["mem_len"])
+        np.testing.assert_array_equal(mem_digest, d["mem_digest"])
+        c_off, c_ids, c_cnt = H.counting_agent(2).query_batch(qv, qo, thr)
+        cnt_digest, cnt_nnz = G.fold_digests(c_off, c_ids, c_cnt)
+        np.testing.assert_array_equal(cnt_nnz, d["cnt_nnz"])
+        np.testing.assert_array_equal(cnt_digest, d["cnt_digest"])
+
+
+@pytest.mark.parametrize("name,fixture", [("hibf8192", "ref_c3_0.05.npz"), ("hibf65536", "ref_c4_0.02.npz")])
+def test_benchmark_layout_matches_reference_build(gpu_lib, name, fixture):
+    """The benchmark workloads' layouts with every user bin at reduced scale: the device build (split user bins
+    chunked by the replayed split table) equals the reference's own build of the same user bins in every IBF."""
+    from hibf_gb300.workloads import WORKLOADS
+
+    wl = WORKLOADS[name]
+    ref = dict(np.load(G.GOLDEN / fixture))
+    offs = ref["ub_offsets"]
+    table, _ = wl.split_table(offs)
+    cfg = B.config(number_of_user_bins=wl.n_user_bins, number_of_hash_functions=wl.h, maximum_fpr=wl.fpr)
+    H = B.build_synthetic(cfg, wl.layout_text(), wl.query.seed, offs, table)
+    _same_index_as_reference(H, ref)
 
 
 @pytest.mark.parametrize("case", G.ibf_config_cases(), ids=lambda c: f"ibfcfg{c['index']}")

@@ -142,3 +142,57 @@ def test_insertion_order_reproduces_reference_bits(oracle, name):
                 ibfs[k].emplace(v, tb)
     for k in range(bins.size):
         assert S.digest(ibfs[k].words().tolist()) == int(d["digests"][k]), f"IBF {k}"
+
+
+@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "same", "synth64",
+                                  "synth600", "synth_t128", "synth_t256", "dups", "synth_h1", "synth_h4",
+                                  "synth_h5", "empty_bins", "relaxed_fpr", "synth_t512"])
+def test_split_table_places_values_like_the_reference_order(name):
+    """The split table (per split user bin: the set's multiplier and mask, and at each chunk boundary the home slot
+    and the values of that slot ranked before it) places every value of every split user bin in the chunk the full
+    replayed hash-set order gives it; for the synthetic user bins the table of the streamed replay is the same."""
+    d = G.hibf_case(name)
+    ubs = _ub_values(d)
+    fpr, rfpr, _, _ = (float(x) for x in d["fpr"])
+    kw = dict(number_of_user_bins=d["n_ub"], number_of_hash_functions=int(d["hash_funs"][0]), maximum_fpr=fpr,
+              relaxed_fpr=rfpr)
+    offs, vals = B.build_inputs(B.config(input_fn=lambda u, it: it.push(ubs[u]), **kw), d["layout_text"])
+    table = B.split_table.inputs(B.config(input_fn=lambda u, it: it.push(ubs[u]), **kw), d["layout_text"])
+    a = table.arrays()
+    assert a["user_bin"].size > 0
+    for i, u in enumerate(a["user_bin"]):
+        v = vals[offs[u]:offs[u + 1]]
+        assert int(a["n_values"][i]) == v.size
+        got = table.chunks(int(u), v)
+        # the reference order puts position p in chunk p // ceil(n / technical bins); compare chunk by chunk
+        lay_ntb = _technical_bins(d, int(u))
+        want = np.arange(v.size, dtype=np.uint64) // np.uint64(-(-v.size // lay_ntb) if v.size else 1)
+        np.testing.assert_array_equal(got, want, err_msg=f"user bin {u}")
+    if "synthetic_seed" in d:
+        t2 = B.split_table.synthetic(B.config(**kw), d["layout_text"], int(d["synthetic_seed"][0]), d["ub_offsets"])
+        b = t2.arrays()
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    # an imported copy answers the same
+    t3 = B.split_table.from_arrays(a)
+    u = int(a["user_bin"][0])
+    np.testing.assert_array_equal(t3.chunks(u, vals[offs[u]:offs[u + 1]]), table.chunks(u, vals[offs[u]:offs[u + 1]]))
+
+
+def _technical_bins(d, u):
+    T = G.tables(d)
+    return int(np.count_nonzero(T["user_bin"] == np.uint64(u)))
+
+
+@pytest.mark.gpu
+def test_split_table_rejects_a_table_of_other_sizes(gpu_lib):
+    d = G.hibf_case("synth64")
+    kw = dict(number_of_user_bins=d["n_ub"], number_of_hash_functions=int(d["hash_funs"][0]),
+              maximum_fpr=float(d["fpr"][0]), relaxed_fpr=float(d["fpr"][1]))
+    a = B.split_table.synthetic(B.config(**kw), d["layout_text"], int(d["synthetic_seed"][0]),
+                                d["ub_offsets"]).arrays()
+    a["n_values"] = a["n_values"].copy()
+    a["n_values"][0] += 1
+    bad = B.split_table.from_arrays(a)
+    with pytest.raises(B.N.InvalidArgument):
+        B.build_synthetic(B.config(**kw), d["layout_text"], int(d["synthetic_seed"][0]), d["ub_offsets"], bad)

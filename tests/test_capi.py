@@ -1,5 +1,6 @@
-"""The C-ABI library: it builds, loads, and exports every entry point include/hibf_gb300.h declares.  CPU only:
-argument validation that happens before any device work is checked too; nothing here launches a kernel."""
+"""The C-ABI library: it builds, loads, and exports every entry point include/hibf_gb300.h and
+include/hibf_gb300_diagnostics.h declare.  CPU only: argument validation that happens before any device work is
+checked too; nothing here launches a kernel."""
 
 import ctypes
 import re
@@ -9,7 +10,8 @@ import pytest
 
 from hibf_gb300 import _build, _native as N
 
-HEADER = Path(__file__).resolve().parents[1] / "include" / "hibf_gb300.h"
+INCLUDE = Path(__file__).resolve().parents[1] / "include"
+HEADERS = [INCLUDE / "hibf_gb300.h", INCLUDE / "hibf_gb300_diagnostics.h"]
 
 
 @pytest.fixture(scope="module")
@@ -19,7 +21,7 @@ def lib():
 
 
 def declared():
-    text = HEADER.read_text()
+    text = "".join(h.read_text() for h in HEADERS)
     return sorted(set(re.findall(r"\b(hibf_gpu_\w+)\s*\(", text)))
 
 

@@ -176,6 +176,30 @@ def test_hibf_unit_expectations(oracle):
     assert all(int(c[ub]) >= 2 * ub + 2 for ub in range(500))
 
 
+def test_c1_oracle_answers_like_the_reference(oracle):
+    """The 64-user-bin workload (BASELINE config 1): the oracle's HIBF with the reference's tables, filled in the
+    builder's insertion order, holds the reference's bits in every IBF, and answers all 10,000 queries
+    (membership_for + sort_results at t = 125, counting_agent<uint16_t>::bulk_count at t = 125) with the
+    reference's per-query lengths and digests (hierarchical_interleaved_bloom_filter.hpp:424-439, 549-566)."""
+    from hibf_gb300 import build as B
+    from hibf_gb300 import synthetic as S
+
+    d = G.c1_reference()
+    offs = d["ub_offsets"]
+    ubs = [S.user_bin_values(1, offs, u) for u in range(64)]
+    cfg = B.config(input_fn=lambda u, it: it.push(ubs[u]), number_of_user_bins=64, number_of_hash_functions=2,
+                   maximum_fpr=0.05)
+    o2, vals = B.build_inputs(cfg, d["layout_text"])
+    t = dict(n_user_bins=64, bins=d["bins"], bin_size=d["bin_size"], hash_funs=d["hash_funs"],
+             next_ibf=d["next_ibf"], user_bin=d["user_bin"])
+    O = G.oracle_hibf_from_inputs(oracle, t, o2, vals)
+    for k in range(d["bins"].size):
+        assert S.digest(O.words(k).tolist()) == int(d["digests"][k]), f"IBF {k}"
+    r = O.query_batch(d["q_values"], d["q_offsets"], d["thresholds"], d["thresholds"], threads=4)
+    for key in ("mem_len", "mem_digest", "cnt_nnz", "cnt_digest"):
+        np.testing.assert_array_equal(r[key], d[key], err_msg=key)
+
+
 def test_c1_reference_fixture_shape():
     z = np.load(G.GOLDEN / "c1_reference.npz")
     assert z["bins"].size == 3 and z["mem_len"].size == 10000
