@@ -4,17 +4,22 @@
 Default workload (hibf8192): 8,192 user bins (log-normal sizes, median 2e5, sigma 1.5, clipped [1e3, 5e7]; 4.9e9
 values; layout from the reference's DP), h=2, fpr 0.05, tmax 64; one step = membership_for + sort_results for
 1,000,000 queries of length U[20, 2000] (70% from 1-3 user bins with 2% noise, 30% uniform), threshold
-ceil(0.7 * length).  Inputs (8 GB of query values) and the index (13.4 GB) are both larger than L2.
+ceil(0.7 * length).  Inputs (8 GB of query values) and the index (13.4 GB) are both larger than L2.  The index is
+the reference's filter: split user bins are chunked in the reference's hash-set order (committed split table), and
+every IBF is compared with the reference's own build of the same workload (tests/golden/ref_c3_1.npz).  A sub-record
+measures the 65,536-user-bin workload the same way (--no-c4 skips it).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload hibf8192|hibf64]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload hibf8192|...]
 
 Prints one JSON line (rank 0).  Under torchrun each rank holds its own replica and answers the full batch
-(replicas only, weak scaling); the step time is the maximum over ranks.
+(replicas only, weak scaling); the step time is the maximum over ranks.  The compact `parity` object is the line's
+last key.
 """
 
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import platform
@@ -22,7 +27,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 from pathlib import Path
 
@@ -30,6 +34,7 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+GOLDEN = ROOT / "tests" / "golden"
 
 METRIC = "HIBF query values/s on 1 GB300, batched vs plain (bit-exact); p99 serve latency"
 WORKLOAD_DESC = {
@@ -45,6 +50,7 @@ WORKLOAD_DESC["ibf1024"] = ("IBF 1,024 bins x 2^26 bits (8 GiB), h=3, emplace of
                              "bulk_contains + bulk_count<uint16> over 2^24 query values, 50% present in a random bin")
 IBF1024 = dict(bins=1024, bin_size=1 << 26, h=3, values_per_bin=5_000_000, n_queries=1 << 24, seed=1)
 REASON_KEYS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+REF_TAG = {"hibf8192": "c3", "hibf65536": "c4"}
 
 
 def parse_args():
@@ -60,6 +66,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end measurement (0: --steps)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-c4", action="store_true", help="skip the 65,536-user-bin sub-record")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel schedule")
     ap.add_argument("--tuning", type=str, default="",
                     help="fixed kernel schedule 'values_per_lane,fetch_bytes,counter_bits[,adaptive_step,ee_min]' "
@@ -130,7 +137,7 @@ def peaks():
 
 
 def traffic_per_value_visit(workload="hibf8192"):
-    """DRAM bytes per (value, IBF) visit of the query kernel from the committed ncu summary, if present."""
+    """DRAM bytes per executed (value, IBF) visit of the query kernel from the committed ncu summary, if present."""
     p = ROOT / "profiles" / "traffic.txt"
     if not p.exists():
         return None
@@ -141,7 +148,6 @@ def traffic_per_value_visit(workload="hibf8192"):
     return None
 
 
-# ------------------------------------------------------------------------------------------------------------------
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -149,18 +155,86 @@ def dist_env():
     return rank, world, local
 
 
+def host_ram_bytes():
+    try:
+        return os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    except (ValueError, OSError):
+        return 1 << 40
+
+
+def scaled(offs: np.ndarray, scale: float) -> np.ndarray:
+    if scale == 1.0:
+        return offs
+    sizes = np.maximum(1, np.floor(np.diff(offs.astype(np.float64)) * scale)).astype(np.uint64)
+    out = np.zeros(sizes.size + 1, np.uint64)
+    np.cumsum(sizes, out=out[1:])
+    return out
+
+
+def config_of(wl, nq, nv, n_ibfs, scale, world) -> dict:
+    """The workload as both arms name it (the reference arm's line carries the same dict)."""
+    return {"workload": WORKLOAD_DESC[wl.name], "name": wl.name, "n_user_bins": wl.n_user_bins,
+            "queries_per_step": nq, "values_per_step": nv, "n_ibfs": n_ibfs, "parallelism": f"replicas x{world}",
+            "size_scale": scale, "l2": "inputs (values) and the index are larger than L2; no flush"}
+
+
+def value_inserts(layout_text: str, offs: np.ndarray) -> int:
+    """Inserted (value, IBF) pairs of a build: every value into its own IBF and every ancestor's merged bin."""
+    n = 0
+    for line in layout_text.splitlines():
+        if not line or line[0] in "#@":
+            continue
+        idx, bins, _ = line.split("\t")
+        u = int(idx)
+        n += int(offs[u + 1] - offs[u]) * len(bins.split(";"))
+    return n
+
+
+def reference_build(wl, scale):
+    """The reference's own build of this workload at this scale (tables and per-IBF digests), if committed."""
+    if wl.name not in REF_TAG:
+        return None
+    p = GOLDEN / f"ref_{REF_TAG[wl.name]}_{scale:g}.npz"
+    return dict(np.load(p)) if p.exists() else None
+
+
+def index_vs_reference(hibf, wl, scale, offs):
+    """Every IBF of the device index (matched by path of merged bins) against the reference's own build's digest."""
+    from hibf_gb300.hibf import ibf_paths
+
+    ref = reference_build(wl, scale)
+    if ref is None or not np.array_equal(ref["ub_offsets"], offs):
+        return {"index_reference": "no committed reference build of this workload at this scale"}
+    got = hibf.digests()
+    t = hibf.tables()
+    mine = ibf_paths(t["bins"], t["next_ibf"], t["user_bin"])
+    theirs = ibf_paths(ref["bins"], ref["next_ibf"], ref["user_bin"])
+    equal = sum(1 for p, k in theirs.items() if p in mine and int(got[mine[p]]) == int(ref["digests"][k]))
+    return {"index_ibfs": len(theirs), "index_ibfs_equal_reference": equal,
+            "index_equals_reference": equal == len(theirs) == len(mine),
+            "index_reference": f"tests/golden/ref_{REF_TAG[wl.name]}_{scale:g}.npz (reference build, per-IBF digests)"}
+
+
 def build_index(wl, scale=1.0):
+    """The reference's filter on the device: the workload's layout, user bins from the generator, split user bins
+    chunked by the committed (or replayed) split table.  Returns (hibf, offsets, build record)."""
     from hibf_gb300 import build as B
 
-    offs = wl.user_bin_offsets()
-    if scale != 1.0:
-        sizes = np.maximum(1, np.floor(np.diff(offs.astype(np.float64)) * scale)).astype(np.uint64)
-        offs = np.zeros(sizes.size + 1, np.uint64)
-        np.cumsum(sizes, out=offs[1:])
+    offs = scaled(wl.user_bin_offsets(), scale)
+    t0 = time.perf_counter()
+    table, table_note = wl.split_table(offs)
+    t_table = time.perf_counter() - t0
     cfg = B.config(number_of_user_bins=wl.n_user_bins, number_of_hash_functions=wl.h, maximum_fpr=wl.fpr)
     t0 = time.perf_counter()
-    hibf = B.build_synthetic(cfg, wl.layout_text(), wl.query.seed, offs)
-    return hibf, offs, time.perf_counter() - t0
+    hibf = B.build_synthetic(cfg, wl.layout_text(), wl.query.seed, offs, table)
+    build_s = time.perf_counter() - t0
+    ins = value_inserts(wl.layout_text(), offs)
+    rec = {"seconds": build_s, "values": int(offs[-1]), "value_inserts": ins, "inserts_per_s": ins / build_s,
+           "algorithmic_GBps": ins * wl.h * 64 / build_s / 1e9, "bytes_per_insert": wl.h * 64,
+           "split_table": table_note, "split_table_s": t_table,
+           "form": "hibf_gpu_hibf_build_synthetic: host plan, values generated on the device, atomicOr inserts; "
+                   "the time includes planning and allocating the store"}
+    return hibf, offs, rec
 
 
 def oracle_from_device(hibf):
@@ -174,32 +248,6 @@ def oracle_from_device(hibf):
         addr, n = OH.data_ptr(k)
         N.call("hibf_gpu_hibf_download_words", hibf._h, k, addr, n)
     return OH
-
-
-def host_ram_bytes():
-    try:
-        return os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
-    except (ValueError, OSError):
-        return 1 << 40
-
-
-def cpu_baseline_scaled(args, wl, scale):
-    """CPU baseline and oracle parity on the same layout with every user bin scaled by `scale`."""
-    hibf, offs, _ = build_index(wl, scale)
-    OH = oracle_from_device(hibf)
-    threads = os.cpu_count() or 1
-    s = cpu_sample(OH, wl, offs, args.cpu_seconds, threads)
-    cpu = {"value": s["values"] / s["seconds"], "unit": "values/s", "cores": threads, "kind": "port",
-           "sample": f"{s['queries']} queries ({s['values']} values) on the same layout with user bins at {scale} of "
-                     f"their size (the full index does not fit host memory for the oracle), membership_for + "
-                     f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads",
-           **cpu_extra(OH, wl, offs)}
-    o_off, o_ids = OH.membership_batch(s["v"], s["qo"], s["thr"], threads=threads)
-    g_off, g_ids, _ = hibf.membership_agent().query_batch(s["v"], s["qo"], s["thr"])
-    n = s["queries"]
-    return cpu, {"oracle_sample_queries": n, "oracle_sample_index_scale": scale,
-                 "oracle_sample_equal": bool(np.array_equal(o_off, g_off) and np.array_equal(o_ids, g_ids)),
-                 **count_parity(OH, hibf, s, threads)}
 
 
 def _mix64(z):
@@ -226,40 +274,48 @@ def count_digests(offs, ids, cnts):
     return d, lens.astype(np.uint64)
 
 
-def count_parity(OH, hibf, s, threads, n_max=50_000):
-    """counting_agent<uint16>::bulk_count of the device against the oracle on the sample's first queries."""
-    n = min(s["queries"], n_max)
-    qo = s["qo"][:n + 1]
-    v, thr = s["v"][:int(qo[-1])], s["thr"][:n]
-    o = OH.query_batch(v, qo, thr, thr, threads=threads)
-    g_off, g_ids, g_cnt = hibf.counting_agent(2).query_batch(v, qo, thr)
-    dg, nnz = count_digests(g_off, g_ids, g_cnt)
-    return {"oracle_count_sample_queries": n,
-            "oracle_count_sample_equal": bool(np.array_equal(dg, o["cnt_digest"]) and np.array_equal(nnz, o["cnt_nnz"]))}
-
-
-def cpu_extra(OH, wl, offs):
-    """Host architecture and a one-thread figure beside the all-cores CPU baseline (a short bounded sample)."""
-    s1 = cpu_sample(OH, wl, offs, 3.0, 1)
-    return {"machine": platform.machine(), "value_1_thread": s1["values"] / s1["seconds"],
-            "sample_1_thread": f"first {s1['queries']} queries ({s1['values']} values), one thread"}
-
-
-def cpu_sample(OH, wl, offs, budget_s, threads, first=0):
-    """Times the oracle's membership_for + sort_results on a bounded sample of the workload's queries."""
-    probe = min(wl.n_queries, 400)
-    qo, thr = wl.query_offsets(first, probe)
-    v = wl.queries_host(offs, first, probe, qo)
+def cpu_sample(OH, qgen, budget_s, threads, first=0, n_total=None):
+    """Times the oracle's membership_for + sort_results on a bounded sample of the workload's queries; qgen(first, n)
+    returns (values, query offsets, thresholds)."""
+    probe = 400 if n_total is None else min(n_total, 400)
+    v, qo, thr = qgen(first, probe)
     t0 = time.perf_counter()
     OH.run_queries(v, qo, thr, thr, mode=1, threads=threads)
     dt = max(time.perf_counter() - t0, 1e-6)
-    n = int(min(wl.n_queries - first, max(probe, probe * budget_s / dt)))
-    qo, thr = wl.query_offsets(first, n)
-    v = wl.queries_host(offs, first, n, qo)
+    n = int(max(probe, probe * budget_s / dt))
+    if n_total is not None:
+        n = min(n, n_total - first)
+    v, qo, thr = qgen(first, n)
     t0 = time.perf_counter()
     pairs, chk = OH.run_queries(v, qo, thr, thr, mode=1, threads=threads)
     dt = time.perf_counter() - t0
     return dict(values=int(qo[-1]), queries=n, seconds=dt, value_visits=pairs, checksum=chk, qo=qo, thr=thr, v=v)
+
+
+def product_qgen(wl, offs):
+    def gen(first, n):
+        qo, thr = wl.query_offsets(first, n)
+        return wl.queries_host(offs, first, n, qo), qo, thr
+    return gen
+
+
+def oracle_parity(OH, hibf, s, res_offs, res_ids, threads, n_count=50_000):
+    """The device's membership lists (from the batch) and counting_agent<uint16>::bulk_count (recomputed on the
+    first n_count queries) against the oracle on the same bits."""
+    o_off, o_ids = OH.membership_batch(s["v"], s["qo"], s["thr"], threads=threads)
+    n = s["queries"]
+    out = {"oracle_sample_queries": n,
+           "oracle_sample_equal": bool(np.array_equal(o_off, res_offs[:n + 1]) and
+                                       np.array_equal(o_ids, res_ids[:int(res_offs[n])]))}
+    m = min(n, n_count)
+    qo = s["qo"][:m + 1]
+    v, thr = s["v"][:int(qo[-1])], s["thr"][:m]
+    o = OH.query_batch(v, qo, thr, thr, threads=threads)
+    g_off, g_ids, g_cnt = hibf.counting_agent(2).query_batch(v, qo, thr)
+    dg, nnz = count_digests(g_off, g_ids, g_cnt)
+    out["oracle_count_sample_queries"] = m
+    out["oracle_count_sample_equal"] = bool(np.array_equal(dg, o["cnt_digest"]) and np.array_equal(nnz, o["cnt_nnz"]))
+    return out
 
 
 def _ranks(x):
@@ -339,20 +395,34 @@ def learned_scheduler(hibf, tuning, d_v, d_qo, d_thr, qo, nq, n, stream):
                      "hibf_gb300/csrc/cost_model.cu"}
 
 
-# ------------------------------------------------------------------------------------------------------------------
-def run_ours(args, wl, rank, world, local):
+def h2d_probe(nbytes):
+    """The host-to-device rate of one pinned copy of `nbytes` in this process (CUDA events)."""
+    import torch
+
+    h = torch.empty(nbytes // 8, dtype=torch.int64, pin_memory=True)
+    d = torch.empty_like(h, device="cuda")
+    d.copy_(h, non_blocking=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    d.copy_(h, non_blocking=True)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    del h, d
+    return nbytes / (ms / 1e3) / 1e9
+
+
+def measure_hibf(args, wl, world, stream, full):
+    """Builds the workload's index and measures it: the persistent batch (graph replay, K timed steps), the kernel's
+    roofline, bulk_count, the plain per-query form, the end-to-end host call with its timeline, the CPU oracle and
+    the parity checks.  `full` adds the autotuner, serving and the learned scheduler (headline workload only)."""
     import torch
 
     from hibf_gb300 import _native as N
 
-    torch.cuda.set_device(local)
-    if args.l2_fetch >= 0:
-        N.call("hibf_gpu_set_l2_fetch_granularity", args.l2_fetch)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
-    hibf, offs, build_s = build_index(wl, args.scale)
+    hibf, offs, build = build_index(wl, args.scale)
+    parity = index_vs_reference(hibf, wl, args.scale, offs)
     nq = args.queries or min(wl.n_queries, 1_000_000)
     qo, thr = wl.query_offsets(0, nq)
     nv = int(qo[-1])
@@ -363,11 +433,9 @@ def run_ours(args, wl, rank, world, local):
     wl.queries_device(d_ub.data_ptr(), 0, nq, d_qo.data_ptr(), d_v.data_ptr())
     torch.cuda.synchronize()
 
-    stream = torch.cuda.Stream()
     agent = hibf.membership_agent()
     agent.reserve(nq, nv, nq * 8 + 65536, nq * 8 + 65536)
     agent.set_stream(stream.cuda_stream)
-    # autotune the kernel schedule on the batch's first queries (results are checked identical across schedules)
     tune = None
     if args.tuning:
         f = [int(x) for x in args.tuning.split(",")]
@@ -377,24 +445,21 @@ def run_ours(args, wl, rank, world, local):
                      early_exit_min=f[4])
         agent.tuning = t
         tune = {"fixed": agent.tuning}
-    elif not args.no_autotune:
+    elif full and not args.no_autotune:
         ns = min(nq, args.tune_queries)
         t0 = time.perf_counter()
         trials = agent.autotune(d_v.data_ptr(), d_qo.data_ptr(), ns, d_thr.data_ptr(), reps=2)
-        keys = ("values_per_lane", "fetch_bytes", "counter_bits", "blocks_per_sm", "early_exit_first",
-                "early_exit_step", "early_exit_stages", "early_exit_min")
         tune = {"sample_queries": ns, "seconds": time.perf_counter() - t0, "best": agent.tuning,
-                "default_kernel_ms": trials[0]["kernel_ms"],
-                "best_kernel_ms": min(t["kernel_ms"] for t in trials),
-                "trial_fields": list(keys) + ["kernel_ms"],
-                "trials": [[t[k] for k in keys] + [round(t["kernel_ms"], 4)] for t in trials]}
+                "trials": len(trials), "default_kernel_ms": trials[0]["kernel_ms"],
+                "best_kernel_ms": min(t["kernel_ms"] for t in trials)}
     agent.capture_batch_device(d_v.data_ptr(), d_qo.data_ptr(), nq, d_thr.data_ptr())
     for _ in range(max(args.warmup, 3)):
         agent.replay()
     stream.synchronize()
     agent.status()
 
-    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0] or 0)
+    steps = args.steps if full else max(3, min(args.steps, 10))
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(torch.cuda.current_device())).split(",")[0] or 0)
     clocks = ClockSampler(gpu_index)
     clocks.start()
     if world > 1:
@@ -402,7 +467,7 @@ def run_ours(args, wl, rank, world, local):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         agent.replay()
     e1.record(stream)
     e1.synchronize()
@@ -411,7 +476,7 @@ def run_ours(args, wl, rank, world, local):
         torch.distributed.barrier()
     clk = clocks.stop()
     agent.status()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = e0.elapsed_time(e1) / steps
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -424,20 +489,10 @@ def run_ours(args, wl, rank, world, local):
         stream.synchronize()
         kms.append(agent.kernel_ms())
     kernel_ms = sum(kms) / len(kms)
-    # the device's own random 8-byte read rate at the index's footprint (fully random, and 2 MiB-local)
-    import ctypes as _ct
-
-    probe = {}
-    fp = min(int(hibf.info()["device_bytes"]), 16 << 30)
-    for name, region in (("random", 0), ("window_2MiB", 2 << 20)):
-        rps = _ct.c_double(0)
-        N.call("hibf_gpu_probe_random_reads", fp, region, _ct.byref(rps))
-        probe[name] = rps.value
-    launches_per_step = 8
     res_offs, res_ids, _ = agent.fetch_results(nq)
 
     # plain form: one launch per query on the first P queries
-    P = min(args.plain_queries, nq)
+    P = min(args.plain_queries if full else 1000, nq)
     pa = hibf.membership_agent()
     pa.tuning = agent.tuning
     pa.reserve(P, nv, 65536, P * 8 + 65536)
@@ -451,23 +506,23 @@ def run_ours(args, wl, rank, world, local):
     p1.synchronize()
     plain_s = p0.elapsed_time(p1) / 1e3
     plain_offs, plain_ids, _ = pa.fetch_results(P)
-    plain_equal = bool(np.array_equal(plain_offs, res_offs[:P + 1]) and
-                       np.array_equal(plain_ids, res_ids[:int(res_offs[P])]))
+    parity["plain_equals_batch"] = bool(np.array_equal(plain_offs, res_offs[:P + 1]) and
+                                        np.array_equal(plain_ids, res_ids[:int(res_offs[P])]))
     plain_vps = float(qo[P]) / plain_s
+    del pa
 
-    # counting_agent<uint16>::bulk_count over the same batch: the same traversal with the counts kept (no decided
-    # exit: every count must be exact); its user bins must be the membership lists
+    # counting_agent<uint16>::bulk_count over the same batch (every count exact); its user bins must be the lists
     ca = hibf.counting_agent(2)
     ca.tuning = agent.tuning
     ca.reserve(nq, nv, nq * 8 + 65536, nq * 8 + 65536)
     ca.set_stream(stream.cuda_stream)
     ca.capture_batch_device(d_v.data_ptr(), d_qo.data_ptr(), nq, d_thr.data_ptr(), mode=N.QUERY_COUNT, width=2)
-    for _ in range(3):
+    for _ in range(2):
         ca.replay()
     stream.synchronize()
     ca.status()
     c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    count_steps = max(1, min(args.steps, 5))
+    count_steps = max(1, min(steps, 5))
     c0.record(stream)
     for _ in range(count_steps):
         ca.replay()
@@ -476,14 +531,15 @@ def run_ours(args, wl, rank, world, local):
     ca.status()
     count_ms = c0.elapsed_time(c1) / count_steps
     c_offs, c_ids, c_cnt = ca.fetch_results(nq, mode=N.QUERY_COUNT, width=2)
-    c_thr_ok = bool(np.all(c_cnt.astype(np.uint64) >= np.repeat(thr, np.diff(c_offs).astype(np.int64))))
+    parity["count_user_bins_equal_membership"] = bool(np.array_equal(c_offs, res_offs) and
+                                                      np.array_equal(c_ids, res_ids))
+    parity["counts_at_least_threshold"] = bool(np.all(c_cnt.astype(np.uint64) >= np.repeat(
+        thr, np.diff(c_offs).astype(np.int64))))
     count = {"values_per_s": world * nv / (count_ms / 1e3), "ms_per_step": count_ms, "steps": count_steps,
-             "form": "one persistent launch per batch, CUDA-graph replay, uint16 counts",
-             "user_bins_equal_membership": bool(np.array_equal(c_offs, res_offs) and np.array_equal(c_ids, res_ids)),
-             "counts_at_least_threshold": c_thr_ok}
-    del ca
+             "form": "one persistent launch per batch, CUDA-graph replay, uint16 counts"}
+    del ca, c_offs, c_ids, c_cnt
 
-    # end to end through the C ABI host call: pinned host inputs -> H2D -> batch -> D2H results
+    # end to end through the C ABI host call: pinned host inputs -> H2D -> batch -> D2H results, with its timeline
     h_v = torch.empty(max(nv, 1), dtype=torch.int64, pin_memory=True)
     h_v.copy_(d_v)
     hv = h_v.numpy().view(np.uint64)[:nv]
@@ -492,101 +548,153 @@ def run_ours(args, wl, rank, world, local):
     ea.reserve(nq, nv, nq * 8 + 65536, nq * 8 + 65536)
     for _ in range(2):
         ea.query_batch(hv, qo, thr)
-    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    e2e_steps = args.e2e_steps or (max(3, min(steps, 10)) if full else 3)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    wall, timelines = [], []
     for _ in range(e2e_steps):
+        t0 = time.perf_counter()
         eo, ei, _ = ea.query_batch(hv, qo, thr)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e_equal = bool(np.array_equal(eo, res_offs) and np.array_equal(ei, res_ids))
+        wall.append(time.perf_counter() - t0)
+        timelines.append(ea.last_timeline())
+    e2e_s = sum(wall) / len(wall)
+    parity["e2e_equals_batch"] = bool(np.array_equal(eo, res_offs) and np.array_equal(ei, res_ids))
     h2d = nv * 8 + (nq + 1) * 8 + nq * 8
     d2h = (nq + 1) * 8 + int(eo[-1]) * 8 + 8 * 8 + 16
+    last = timelines[-1]
+    n_chunks = len(last) - 3
+    e2e_timeline = {
+        "chunks": n_chunks,
+        "median_ms": {"values_copied": float(np.median([t[n_chunks - 1] for t in timelines])),
+                      "kernel_start": float(np.median([t[n_chunks] for t in timelines])),
+                      "kernel_end": float(np.median([t[n_chunks + 1] for t in timelines])),
+                      "results_back": float(np.median([t[n_chunks + 2] for t in timelines]))},
+        "h2d_GBps_in_call": nv * 8 / (float(np.median([t[n_chunks - 1] for t in timelines])) / 1e3) / 1e9,
+        "h2d_GBps_probe": h2d_probe(min(nv * 8, 4 << 30)),
+        "wall_ms_per_call": [round(w * 1e3, 2) for w in wall],
+        "note": "ms from the call's first device work; values_copied = the last chunk's copy done",
+    }
+    del ea
 
-    # serving: open-loop Poisson arrivals against the resident index (continuous batching, 4 slots, 4 GiB cap)
     serving = []
-    if not args.no_serve and wl.name == "hibf8192":  # the serving workload runs on the 8,192-user-bin index
+    if full and not args.no_serve and wl.name == "hibf8192":
         from hibf_gb300.serve import server
 
         pool_q = min(nq, 100_000)
         pool_v = hv[:int(qo[pool_q])]
-        for load, dur in ((1e4, 3.0), (1e5, 2.0), (1e6, 2.0)):
+        for load, dur in ((1e4, 10.0), (1e5, 5.0), (1e6, 5.0)):
             srv = server(hibf, slots=4, max_batch_queries=65536, max_batch_values=1 << 27, admission_bytes=4 << 30)
             r = srv.open_loop(pool_v, qo[:pool_q + 1], offered_qps=load, duration_s=dur, max_request_queries=4096,
                               thr_lo=0.5, thr_hi=0.9, seed=int(load))
             r["mean_batch_phases_ms"] = srv.phase_times()
+            if r["requests"] < 10_000:
+                r["p999_ms"] = None  # fewer than 10,000 requests: no meaningful 99.9th percentile
+            if r["requests"] < 1_000:
+                r["p99_note"] = f"{r['requests']} requests: the 99th percentile is near the maximum"
             serving.append(r)
             srv.close()
-
     learned = None
-    if not args.no_learned and nq >= 2 * args.sched_queries:
+    if full and not args.no_learned and nq >= 2 * args.sched_queries:
         learned = learned_scheduler(hibf, agent.tuning, d_v, d_qo, d_thr, qo, nq, args.sched_queries, stream)
 
-    out = None
-    if rank == 0:
-        hbm, peak_kind = peaks()
-        bytes_per_visit = wl.h * 1 * 32  # h rows of ceil(tb/256) = 1 sector each (every IBF has tb <= tmax <= 256)
-        # algorithmic bytes: h sectors for every (value, IBF) visit the reference's traversal implies; the kernel
-        # reads fewer (a task stops once its outcome is fixed), reported beside as achieved_executed
-        achieved = visits * bytes_per_visit / (kernel_ms / 1e3) / 1e9
-        achieved_executed = executed * bytes_per_visit / (kernel_ms / 1e3) / 1e9
-        tpv = traffic_per_value_visit(wl.name)
-        cpu = None
-        parity = {"plain_equals_batch": plain_equal, "e2e_equals_batch": e2e_equal}
-        if not args.no_cpu and int(hibf.info()["device_bytes"]) > host_ram_bytes() // 4:
-            # the oracle holds the whole index in host memory: on an index this large it runs on the same layout at
-            # 1/50 of every user bin's size, against the device answering the same queries on that index
-            cpu, small = cpu_baseline_scaled(args, wl, 0.02)
-            parity.update(small)
-        elif not args.no_cpu:
+    # CPU oracle (all host cores) on the same bits, and parity on its sample
+    cpu = None
+    if not args.no_cpu:
+        dev_bytes = int(hibf.info()["device_bytes"])
+        if dev_bytes < 0.6 * host_ram_bytes():
             OH = oracle_from_device(hibf)
             threads = os.cpu_count() or 1
-            s = cpu_sample(OH, wl, offs, args.cpu_seconds, threads)
+            qgen = product_qgen(wl, offs)
+            s = cpu_sample(OH, qgen, args.cpu_seconds, threads, n_total=nq)
+            s1 = cpu_sample(OH, qgen, 3.0, 1, n_total=nq)
             cpu = {"value": s["values"] / s["seconds"], "unit": "values/s", "cores": threads, "kind": "port",
+                   "machine": platform.machine(), "value_1_thread": s1["values"] / s1["seconds"],
                    "sample": f"first {s['queries']} queries ({s['values']} values) of the batch, membership_for + "
-                             f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads",
-                   **cpu_extra(OH, wl, offs)}
-            o_off, o_ids = OH.membership_batch(s["v"], s["qo"], s["thr"], threads=threads)
-            n = s["queries"]
-            parity["oracle_sample_queries"] = n
-            parity["oracle_sample_equal"] = bool(np.array_equal(o_off, res_offs[:n + 1]) and
-                                                 np.array_equal(o_ids, res_ids[:int(res_offs[n])]))
-            parity.update(count_parity(OH, hibf, s, threads))
-        value = world * nv / (ms / 1e3)
+                             f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads on the full index"}
+            parity.update(oracle_parity(OH, hibf, s, res_offs, res_ids, threads))
+            del OH
+            gc.collect()
+        else:
+            parity["oracle"] = f"skipped: the {dev_bytes / 1e9:.0f} GB index exceeds 60% of host memory"
+
+    hbm, peak_kind = peaks()
+    bytes_per_visit = wl.h * 32  # h rows of ceil(tb/256) = 1 sector each (every IBF has tb <= tmax <= 256)
+    achieved = visits * bytes_per_visit / (kernel_ms / 1e3) / 1e9
+    achieved_executed = executed * bytes_per_visit / (kernel_ms / 1e3) / 1e9
+    tpv = traffic_per_value_visit(wl.name)
+    value = world * nv / (ms / 1e3)
+    out = {
+        "value": value, "unit": "values/s", "ms_per_step": ms, "steps": steps,
+        "config": config_of(wl, nq, nv, hibf.n_ibfs, args.scale, world),
+        "index_bytes": int(hibf.info()["device_bytes"]),
+        "queries_per_s": world * nq / (ms / 1e3),
+        "e2e": {"value": world * nv / e2e_s, "unit": "values/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                "call": "hibf_gpu_agent_query_batch (host buffers, pinned)", "timeline": e2e_timeline},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "achieved_executed": achieved_executed,
+                     "frac_executed": achieved_executed / hbm,
+                     "traffic": (tpv * executed) if tpv is not None else None,
+                     "dram_bytes_per_executed_visit": tpv,
+                     "kernel": "k_query", "kernel_ms": kernel_ms, "value_visits": visits,
+                     "value_visits_executed": executed, "tasks": tasks,
+                     "algorithmic_bytes_per_value_visit": bytes_per_visit,
+                     "row_reads_per_s": executed * wl.h / (kernel_ms / 1e3)},
+        "cpu_baseline": cpu, "clocks": clk,
+        "plain": {"values_per_s": plain_vps, "queries": P, "form": "one launch per query"},
+        "batched_vs_plain": value / world / plain_vps,
+        "bulk_count": count, "build": build, "autotune": tune, "learned_scheduler": learned,
+        "serving": serving, "parity": parity,
+        "gpu_launches": 8 * steps,
+    }
+    del agent, hibf, d_v, d_qo, d_thr, d_ub, h_v
+    gc.collect()
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_ours(args, wl, rank, world, local):
+    import torch
+
+    from hibf_gb300 import _native as N
+    from hibf_gb300.workloads import WORKLOADS
+
+    torch.cuda.set_device(local)
+    if args.l2_fetch >= 0:
+        N.call("hibf_gpu_set_l2_fetch_granularity", args.l2_fetch)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    m = measure_hibf(args, wl, world, stream, full=True)
+    c4 = None
+    if wl.name == "hibf8192" and not args.no_c4 and args.scale == 1.0 and not args.queries:
+        w4 = WORKLOADS["hibf65536"]
+        m4 = measure_hibf(args, w4, world, stream, full=False)
+        c4 = {k: m4[k] for k in ("value", "unit", "ms_per_step", "steps", "config", "index_bytes", "queries_per_s",
+                                 "e2e", "roofline", "cpu_baseline", "plain", "batched_vs_plain", "bulk_count",
+                                 "build", "clocks")}
+        m["parity"].update({"c4_" + k: v for k, v in m4["parity"].items()})
+    out = None
+    if rank == 0:
+        serving = m["serving"]
+        parity = m.pop("parity")
         out = {
-            "metric": METRIC, "value": value, "unit": "values/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "metric": METRIC, "value": m["value"], "unit": "values/s", "n_gpus": world, "steps": m["steps"],
+            "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64",
             "data": "synthetic: seeded splitmix64 user bins and queries (include/hibf_gb300_synthetic.h)",
-            "config": {"workload": WORKLOAD_DESC[wl.name], "name": wl.name, "n_user_bins": wl.n_user_bins,
-                       "queries_per_step": nq, "values_per_step": nv, "n_ibfs": hibf.n_ibfs,
-                       "index_bytes": int(hibf.info()["device_bytes"]), "parallelism": f"replicas x{world}",
-                       "size_scale": args.scale, "l2_fetch_granularity": args.l2_fetch,
-                       "l2": "inputs (values) and the index are larger than L2; no flush",
-                       "form": "one persistent launch per batch, CUDA-graph replay"},
-            "queries_per_s": world * nq / (ms / 1e3),
-            "e2e": {"value": world * nv / e2e_s, "unit": "values/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
-                    "call": "hibf_gpu_agent_query_batch (host buffers, pinned)"},
-            "plain": {"values_per_s": plain_vps, "queries": P, "form": "one launch per query"},
-            "bulk_count": count,
-            "batched_vs_plain": value / world / plain_vps,
-            "gpu_launches": launches_per_step * args.steps,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "peak_kind": peak_kind, "achieved_executed": achieved_executed,
-                         "frac_executed": achieved_executed / hbm,
-                         "traffic": (tpv * executed) if tpv is not None else None,
-                         "kernel": "k_query", "kernel_ms": kernel_ms, "value_visits": visits,
-                         "value_visits_executed": executed, "tasks": tasks,
-                         "algorithmic_bytes_per_value_visit": bytes_per_visit,
-                         "row_reads_per_s": executed * wl.h / (kernel_ms / 1e3),
-                         "random_read_ceiling": {"footprint_bytes": fp, "reads_per_s_random": probe["random"],
-                                                 "reads_per_s_2MiB_windows": probe["window_2MiB"],
-                                                 "probe": "hibf_gpu_probe_random_reads"}},
-            "cpu_baseline": cpu, "clocks": clk, "build_s": build_s, "parity": parity, "autotune": tune,
-            "learned_scheduler": learned,
+            "config": m["config"], "gpu_launches": m["gpu_launches"], "e2e": m["e2e"], "roofline": m["roofline"],
+            "cpu_baseline": m["cpu_baseline"], "clocks": m["clocks"],
+            "form": "one persistent launch per batch, CUDA-graph replay",
+            "index_bytes": m["index_bytes"], "queries_per_s": m["queries_per_s"], "plain": m["plain"],
+            "batched_vs_plain": m["batched_vs_plain"], "bulk_count": m["bulk_count"], "build": m["build"],
+            "autotune": m["autotune"], "learned_scheduler": m["learned_scheduler"],
             "serving": serving, "p99_serve_latency_ms": serving[-1]["p99_ms"] if serving else None,
             "serving_config": "open-loop Poisson, request sizes log-uniform 1-4096 queries from the batch's first "
                               "100k queries, thresholds U(0.5,0.9)*len, 4 slots, 4 GiB admission cap",
+            "c4": c4,
+            "parity": parity,
         }
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -594,47 +702,66 @@ def run_ours(args, wl, rank, world, local):
 
 
 def run_reference(args, wl, rank, world, local):
-    """The reference CPU path on the host cores: the C restatement of the reference's query (oracle/hibf_oracle.c)
-    with all host threads.  The index bits are built on the device and downloaded once (set-up, not timed)."""
+    """The reference CPU path on the host cores, with nothing of the product loaded: the C restatement of the
+    reference's query (oracle/hibf_oracle.c) on all host threads, over an index the oracle fills itself from the
+    reference's own tables (tests/golden/ref_*.npz), the committed split table and the generator; its IBFs are
+    compared with the reference's digests before timing."""
     if rank != 0:
         return None
-    import torch
+    from oracle.bindings import Oracle, build_oracle
 
-    torch.cuda.set_device(local)
-    hibf, offs, _ = build_index(wl, args.scale)
-    scale_note = ""
-    if int(hibf.info()["device_bytes"]) > host_ram_bytes() // 4:
-        # the oracle needs the index in host memory: the same layout with user bins at 1/50 of their size
-        del hibf
-        hibf, offs, _ = build_index(wl, 0.02)
-        scale_note = "; index at 0.02 of every user bin's size (the full one does not fit host memory)"
-    OH = oracle_from_device(hibf)
-    del hibf
+    build_oracle()
+    O = Oracle()
+    ref = reference_build(wl, args.scale)
+    table_file = GOLDEN / (wl.split_table_file or "")
+    if ref is None or not wl.split_table_file or not table_file.exists():
+        return {"impl": "reference", "unavailable": f"no committed reference build and split table of {wl.name} at "
+                                                    f"scale {args.scale:g}"}
+    q = wl.query
+    offs = scaled(O.synth_user_bin_offsets(q.seed, wl.size_law, wl.size_p0, wl.size_p1, wl.size_lo, wl.size_hi,
+                                           wl.n_user_bins), args.scale)
+    split = dict(np.load(table_file))
+    if not np.array_equal(ref["ub_offsets"], offs) or not np.array_equal(
+            np.diff(offs)[split["user_bin"].astype(np.int64)], split["n_values"]):
+        return {"impl": "reference", "unavailable": "the committed reference build does not match this host's sizes"}
     threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    OH = O.hibf(dict(n_user_bins=wl.n_user_bins, bins=ref["bins"], bin_size=ref["bin_size"],
+                     hash_funs=ref["hash_funs"], next_ibf=ref["next_ibf"], user_bin=ref["user_bin"]))
+    OH.fill_synthetic(q.seed, offs, split, threads)
+    fill_s = time.perf_counter() - t0
+    digests_equal = bool(np.array_equal(OH.digests(threads), ref["digests"]))
+    nq = args.queries or min(wl.n_queries, 1_000_000)
+
+    def qgen(first, n):
+        return O.synth_queries(q, offs, first, n, threads)
+
     per_step = max(1.0, min(args.cpu_seconds, 60.0 / max(1, args.steps + args.warmup)))
     first = 0
     for _ in range(args.warmup):
-        s = cpu_sample(OH, wl, offs, per_step, threads, first)
-        first = (first + s["queries"]) % max(1, wl.n_queries - 1)
+        s = cpu_sample(OH, qgen, per_step, threads, first, n_total=nq)
+        first = (first + s["queries"]) % max(1, nq - 1)
     vals, secs, nqs = 0, 0.0, 0
     for _ in range(args.steps):
-        s = cpu_sample(OH, wl, offs, per_step, threads, first)
-        first = (first + s["queries"]) % max(1, wl.n_queries - 1)
+        s = cpu_sample(OH, qgen, per_step, threads, first, n_total=nq)
+        first = (first + s["queries"]) % max(1, nq - 1)
         vals += s["values"]
         secs += s["seconds"]
         nqs += s["queries"]
     value = vals / secs
+    nv = int(O.synth_query_offsets(q, 0, nq)[0][-1])  # the step's values, as the GPU arm counts them
     sample = (f"{args.steps} steps of ~{per_step:.1f} s, {nqs} queries ({vals} values) in total, membership_for + "
-              f"sort_results" + scale_note)
+              f"sort_results, oracle/hibf_oracle.c with {threads} OpenMP threads; index filled by the oracle in "
+              f"{fill_s:.0f} s, every IBF equal to the reference's build: {digests_equal}")
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "values/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic: seeded splitmix64 user bins and queries (include/hibf_gb300_synthetic.h)",
-            "config": {"workload": WORKLOAD_DESC[wl.name], "name": wl.name, "n_user_bins": wl.n_user_bins},
+            "config": config_of(wl, nq, nv, int(ref["bins"].size), args.scale, world),
             "cpu_baseline": {"value": value, "unit": "values/s", "cores": threads, "kind": "port",
-                             "machine": platform.machine(),
-                             "sample": sample + "; oracle/hibf_oracle.c (the reference's sources are not on this host)"},
-            "e2e": {"value": value, "unit": "values/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "machine": platform.machine(), "sample": sample},
+            "e2e": {"value": value, "unit": "values/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "parity": {"index_equals_reference": digests_equal}}
 
 
 def ibf_oracle_from_device(ibf, w):

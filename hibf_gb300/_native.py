@@ -152,6 +152,7 @@ _SIGS = [
     ("hibf_gpu_agent_set_stream", None, [vp, vp]),
     ("hibf_gpu_agent_reserve", None, [vp, u64, u64, u64, u64]),
     ("hibf_gpu_agent_membership_for", None, [vp, vp, u64, ctypes.c_uint16, ctypes.POINTER(u64p), u64p]),
+    ("hibf_gpu_agent_membership_for_unsorted", None, [vp, vp, u64, ctypes.c_uint16, ctypes.POINTER(u64p), u64p]),
     ("hibf_gpu_agent_bulk_count", None, [vp, vp, u64, u64, ci, ctypes.POINTER(vp)]),
     ("hibf_gpu_agent_query_batch", None,
      [vp, ci, vp, vp, u64, vp, ci, ctypes.POINTER(u64p), ctypes.POINTER(u64p), ctypes.POINTER(vp)]),

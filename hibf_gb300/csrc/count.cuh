@@ -103,6 +103,10 @@ __device__ __forceinline__ void load_row_words(uint64_t const * p, uint64_t (&w)
     }
 }
 
+// Values are read with ld.global.cg (cached in L2 only): a streamed host batch's values are written by the copy
+// engine while the kernel runs, and a task reads them only after their chunk's arrival counter (query.cuh), so the
+// loads must not come from a non-coherent cache.  Each task reads its values once, so L1 gives them nothing.
+//
 // One warp counts vals[0, n) into counts[0, 64 * LPV * W) with H hash functions.  ATOMIC: counters shared with other
 // warps.  A row is read by LPV lanes, each loading W consecutive words (W = 2: one 16-byte load; the row stride
 // must then be even).  Each lane hashes U values per pass and keeps their H row offsets; the row words of
@@ -139,7 +143,7 @@ __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const
         for (int u = 0; u < U; ++u)
         {
             uint64_t const idx = base + static_cast<uint64_t>(u * 32 + lane);
-            uint64_t const v = idx < n ? vals[idx] : 0u;
+            uint64_t const v = idx < n ? __ldcg(vals + idx) : 0u;
 #pragma unroll
             for (int i = 0; i < H; ++i)
                 off[u][i] = hash_row(v, c_hash_seeds[i], rp.hash_shift, rp.bin_size) * rp.row_words;
@@ -223,7 +227,7 @@ __device__ __forceinline__ void warp_count_wide(row_params const & rp, uint64_t 
 {
     for (uint64_t i = 0; i < n; ++i)
     {
-        uint64_t const v = vals[i];
+        uint64_t const v = __ldcg(vals + i);
         uint64_t off[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k)

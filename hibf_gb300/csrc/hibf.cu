@@ -635,6 +635,50 @@ std::vector<uint64_t> stream_chunks(uint64_t const * qoff, uint64_t nq)
 // answers the queries of arrived chunks while later chunks are still being copied.  Every copy is issued before the
 // kernel launch: a host call after the launch can block until the kernel ends (the first launch of a lazily loaded
 // kernel waits for the device's running work), and the kernel would then wait for chunks nobody issued.
+// Position of every user bin in the order membership_for_impl reports it (HIBF.hpp:322-355): the technical bins of
+// an IBF in order, a merged bin's subtree in place of the merged bin, a user bin where its run of bins ends.  A user
+// bin sits in one place of the hierarchy, so ordering a result by this rank gives the reference's output before
+// sort_results().  Computed once per HIBF.
+std::vector<uint64_t> const & traversal_rank(hibf_gpu_hibf * h)
+{
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->trav_rank.empty() || h->n_user_bins == 0)
+        return h->trav_rank;
+    std::vector<uint64_t> off(h->n_ibfs + 1, 0);
+    for (uint64_t k = 0; k < h->n_ibfs; ++k)
+        off[k + 1] = off[k] + h->bins[k];
+    std::vector<uint64_t> rank(h->n_user_bins, UINT64_MAX);
+    std::vector<uint8_t> entered(h->n_ibfs, 0);
+    uint64_t r = 0;
+    std::vector<std::pair<uint64_t, uint64_t>> stack{{0, 0}};
+    entered[0] = 1;
+    while (!stack.empty())
+    {
+        auto const [k, b] = stack.back();
+        stack.pop_back();
+        if (b >= h->bins[k])
+            continue;
+        stack.emplace_back(k, b + 1);
+        uint64_t const i = off[k] + b;
+        uint64_t const u = h->user_bin_id[i];
+        if (u == HIBF_GPU_BIN_MERGED)
+        {
+            uint64_t const c = h->next_ibf_id[i];
+            if (c != k && c < h->n_ibfs && !entered[c])
+            {
+                entered[c] = 1;
+                stack.emplace_back(c, 0);
+            }
+        }
+        else if (u < h->n_user_bins && (b + 1 == h->bins[k] || h->user_bin_id[i + 1] != u) && rank[u] == UINT64_MAX)
+        {
+            rank[u] = r++;
+        }
+    }
+    h->trav_rank = std::move(rank);
+    return h->trav_rank;
+}
+
 void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t const * qoff, uint64_t nq,
                 uint64_t const * thr, int width, bool plain)
 {
@@ -1814,6 +1858,27 @@ extern "C"
                 host_batch(a, HIBF_GPU_QUERY_MEMBERSHIP, values, qoff, 1, &thr, 2, true);
                 uint64_t const nr = a->h_roff.as<uint64_t>()[1];
                 a->single_ids.assign(a->h_ids.as<uint64_t>(), a->h_ids.as<uint64_t>() + nr);
+                *ids = a->single_ids.data();
+                *n_ids = nr;
+            });
+    }
+
+    int hibf_gpu_agent_membership_for_unsorted(hibf_gpu_agent * a, uint64_t const * values, uint64_t n,
+                                               uint16_t threshold, uint64_t const ** ids, uint64_t * n_ids)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || (n && !values) || !ids || !n_ids)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                uint64_t const qoff[2] = {0, n};
+                uint64_t const thr = threshold;
+                host_batch(a, HIBF_GPU_QUERY_MEMBERSHIP, values, qoff, 1, &thr, 2, true);
+                uint64_t const nr = a->h_roff.as<uint64_t>()[1];
+                a->single_ids.assign(a->h_ids.as<uint64_t>(), a->h_ids.as<uint64_t>() + nr);
+                std::vector<uint64_t> const & rank = traversal_rank(a->h);
+                std::sort(a->single_ids.begin(), a->single_ids.end(),
+                          [&](uint64_t x, uint64_t y) { return rank[x] < rank[y]; });
                 *ids = a->single_ids.data();
                 *n_ids = nr;
             });

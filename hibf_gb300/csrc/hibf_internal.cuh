@@ -52,6 +52,8 @@ struct hibf_gpu_hibf
     std::vector<uint64_t> prev_ibf, prev_bin;
     std::vector<std::vector<uint64_t>> occupancy;
     std::vector<uint8_t> track_occupancy;
+    // every user bin's position in membership_for's traversal order (computed on first use, under `mu`)
+    std::vector<uint64_t> trav_rank;
     cudaStream_t stream{};
     std::mutex mu;
 };

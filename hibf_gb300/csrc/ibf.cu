@@ -564,11 +564,24 @@ void launch_emplace(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t const 
     HG_CUDA(cudaGetLastError());
 }
 
-void launch_count(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int width, void * d_out, cudaStream_t s)
+// Per-bin counters bulk_count accumulates for filter f (a multiple of 64, at least its technical bins).
+uint64_t count_counters(hibf_gpu_ibf const * f)
 {
-    uint64_t const nc = 64u * (f->bin_words <= 32 ? (1u << f->lpv_log2()) : f->bin_words);
-    f->totals.ensure(nc * sizeof(unsigned long long));
-    HG_CUDA(cudaMemsetAsync(f->totals.p, 0, nc * sizeof(unsigned long long), s));
+    return 64u * (f->bin_words <= 32 ? (1u << f->lpv_log2()) : f->bin_words);
+}
+
+// bulk_count of n device values into d_out.  `totals` is device scratch for count_counters(f) 64-bit totals; null
+// means the filter's own buffer (grown on demand, the only allocation here).
+void launch_count(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int width, void * d_out, cudaStream_t s,
+                  unsigned long long * totals = nullptr)
+{
+    uint64_t const nc = count_counters(f);
+    if (!totals)
+    {
+        f->totals.ensure(nc * sizeof(unsigned long long));
+        totals = f->totals.as<unsigned long long>();
+    }
+    HG_CUDA(cudaMemsetAsync(totals, 0, nc * sizeof(unsigned long long), s));
     if (n)
     {
         unsigned const block = 256;
@@ -585,11 +598,10 @@ void launch_count(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int w
             HG_CUDA(cudaFuncSetAttribute(bulk_count_kernel(f->hash_funs, priv),
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
         bulk_count_kernel(f->hash_funs, priv)<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk,
-                                                                        f->totals.as<unsigned long long>(),
-                                                                        static_cast<uint32_t>(nc));
+                                                                        totals, static_cast<uint32_t>(nc));
         HG_CUDA(cudaGetLastError());
     }
-    k_store_counts<<<grid_for(f->bins, 256), 256, 0, s>>>(f->totals.as<unsigned long long>(), f->bins, width, d_out);
+    k_store_counts<<<grid_for(f->bins, 256), 256, 0, s>>>(totals, f->bins, width, d_out);
     HG_CUDA(cudaGetLastError());
 }
 
@@ -1179,9 +1191,10 @@ extern "C"
     }
 
     // Same result as hibf_gpu_ibf_bulk_count_d, for callers that cannot allocate device memory.  The counting
-    // scratch is the static array above: this call makes no cudaMalloc, cudaFree or other allocating call.  The first
-    // call on a device looks up the array's device address (issue it before any stream capture); calls that overlap
-    // on the GPU share the array and race; the totals are cleared at the start of every call.
+    // scratch is the static array above, passed to the same launch as bulk_count_d: this call makes no cudaMalloc,
+    // cudaFree or other allocating call.  The first call on a device looks up the array's device address and keeps it
+    // for the process (issue it before any stream capture; a device reset after it is not supported); calls that
+    // overlap on the GPU share the array and race; the totals are cleared at the start of every call.
     int hibf_gpu_ibf_bulk_count_noalloc_d(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t n, int width,
                                           void * d_out, void * stream)
     {
@@ -1192,31 +1205,11 @@ extern "C"
                     fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
                 if (!width_ok(width))
                     fail(HIBF_GPU_ERR_INVALID_ARG, "width must be 1, 2, 4 or 8");
-                uint64_t const nc = 64u * (f->bin_words <= 32 ? (1u << f->lpv_log2()) : f->bin_words);
-                if (nc > kNoAllocMaxCounters)
+                if (count_counters(f) > kNoAllocMaxCounters)
                     fail(HIBF_GPU_ERR_INVALID_ARG, "hibf_gpu_ibf_bulk_count_noalloc_d supports at most " +
                                                        std::to_string(kNoAllocMaxCounters) +
                                                        " bins; use hibf_gpu_ibf_bulk_count_d");
-                cudaStream_t const s = pick(f, stream);
-                unsigned long long * totals = noalloc_totals();
-                HG_CUDA(cudaMemsetAsync(totals, 0, nc * sizeof(unsigned long long), s));
-                if (n)
-                {
-                    unsigned const block = 256;
-                    uint64_t const chunk = 2048;
-                    uint64_t const warps = (n + chunk - 1) / chunk;
-                    unsigned const grid = static_cast<unsigned>(std::max<uint64_t>(
-                        1, std::min<uint64_t>((warps + 7) / 8, static_cast<uint64_t>(sm_count()) * 4u)));
-                    size_t const smem = nc * sizeof(uint32_t);
-                    if (smem > 48 * 1024)
-                        HG_CUDA(cudaFuncSetAttribute(bulk_count_kernel(f->hash_funs, false), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     static_cast<int>(smem)));
-                    bulk_count_kernel(f->hash_funs, false)<<<grid, block, smem, s>>>(f->rp(), f->lpv_log2(), d_values, n, chunk, totals,
-                                                           static_cast<uint32_t>(nc));
-                    HG_CUDA(cudaGetLastError());
-                }
-                k_store_counts<<<grid_for(f->bins, 256), 256, 0, s>>>(totals, f->bins, width, d_out);
-                HG_CUDA(cudaGetLastError());
+                launch_count(f, d_values, n, width, d_out, pick(f, stream), noalloc_totals());
             });
     }
 

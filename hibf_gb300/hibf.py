@@ -28,6 +28,29 @@ def _u64(a) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(a, dtype=np.uint64).reshape(-1))
 
 
+def ibf_paths(bins, next_ibf, user_bin) -> dict:
+    """{path of merged bins from the root: IBF index}.  The reference numbers the IBFs below the root in a shuffled
+    order (src/hierarchical_interleaved_bloom_filter.cpp:111-116), so two builds of one layout are compared IBF by
+    IBF through these paths."""
+    bins = [int(b) for b in bins]
+    off = np.zeros(len(bins) + 1, np.int64)
+    off[1:] = np.cumsum(bins)
+    nxt, ub = _u64(next_ibf), _u64(user_bin)
+    out = {(): 0}
+    seen = {0}
+    stack = [(0, ())]
+    while stack:
+        k, path = stack.pop()
+        for b in range(bins[k]):
+            i = off[k] + b
+            c = int(nxt[i])
+            if int(ub[i]) == N.BIN_MERGED and c != k and c not in seen:
+                seen.add(c)
+                out[path + (b,)] = c
+                stack.append((c, path + (b,)))
+    return out
+
+
 def traversal_rank(n_user_bins: int, bins, next_ibf, user_bin) -> np.ndarray:
     """Position of every user bin in the order membership_for reports it (HIBF.hpp:322-355): bins scanned in
     order, merged bins descended in place.  A user bin occurs in one place, so sorting a result by this rank gives
@@ -257,6 +280,15 @@ class _agent_base:
         N.call("hibf_gpu_agent_input_chunks", self._a, ctypes.byref(n))
         return int(n.value)
 
+    def last_timeline(self) -> list[float]:
+        """ms from the last host batch's first device work: each value chunk's copy done, kernel start, kernel end,
+        results back in host memory (hibf_gpu_agent_last_timeline)."""
+        n = ctypes.c_uint32(0)
+        N.call("hibf_gpu_agent_last_timeline", self._a, None, 0, ctypes.byref(n))
+        out = (ctypes.c_double * n.value)()
+        N.call("hibf_gpu_agent_last_timeline", self._a, out, n.value, ctypes.byref(n))
+        return list(out)
+
     def set_order(self, d_order: int | None, n_queries: int = 0) -> None:
         """Claim order of root tasks for later batches of exactly n_queries queries (device uint32 permutation;
         None: query order)."""
@@ -327,11 +359,9 @@ class membership_agent_type(_agent_base):
         """User bins whose summed counts reach `threshold`, in the reference's traversal order."""
         v = _u64(values)
         ids, n = N.u64p(), ctypes.c_uint64(0)
-        N.call("hibf_gpu_agent_membership_for", self._a, v.ctypes.data if v.size else None, v.size, int(threshold),
-               ctypes.byref(ids), ctypes.byref(n))
-        res = np.ctypeslib.as_array(ids, shape=(n.value,)).copy() if n.value else np.zeros(0, np.uint64)
-        rank = self.hibf.traversal_rank()
-        self.result_buffer = res[np.argsort(rank[res.astype(np.int64)], kind="stable")] if res.size else res
+        N.call("hibf_gpu_agent_membership_for_unsorted", self._a, v.ctypes.data if v.size else None, v.size,
+               int(threshold), ctypes.byref(ids), ctypes.byref(n))
+        self.result_buffer = np.ctypeslib.as_array(ids, shape=(n.value,)).copy() if n.value else np.zeros(0, np.uint64)
         return self.result_buffer
 
     def sort_results(self) -> np.ndarray:

@@ -105,8 +105,10 @@ int hibf_gpu_ibf_bulk_count_d(hibf_gpu_ibf * ibf, uint64_t const * d_values, uin
  * cudaMalloc's implicit device-wide synchronisation is not acceptable.  The counting scratch is a fixed static
  * device array of HIBF_GPU_NOALLOC_MAX_BINS 64-bit totals (128 KiB, held by every device that loads the library
  * until exit); filters with more bins are rejected with HIBF_GPU_ERR_INVALID_ARG.  The call allocates nothing.
- * Its first call on a device looks the array's address up (make that call before any stream capture).  All calls
- * share the array: calls that overlap on the GPU race; each call clears the totals it uses first. */
+ * Its first call on a device looks the array's address up and keeps it for the life of the process (make that call
+ * before any stream capture; resetting the device afterwards, e.g. cudaDeviceReset, is not supported).  It counts
+ * exactly like hibf_gpu_ibf_bulk_count_d (the same launch, with the static array as its scratch).  All calls share
+ * the array: calls that overlap on the GPU race; each call clears the totals it uses first. */
 #define HIBF_GPU_NOALLOC_MAX_BINS 16384
 int hibf_gpu_ibf_bulk_count_noalloc_d(hibf_gpu_ibf * ibf, uint64_t const * d_values, uint64_t n, int width,
                                       void * d_out, void * stream);
@@ -290,6 +292,11 @@ int hibf_gpu_agent_reserve(hibf_gpu_agent * a, uint64_t max_queries, uint64_t ma
  * query: the plain form, one device launch per call.  *ids points at the agent's sorted result buffer. */
 int hibf_gpu_agent_membership_for(hibf_gpu_agent * a, uint64_t const * values, uint64_t n, uint16_t threshold,
                                   uint64_t const ** ids, uint64_t * n_ids);
+/* membership_agent_type::membership_for alone (hierarchical_interleaved_bloom_filter.hpp:322-355, 424-439): the same
+ * user bins in the order the reference reports them before sort_results() -- depth-first, a merged bin's subtree in
+ * place of the merged bin. */
+int hibf_gpu_agent_membership_for_unsorted(hibf_gpu_agent * a, uint64_t const * values, uint64_t n,
+                                           uint16_t threshold, uint64_t const ** ids, uint64_t * n_ids);
 /* counting_agent_type<value_t>::bulk_count (hierarchical_interleaved_bloom_filter.hpp:463-566) for one query:
  * *counts points at the agent's dense vector of n_user_bins counters of `width` bytes.  threshold must be > 0. */
 int hibf_gpu_agent_bulk_count(hibf_gpu_agent * a, uint64_t const * values, uint64_t n, uint64_t threshold,

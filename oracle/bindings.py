@@ -17,7 +17,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "libhibf_oracle.so"
 REF_SO = HERE / "_ref" / "libhibf_ref.so"
-DEFAULT_REF_DIR = os.environ.get("HIBF_REFERENCE_DIR", "/root/reference")
+# The seqan/hibf source tree: HIBF_REFERENCE_DIR, else a checkout named `reference` beside this repository.
+DEFAULT_REF_DIR = os.environ.get("HIBF_REFERENCE_DIR", str(Path(__file__).resolve().parents[2] / "reference"))
 
 u64 = ctypes.c_uint64
 vp = ctypes.c_void_p
@@ -112,6 +113,14 @@ class Oracle:
         out = np.zeros(n + 1, np.uint64)
         self.lib.orc_synth_user_bin_offsets(seed, law, p0, p1, lo, hi, n, _ptr(out))
         return out
+
+    def synth_query_offsets(self, spec, first, n):
+        """(query offsets, thresholds) of queries first .. first+n-1."""
+        q = QuerySpec(spec.seed, spec.law, spec.len_lo, spec.len_hi, spec.mix_pct, spec.noise_pct, spec.thr_num,
+                      spec.thr_den, spec.n_user_bins)
+        qo, thr = np.zeros(n + 1, np.uint64), np.zeros(max(n, 1), np.uint64)
+        self.lib.orc_synth_queries(ctypes.byref(q), None, first, n, _ptr(qo), _ptr(thr), None, 0)
+        return qo, thr[:n]
 
     def synth_queries(self, spec, ub_offsets, first, n, threads=0):
         """(values, query offsets, thresholds) of queries first .. first+n-1; `spec` has the fields of

@@ -1,6 +1,7 @@
 """Generates the golden vectors in tests/golden from the REFERENCE itself.
 
-Run where the seqan/hibf source tree is available (default /root/reference, or HIBF_REFERENCE_DIR):
+Run where the seqan/hibf source tree is available (a checkout named `reference` beside this repository, or
+HIBF_REFERENCE_DIR):
 
     python tests/golden/make_golden.py
 

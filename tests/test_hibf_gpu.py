@@ -56,7 +56,8 @@ def test_hibf_batch_matches_reference(gpu_lib, name, mode):
         np.testing.assert_array_equal(dense, d[f"count{w}"])
 
 
-@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "synth64", "synth600"])
+@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "synth64", "synth600",
+                                  "synth_t256", "dups"])
 def test_hibf_single_query_agents_match_reference(gpu_lib, name):
     d = G.hibf_case(name)
     H = _gpu_hibf(d)
