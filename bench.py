@@ -451,7 +451,25 @@ def measure_hibf(args, wl, world, stream, full):
         trials = agent.autotune(d_v.data_ptr(), d_qo.data_ptr(), ns, d_thr.data_ptr(), reps=2)
         tune = {"sample_queries": ns, "seconds": time.perf_counter() - t0, "best": agent.tuning,
                 "trials": len(trials), "default_kernel_ms": trials[0]["kernel_ms"],
-                "best_kernel_ms": min(t["kernel_ms"] for t in trials)}
+                "best_kernel_ms": min(t["kernel_ms"] for t in trials),
+                "schedule_trials_ms": {("levels" if t["schedule"] else "queue"): round(t["kernel_ms"], 4)
+                                       for t in trials[:13] if t["schedule"] or t == trials[0]}}
+    elif not full and not args.no_autotune:
+        # the sub-record's workload: the two task schedules compared on a sample, the faster kept
+        ns = min(nq, args.tune_queries)
+        ab = {}
+        for sched in (N.SCHEDULE_QUEUE, N.SCHEDULE_LEVELS):
+            agent.tuning = dict(agent.tuning, schedule=sched)
+            ks = []
+            for _ in range(3):
+                agent.query_batch_device(d_v.data_ptr(), d_qo.data_ptr(), ns, d_thr.data_ptr())
+                stream.synchronize()
+                ks.append(agent.kernel_ms())
+            agent.status()
+            ab["levels" if sched else "queue"] = float(np.median(ks[1:]))
+        agent.tuning = dict(agent.tuning, schedule=N.SCHEDULE_LEVELS if ab["levels"] < ab["queue"] else
+                            N.SCHEDULE_QUEUE)
+        tune = {"sample_queries": ns, "schedule_trials_ms": ab, "best": agent.tuning}
     agent.capture_batch_device(d_v.data_ptr(), d_qo.data_ptr(), nq, d_thr.data_ptr())
     for _ in range(max(args.warmup, 3)):
         agent.replay()
@@ -586,6 +604,7 @@ def measure_hibf(args, wl, world, stream, full):
             r = srv.open_loop(pool_v, qo[:pool_q + 1], offered_qps=load, duration_s=dur, max_request_queries=4096,
                               thr_lo=0.5, thr_hi=0.9, seed=int(load))
             r["mean_batch_phases_ms"] = srv.phase_times()
+            r["tail_batch_phases"] = srv.tail_phases(0.99)
             if r["requests"] < 10_000:
                 r["p999_ms"] = None  # fewer than 10,000 requests: no meaningful 99.9th percentile
             if r["requests"] < 1_000:

@@ -30,6 +30,8 @@ ERR_CYCLE = 9
 
 QUERY_MEMBERSHIP = 1
 QUERY_COUNT = 2
+SCHEDULE_QUEUE = 0
+SCHEDULE_LEVELS = 1
 EARLY_EXIT_ADAPTIVE = 0xFFFFFFFF  # hibf_gpu_tuning.early_exit_stages: checks where the outcome can first change
 
 BIN_MERGED = (1 << 64) - 1
@@ -65,7 +67,7 @@ class Tuning(ctypes.Structure):
 
     _fields_ = [(n, ctypes.c_uint32) for n in ("values_per_lane", "fetch_bytes", "counter_bits", "blocks_per_sm",
                                                  "early_exit_first", "early_exit_step", "early_exit_stages",
-                                                 "early_exit_min", "block_queries")]
+                                                 "early_exit_min", "block_queries", "schedule")]
 
     def as_dict(self) -> dict:
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -203,6 +205,7 @@ _SIGS = [
     ("hibf_gpu_server_now", ctypes.c_double, []),
     ("hibf_gpu_server_stats", None, [vp, u64p]),
     ("hibf_gpu_server_phase_times", None, [vp, ctypes.POINTER(ctypes.c_double)]),
+    ("hibf_gpu_server_batch_log", None, [vp, ctypes.POINTER(ctypes.c_double), u64, u64p]),
     ("hibf_gpu_server_open_loop", None, [vp, vp, vp, u64, ctypes.c_double, ctypes.c_double, u64, ctypes.c_double,
                                          ctypes.c_double, u64, ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_probe_random_reads", None, [u64, u64, ctypes.POINTER(ctypes.c_double)]),

@@ -43,6 +43,106 @@ __global__ void k_init_ctrl(unsigned long long * ctrl, unsigned long long * stat
         stats[threadIdx.x] = 0;
 }
 
+// ---- level schedule: the tasks one level appended (tasks[0, ctrl[C_TAIL])), grouped by IBF for the next level ----
+// Per IBF the number of queued tasks (a block-local histogram in shared memory when the IBFs fit, else global atomics).
+__global__ void k_level_hist(unsigned long long const * __restrict__ tasks, unsigned long long const * ctrl,
+                             uint64_t task_cap, unsigned int * hist, uint32_t n_ibfs, int use_smem)
+{
+    extern __shared__ unsigned int s_hist[];
+    uint64_t const n = min(static_cast<uint64_t>(ctrl[C_TAIL]), task_cap);
+    if (use_smem)
+    {
+        for (uint32_t i = threadIdx.x; i < n_ibfs; i += blockDim.x)
+            s_hist[i] = 0;
+        __syncthreads();
+    }
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        uint32_t const k = static_cast<uint32_t>(tasks[i]) & kNodeMask;
+        if (k < n_ibfs)
+            atomicAdd(use_smem ? s_hist + k : hist + k, 1u);
+    }
+    if (use_smem)
+    {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n_ibfs; i += blockDim.x)
+            if (s_hist[i])
+                atomicAdd(hist + i, s_hist[i]);
+    }
+}
+
+// One block: exclusive scan of the histogram into per-IBF write cursors; the level's task count moves to *count and
+// the claim and append counters restart for the next level.
+__global__ void k_level_scan(unsigned int * hist, uint32_t n_ibfs, unsigned long long * ctrl, uint64_t task_cap,
+                             unsigned long long * count)
+{
+    __shared__ unsigned int s_warp[32];
+    __shared__ unsigned int s_carry;
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0)
+        s_carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n_ibfs; base += blockDim.x)
+    {
+        uint32_t const i = base + threadIdx.x;
+        unsigned int const x = i < n_ibfs ? hist[i] : 0u;
+        unsigned int y = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            unsigned int const t = __shfl_up_sync(kFullMask, y, o);
+            if (lane >= o)
+                y += t;
+        }
+        if (lane == 31)
+            s_warp[warp] = y;
+        __syncthreads();
+        if (warp == 0)
+        {
+            unsigned int z = lane < static_cast<int>(blockDim.x >> 5) ? s_warp[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                unsigned int const t = __shfl_up_sync(kFullMask, z, o);
+                if (lane >= o)
+                    z += t;
+            }
+            s_warp[lane] = z;
+        }
+        __syncthreads();
+        unsigned int const excl = s_carry + (warp ? s_warp[warp - 1] : 0u) + y - x;
+        if (i < n_ibfs)
+            hist[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_carry += s_warp[(blockDim.x >> 5) - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        *count = min(static_cast<uint64_t>(ctrl[C_TAIL]), task_cap);
+        ctrl[C_TAIL] = 0;
+        ctrl[C_HEAD] = 0;
+    }
+}
+
+// Places every task of the level at its IBF's cursor (the order within one IBF is the atomics' order; results do not
+// depend on the order in which tasks run).
+__global__ void k_level_scatter(unsigned long long const * __restrict__ tasks, unsigned long long const * count,
+                                unsigned int * cursor, unsigned long long * __restrict__ sorted, uint32_t n_ibfs)
+{
+    uint64_t const n = *count;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        unsigned long long const t = tasks[i];
+        uint32_t const k = static_cast<uint32_t>(t) & kNodeMask;
+        if (k < n_ibfs)
+            sorted[atomicAdd(cursor + k, 1u)] = t;
+    }
+}
+
 // ---- exclusive scan of the per-query result counts -> result offsets (n + 1 entries) ----
 constexpr int kScanBlock = 1024;
 
@@ -347,6 +447,8 @@ struct hibf_gpu_agent
     uint64_t qwork_n{};                    // its length: batches may have at most this many queries
     // device workspace
     dbuf ctrl, stats, tasks, rec_q, rec_ub, rec_cnt, qcount, cursor, roff, bsum, out_ids, out_cnt, out_cntw, large;
+    // level schedule: a level's tasks grouped by IBF, the per-IBF histogram / cursors, the level's task count
+    dbuf lvl_tasks, lvl_hist, lvl_count;
     // host-call staging
     dbuf in_values, in_qoff, in_thr;
     // streamed host batches: value chunks copied on copy_stream while the kernel answers the arrived ones
@@ -386,6 +488,12 @@ void ensure_capacity(hibf_gpu_agent * a, uint64_t nq, uint64_t tasks, uint64_t r
     {
         a->tasks.ensure(tasks * 8);
         a->cap_tasks = tasks;
+    }
+    if (a->tune.schedule == HIBF_GPU_SCHEDULE_LEVELS) // no-ops once large enough
+    {
+        a->lvl_tasks.ensure(a->cap_tasks * 8);
+        a->lvl_hist.ensure(a->h->n_ibfs * 4);
+        a->lvl_count.ensure(8);
     }
     if (results > a->cap_results)
     {
@@ -504,7 +612,8 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
     cudaStream_t s = a->stream;
     k_init_ctrl<<<1, 32, 0, s>>>(a->ctrl.as<unsigned long long>(), a->stats.as<unsigned long long>(), nq);
     HG_CUDA(cudaGetLastError());
-    HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, a->cap_tasks * 8, s));
+    if (a->tune.schedule != HIBF_GPU_SCHEDULE_LEVELS || nq <= a->tune.block_queries)
+        HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, a->cap_tasks * 8, s)); // the queue's empty-slot marks
     HG_CUDA(cudaMemsetAsync(a->qcount.p, 0, std::max<uint64_t>(nq, 1) * 4, s));
     if (a->qwork && nq)
         HG_CUDA(cudaMemsetAsync(a->qwork, 0, nq * 8, s));
@@ -525,9 +634,47 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         HG_CUDA(cudaStreamIsCapturing(s, &cap));
         unsigned const rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
-        (blk ? query_block_kernel(h->hash_count) : query_kernel(h->hash_count, a->variant))<<<grid, 256,
-                                                                                           query_smem(h), s>>>(p);
-        HG_CUDA(cudaGetLastError());
+        if (!blk && a->tune.schedule == HIBF_GPU_SCHEDULE_LEVELS)
+        {
+            // one launch per level: the roots, then each level's appended tasks grouped by IBF
+            if (!a->lvl_tasks.p || a->lvl_tasks.bytes < a->cap_tasks * 8 || !a->lvl_hist.p ||
+                a->lvl_hist.bytes < h->n_ibfs * 4 || !a->lvl_count.p)
+                fail(HIBF_GPU_ERR_LOGIC, "level schedule buffers missing (set the tuning through set_tuning)");
+            unsigned const grid_full = static_cast<unsigned>(full);
+            p.level = 1;
+            query_kernel(h->hash_count, a->variant)<<<grid_full, 256, query_smem(h), s>>>(p);
+            HG_CUDA(cudaGetLastError());
+            uint32_t const n_ibfs = static_cast<uint32_t>(h->n_ibfs);
+            int const use_smem = n_ibfs <= 12288;
+            unsigned const sort_grid = static_cast<unsigned>(sm_count()) * 4u;
+            for (uint32_t d = 1; d <= h->max_depth; ++d)
+            {
+                HG_CUDA(cudaMemsetAsync(a->lvl_hist.p, 0, n_ibfs * 4u, s));
+                k_level_hist<<<sort_grid, 256, use_smem ? n_ibfs * 4u : 0u, s>>>(
+                    a->tasks.as<unsigned long long>(), a->ctrl.as<unsigned long long>(), a->cap_tasks,
+                    a->lvl_hist.as<unsigned int>(), n_ibfs, use_smem);
+                HG_CUDA(cudaGetLastError());
+                k_level_scan<<<1, 1024, 0, s>>>(a->lvl_hist.as<unsigned int>(), n_ibfs,
+                                                a->ctrl.as<unsigned long long>(), a->cap_tasks,
+                                                a->lvl_count.as<unsigned long long>());
+                HG_CUDA(cudaGetLastError());
+                k_level_scatter<<<sort_grid, 256, 0, s>>>(a->tasks.as<unsigned long long>(),
+                                                          a->lvl_count.as<unsigned long long>(),
+                                                          a->lvl_hist.as<unsigned int>(),
+                                                          a->lvl_tasks.as<unsigned long long>(), n_ibfs);
+                HG_CUDA(cudaGetLastError());
+                p.in_tasks = a->lvl_tasks.as<unsigned long long>();
+                p.in_count = a->lvl_count.as<unsigned long long>();
+                query_kernel(h->hash_count, a->variant)<<<grid_full, 256, query_smem(h), s>>>(p);
+                HG_CUDA(cudaGetLastError());
+            }
+        }
+        else
+        {
+            (blk ? query_block_kernel(h->hash_count) : query_kernel(h->hash_count, a->variant))<<<grid, 256,
+                                                                                               query_smem(h), s>>>(p);
+            HG_CUDA(cudaGetLastError());
+        }
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k1, s, rec_flags));
     }
     launch_postprocess(a, nq, mode, width);
@@ -859,6 +1006,8 @@ void check_tuning(hibf_gpu_tuning const & t, hibf_gpu_hibf const * h)
                                        "words; this hierarchy takes the default (1, 8, 7)");
     if (t.blocks_per_sm > 32)
         fail(HIBF_GPU_ERR_INVALID_ARG, "blocks_per_sm must be in [0, 32]");
+    if (t.schedule != HIBF_GPU_SCHEDULE_QUEUE && t.schedule != HIBF_GPU_SCHEDULE_LEVELS)
+        fail(HIBF_GPU_ERR_INVALID_ARG, "schedule must be HIBF_GPU_SCHEDULE_QUEUE or HIBF_GPU_SCHEDULE_LEVELS");
     if (t.early_exit_stages == HIBF_GPU_EARLY_EXIT_ADAPTIVE)
     {
         if (t.early_exit_step == 0)
@@ -934,6 +1083,11 @@ void tune_search(uint32_t hash_count, uint64_t max_row_words, hibf_gpu_tune_meas
             run(t);
         }
     }
+    {
+        hibf_gpu_tuning t = best;
+        t.schedule = HIBF_GPU_SCHEDULE_LEVELS;
+        run(t);
+    }
     hibf_gpu_tuning const k = best;
     static constexpr uint32_t schedules[][2] = {{0, 0},   {10, 10}, {20, 10}, {30, 10}, {50, 10},
                                                 {30, 20}, {50, 20}, {40, 5},  {50, 5},  {60, 5}};
@@ -999,6 +1153,7 @@ int autotune_measure(hibf_gpu_tuning const * t, void * user, double * kernel_ms)
             hibf_gpu_agent * a = c.a;
             a->tune = *t;
             a->variant = variant_of(*t);
+            ensure_capacity(a, a->cap_queries, a->cap_tasks, a->cap_results); // the level schedule's buffers
             std::vector<double> ms;
             for (int r = -1; r < c.reps; ++r)
             {
@@ -1043,6 +1198,7 @@ extern "C"
         t->early_exit_stages = HIBF_GPU_EARLY_EXIT_ADAPTIVE;
         t->early_exit_min = 256;
         t->block_queries = 8192;
+        t->schedule = HIBF_GPU_SCHEDULE_QUEUE;
     }
 
     int hibf_gpu_agent_set_tuning(hibf_gpu_agent * a, hibf_gpu_tuning const * t)
@@ -1055,6 +1211,7 @@ extern "C"
                 check_tuning(*t, a->h);
                 a->tune = *t;
                 a->variant = variant_of(*t);
+                ensure_capacity(a, a->cap_queries, a->cap_tasks, a->cap_results); // level buffers, if now needed
                 if (a->graph)
                 {
                     HG_CUDA(cudaGraphExecDestroy(a->graph));
@@ -1177,6 +1334,7 @@ extern "C"
                 }
                 a->tune = best;
                 a->variant = variant_of(best);
+                ensure_capacity(a, a->cap_queries, a->cap_tasks, a->cap_results);
                 if (n_trials)
                     *n_trials = all.size();
                 if (trials)

@@ -121,6 +121,12 @@ struct query_params
     uint64_t const * arrive_first;
     uint32_t arrive_chunks;
     uint64_t arrive_limit_ns;
+    // level schedule (HIBF_GPU_SCHEDULE_LEVELS): this launch answers one level of tasks and only appends the tasks of
+    // the next level (emit_task); claims run from 0 to the level's size and stop there.  The root level (in_tasks
+    // null) claims the implicit root tasks; a later level claims in_tasks[0, *in_count), grouped by IBF.
+    uint32_t level;
+    unsigned long long const * in_tasks;
+    unsigned long long const * in_count;
 };
 
 using query_kernel_t = void (*)(query_params);
@@ -604,7 +610,43 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query(query_para
         s_held_need[w] = s_backoff[w] = s_polls[w] = 0;
     }
     __syncwarp();
-    for (;;)
+    if (p.level)
+    {
+        // level schedule: claim the level's tasks in order; no task of this launch waits for another
+        uint64_t const n_level = p.in_tasks ? *p.in_count : p.n_queries;
+        for (;;)
+        {
+            unsigned long long idx = 0;
+            if (lane == 0)
+                idx = atomicAdd(p.ctrl + C_HEAD, 1ull);
+            idx = __shfl_sync(kFullMask, idx, 0);
+            if (idx >= n_level)
+                break;
+            unsigned long long task;
+            if (p.in_tasks)
+            {
+                task = p.in_tasks[idx];
+            }
+            else
+            {
+                uint64_t const q = p.order ? p.order[idx] : idx;
+                if (q >= p.n_queries)
+                {
+                    if (lane == 0)
+                        atomicOr(p.ctrl + C_ERROR, E_ORDER);
+                    continue;
+                }
+                bool ok = true;
+                if (p.arrived && lane == 0)
+                    ok = wait_arrival(p, q);
+                if (!__shfl_sync(kFullMask, static_cast<int>(ok), 0))
+                    break; // E_TIMEOUT is set
+                task = make_task(q, 0u, 0u);
+            }
+            process_task<H, V>(p, task, counts, lane, n_tasks, n_visits, n_executed);
+        }
+    }
+    for (; !p.level;)
     {
         unsigned long long task = kEmpty;
         unsigned long long held = s_held[w];

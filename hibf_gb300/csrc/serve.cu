@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <array>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -96,6 +97,10 @@ struct hibf_gpu_server
     // summed seconds per batch phase: queueing of the batch's oldest request, staging + launch, until the batch's
     // device work is done, result fetch, per-request split
     double t_queue{}, t_stage{}, t_device{}, t_fetch{}, t_split{};
+    // per batch (the first kBatchLogCap): oldest request's arrival, slot start, launched, device done, results
+    // fetched, requests finished (seconds, now_s clock), queries, values
+    static constexpr size_t kBatchLogCap = 1u << 20;
+    std::vector<std::array<double, 8>> batch_log;
     // page-locked host ranges [begin, end) registered with the server, and whether the server pinned them
     struct host_range
     {
@@ -268,6 +273,9 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     S->t_device += t_device_done - t_launched;
     S->t_fetch += t_fetched - t_device_done;
     S->t_split += t - t_fetched;
+    if (S->batch_log.size() < hibf_gpu_server::kBatchLogCap)
+        S->batch_log.push_back({t_oldest, t_start, t_launched, t_device_done, t_fetched, t, static_cast<double>(nq),
+                                static_cast<double>(sl.nv)});
     return requeue;
 }
 
@@ -595,6 +603,20 @@ extern "C"
                 out[2] = S->t_device / n;
                 out[3] = S->t_fetch / n;
                 out[4] = S->t_split / n;
+            });
+    }
+
+    int hibf_gpu_server_batch_log(hibf_gpu_server * S, double * out, uint64_t cap, uint64_t * n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !n || (cap && !out))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(S->mu);
+                *n = S->batch_log.size();
+                for (uint64_t i = 0; i < std::min<uint64_t>(cap, S->batch_log.size()); ++i)
+                    std::copy(S->batch_log[i].begin(), S->batch_log[i].end(), out + 8 * i);
             });
     }
 

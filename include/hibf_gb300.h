@@ -381,7 +381,13 @@ typedef struct hibf_gpu_tuning
     uint32_t early_exit_min;    /* tasks with fewer values are counted in one stage */
     uint32_t block_queries;     /* batches of at most this many queries run one task per block of 8 warps (latency
                                    mode: each task's values split over the warps, no early exit); 0: never */
+    uint32_t schedule;          /* HIBF_GPU_SCHEDULE_QUEUE: one persistent launch, child tasks run as they appear;
+                                   HIBF_GPU_SCHEDULE_LEVELS: one launch per level of the hierarchy, each level's tasks
+                                   grouped by IBF first, so the warps running at any moment read a few IBFs, which
+                                   L2 holds (the root level as in the queue) */
 } hibf_gpu_tuning;
+#define HIBF_GPU_SCHEDULE_QUEUE 0u
+#define HIBF_GPU_SCHEDULE_LEVELS 1u
 /* (values_per_lane, fetch_bytes, counter_bits) in {(1,8,7) (2,8,7) (1,8,5) (2,8,5) (1,16,7) (1,16,5)}; hierarchies
  * with more than 3 hash functions or rows of more than 4 words (over 256 technical bins) take (1,8,7) only. */
 void hibf_gpu_tuning_default(hibf_gpu_tuning * t);
@@ -485,6 +491,10 @@ double hibf_gpu_server_now(void);
 /* Mean seconds per batch since creation: queueing of the batch's oldest request, staging + launch, device work,
  * result fetch, per-request split. */
 int hibf_gpu_server_phase_times(hibf_gpu_server * s, double out[5]);
+/* Per batch, in the order batches finished (at most 2^20 are kept): 8 doubles -- the arrival of its oldest request,
+ * the slot's start, the launch, device work done, results fetched, requests finished (seconds on the server's
+ * clock, hibf_gpu_server_now), its queries and values.  *n receives the batch count; at most `cap` are written. */
+int hibf_gpu_server_batch_log(hibf_gpu_server * s, double * out, uint64_t cap, uint64_t * n);
 int hibf_gpu_server_stats(hibf_gpu_server * s, uint64_t out[4]);
 /* Open-loop Poisson load from a pool of queries (host CSR): request sizes log-uniform in [1, max_request_queries],
  * per-request thresholds ceil(f * length), f uniform in [thr_lo, thr_hi].  out: achieved queries/s, p50, p99, p99.9

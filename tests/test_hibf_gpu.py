@@ -453,3 +453,90 @@ def test_streamed_host_batch_with_empty_queries_and_zero_thresholds(gpu_lib):
     assert empty.sum() > 1000 and np.all(np.diff(offs)[empty] == 0)
     zero = thr == 0
     assert zero.sum() > 50 and np.all(np.diff(offs)[zero] == d["n_ub"])
+
+
+@pytest.mark.parametrize("name", G.HIBF_CASES)
+def test_level_schedule_gives_the_reference_results(gpu_lib, name):
+    """HIBF_GPU_SCHEDULE_LEVELS (one launch per level, each level's tasks grouped by IBF): membership lists and
+    counts equal the reference's with the adaptive early exit and without one, in a permuted claim order, and from
+    a graph-captured batch replayed twice."""
+    import torch
+
+    d = G.hibf_case(name)
+    H = _gpu_hibf(d)
+    a = H.membership_agent()
+    qv, qo = d["q_values"], d["q_offsets"]
+    nq = qo.size - 1
+    exp = G.mem_lists(d, "mem_sorted")
+    w = 2 if "count2" in d else 8
+    for ee in (dict(), dict(early_exit_stages=0)):
+        a.tuning = dict(a.tuning, block_queries=0, schedule=N.SCHEDULE_LEVELS, **ee)
+        offs, ids, _ = a.query_batch(qv, qo, d["mem_t"])
+        for i, (g, e) in enumerate(zip(_split(offs, ids), exp)):
+            np.testing.assert_array_equal(g, e, err_msg=f"{ee} query {i}")
+        offs, ids, cnts = a.query_batch(qv, qo, d["cnt_t"], mode=N.QUERY_COUNT, width=w)
+        dense = np.zeros_like(d[f"count{w}"])
+        for i in range(nq):
+            dense[i, ids[offs[i]:offs[i + 1]].astype(np.int64)] = cnts[offs[i]:offs[i + 1]]
+        np.testing.assert_array_equal(dense, d[f"count{w}"], err_msg=str(ee))
+    if nq == 0:
+        return
+    dv = torch.from_numpy(qv.view(np.int64)).cuda() if qv.size else torch.zeros(1, dtype=torch.int64, device="cuda")
+    dq = torch.from_numpy(qo.view(np.int64)).cuda()
+    dt = torch.from_numpy(d["mem_t"].astype(np.uint64).view(np.int64)).cuda()
+    perm = np.random.default_rng(3).permutation(nq).astype(np.uint32)
+    dperm = torch.from_numpy(perm.view(np.int32)).cuda()
+    a.set_order(dperm.data_ptr(), nq)
+    offs, ids, _ = a.query_batch(qv, qo, d["mem_t"])
+    for i, (g, e) in enumerate(zip(_split(offs, ids), exp)):
+        np.testing.assert_array_equal(g, e, err_msg=f"ordered query {i}")
+    a.set_order(None)
+    a.reserve(nq, max(qv.size, 1), nq * 8 + 65536, nq * 64 + 65536)
+    a.capture_batch_device(dv.data_ptr(), dq.data_ptr(), nq, dt.data_ptr())
+    for _ in range(2):
+        a.replay()
+        offs, ids, _ = a.fetch_results(nq)
+        for i, (g, e) in enumerate(zip(_split(offs, ids), exp)):
+            np.testing.assert_array_equal(g, e, err_msg=f"replayed query {i}")
+
+
+def test_level_schedule_streamed_host_batch(gpu_lib, oracle):
+    """A streamed host batch (values copied in chunks while the root level waits for them) under the level
+    schedule: the oracle's results."""
+    d = G.hibf_case("synth600")
+    H = _gpu_hibf(d)
+    vals, qo, thr = _long_batch(d, 24000, np.random.default_rng(17))
+    a = H.membership_agent()
+    a.tuning = dict(a.tuning, schedule=N.SCHEDULE_LEVELS)
+    offs, ids, _ = a.query_batch(vals, qo, thr)
+    assert a.input_chunks() > 2
+    O = oracle.hibf(G.tables(d))
+    o_off, o_ids = O.membership_batch(vals, qo, thr, threads=8)
+    np.testing.assert_array_equal(offs, o_off)
+    np.testing.assert_array_equal(ids, o_ids)
+    t = a.last_timeline()
+    assert len(t) == a.input_chunks() + 3 and t[-1] >= t[-2] >= t[-3]
+
+
+def test_autotune_on_a_throughput_batch_tries_the_level_schedule(gpu_lib, oracle):
+    """A batch above block_queries runs the persistent kernel, so the search times the level schedule too; whichever
+    it keeps, the results are the oracle's."""
+    import torch
+
+    d = G.hibf_case("synth600")
+    H = _gpu_hibf(d)
+    vals, qo, thr = _long_batch(d, 12000, np.random.default_rng(23))
+    nq = qo.size - 1
+    a = H.membership_agent()
+    dv = torch.from_numpy(vals.view(np.int64)).cuda()
+    dq = torch.from_numpy(qo.view(np.int64)).cuda()
+    dt = torch.from_numpy(thr.view(np.int64)).cuda()
+    a.reserve(nq, vals.size, nq * 8 + 65536, nq * 16 + 65536)
+    torch.cuda.synchronize()
+    trials = a.autotune(dv.data_ptr(), dq.data_ptr(), nq, dt.data_ptr(), reps=1)
+    assert any(t["schedule"] == N.SCHEDULE_LEVELS for t in trials)
+    offs, ids, _ = a.query_batch(vals, qo, thr)
+    O = oracle.hibf(G.tables(d))
+    o_off, o_ids = O.membership_batch(vals, qo, thr, threads=8)
+    np.testing.assert_array_equal(offs, o_off)
+    np.testing.assert_array_equal(ids, o_ids)

@@ -27,7 +27,7 @@ def test_default_schedule():
     N.lib().hibf_gpu_tuning_default(ctypes.byref(t))
     assert t.as_dict() == dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, blocks_per_sm=0, early_exit_first=0,
                                early_exit_step=32, early_exit_stages=N.EARLY_EXIT_ADAPTIVE, early_exit_min=256,
-                               block_queries=8192)
+                               block_queries=8192, schedule=N.SCHEDULE_QUEUE)
 
 
 def cost(t):
@@ -38,6 +38,7 @@ def cost(t):
     c += 0.0 if t["early_exit_stages"] == 0 else abs(t["early_exit_first"] - 20) / 100 + t["early_exit_step"] / 1000
     c += 0.5 if t["early_exit_stages"] == 0 else 0.0
     c += abs(t["early_exit_min"] - 128) / 10000
+    c -= 0.25 * (t["schedule"] == N.SCHEDULE_LEVELS)
     return c
 
 
@@ -46,14 +47,17 @@ def test_search_finds_the_minimum_over_all_stages():
     assert kernel(best) == (1, 16, 5) and best["blocks_per_sm"] == 0
     assert (best["early_exit_first"], best["early_exit_step"], best["early_exit_min"]) == (20, 10, 128)
     assert best["early_exit_stages"] == 8  # checkpoints 20, 30, ..., 90 percent
+    assert best["schedule"] == N.SCHEDULE_LEVELS
     assert min(tr["kernel_ms"] for tr in trials) == pytest.approx(cost(best))
-    # stage 1: all six kernels at two occupancies (the default adaptive schedule); stage 2: ten fixed checkpoint
-    # schedules and the other adaptive step; stage 3: four minimums
+    # stage 1: all six kernels at two occupancies (the default adaptive schedule); then the level schedule with the
+    # fastest; stage 2: ten fixed checkpoint schedules and the other adaptive step; stage 3: four minimums
     assert {kernel(tr) for tr in trials[:12]} == VARIANTS
-    assert len(trials) == 12 + 11 + 4
+    assert trials[12]["schedule"] == N.SCHEDULE_LEVELS and kernel(trials[12]) == (1, 16, 5)
+    assert len(trials) == 12 + 1 + 11 + 4
     assert trials[0] == dict(best | dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, early_exit_first=0,
                                          early_exit_step=32, early_exit_stages=N.EARLY_EXIT_ADAPTIVE,
-                                         early_exit_min=256), kernel_ms=trials[0]["kernel_ms"])
+                                         early_exit_min=256, schedule=N.SCHEDULE_QUEUE),
+                             kernel_ms=trials[0]["kernel_ms"])
 
 
 def test_search_respects_what_the_hierarchy_admits():
@@ -62,13 +66,13 @@ def test_search_respects_what_the_hierarchy_admits():
     for h, words in ((4, 1), (5, 4), (2, 8), (3, 16)):  # more hashes or wider rows: the default kernel only
         _, trials = tune_search(h, words, cost)
         assert {kernel(tr) for tr in trials} == {(1, 8, 7)}
-        assert len(trials) == 2 + 11 + 4
+        assert len(trials) == 2 + 1 + 11 + 4
 
 
 def test_search_without_early_exit_skips_its_minimum():
     best, trials = tune_search(3, 4, lambda t: 1.0 if t["early_exit_stages"] == 0 else 2.0)
     assert best["early_exit_stages"] == 0
-    assert len(trials) == 12 + 11  # no minimum-length stage when early exit is off
+    assert len(trials) == 12 + 1 + 11  # no minimum-length stage when early exit is off
 
 
 def test_search_reports_measurement_failures():

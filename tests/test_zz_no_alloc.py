@@ -54,7 +54,9 @@ def test_noalloc_bulk_count_equals_bulk_count(gpu_lib, bins, width):
             # every bin holds >= 12 stored values and is hit by each of them at least once more than stored: compare
             # the wrapped uint8 counts with the exact 64-bit ones
             full = torch.zeros(bins, dtype=torch.int64, device="cuda")
+            torch.cuda.synchronize()  # the zero fill runs on torch's stream, the count on the filter's
             N.call("hibf_gpu_ibf_bulk_count_d", ibf._h, d_q.data_ptr(), q.size, 8, full.data_ptr(), None)
+            N.call("hibf_gpu_ibf_status", ibf._h)
             exact = full.cpu().numpy().view(np.uint64)
             np.testing.assert_array_equal(got.astype(np.uint64), exact % np.uint64(256))
             if bins == 1000:
