@@ -69,8 +69,9 @@ def parse_args():
     ap.add_argument("--no-c4", action="store_true", help="skip the 65,536-user-bin sub-record")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel schedule")
     ap.add_argument("--tuning", type=str, default="",
-                    help="fixed kernel schedule 'values_per_lane,fetch_bytes,counter_bits[,adaptive_step,ee_min]' "
-                         "(skips the autotuner; the two optional fields select the adaptive early exit)")
+                    help="fixed kernel schedule 'values_per_lane,fetch_bytes,counter_bits[,adaptive_step,ee_min"
+                         "[,schedule]]' (skips the autotuner; the optional fields select the adaptive early exit and "
+                         "the task schedule: 0 work queue, 1 level by level)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned scheduler measurement")
     ap.add_argument("--sched-queries", type=int, default=20000, help="batch size of the learned scheduler test")
     ap.add_argument("--tune-queries", type=int, default=200_000, help="sample batch of the autotuner")
@@ -443,6 +444,8 @@ def measure_hibf(args, wl, world, stream, full):
         if len(f) >= 5:
             t.update(early_exit_first=0, early_exit_step=f[3], early_exit_stages=N.EARLY_EXIT_ADAPTIVE,
                      early_exit_min=f[4])
+        if len(f) >= 6:
+            t.update(schedule=f[5])
         agent.tuning = t
         tune = {"fixed": agent.tuning}
     elif full and not args.no_autotune:
@@ -692,7 +695,7 @@ def run_ours(args, wl, rank, world, local):
         m4 = measure_hibf(args, w4, world, stream, full=False)
         c4 = {k: m4[k] for k in ("value", "unit", "ms_per_step", "steps", "config", "index_bytes", "queries_per_s",
                                  "e2e", "roofline", "cpu_baseline", "plain", "batched_vs_plain", "bulk_count",
-                                 "build", "clocks")}
+                                 "build", "autotune", "clocks")}
         m["parity"].update({"c4_" + k: v for k, v in m4["parity"].items()})
     out = None
     if rank == 0:
