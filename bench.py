@@ -448,31 +448,38 @@ def measure_hibf(args, wl, world, stream, full):
             t.update(schedule=f[5])
         agent.tuning = t
         tune = {"fixed": agent.tuning}
-    elif full and not args.no_autotune:
-        ns = min(nq, args.tune_queries)
-        t0 = time.perf_counter()
-        trials = agent.autotune(d_v.data_ptr(), d_qo.data_ptr(), ns, d_thr.data_ptr(), reps=2)
-        tune = {"sample_queries": ns, "seconds": time.perf_counter() - t0, "best": agent.tuning,
-                "trials": len(trials), "default_kernel_ms": trials[0]["kernel_ms"],
-                "best_kernel_ms": min(t["kernel_ms"] for t in trials),
-                "schedule_trials_ms": {("levels" if t["schedule"] else "queue"): round(t["kernel_ms"], 4)
-                                       for t in trials[:13] if t["schedule"] or t == trials[0]}}
-    elif not full and not args.no_autotune:
-        # the sub-record's workload: the two task schedules compared on a sample, the faster kept
-        ns = min(nq, args.tune_queries)
+    elif not args.no_autotune:
+        tune = {}
+        if full:
+            ns = min(nq, args.tune_queries)
+            t0 = time.perf_counter()
+            trials = agent.autotune(d_v.data_ptr(), d_qo.data_ptr(), ns, d_thr.data_ptr(), reps=2)
+            tune = {"sample_queries": ns, "seconds": time.perf_counter() - t0, "sample_best": agent.tuning,
+                    "trials": len(trials), "default_kernel_ms": trials[0]["kernel_ms"],
+                    "best_kernel_ms": min(t["kernel_ms"] for t in trials)}
+        # the task schedule is decided on the whole batch: grouping a level's tasks by IBF pays more the more tasks
+        # share an IBF, which a sample understates
+        base = agent.tuning
         ab = {}
-        for sched in (N.SCHEDULE_QUEUE, N.SCHEDULE_LEVELS):
-            agent.tuning = dict(agent.tuning, schedule=sched)
+        for label, extra in (("queue", dict(schedule=N.SCHEDULE_QUEUE, level_values_per_lane=0)),
+                             ("levels", dict(schedule=N.SCHEDULE_LEVELS, level_values_per_lane=0)),
+                             ("levels_2_values_per_lane_below_root",
+                              dict(schedule=N.SCHEDULE_LEVELS, level_values_per_lane=2))):
+            try:
+                agent.tuning = dict(base, **extra)
+            except N.InvalidArgument:
+                continue  # no such kernel for this hierarchy
             ks = []
-            for _ in range(3):
-                agent.query_batch_device(d_v.data_ptr(), d_qo.data_ptr(), ns, d_thr.data_ptr())
+            for _ in range(2):
+                agent.query_batch_device(d_v.data_ptr(), d_qo.data_ptr(), nq, d_thr.data_ptr())
                 stream.synchronize()
                 ks.append(agent.kernel_ms())
             agent.status()
-            ab["levels" if sched else "queue"] = float(np.median(ks[1:]))
-        agent.tuning = dict(agent.tuning, schedule=N.SCHEDULE_LEVELS if ab["levels"] < ab["queue"] else
-                            N.SCHEDULE_QUEUE)
-        tune = {"sample_queries": ns, "schedule_trials_ms": ab, "best": agent.tuning}
+            ab[label] = (min(ks), dict(agent.tuning))
+        best = min(ab, key=lambda k: ab[k][0])
+        agent.tuning = ab[best][1]
+        tune.update(schedule_trials_full_batch_ms={k: round(v[0], 3) for k, v in ab.items()}, schedule=best,
+                    best=agent.tuning)
     agent.capture_batch_device(d_v.data_ptr(), d_qo.data_ptr(), nq, d_thr.data_ptr())
     for _ in range(max(args.warmup, 3)):
         agent.replay()
@@ -510,7 +517,17 @@ def measure_hibf(args, wl, world, stream, full):
         stream.synchronize()
         kms.append(agent.kernel_ms())
     kernel_ms = sum(kms) / len(kms)
+    level_ms = agent.level_ms()
     res_offs, res_ids, _ = agent.fetch_results(nq)
+    # the device's own random 8-byte read rate at the index's footprint (fully random, and 2 MiB-local)
+    import ctypes as _ct
+
+    probe = {}
+    fp = min(int(hibf.info()["device_bytes"]), 16 << 30)
+    for name, region in (("random", 0), ("window_2MiB", 2 << 20)):
+        rps = _ct.c_double(0)
+        N.call("hibf_gpu_probe_random_reads", fp, region, _ct.byref(rps))
+        probe[name] = rps.value
 
     # plain form: one launch per query on the first P queries
     P = min(args.plain_queries if full else 1000, nq)
@@ -660,13 +677,19 @@ def measure_hibf(args, wl, world, stream, full):
                      "kernel": "k_query", "kernel_ms": kernel_ms, "value_visits": visits,
                      "value_visits_executed": executed, "tasks": tasks,
                      "algorithmic_bytes_per_value_visit": bytes_per_visit,
-                     "row_reads_per_s": executed * wl.h / (kernel_ms / 1e3)},
+                     "row_reads_per_s": executed * wl.h / (kernel_ms / 1e3),
+                     "level_ms": [round(x, 3) for x in level_ms],
+                     "random_read_ceiling": {"footprint_bytes": fp, "reads_per_s_random": probe["random"],
+                                             "reads_per_s_2MiB_windows": probe["window_2MiB"],
+                                             "probe": "hibf_gpu_probe_random_reads"}},
         "cpu_baseline": cpu, "clocks": clk,
         "plain": {"values_per_s": plain_vps, "queries": P, "form": "one launch per query"},
         "batched_vs_plain": value / world / plain_vps,
         "bulk_count": count, "build": build, "autotune": tune, "learned_scheduler": learned,
         "serving": serving, "parity": parity,
-        "gpu_launches": 8 * steps,
+        # per step: control reset, the query kernel (one launch per level, and three grouping kernels between
+        # levels, under the level schedule), six compaction kernels
+        "gpu_launches": steps * (1 + (1 if not level_ms else 1 + 4 * (len(level_ms) - 1)) + 6),
     }
     del agent, hibf, d_v, d_qo, d_thr, d_ub, h_v
     gc.collect()

@@ -67,7 +67,8 @@ class Tuning(ctypes.Structure):
 
     _fields_ = [(n, ctypes.c_uint32) for n in ("values_per_lane", "fetch_bytes", "counter_bits", "blocks_per_sm",
                                                  "early_exit_first", "early_exit_step", "early_exit_stages",
-                                                 "early_exit_min", "block_queries", "schedule")]
+                                                 "early_exit_min", "block_queries", "schedule",
+                                                 "level_values_per_lane")]
 
     def as_dict(self) -> dict:
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -171,6 +172,8 @@ _SIGS = [
     ("hibf_gpu_agent_capture_batch_d", None, [vp, ci, vp, vp, u64, vp, ci]),
     ("hibf_gpu_agent_replay", None, [vp]),
     ("hibf_gpu_agent_kernel_ms", None, [vp, ctypes.POINTER(ctypes.c_float)]),
+    ("hibf_gpu_agent_level_ms", None, [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_uint32,
+                                       ctypes.POINTER(ctypes.c_uint32)]),
     ("hibf_gpu_agent_input_chunks", None, [vp, ctypes.POINTER(ctypes.c_uint32)]),
     ("hibf_gpu_agent_last_timeline", None, [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
                                             ctypes.POINTER(ctypes.c_uint32)]),

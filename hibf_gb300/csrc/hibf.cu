@@ -439,6 +439,7 @@ struct hibf_gpu_agent
     uint64_t cap_queries{}, cap_tasks{}, cap_results{};
     hibf_gpu_tuning tune{};                // schedule of the persistent kernel
     int variant{0};                        // kernel variant of `tune`
+    int child_variant{0};                  // kernel variant of the levels below the root (level schedule)
     int max_blocks[kQueryVariants]{};      // resident 256-thread blocks per SM of each variant
     int max_blocks_blk{};                  // and of the block-per-task kernel
     uint32_t const * order{};              // claim order of the root tasks (device; null = query order)
@@ -447,8 +448,12 @@ struct hibf_gpu_agent
     uint64_t qwork_n{};                    // its length: batches may have at most this many queries
     // device workspace
     dbuf ctrl, stats, tasks, rec_q, rec_ub, rec_cnt, qcount, cursor, roff, bsum, out_ids, out_cnt, out_cntw, large;
-    // level schedule: a level's tasks grouped by IBF, the per-IBF histogram / cursors, the level's task count
+    // level schedule: a level's tasks grouped by IBF, the per-IBF histogram / cursors, the level's task count; an
+    // event after each level of the last batch (timing)
     dbuf lvl_tasks, lvl_hist, lvl_count;
+    std::vector<cudaEvent_t> ev_lvl;
+    uint32_t last_levels{};
+    bool force_queue{}; // set for the duration of a streamed host batch
     // host-call staging
     dbuf in_values, in_qoff, in_thr;
     // streamed host batches: value chunks copied on copy_stream while the kernel answers the arrived ones
@@ -634,16 +639,29 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         HG_CUDA(cudaStreamIsCapturing(s, &cap));
         unsigned const rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
-        if (!blk && a->tune.schedule == HIBF_GPU_SCHEDULE_LEVELS)
+        a->last_levels = 0;
+        if (!blk && a->tune.schedule == HIBF_GPU_SCHEDULE_LEVELS && !a->force_queue)
         {
             // one launch per level: the roots, then each level's appended tasks grouped by IBF
             if (!a->lvl_tasks.p || a->lvl_tasks.bytes < a->cap_tasks * 8 || !a->lvl_hist.p ||
                 a->lvl_hist.bytes < h->n_ibfs * 4 || !a->lvl_count.p)
                 fail(HIBF_GPU_ERR_LOGIC, "level schedule buffers missing (set the tuning through set_tuning)");
+            while (a->ev_lvl.size() <= h->max_depth)
+            {
+                cudaEvent_t e{};
+                HG_CUDA(cudaEventCreate(&e));
+                a->ev_lvl.push_back(e);
+            }
             unsigned const grid_full = static_cast<unsigned>(full);
+            int const child_variant = a->child_variant;
+            int const child_fit = a->max_blocks[child_variant];
+            int const child_per_sm =
+                a->tune.blocks_per_sm ? std::min<int>(child_fit, static_cast<int>(a->tune.blocks_per_sm)) : child_fit;
+            unsigned const grid_child = static_cast<unsigned>(sm_count()) * static_cast<unsigned>(child_per_sm);
             p.level = 1;
             query_kernel(h->hash_count, a->variant)<<<grid_full, 256, query_smem(h), s>>>(p);
             HG_CUDA(cudaGetLastError());
+            HG_CUDA(cudaEventRecordWithFlags(a->ev_lvl[0], s, rec_flags));
             uint32_t const n_ibfs = static_cast<uint32_t>(h->n_ibfs);
             int const use_smem = n_ibfs <= 12288;
             unsigned const sort_grid = static_cast<unsigned>(sm_count()) * 4u;
@@ -665,9 +683,11 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
                 HG_CUDA(cudaGetLastError());
                 p.in_tasks = a->lvl_tasks.as<unsigned long long>();
                 p.in_count = a->lvl_count.as<unsigned long long>();
-                query_kernel(h->hash_count, a->variant)<<<grid_full, 256, query_smem(h), s>>>(p);
+                query_kernel(h->hash_count, child_variant)<<<grid_child, 256, query_smem(h), s>>>(p);
                 HG_CUDA(cudaGetLastError());
+                HG_CUDA(cudaEventRecordWithFlags(a->ev_lvl[d], s, rec_flags));
             }
+            a->last_levels = h->max_depth + 1;
         }
         else
         {
@@ -842,6 +862,15 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
         qb = stream_chunks(qoff, nq);
     bool const streamed = qb.size() > 2;
     a->last_chunks = streamed ? static_cast<uint32_t>(qb.size() - 1) : 0u;
+    struct queue_guard // a streamed batch runs the work queue (children run while later roots are still copied)
+    {
+        hibf_gpu_agent * a;
+        ~queue_guard()
+        {
+            a->force_queue = false;
+        }
+    } const queue_reset{a};
+    a->force_queue = streamed;
     uint64_t tasks = std::max<uint64_t>(a->cap_tasks, nq * 4 + 1024);
     uint64_t results = std::max<uint64_t>(a->cap_results, nq * 4 + 1024);
     ensure_capacity(a, std::max<uint64_t>(nq, 1), tasks, results); // allocations synchronise: before any copy
@@ -996,8 +1025,20 @@ int variant_of(hibf_gpu_tuning const & t)
     return -1;
 }
 
+// The kernel variant of the levels below the root: values_per_lane replaced by level_values_per_lane when set.
+int child_variant_of(hibf_gpu_tuning t)
+{
+    if (t.level_values_per_lane)
+        t.values_per_lane = t.level_values_per_lane;
+    return variant_of(t);
+}
+
 void check_tuning(hibf_gpu_tuning const & t, hibf_gpu_hibf const * h)
 {
+    int const cv = child_variant_of(t);
+    if (cv < 0 || (cv != 0 && !variants_apply(h->hash_count, max_bin_words(h))))
+        fail(HIBF_GPU_ERR_INVALID_ARG, "no query kernel for level_values_per_lane with this fetch_bytes and "
+                                       "counter_bits on this hierarchy");
     int const v = variant_of(t);
     if (v < 0)
         fail(HIBF_GPU_ERR_INVALID_ARG, "no query kernel for this (values_per_lane, fetch_bytes, counter_bits)");
@@ -1034,6 +1075,12 @@ hibf_gpu_tuning with_adaptive(hibf_gpu_tuning t, uint32_t min_values)
     t.early_exit_first = 0;
     t.early_exit_step = min_values;
     t.early_exit_stages = HIBF_GPU_EARLY_EXIT_ADAPTIVE;
+    return t;
+}
+
+hibf_gpu_tuning with_vpl(hibf_gpu_tuning t, uint32_t vpl)
+{
+    t.values_per_lane = vpl;
     return t;
 }
 
@@ -1087,6 +1134,9 @@ void tune_search(uint32_t hash_count, uint64_t max_row_words, hibf_gpu_tune_meas
         hibf_gpu_tuning t = best;
         t.schedule = HIBF_GPU_SCHEDULE_LEVELS;
         run(t);
+        t.level_values_per_lane = 2; // more loads in flight where L2 holds the IBFs
+        if (variants_apply(hash_count, max_row_words) && variant_of(with_vpl(t, 2)) >= 0 && t.values_per_lane != 2)
+            run(t);
     }
     hibf_gpu_tuning const k = best;
     static constexpr uint32_t schedules[][2] = {{0, 0},   {10, 10}, {20, 10}, {30, 10}, {50, 10},
@@ -1153,6 +1203,7 @@ int autotune_measure(hibf_gpu_tuning const * t, void * user, double * kernel_ms)
             hibf_gpu_agent * a = c.a;
             a->tune = *t;
             a->variant = variant_of(*t);
+            a->child_variant = child_variant_of(*t);
             ensure_capacity(a, a->cap_queries, a->cap_tasks, a->cap_results); // the level schedule's buffers
             std::vector<double> ms;
             for (int r = -1; r < c.reps; ++r)
@@ -1199,6 +1250,7 @@ extern "C"
         t->early_exit_min = 256;
         t->block_queries = 8192;
         t->schedule = HIBF_GPU_SCHEDULE_QUEUE;
+        t->level_values_per_lane = 0;
     }
 
     int hibf_gpu_agent_set_tuning(hibf_gpu_agent * a, hibf_gpu_tuning const * t)
@@ -1211,6 +1263,7 @@ extern "C"
                 check_tuning(*t, a->h);
                 a->tune = *t;
                 a->variant = variant_of(*t);
+                a->child_variant = child_variant_of(*t);
                 ensure_capacity(a, a->cap_queries, a->cap_tasks, a->cap_results); // level buffers, if now needed
                 if (a->graph)
                 {
@@ -1330,10 +1383,12 @@ extern "C"
                 {
                     a->tune = before;
                     a->variant = variant_of(before);
+                    a->child_variant = child_variant_of(before);
                     throw;
                 }
                 a->tune = best;
                 a->variant = variant_of(best);
+                a->child_variant = child_variant_of(best);
                 ensure_capacity(a, a->cap_queries, a->cap_tasks, a->cap_results);
                 if (n_trials)
                     *n_trials = all.size();
@@ -1964,6 +2019,8 @@ extern "C"
                 }
                 for (cudaEvent_t e : a->tl_chunk)
                     cudaEventDestroy(e);
+                for (cudaEvent_t e : a->ev_lvl)
+                    cudaEventDestroy(e);
                 if (a->copy_stream)
                 {
                     cudaStreamSynchronize(a->copy_stream);
@@ -2252,6 +2309,22 @@ extern "C"
                 *n = qb.size();
                 std::copy(qb.begin(), qb.begin() + static_cast<std::ptrdiff_t>(std::min<uint64_t>(cap, qb.size())),
                           first_queries);
+            });
+    }
+
+    int hibf_gpu_agent_level_ms(hibf_gpu_agent * a, float * ms, uint32_t cap, uint32_t * n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !n || (cap && !ms))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *n = a->last_levels;
+                if (a->last_levels == 0)
+                    return;
+                HG_CUDA(cudaEventSynchronize(a->ev_lvl[a->last_levels - 1]));
+                for (uint32_t d = 0; d < std::min(cap, a->last_levels); ++d)
+                    HG_CUDA(cudaEventElapsedTime(ms + d, d ? a->ev_lvl[d - 1] : a->ev_k0, a->ev_lvl[d]));
             });
     }
 

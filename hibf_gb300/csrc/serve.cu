@@ -63,6 +63,7 @@ struct slot
     hibf_gpu_agent * agent{};
     cudaStream_t stream{};
     cudaEvent_t ev{};
+    cudaEvent_t ev_in{}, ev_q{}; // timing: before the batch's input copies, before its launch
     std::vector<request *> reqs;
     uint64_t nq{}, nv{}, bytes{};
     dbuf d_values, d_qoff, d_thr;
@@ -98,9 +99,10 @@ struct hibf_gpu_server
     // device work is done, result fetch, per-request split
     double t_queue{}, t_stage{}, t_device{}, t_fetch{}, t_split{};
     // per batch (the first kBatchLogCap): oldest request's arrival, slot start, launched, device done, results
-    // fetched, requests finished (seconds, now_s clock), queries, values
+    // fetched, requests finished (seconds, now_s clock), queries, values, device time of its input copies and of
+    // its query kernel (seconds, CUDA events)
     static constexpr size_t kBatchLogCap = 1u << 20;
-    std::vector<std::array<double, 8>> batch_log;
+    std::vector<std::array<double, 10>> batch_log;
     // page-locked host ranges [begin, end) registered with the server, and whether the server pinned them
     struct host_range
     {
@@ -176,6 +178,7 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     uint64_t * ht = sl.h_thr.as<uint64_t>();
     uint64_t q = 0, v = 0;
     ho[0] = 0;
+    HG_CUDA(cudaEventRecord(sl.ev_in, sl.stream));
     uint64_t staged_from = 0; // start of the current run of staged requests
     auto flush_staged = [&](uint64_t to)
     {
@@ -210,6 +213,7 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     HG_CUDA(cudaMemcpyAsync(sl.d_qoff.p, ho, (nq + 1) * 8, cudaMemcpyHostToDevice, sl.stream));
     HG_CUDA(cudaMemcpyAsync(sl.d_thr.p, ht, std::max<uint64_t>(nq, 1) * 8, cudaMemcpyHostToDevice, sl.stream));
     void const * cnt = nullptr;
+    HG_CUDA(cudaEventRecord(sl.ev_q, sl.stream));
     int st = hibf_gpu_agent_query_batch_d(sl.agent, HIBF_GPU_QUERY_MEMBERSHIP, sl.d_values.as<uint64_t>(),
                                           sl.d_qoff.as<uint64_t>(), nq, sl.d_thr.as<uint64_t>(), 2, &sl.d_roff,
                                           &sl.d_ids, &cnt);
@@ -265,6 +269,10 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     double const t = now_s();
     for (request * r : sl.reqs)
         finish(r, HIBF_GPU_OK, t);
+    float copy_ms = 0, kernel_ms = 0;
+    if (cudaEventElapsedTime(&copy_ms, sl.ev_in, sl.ev_q) != cudaSuccess ||
+        hibf_gpu_agent_kernel_ms(sl.agent, &kernel_ms) != HIBF_GPU_OK)
+        (void)cudaGetLastError();
     std::lock_guard<std::mutex> lk(S->mu);
     ++S->batches;
     S->batched_queries += nq;
@@ -275,7 +283,7 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     S->t_split += t - t_fetched;
     if (S->batch_log.size() < hibf_gpu_server::kBatchLogCap)
         S->batch_log.push_back({t_oldest, t_start, t_launched, t_device_done, t_fetched, t, static_cast<double>(nq),
-                                static_cast<double>(sl.nv)});
+                                static_cast<double>(sl.nv), copy_ms * 1e-3, kernel_ms * 1e-3});
     return requeue;
 }
 
@@ -350,6 +358,8 @@ extern "C"
                         fail(st, "agent creation failed");
                     HG_CUDA(cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking));
                     HG_CUDA(cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming));
+                    HG_CUDA(cudaEventCreate(&sl->ev_in));
+                    HG_CUDA(cudaEventCreate(&sl->ev_q));
                     st = hibf_gpu_agent_set_stream(sl->agent, sl->stream);
                     if (st != HIBF_GPU_OK)
                         fail(st, "agent stream");
@@ -433,6 +443,8 @@ extern "C"
                     cudaStreamSynchronize(sl->stream);
                     hibf_gpu_agent_destroy(sl->agent);
                     cudaEventDestroy(sl->ev);
+                    cudaEventDestroy(sl->ev_in);
+                    cudaEventDestroy(sl->ev_q);
                     cudaStreamDestroy(sl->stream);
                 }
                 delete S;
@@ -616,7 +628,7 @@ extern "C"
                 std::lock_guard<std::mutex> lk(S->mu);
                 *n = S->batch_log.size();
                 for (uint64_t i = 0; i < std::min<uint64_t>(cap, S->batch_log.size()); ++i)
-                    std::copy(S->batch_log[i].begin(), S->batch_log[i].end(), out + 8 * i);
+                    std::copy(S->batch_log[i].begin(), S->batch_log[i].end(), out + 10 * i);
             });
     }
 

@@ -280,6 +280,13 @@ class _agent_base:
         N.call("hibf_gpu_agent_input_chunks", self._a, ctypes.byref(n))
         return int(n.value)
 
+    def level_ms(self) -> list[float]:
+        """Per level of the last batch under the level schedule: device ms (root first); [] for the queue."""
+        n = ctypes.c_uint32(0)
+        out = (ctypes.c_float * 16)()
+        N.call("hibf_gpu_agent_level_ms", self._a, out, 16, ctypes.byref(n))
+        return [float(out[i]) for i in range(min(n.value, 16))]
+
     def last_timeline(self) -> list[float]:
         """ms from the last host batch's first device work: each value chunk's copy done, kernel start, kernel end,
         results back in host memory (hibf_gpu_agent_last_timeline)."""

@@ -101,13 +101,14 @@ class server:
         return dict(zip(("queue_ms", "stage_ms", "device_ms", "fetch_ms", "split_ms"), (x * 1e3 for x in out)))
 
     def batch_log(self) -> np.ndarray:
-        """Per batch: oldest arrival, slot start, launched, device done, fetched, finished (s), queries, values."""
+        """Per batch: oldest arrival, slot start, launched, device done, fetched, finished (s), queries, values,
+        device time of the input copies and of the query kernel (s)."""
         n = ctypes.c_uint64(0)
         N.call("hibf_gpu_server_batch_log", self._s, None, 0, ctypes.byref(n))
-        out = np.zeros(max(n.value, 1) * 8, np.float64)
+        out = np.zeros(max(n.value, 1) * 10, np.float64)
         N.call("hibf_gpu_server_batch_log", self._s, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n.value,
                ctypes.byref(n))
-        return out[:n.value * 8].reshape(n.value, 8)
+        return out[:n.value * 10].reshape(n.value, 10)
 
     def tail_phases(self, quantile: float = 0.99) -> dict:
         """Phase times (ms) of the batches whose oldest request waited longest (the top 1 - quantile share), beside
@@ -116,11 +117,11 @@ class server:
         if log.shape[0] == 0:
             return {}
         ph = np.stack([log[:, 1] - log[:, 0], log[:, 2] - log[:, 1], log[:, 3] - log[:, 2], log[:, 4] - log[:, 3],
-                       log[:, 5] - log[:, 4]], axis=1) * 1e3
+                       log[:, 5] - log[:, 4], log[:, 8], log[:, 9]], axis=1) * 1e3
         total = log[:, 5] - log[:, 0]
         cut = np.quantile(total, quantile)
         tail = ph[total >= cut]
-        names = ("queue_ms", "stage_ms", "device_ms", "fetch_ms", "split_ms")
+        names = ("queue_ms", "stage_ms", "device_ms", "fetch_ms", "split_ms", "copy_in_ms", "kernel_ms")
         return {"batches": int(log.shape[0]), "tail_batches": int(tail.shape[0]),
                 "median_batch": dict(zip(names, np.median(ph, axis=0).round(4).tolist())),
                 "tail_mean": dict(zip(names, tail.mean(axis=0).round(4).tolist())),

@@ -343,6 +343,10 @@ int hibf_gpu_agent_capture_batch_d(hibf_gpu_agent * a, int mode, uint64_t const 
 int hibf_gpu_agent_replay(hibf_gpu_agent * a);
 /* Device time of the persistent query kernel of the agent's last batch (CUDA events on the agent's stream). */
 int hibf_gpu_agent_kernel_ms(hibf_gpu_agent * a, float * ms);
+/* Under HIBF_GPU_SCHEDULE_LEVELS: device time of each level of the agent's last batch (the root first; a level's time
+ * includes grouping its tasks by IBF).  *n receives the level count (0 for a batch run by the queue); at most `cap`
+ * are written. */
+int hibf_gpu_agent_level_ms(hibf_gpu_agent * a, float * ms, uint32_t cap, uint32_t * n);
 /* Number of chunks in which the agent's last host batch streamed its values (0: copied whole before the launch). */
 int hibf_gpu_agent_input_chunks(hibf_gpu_agent const * a, uint32_t * chunks);
 /* Timeline of the agent's last host batch (hibf_gpu_agent_query_batch), in ms from the call's first device work:
@@ -384,7 +388,10 @@ typedef struct hibf_gpu_tuning
     uint32_t schedule;          /* HIBF_GPU_SCHEDULE_QUEUE: one persistent launch, child tasks run as they appear;
                                    HIBF_GPU_SCHEDULE_LEVELS: one launch per level of the hierarchy, each level's tasks
                                    grouped by IBF first, so the warps running at any moment read a few IBFs, which
-                                   L2 holds (the root level as in the queue) */
+                                   L2 holds (the root level as in the queue).  A streamed host batch always runs
+                                   the queue: its roots arrive over the copy and children run in between */
+    uint32_t level_values_per_lane; /* HIBF_GPU_SCHEDULE_LEVELS: values_per_lane of the levels below the root, whose
+                                       IBFs L2 mostly holds (more loads in flight per lane); 0: values_per_lane */
 } hibf_gpu_tuning;
 #define HIBF_GPU_SCHEDULE_QUEUE 0u
 #define HIBF_GPU_SCHEDULE_LEVELS 1u
@@ -491,9 +498,10 @@ double hibf_gpu_server_now(void);
 /* Mean seconds per batch since creation: queueing of the batch's oldest request, staging + launch, device work,
  * result fetch, per-request split. */
 int hibf_gpu_server_phase_times(hibf_gpu_server * s, double out[5]);
-/* Per batch, in the order batches finished (at most 2^20 are kept): 8 doubles -- the arrival of its oldest request,
+/* Per batch, in the order batches finished (at most 2^20 are kept): 10 doubles -- the arrival of its oldest request,
  * the slot's start, the launch, device work done, results fetched, requests finished (seconds on the server's
- * clock, hibf_gpu_server_now), its queries and values.  *n receives the batch count; at most `cap` are written. */
+ * clock, hibf_gpu_server_now), its queries and values, and the device time (s, CUDA events) of its input copies and
+ * of its query kernel.  *n receives the batch count; at most `cap` are written. */
 int hibf_gpu_server_batch_log(hibf_gpu_server * s, double * out, uint64_t cap, uint64_t * n);
 int hibf_gpu_server_stats(hibf_gpu_server * s, uint64_t out[4]);
 /* Open-loop Poisson load from a pool of queries (host CSR): request sizes log-uniform in [1, max_request_queries],

@@ -27,7 +27,7 @@ def test_default_schedule():
     N.lib().hibf_gpu_tuning_default(ctypes.byref(t))
     assert t.as_dict() == dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, blocks_per_sm=0, early_exit_first=0,
                                early_exit_step=32, early_exit_stages=N.EARLY_EXIT_ADAPTIVE, early_exit_min=256,
-                               block_queries=8192, schedule=N.SCHEDULE_QUEUE)
+                               block_queries=8192, schedule=N.SCHEDULE_QUEUE, level_values_per_lane=0)
 
 
 def cost(t):
@@ -56,7 +56,8 @@ def test_search_finds_the_minimum_over_all_stages():
     assert len(trials) == 12 + 1 + 11 + 4
     assert trials[0] == dict(best | dict(values_per_lane=1, fetch_bytes=8, counter_bits=7, early_exit_first=0,
                                          early_exit_step=32, early_exit_stages=N.EARLY_EXIT_ADAPTIVE,
-                                         early_exit_min=256, schedule=N.SCHEDULE_QUEUE),
+                                         early_exit_min=256, schedule=N.SCHEDULE_QUEUE,
+                                         level_values_per_lane=0),
                              kernel_ms=trials[0]["kernel_ms"])
 
 
@@ -72,7 +73,9 @@ def test_search_respects_what_the_hierarchy_admits():
 def test_search_without_early_exit_skips_its_minimum():
     best, trials = tune_search(3, 4, lambda t: 1.0 if t["early_exit_stages"] == 0 else 2.0)
     assert best["early_exit_stages"] == 0
-    assert len(trials) == 12 + 1 + 11  # no minimum-length stage when early exit is off
+    # the level schedule, then its two values per lane below the root (the default kernel has one)
+    assert len(trials) == 12 + 2 + 11  # no minimum-length stage when early exit is off
+    assert trials[13]["schedule"] == N.SCHEDULE_LEVELS and trials[13]["level_values_per_lane"] == 2
 
 
 def test_search_reports_measurement_failures():
