@@ -469,8 +469,12 @@ def test_level_schedule_gives_the_reference_results(gpu_lib, name):
     nq = qo.size - 1
     exp = G.mem_lists(d, "mem_sorted")
     w = 2 if "count2" in d else 8
-    for ee in (dict(), dict(early_exit_stages=0)):
-        a.tuning = dict(a.tuning, block_queries=0, schedule=N.SCHEDULE_LEVELS, **ee)
+    for ee in (dict(), dict(early_exit_stages=0), dict(level_values_per_lane=2)):
+        try:
+            a.tuning = dict(a.tuning, block_queries=0, schedule=N.SCHEDULE_LEVELS, **ee)
+        except hg.InvalidArgument:
+            assert "level_values_per_lane" in ee  # more than 3 hashes or rows wider than 4 words: default kernel
+            continue
         offs, ids, _ = a.query_batch(qv, qo, d["mem_t"])
         for i, (g, e) in enumerate(zip(_split(offs, ids), exp)):
             np.testing.assert_array_equal(g, e, err_msg=f"{ee} query {i}")
@@ -498,6 +502,8 @@ def test_level_schedule_gives_the_reference_results(gpu_lib, name):
         offs, ids, _ = a.fetch_results(nq)
         for i, (g, e) in enumerate(zip(_split(offs, ids), exp)):
             np.testing.assert_array_equal(g, e, err_msg=f"replayed query {i}")
+    levels = a.level_ms()
+    assert len(levels) == H.info()["max_depth"] + 1 and all(x >= 0 for x in levels)
 
 
 def test_level_schedule_streamed_host_batch(gpu_lib, oracle):
