@@ -1,9 +1,9 @@
-"""What the learned scheduler gains: on the 8,192-user-bin workload's layout (user bins scaled to 1% so the index
-builds in a second), a model trained on one batch's measured per-query work predicts another batch's work better
-than the query length does (rank correlation), and ordering by its prediction shortens the batch's list schedule
-against claiming in query order."""
-
-import heapq
+"""What the learned scheduler gains, measured: on the 8,192-user-bin workload's layout (user bins scaled to 1% so the
+index builds in a second), a model trained on one batch's measured per-query work predicts another batch's work
+better than the query length does (rank correlation), and the persistent kernel, claiming root tasks in the order of
+its prediction, answers that batch faster than in query order (the kernel's claim order without a scheduler) by CUDA
+events.  Ordering by query length, a heuristic that needs no model, is timed beside it and reported: on this
+workload it captures nearly the same gain (the learned part's margin over it is within a few percent)."""
 
 import numpy as np
 import pytest
@@ -19,15 +19,6 @@ def _ranks(x):
 
 def spearman(a, b):
     return float(np.corrcoef(_ranks(np.asarray(a, float)), _ranks(np.asarray(b, float)))[0, 1])
-
-
-def makespan(work, order, workers):
-    """Greedy list scheduling: each worker takes the next query in `order` when it becomes free."""
-    heap = [0.0] * workers
-    for q in order:
-        t = heapq.heappop(heap)
-        heapq.heappush(heap, t + float(work[q]))
-    return max(heap)
 
 
 def _batch(wl, offs, first, n):
@@ -56,7 +47,7 @@ def _features_and_work(agent, b, n):
     return feats, work
 
 
-def test_learned_order_beats_length_order(gpu_lib):
+def test_learned_order_shortens_the_measured_kernel(gpu_lib):
     import torch
 
     from hibf_gb300 import build as B
@@ -94,16 +85,25 @@ def test_learned_order_beats_length_order(gpu_lib):
     torch.cuda.synchronize()
     learned = order.cpu().numpy().astype(np.int64)
     assert np.array_equal(np.sort(learned), np.arange(n))
-    by_length = np.argsort(-length, kind="stable")
-    fifo = np.arange(n)
-    workers = 2432  # resident warps of the persistent kernel on 152 SMs
-    m_learned, m_length, m_fifo = (makespan(work, o, workers) for o in (learned, by_length, fifo))
-    # largest-first by prediction shortens the schedule against claiming in query order (the method without the
-    # model); ordering by length, a heuristic that needs no model, is reported beside it by bench.py
-    assert m_learned < 0.9 * m_fifo, (m_learned, m_length, m_fifo)
+    by_length = torch.from_numpy(np.argsort(-length, kind="stable").astype(np.int32)).cuda()
+    qo, thr, v, dv, dq, dt = test
+
+    def kernel_ms(d_order):
+        agent.set_order(d_order.data_ptr() if d_order is not None else None, n)
+        ks = []
+        for _ in range(9):
+            agent.query_batch_device(dv.data_ptr(), dq.data_ptr(), n, dt.data_ptr())
+            agent.status()
+            ks.append(agent.kernel_ms())
+        agent.set_order(None)
+        return float(np.median(ks[2:]))
+
+    t_query, t_length, t_learned = (kernel_ms(o) for o in (None, by_length, order))
+    # the model's order against the claim order without a scheduler; length order reported beside it
+    assert t_learned < 0.95 * t_query, dict(query=t_query, length=t_length, learned=t_learned)
+    print(f"kernel ms: query order {t_query:.4f}, length order {t_length:.4f}, learned order {t_learned:.4f}")
 
     # the ordered batch answers exactly as the unordered one
-    qo, thr, v, dv, dq, dt = test
     base = agent.query_batch(v, qo, thr)
     agent.set_order(order.data_ptr(), n)
     got = agent.query_batch(v, qo, thr)
