@@ -524,6 +524,7 @@ query_params base_params(hibf_gpu_agent * a, uint64_t const * d_values, uint64_t
     p.thr = d_thr;
     p.count_mask = count_mask;
     p.n_queries = nq;
+    p.n_nodes = static_cast<uint32_t>(h->n_ibfs);
     p.q_base = 0;
     p.max_depth = h->max_depth;
     p.counters_per_warp = h->counters_per_warp;
@@ -617,7 +618,12 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
     cudaStream_t s = a->stream;
     k_init_ctrl<<<1, 32, 0, s>>>(a->ctrl.as<unsigned long long>(), a->stats.as<unsigned long long>(), nq);
     HG_CUDA(cudaGetLastError());
-    if (a->tune.schedule != HIBF_GPU_SCHEDULE_LEVELS || nq <= a->tune.block_queries)
+    // One decision for the whole batch.  The queue (persistent or block kernel) waits on empty-slot marks in the
+    // task array, so every batch it runs starts from a fully marked array; the level schedule reads only the slots
+    // a finished launch wrote.
+    bool const blk = nq <= a->tune.block_queries;
+    bool const levels = !blk && a->tune.schedule == HIBF_GPU_SCHEDULE_LEVELS && !a->force_queue;
+    if (!levels)
         HG_CUDA(cudaMemsetAsync(a->tasks.p, 0xFF, a->cap_tasks * 8, s)); // the queue's empty-slot marks
     HG_CUDA(cudaMemsetAsync(a->qcount.p, 0, std::max<uint64_t>(nq, 1) * 4, s));
     if (a->qwork && nq)
@@ -626,7 +632,6 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
     {
         query_params p = base_params(a, d_values, d_qoff, d_thr, nq, mask_for(mode, width));
         p.decide = mode == HIBF_GPU_QUERY_MEMBERSHIP;
-        bool const blk = nq <= a->tune.block_queries;
         int const fit = blk ? a->max_blocks_blk : a->max_blocks[a->variant];
         int const per_sm = a->tune.blocks_per_sm ? std::min<int>(fit, static_cast<int>(a->tune.blocks_per_sm)) : fit;
         uint64_t const full = static_cast<uint64_t>(sm_count()) * static_cast<uint64_t>(per_sm);
@@ -640,7 +645,7 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         unsigned const rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
         a->last_levels = 0;
-        if (!blk && a->tune.schedule == HIBF_GPU_SCHEDULE_LEVELS && !a->force_queue)
+        if (levels)
         {
             // one launch per level: the roots, then each level's appended tasks grouped by IBF
             if (!a->lvl_tasks.p || a->lvl_tasks.bytes < a->cap_tasks * 8 || !a->lvl_hist.p ||
@@ -749,6 +754,8 @@ int read_status(hibf_gpu_agent * a)
         return HIBF_GPU_ERR_LOGIC;
     if (e & E_ORDER)
         return HIBF_GPU_ERR_INVALID_ARG;
+    if (e & E_TASK)
+        return HIBF_GPU_ERR_LOGIC;
     if (e & (E_OVERFLOW_REC | E_OVERFLOW_TASK))
         return HIBF_GPU_ERR_OVERFLOW;
     return HIBF_GPU_OK;
@@ -976,7 +983,8 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
             fail(st, st == HIBF_GPU_ERR_TIMEOUT     ? "device wait limit expired" :
                      st == HIBF_GPU_ERR_CYCLE       ? "merged bins form a cycle (descent deeper than the hierarchy)" :
                      st == HIBF_GPU_ERR_INVALID_ARG ? "a claim-order entry is not a query index of the batch" :
-                     st == HIBF_GPU_ERR_LOGIC       ? "a tuned kernel variant met an IBF it does not handle" :
+                     st == HIBF_GPU_ERR_LOGIC       ? "a tuned kernel variant met an IBF it does not handle, or a "
+                                                      "task named a query or IBF out of range" :
                                                       "batch capacity exceeded");
         if (c[C_ERROR] & E_OVERFLOW_TASK)
             tasks *= 4;

@@ -61,6 +61,7 @@ constexpr unsigned long long E_TIMEOUT = 4ull;
 constexpr unsigned long long E_CYCLE = 8ull;
 constexpr unsigned long long E_VARIANT = 16ull; // a tuned variant met a row of more than 4 words (host rejects this)
 constexpr unsigned long long E_ORDER = 32ull;   // a claim-order entry was not a query index (skipped)
+constexpr unsigned long long E_TASK = 64ull;    // a task word named a query or IBF out of range (skipped)
 
 // Tuning variants of the counting loop (compile-time), one kernel each:
 //   UM  values hashed per lane per pass, as a multiple of max(1, 4 / lanes-per-row): more row loads in flight
@@ -87,6 +88,7 @@ struct query_params
     uint64_t const * thr;
     uint64_t count_mask;
     uint64_t n_queries;
+    uint32_t n_nodes; // IBFs of the hierarchy: a task naming another is skipped (E_TASK), never dereferenced
     uint64_t q_base; // added to the query index in records and per-query counters (plain form)
     uint32_t max_depth;
     uint32_t counters_per_warp;
@@ -492,6 +494,16 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
     uint64_t const q = task >> 32;
     uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
     uint32_t const k = static_cast<uint32_t>(task) & kNodeMask;
+    if (q >= p.n_queries || k >= p.n_nodes)
+    {
+        if (lane == 0)
+        {
+            atomicOr(p.ctrl + C_ERROR, E_TASK);
+            __threadfence();
+            atomicAdd(p.ctrl + C_PENDING, ~0ull);
+        }
+        return;
+    }
     dev_node const nd = p.nodes[k];
     uint64_t const b0 = p.qoff[q];
     uint64_t const n = p.qoff[q + 1] - b0;
@@ -857,6 +869,17 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query_blk(query_
         }
         uint64_t const q = task >> 32;
         uint32_t const depth = static_cast<uint32_t>(task >> kNodeBits) & 63u;
+        if (q >= p.n_queries || (static_cast<uint32_t>(task) & kNodeMask) >= p.n_nodes)
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicOr(p.ctrl + C_ERROR, E_TASK);
+                __threadfence();
+                atomicAdd(p.ctrl + C_PENDING, ~0ull);
+            }
+            __syncthreads();
+            continue;
+        }
         dev_node const nd = p.nodes[static_cast<uint32_t>(task) & kNodeMask];
         uint64_t const b0 = p.qoff[q];
         uint64_t const n = p.qoff[q + 1] - b0;

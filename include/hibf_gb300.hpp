@@ -354,8 +354,7 @@ public:
     hierarchical_interleaved_bloom_filter & operator=(hierarchical_interleaved_bloom_filter const &) = delete;
     hierarchical_interleaved_bloom_filter(hierarchical_interleaved_bloom_filter && o) noexcept :
         number_of_user_bins{o.number_of_user_bins},
-        h_{std::exchange(o.h_, nullptr)},
-        rank_{std::move(o.rank_)}
+        h_{std::exchange(o.h_, nullptr)}
     {}
     ~hierarchical_interleaved_bloom_filter()
     {
@@ -390,10 +389,9 @@ public:
             auto const v = detail::to_vector(values);
             uint64_t const * ids = nullptr;
             uint64_t n = 0;
-            if (hibf_gpu_agent_membership_for(a_, v.data(), v.size(), threshold, &ids, &n) != HIBF_GPU_OK)
+            if (hibf_gpu_agent_membership_for_unsorted(a_, v.data(), v.size(), threshold, &ids, &n) != HIBF_GPU_OK)
                 std::terminate();
             result_.assign(ids, ids + n);
-            std::ranges::sort(result_, [&](uint64_t x, uint64_t y) { return h_->rank_[x] < h_->rank_[y]; });
             return result_;
         }
         // hierarchical_interleaved_bloom_filter.hpp:380-383
@@ -532,49 +530,14 @@ private:
         c.input_fn(static_cast<size_t>(user_bin), insert_iterator{sink});
     }
 
-    // Position of every user bin in the order membership_for reports it: bins scanned in order, merged bins
-    // descended in place (a user bin occurs in one place).
     void load_tables()
     {
         uint64_t info[4];
         check(hibf_gpu_hibf_info(h_, info));
         number_of_user_bins = info[0];
-        uint64_t const n_ibfs = info[1];
-        std::vector<uint64_t> bins(n_ibfs);
-        check(hibf_gpu_hibf_get_tables(h_, bins.data(), nullptr, nullptr, nullptr, nullptr));
-        std::vector<uint64_t> off(n_ibfs + 1, 0);
-        for (uint64_t k = 0; k < n_ibfs; ++k)
-            off[k + 1] = off[k] + bins[k];
-        std::vector<uint64_t> next(off[n_ibfs]), ub(off[n_ibfs]);
-        check(hibf_gpu_hibf_get_tables(h_, nullptr, nullptr, nullptr, next.data(), ub.data()));
-        rank_.assign(number_of_user_bins, std::numeric_limits<uint64_t>::max());
-        uint64_t r = 0;
-        std::vector<std::pair<uint64_t, uint64_t>> stack{{0, 0}};
-        uint64_t steps = 0;
-        while (!stack.empty() && steps++ <= 4 * (off[n_ibfs] + 1))
-        {
-            auto [k, b] = stack.back();
-            stack.pop_back();
-            if (b >= bins[k])
-                continue;
-            stack.emplace_back(k, b + 1);
-            uint64_t const i = off[k] + b;
-            uint64_t const u = ub[i];
-            if (u == HIBF_GPU_BIN_MERGED)
-            {
-                if (next[i] != k)
-                    stack.emplace_back(next[i], 0);
-            }
-            else if (u != HIBF_GPU_BIN_DELETED && (b + 1 == bins[k] || ub[i + 1] != u) && u < number_of_user_bins &&
-                     rank_[u] == std::numeric_limits<uint64_t>::max())
-            {
-                rank_[u] = r++;
-            }
-        }
     }
 
     hibf_gpu_hibf * h_{};
-    std::vector<uint64_t> rank_;
 };
 
 } // namespace hibf_gb300
