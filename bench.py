@@ -518,6 +518,7 @@ def measure_hibf(args, wl, world, stream, full):
         kms.append(agent.kernel_ms())
     kernel_ms = sum(kms) / len(kms)
     level_ms = agent.level_ms()
+    level_work = agent.level_work()
     res_offs, res_ids, _ = agent.fetch_results(nq)
     # the device's own random 8-byte read rate at the index's footprint (fully random, and 2 MiB-local)
     import ctypes as _ct
@@ -609,6 +610,8 @@ def measure_hibf(args, wl, world, stream, full):
         "h2d_GBps_in_call": nv * 8 / (float(np.median([t[n_chunks - 1] for t in timelines])) / 1e3) / 1e9,
         "h2d_GBps_probe": h2d_probe(min(nv * 8, 4 << 30)),
         "wall_ms_per_call": [round(w * 1e3, 2) for w in wall],
+        "values_copied_ms_per_call": [round(t[n_chunks - 1], 2) for t in timelines],
+        "results_back_ms_per_call": [round(t[n_chunks + 2], 2) for t in timelines],
         "note": "ms from the call's first device work; values_copied = the last chunk's copy done",
     }
     del ea
@@ -619,7 +622,29 @@ def measure_hibf(args, wl, world, stream, full):
 
         pool_q = min(nq, 100_000)
         pool_v = hv[:int(qo[pool_q])]
-        for load, dur in ((1e4, 10.0), (1e5, 5.0), (1e6, 5.0)):
+
+        def pool_copy_ms(mb=29):
+            """Device time of plain copies of pool slices (CUDA events on a side stream): the link's own rate."""
+            n = int(mb * (1 << 20) / 8)
+            dst = torch.empty(n, dtype=torch.int64, device="cuda")
+            side = torch.cuda.Stream()
+            ms = []
+            for rep in range(5):
+                a = (rep * 1_000_003) % (pool_v.size - n)
+                src = h_v[a:a + n]
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(side):
+                    e0.record(side)
+                    dst.copy_(src, non_blocking=True)
+                    e1.record(side)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+                time.sleep(0.02)
+            return round(float(np.median(ms)), 4)
+
+        pool_copy_before = pool_copy_ms()
+        # 1e5 and 1e6 queries/s run for at least 10,000 requests (about 490 queries per request)
+        for load, dur in ((1e4, 10.0), (1e5, 50.0), (1e6, 5.0)):
             srv = server(hibf, slots=4, max_batch_queries=65536, max_batch_values=1 << 27, admission_bytes=4 << 30)
             r = srv.open_loop(pool_v, qo[:pool_q + 1], offered_qps=load, duration_s=dur, max_request_queries=4096,
                               thr_lo=0.5, thr_hi=0.9, seed=int(load))
@@ -631,6 +656,8 @@ def measure_hibf(args, wl, world, stream, full):
                 r["p99_note"] = f"{r['requests']} requests: the 99th percentile is near the maximum"
             serving.append(r)
             srv.close()
+        # plain copies from the request pool before the server read it (cold pages) and after the load points
+        serving[0]["pool_copy_29MB_ms"] = {"before": pool_copy_before, "after": pool_copy_ms()}
     learned = None
     if full and not args.no_learned and nq >= 2 * args.sched_queries:
         learned = learned_scheduler(hibf, agent.tuning, d_v, d_qo, d_thr, qo, nq, args.sched_queries, stream)
@@ -679,6 +706,8 @@ def measure_hibf(args, wl, world, stream, full):
                      "algorithmic_bytes_per_value_visit": bytes_per_visit,
                      "row_reads_per_s": executed * wl.h / (kernel_ms / 1e3),
                      "level_ms": [round(x, 3) for x in level_ms],
+                     "level_value_visits": [w["value_visits"] for w in level_work],
+                     "level_value_visits_executed": [w["value_visits_executed"] for w in level_work],
                      "random_read_ceiling": {"footprint_bytes": fp, "reads_per_s_random": probe["random"],
                                              "reads_per_s_2MiB_windows": probe["window_2MiB"],
                                              "probe": "hibf_gpu_probe_random_reads"}},

@@ -82,6 +82,15 @@ class Tuning(ctypes.Structure):
         return t
 
 
+class Timer(ctypes.Structure):
+    """hibf_gpu_timer: one build phase's seconds, longest interval and interval count."""
+
+    _fields_ = [("seconds", ctypes.c_double), ("max_seconds", ctypes.c_double), ("count", u64)]
+
+
+TIMER_NAMES = ("index_allocation", "user_bin_io", "merge_kmers", "fill_ibf")
+
+
 class TuneTrial(ctypes.Structure):
     _fields_ = [("tuning", Tuning), ("kernel_ms", ctypes.c_double)]
 
@@ -150,6 +159,7 @@ _SIGS = [
     ("hibf_gpu_hibf_upload_words", None, [vp, u64, vp, u64]),
     ("hibf_gpu_hibf_download_words", None, [vp, u64, vp, u64]),
     ("hibf_gpu_hibf_digests", None, [vp, vp, ctypes.c_uint32]),
+    ("hibf_gpu_hibf_build_timers", None, [vp, ctypes.POINTER(Timer)]),
     ("hibf_gpu_agent_create", None, [vp, ctypes.POINTER(vp)]),
     ("hibf_gpu_agent_destroy", None, [vp]),
     ("hibf_gpu_agent_set_stream", None, [vp, vp]),
@@ -174,6 +184,7 @@ _SIGS = [
     ("hibf_gpu_agent_kernel_ms", None, [vp, ctypes.POINTER(ctypes.c_float)]),
     ("hibf_gpu_agent_level_ms", None, [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_uint32,
                                        ctypes.POINTER(ctypes.c_uint32)]),
+    ("hibf_gpu_agent_level_work", None, [vp, vp, vp, vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
     ("hibf_gpu_agent_input_chunks", None, [vp, ctypes.POINTER(ctypes.c_uint32)]),
     ("hibf_gpu_agent_last_timeline", None, [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
                                             ctypes.POINTER(ctypes.c_uint32)]),

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <condition_variable>
 #include <cstring>
@@ -779,190 +780,6 @@ __global__ void k_insert_jobs(dev_node const * __restrict__ nodes, insert_job co
     }
 }
 
-// ---- windowed inserts -------------------------------------------------------------------------------------------
-// The same bits as k_insert_jobs, set window by window.  Word w of IBF k has the global index G = word_base[k] + w
-// (IBF k's words follow IBF k-1's); G falls into window G >> shift.  A first pass counts each window's updates, a
-// second writes every update as (window-local word << 6 | bit) grouped by window, and a third applies them in that
-// order, so the words of the window being applied are in L2 while its updates land.  Direct atomics cost a 64-byte
-// DRAM read and a write-back per 8-byte update (profiles/k_insert_jobs_hibf8192_scale0.05_full.md); grouped, each
-// window's words move about once per chunk of updates.
-constexpr uint32_t kMaxWindows = 4096; // per-block window counters and cursors fit 48 KB of shared memory
-
-struct win_args
-{
-    dev_node const * nodes;
-    insert_job const * jobs;
-    uint64_t const * job_end;
-    uint32_t n_jobs;
-    uint64_t seed;
-    uint64_t const * values;
-    dev_split const * splits;
-    dev_bnd const * bnds;
-    uint64_t const * before;
-    uint64_t const * word_base; // n_ibfs + 1 prefix sums of the stores' words
-    uint32_t n_ibfs;
-    uint32_t shift;     // window = G >> shift
-    uint32_t n_windows;
-};
-
-// The job holding flattened position i, from a hint that never passes it.
-__device__ __forceinline__ uint32_t job_of(win_args const & a, uint64_t i, uint32_t j)
-{
-    while (a.job_end[j] <= i)
-        ++j;
-    return j;
-}
-
-__device__ __forceinline__ uint32_t first_job(win_args const & a, uint64_t i)
-{
-    uint32_t lo = 0, hi = a.n_jobs;
-    while (lo < hi)
-    {
-        uint32_t const mid = (lo + hi) >> 1;
-        if (a.job_end[mid] > i)
-            hi = mid;
-        else
-            lo = mid + 1;
-    }
-    return lo;
-}
-
-// Calls f(G, bit) for each hash function's update of flattened position i (nothing for a bin past the IBF's bins,
-// which k_insert_jobs skips as well).
-template <typename F>
-__device__ __forceinline__ void updates_of(win_args const & a, uint64_t i, uint32_t j, F && f)
-{
-    insert_job const jb = a.jobs[j];
-    uint64_t const local = i - (a.job_end[j] - jb.n);
-    uint64_t const v = a.values ? a.values[jb.start + local] : hg_stream_at(a.seed, jb.start + local);
-    uint64_t const b = jb.first_bin + (jb.split ? split_chunk_d(v, a.splits[jb.split - 1], a.bnds, a.before) : 0u);
-    dev_node const nd = a.nodes[jb.ibf];
-    if (b >= nd.bins)
-        return;
-    uint64_t const g0 = a.word_base[jb.ibf] + (b >> 6);
-    for (uint32_t k = 0; k < nd.hash_funs; ++k)
-        f(g0 + hash_row(v, c_hash_seeds[k], nd.hash_shift, nd.bin_size) * nd.row_words, static_cast<uint32_t>(b & 63u));
-}
-
-// Pass 1: updates per window of positions [begin, end).
-__global__ void k_win_count(win_args a, uint64_t begin, uint64_t end, unsigned long long * hist)
-{
-    __shared__ unsigned int s_hist[kMaxWindows];
-    for (uint32_t w = threadIdx.x; w < a.n_windows; w += blockDim.x)
-        s_hist[w] = 0;
-    __syncthreads();
-    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-    uint64_t i = begin + blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
-    if (i < end)
-    {
-        uint32_t j = first_job(a, i);
-        for (; i < end; i += stride)
-        {
-            j = job_of(a, i, j);
-            updates_of(a, i, j, [&](uint64_t g, uint32_t) { atomicAdd(s_hist + (g >> a.shift), 1u); });
-        }
-    }
-    __syncthreads();
-    for (uint32_t w = threadIdx.x; w < a.n_windows; w += blockDim.x)
-        if (s_hist[w])
-            atomicAdd(hist + w, static_cast<unsigned long long>(s_hist[w]));
-}
-
-// One block: exclusive scan of the window counts into offsets (n_windows + 1) and write cursors.
-__global__ void k_win_scan(unsigned long long const * hist, uint32_t n_windows, unsigned long long * offsets,
-                           unsigned long long * cursor)
-{
-    if (threadIdx.x == 0)
-    {
-        unsigned long long acc = 0;
-        for (uint32_t w = 0; w < n_windows; ++w)
-        {
-            offsets[w] = acc;
-            cursor[w] = acc;
-            acc += hist[w];
-        }
-        offsets[n_windows] = acc;
-    }
-}
-
-// Pass 2: every update of positions [begin, end) at its window's cursor.  A block takes a contiguous run of
-// positions, counts its updates per window in shared memory, reserves one range per window with a single global
-// atomic, then writes its updates into the ranges.
-__global__ void k_win_scatter(win_args a, uint64_t begin, uint64_t end, uint64_t per_block,
-                              unsigned long long * cursor, uint32_t * __restrict__ entries)
-{
-    __shared__ unsigned int s_cnt[kMaxWindows];
-    __shared__ unsigned long long s_base[kMaxWindows];
-    uint64_t const b0 = begin + blockIdx.x * per_block;
-    uint64_t const b1 = min(end, b0 + per_block);
-    if (b0 >= b1)
-        return;
-    for (uint32_t w = threadIdx.x; w < a.n_windows; w += blockDim.x)
-        s_cnt[w] = 0;
-    __syncthreads();
-    uint32_t const j0 = first_job(a, b0);
-    {
-        uint32_t j = j0;
-        for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x)
-        {
-            j = job_of(a, i, j);
-            updates_of(a, i, j, [&](uint64_t g, uint32_t) { atomicAdd(s_cnt + (g >> a.shift), 1u); });
-        }
-    }
-    __syncthreads();
-    for (uint32_t w = threadIdx.x; w < a.n_windows; w += blockDim.x)
-    {
-        if (s_cnt[w])
-            s_base[w] = atomicAdd(cursor + w, static_cast<unsigned long long>(s_cnt[w]));
-        s_cnt[w] = 0;
-    }
-    __syncthreads();
-    uint64_t const local_mask = (1ull << a.shift) - 1u;
-    uint32_t j = j0;
-    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x)
-    {
-        j = job_of(a, i, j);
-        updates_of(a, i, j,
-                   [&](uint64_t g, uint32_t bit)
-                   {
-                       uint32_t const w = static_cast<uint32_t>(g >> a.shift);
-                       unsigned long long const pos = s_base[w] + atomicAdd(s_cnt + w, 1u);
-                       entries[pos] = static_cast<uint32_t>(((g & local_mask) << 6) | bit);
-                   });
-    }
-}
-
-// Pass 3: the updates in window order.  Threads stride through the array together, so the updates in flight at a
-// time belong to one or two windows.
-__global__ void k_win_apply(win_args a, uint32_t const * __restrict__ entries, unsigned long long const * offsets)
-{
-    uint64_t const n_entries = offsets[a.n_windows];
-    uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-    uint32_t w = 0, k = 0;
-    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n_entries; i += stride)
-    {
-        while (offsets[w + 1] <= i)
-            ++w;
-        uint32_t const e = entries[i];
-        uint64_t const g = (static_cast<uint64_t>(w) << a.shift) + (e >> 6);
-        if (g < a.word_base[k] || g >= a.word_base[k + 1])
-        {
-            uint32_t lo = 0, hi = a.n_ibfs; // the IBF whose words hold g
-            while (hi - lo > 1u)
-            {
-                uint32_t const mid = (lo + hi) >> 1;
-                if (a.word_base[mid] <= g)
-                    lo = mid;
-                else
-                    hi = mid;
-            }
-            k = lo;
-        }
-        atomicOr(reinterpret_cast<unsigned long long *>(const_cast<uint64_t *>(a.nodes[k].words) + (g - a.word_base[k])),
-                 1ull << (e & 63u));
-    }
-}
-
 // The split table on the device (uploaded once per build).
 struct dev_split_table
 {
@@ -994,66 +811,6 @@ void upload_split_table(hibf_gpu_split_table const & t, dev_split_table & dt, cu
     HG_CUDA(cudaStreamSynchronize(s)); // the host vectors may go away
 }
 
-// The windowed inserts of `total` flattened positions (jobs and their ends already on the device); false when the
-// build is too small to gain from them or the device has too little free memory for the update buffer.
-bool run_jobs_windowed(hibf_gpu_hibf * h, insert_job const * d_jobs, uint64_t const * d_end, uint32_t n_jobs,
-                       uint64_t total, uint64_t seed, uint64_t const * d_values, dev_split_table const * dt,
-                       cudaStream_t s)
-{
-    uint64_t hf = 0;
-    for (uint64_t k = 0; k < h->n_ibfs; ++k)
-        hf = std::max<uint64_t>(hf, h->hash_funs[k]);
-    if (total * hf < (1ull << 24))
-        return false;
-    std::vector<uint64_t> base(h->n_ibfs + 1, 0);
-    for (uint64_t k = 0; k < h->n_ibfs; ++k)
-        base[k + 1] = base[k] + h->bin_size[k] * h->row_words[k];
-    uint32_t shift = 22; // windows of at least 32 MB
-    while ((base.back() >> shift) + 1 > kMaxWindows)
-        ++shift;
-    if (shift > 26) // the window-local word and the bit must fit 32 bits
-        return false;
-    uint32_t const n_windows = static_cast<uint32_t>((base.back() >> shift) + 1);
-    size_t free_b = 0, total_b = 0;
-    HG_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    uint64_t const cap = std::min<uint64_t>(free_b / 2, 64ull << 30) / 4; // updates per chunk
-    if (cap < (1ull << 24))
-        return false;
-    uint64_t const per_chunk = std::max<uint64_t>(1, cap / hf); // positions per chunk
-    dbuf d_base, d_hist, d_off, d_cur, d_entries;
-    d_base.ensure(base.size() * 8);
-    d_hist.ensure(n_windows * 8ull);
-    d_off.ensure((n_windows + 1ull) * 8);
-    d_cur.ensure(n_windows * 8ull);
-    d_entries.ensure(std::min(total, per_chunk) * hf * 4);
-    HG_CUDA(cudaMemcpyAsync(d_base.p, base.data(), base.size() * 8, cudaMemcpyHostToDevice, s));
-    win_args a{h->d_nodes.as<dev_node>(), d_jobs, d_end, n_jobs, seed, d_values,
-               dt ? dt->splits.as<dev_split>() : nullptr, dt ? dt->bnds.as<dev_bnd>() : nullptr,
-               dt ? dt->before.as<uint64_t>() : nullptr, d_base.as<uint64_t>(), static_cast<uint32_t>(h->n_ibfs),
-               shift, n_windows};
-    unsigned const block = 256;
-    unsigned const wide = static_cast<unsigned>(sm_count()) * 8u;
-    constexpr uint64_t kPerBlock = 4096; // positions per scatter block
-    for (uint64_t p0 = 0; p0 < total; p0 += per_chunk)
-    {
-        uint64_t const p1 = std::min(total, p0 + per_chunk);
-        HG_CUDA(cudaMemsetAsync(d_hist.p, 0, n_windows * 8ull, s));
-        k_win_count<<<wide, block, 0, s>>>(a, p0, p1, d_hist.as<unsigned long long>());
-        HG_CUDA(cudaGetLastError());
-        k_win_scan<<<1, 32, 0, s>>>(d_hist.as<unsigned long long>(), n_windows, d_off.as<unsigned long long>(),
-                                     d_cur.as<unsigned long long>());
-        HG_CUDA(cudaGetLastError());
-        unsigned const sgrid = static_cast<unsigned>((p1 - p0 + kPerBlock - 1) / kPerBlock);
-        k_win_scatter<<<sgrid, block, 0, s>>>(a, p0, p1, kPerBlock, d_cur.as<unsigned long long>(),
-                                              d_entries.as<uint32_t>());
-        HG_CUDA(cudaGetLastError());
-        k_win_apply<<<wide, block, 0, s>>>(a, d_entries.as<uint32_t>(), d_off.as<unsigned long long>());
-        HG_CUDA(cudaGetLastError());
-    }
-    HG_CUDA(cudaStreamSynchronize(s)); // the buffers are freed on return
-    return true;
-}
-
 void run_jobs(hibf_gpu_hibf * h, std::vector<insert_job> const & jobs, uint64_t seed, uint64_t const * d_values,
               dev_split_table const * dt, cudaStream_t s)
 {
@@ -1073,9 +830,6 @@ void run_jobs(hibf_gpu_hibf * h, std::vector<insert_job> const & jobs, uint64_t 
     de.ensure(end.size() * 8);
     HG_CUDA(cudaMemcpyAsync(dj.p, jobs.data(), jobs.size() * sizeof(insert_job), cudaMemcpyHostToDevice, s));
     HG_CUDA(cudaMemcpyAsync(de.p, end.data(), end.size() * 8, cudaMemcpyHostToDevice, s));
-    if (run_jobs_windowed(h, dj.as<insert_job>(), de.as<uint64_t>(), static_cast<uint32_t>(jobs.size()), acc, seed,
-                          d_values, dt, s))
-        return;
     unsigned const block = 256;
     uint64_t const want = (acc + block - 1) / block;
     unsigned const grid = static_cast<unsigned>(std::min<uint64_t>(want, static_cast<uint64_t>(sm_count()) * 16));
@@ -1218,6 +972,11 @@ uint64_t union_size_device(std::vector<std::vector<uint64_t>> const & sets, std:
 namespace
 {
 
+double seconds_since(std::chrono::steady_clock::time_point t0)
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
 // The plan of a synthetic build: pairwise distinct user bins of the given stream ranges, unions sized by sums.
 plan_t synthetic_plan(hibf_gpu_build_config const & cfg, char const * layout_text, uint64_t const * user_bin_offsets)
 {
@@ -1242,10 +1001,21 @@ plan_t synthetic_plan(hibf_gpu_build_config const & cfg, char const * layout_tex
 // sets and the union sizes are sorts on the device (sets.cu); without one (planning only) host hash sets.
 //
 // With `table` the split user bins keep their input order and `table` receives their split table (the device
-// chunks them); without it they are reordered into the reference's chunk order on the host.
+// chunks them); without it they are reordered into the reference's chunk order on the host.  `timers` (optional)
+// receives the user_bin_io and merge_kmers intervals.
 plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_text, hibf_gpu_input_fn input_fn,
-                   void * user, std::vector<std::vector<uint64_t>> & sets_out, hibf_gpu_split_table * table)
+                   void * user, std::vector<std::vector<uint64_t>> & sets_out, hibf_gpu_split_table * table,
+                   phase_timer * timers = nullptr)
 {
+    using clock = std::chrono::steady_clock;
+    phase_timer scratch[n_timers];
+    phase_timer * const T = timers ? timers : scratch;
+    auto read_user_bin = [&](uint64_t u, hibf_gpu_sink & sink)
+    {
+        auto const t0 = clock::now();
+        input_fn(user, u, &sink);
+        T[timer_user_bin_io].add(seconds_since(t0));
+    };
     hibf_gpu_build_config const * cfg = &cfg_ref;
     uint64_t const nub = cfg->number_of_user_bins;
     bool const device = device_present();
@@ -1260,24 +1030,29 @@ plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_te
         for (uint64_t u = 0; u < nub; ++u)
         {
             hibf_gpu_sink sink;
-            input_fn(user, u, &sink);
+            read_user_bin(u, sink);
             all.insert(all.end(), sink.values.begin(), sink.values.end());
             off[u + 1] = all.size();
         }
+        auto const t0 = clock::now();
         distinct_sets_device(all.data(), off, sets);
+        T[timer_merge_kmers].add(seconds_since(t0));
     }
     else
     {
+        auto const t0 = clock::now();
+        double const io0 = T[timer_user_bin_io].seconds;
         for (uint64_t u = 0; u < nub; ++u)
         {
             hibf_gpu_sink sink;
-            input_fn(user, u, &sink);
+            read_user_bin(u, sink);
             std::unordered_set<uint64_t> seen;
             seen.reserve(sink.values.size() * 2);
             for (uint64_t v : sink.values)
                 if (seen.insert(v).second)
                     sets[u].push_back(v);
         }
+        T[timer_merge_kmers].add(seconds_since(t0) - (T[timer_user_bin_io].seconds - io0));
     }
     for (uint64_t u = 0; u < nub; ++u)
         distinct[u] = sets[u].size();
@@ -1285,6 +1060,7 @@ plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_te
     plan_t const P0 = make_plan(*cfg, L, distinct, [](size_t) { return uint64_t{1}; });
     // exact distinct counts of subtree unions (merged max bins), or sums for disjoint user bins
     std::vector<uint64_t> sums;
+    auto const t_union = clock::now();
     if (cfg->user_bins_disjoint)
         sums = disjoint_unions(P0, distinct, L);
     else
@@ -1324,12 +1100,15 @@ plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_te
             sums[n] = un.size();
         }
     }
+    T[timer_merge_kmers].add(seconds_since(t_union));
     plan_t const P = make_plan(*cfg, L, distinct, [&](size_t node) { return sums[node]; });
     unsigned const threads = static_cast<unsigned>(cfg->threads);
+    auto const t_split = clock::now();
     if (table)
     {
         compute_split_table(
             P, [&](uint64_t u, auto && f) { for (uint64_t v : sets[u]) f(v); }, threads, *table);
+        T[timer_merge_kmers].add(seconds_since(t_split));
         return P;
     }
     // split user bins in the reference's chunk order
@@ -1337,7 +1116,23 @@ plan_t plan_inputs(hibf_gpu_build_config const & cfg_ref, char const * layout_te
     for (uint64_t u = 0; u < nub; ++u)
         if (P.ub_rec[u].ntb > 1)
             sets[u] = std::move(split[u]);
+    T[timer_merge_kmers].add(seconds_since(t_split));
     return P;
+}
+
+// create_from_plan with the index_allocation interval: the stores are allocated and zeroed when it returns.
+hibf_gpu_hibf * allocate_timed(plan_t const & P, uint64_t n_user_bins, phase_timer & t)
+{
+    auto const t0 = std::chrono::steady_clock::now();
+    hibf_gpu_hibf * h = create_from_plan(P, n_user_bins);
+    cudaError_t const e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess)
+    {
+        hibf_gpu_hibf_destroy(h);
+        fail(HIBF_GPU_ERR_CUDA, cudaGetErrorString(e));
+    }
+    t.add(seconds_since(t0));
+    return h;
 }
 
 } // namespace
@@ -1670,9 +1465,11 @@ extern "C"
                 *out = nullptr;
                 uint64_t const nub = cfg->number_of_user_bins;
                 plan_t const P = synthetic_plan(*cfg, layout_text, user_bin_offsets);
+                phase_timer timers[n_timers];
                 hibf_gpu_split_table computed;
                 if (!table)
                 {
+                    auto const t0 = std::chrono::steady_clock::now();
                     compute_split_table(
                         P,
                         [&](uint64_t u, auto && f)
@@ -1681,13 +1478,14 @@ extern "C"
                                 f(hg_stream_at(seed, k));
                         },
                         static_cast<unsigned>(cfg->threads), computed);
+                    timers[timer_merge_kmers].add(seconds_since(t0));
                     table = &computed;
                 }
                 std::vector<uint64_t> distinct(nub);
                 for (uint64_t u = 0; u < nub; ++u)
                     distinct[u] = user_bin_offsets[u + 1] - user_bin_offsets[u];
                 std::vector<uint64_t> const entry = check_split_table(P, *table, distinct);
-                hibf_gpu_hibf * h = create_from_plan(P, nub);
+                hibf_gpu_hibf * h = allocate_timed(P, nub, timers[timer_index_allocation]);
                 try
                 {
                     dev_split_table dt;
@@ -1704,7 +1502,10 @@ extern "C"
                             jobs.push_back(insert_job{user_bin_offsets[u], n, 0, static_cast<uint32_t>(ibf),
                                                       static_cast<uint32_t>(bin)});
                     }
+                    auto const t0 = std::chrono::steady_clock::now();
                     run_jobs(h, jobs, seed, nullptr, &dt, h->stream);
+                    timers[timer_fill_ibf].add(seconds_since(t0));
+                    std::copy(timers, timers + n_timers, h->timers);
                 }
                 catch (...)
                 {
@@ -1728,17 +1529,19 @@ extern "C"
                 uint64_t const nub = cfg->number_of_user_bins;
                 std::vector<std::vector<uint64_t>> sets;
                 hibf_gpu_split_table table;
-                plan_t const P = plan_inputs(*cfg, layout_text, input_fn, user, sets, &table);
+                phase_timer timers[n_timers];
+                plan_t const P = plan_inputs(*cfg, layout_text, input_fn, user, sets, &table, timers);
                 std::vector<uint64_t> distinct(nub);
                 for (uint64_t u = 0; u < nub; ++u)
                     distinct[u] = sets[u].size();
                 std::vector<uint64_t> const entry = check_split_table(P, table, distinct);
-                hibf_gpu_hibf * h = create_from_plan(P, nub);
+                hibf_gpu_hibf * h = allocate_timed(P, nub, timers[timer_index_allocation]);
                 try
                 {
                     dev_split_table dt;
                     upload_split_table(table, dt, h->stream);
                     // all distinct values, concatenated, uploaded once
+                    auto const t_io = std::chrono::steady_clock::now();
                     std::vector<uint64_t> off(nub + 1, 0);
                     for (uint64_t u = 0; u < nub; ++u)
                         off[u + 1] = off[u] + sets[u].size();
@@ -1748,6 +1551,8 @@ extern "C"
                         if (!sets[u].empty())
                             HG_CUDA(cudaMemcpyAsync(dv.as<uint64_t>() + off[u], sets[u].data(), sets[u].size() * 8,
                                                     cudaMemcpyHostToDevice, h->stream));
+                    HG_CUDA(cudaStreamSynchronize(h->stream));
+                    timers[timer_user_bin_io].add(seconds_since(t_io));
                     std::vector<insert_job> jobs;
                     for (uint64_t u = 0; u < nub; ++u)
                     {
@@ -1759,7 +1564,10 @@ extern "C"
                             jobs.push_back(
                                 insert_job{off[u], n, 0, static_cast<uint32_t>(ibf), static_cast<uint32_t>(bin)});
                     }
+                    auto const t_fill = std::chrono::steady_clock::now();
                     run_jobs(h, jobs, 0, dv.as<uint64_t>(), &dt, h->stream);
+                    timers[timer_fill_ibf].add(seconds_since(t_fill));
+                    std::copy(timers, timers + n_timers, h->timers);
                 }
                 catch (...)
                 {
@@ -1767,6 +1575,18 @@ extern "C"
                     throw;
                 }
                 *out = h;
+            });
+    }
+
+    int hibf_gpu_hibf_build_timers(hibf_gpu_hibf const * h, hibf_gpu_timer * timers)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h || !timers)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                for (int i = 0; i < n_timers; ++i)
+                    timers[i] = hibf_gpu_timer{h->timers[i].seconds, h->timers[i].max_seconds, h->timers[i].count};
             });
     }
 

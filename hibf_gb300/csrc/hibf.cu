@@ -451,6 +451,10 @@ struct hibf_gpu_agent
     // level schedule: a level's tasks grouped by IBF, the per-IBF histogram / cursors, the level's task count; an
     // event after each level of the last batch (timing)
     dbuf lvl_tasks, lvl_hist, lvl_count;
+    // level schedule: each level's tasks, value visits and executed value visits (kStats words per level)
+    dbuf lvl_stats;
+    hbuf h_lvl_stats;
+    std::vector<uint64_t> last_level_stats;
     std::vector<cudaEvent_t> ev_lvl;
     uint32_t last_levels{};
     bool force_queue{}; // set for the duration of a streamed host batch
@@ -499,6 +503,8 @@ void ensure_capacity(hibf_gpu_agent * a, uint64_t nq, uint64_t tasks, uint64_t r
         a->lvl_tasks.ensure(a->cap_tasks * 8);
         a->lvl_hist.ensure(a->h->n_ibfs * 4);
         a->lvl_count.ensure(8);
+        a->lvl_stats.ensure((a->h->max_depth + 1) * kStats * 8);
+        a->h_lvl_stats.ensure((a->h->max_depth + 1) * kStats * 8);
     }
     if (results > a->cap_results)
     {
@@ -628,6 +634,7 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
     HG_CUDA(cudaMemsetAsync(a->qcount.p, 0, std::max<uint64_t>(nq, 1) * 4, s));
     if (a->qwork && nq)
         HG_CUDA(cudaMemsetAsync(a->qwork, 0, nq * 8, s));
+    a->last_levels = 0;
     if (nq)
     {
         query_params p = base_params(a, d_values, d_qoff, d_thr, nq, mask_for(mode, width));
@@ -644,13 +651,17 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         HG_CUDA(cudaStreamIsCapturing(s, &cap));
         unsigned const rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
-        a->last_levels = 0;
         if (levels)
         {
             // one launch per level: the roots, then each level's appended tasks grouped by IBF
+            uint64_t const stats_bytes = (h->max_depth + 1) * kStats * 8;
             if (!a->lvl_tasks.p || a->lvl_tasks.bytes < a->cap_tasks * 8 || !a->lvl_hist.p ||
-                a->lvl_hist.bytes < h->n_ibfs * 4 || !a->lvl_count.p)
+                a->lvl_hist.bytes < h->n_ibfs * 4 || !a->lvl_count.p || a->lvl_stats.bytes < stats_bytes ||
+                a->h_lvl_stats.bytes < stats_bytes)
                 fail(HIBF_GPU_ERR_LOGIC, "level schedule buffers missing (set the tuning through set_tuning)");
+            // each level counts its work into its own kStats words; read_status sums them
+            HG_CUDA(cudaMemsetAsync(a->lvl_stats.p, 0, stats_bytes, s));
+            unsigned long long * const lvl_stats = a->lvl_stats.as<unsigned long long>();
             while (a->ev_lvl.size() <= h->max_depth)
             {
                 cudaEvent_t e{};
@@ -664,6 +675,7 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
                 a->tune.blocks_per_sm ? std::min<int>(child_fit, static_cast<int>(a->tune.blocks_per_sm)) : child_fit;
             unsigned const grid_child = static_cast<unsigned>(sm_count()) * static_cast<unsigned>(child_per_sm);
             p.level = 1;
+            p.stats = lvl_stats;
             query_kernel(h->hash_count, a->variant)<<<grid_full, 256, query_smem(h), s>>>(p);
             HG_CUDA(cudaGetLastError());
             HG_CUDA(cudaEventRecordWithFlags(a->ev_lvl[0], s, rec_flags));
@@ -688,6 +700,7 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
                 HG_CUDA(cudaGetLastError());
                 p.in_tasks = a->lvl_tasks.as<unsigned long long>();
                 p.in_count = a->lvl_count.as<unsigned long long>();
+                p.stats = lvl_stats + d * kStats;
                 query_kernel(h->hash_count, child_variant)<<<grid_child, 256, query_smem(h), s>>>(p);
                 HG_CUDA(cudaGetLastError());
                 HG_CUDA(cudaEventRecordWithFlags(a->ev_lvl[d], s, rec_flags));
@@ -739,12 +752,28 @@ int read_status(hibf_gpu_agent * a)
 {
     HG_CUDA(cudaMemcpyAsync(a->h_ctrl.p, a->ctrl.p, C_WORDS * 8, cudaMemcpyDeviceToHost, a->stream));
     HG_CUDA(cudaMemcpyAsync(a->h_stats.p, a->stats.p, kStats * 8, cudaMemcpyDeviceToHost, a->stream));
+    uint32_t const levels = a->last_levels;
+    if (levels)
+        HG_CUDA(cudaMemcpyAsync(a->h_lvl_stats.p, a->lvl_stats.p, levels * kStats * 8, cudaMemcpyDeviceToHost,
+                                a->stream));
     HG_CUDA(cudaStreamSynchronize(a->stream));
     unsigned long long const * c = a->h_ctrl.as<unsigned long long>();
     unsigned long long const * st = a->h_stats.as<unsigned long long>();
     a->last_tasks = st[0];
     a->last_visits = st[1];
     a->last_executed = st[2];
+    a->last_level_stats.clear();
+    if (levels)
+    {
+        unsigned long long const * ls = a->h_lvl_stats.as<unsigned long long>();
+        a->last_level_stats.assign(ls, ls + levels * kStats);
+        for (uint32_t d = 0; d < levels; ++d)
+        {
+            a->last_tasks += ls[d * kStats + 0];
+            a->last_visits += ls[d * kStats + 1];
+            a->last_executed += ls[d * kStats + 2];
+        }
+    }
     unsigned long long const e = c[C_ERROR];
     if (e & E_TIMEOUT)
         return HIBF_GPU_ERR_TIMEOUT;
@@ -2333,6 +2362,26 @@ extern "C"
                 HG_CUDA(cudaEventSynchronize(a->ev_lvl[a->last_levels - 1]));
                 for (uint32_t d = 0; d < std::min(cap, a->last_levels); ++d)
                     HG_CUDA(cudaEventElapsedTime(ms + d, d ? a->ev_lvl[d - 1] : a->ev_k0, a->ev_lvl[d]));
+            });
+    }
+
+    int hibf_gpu_agent_level_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits,
+                                  uint64_t * value_visits_executed, uint32_t cap, uint32_t * n)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !n || (cap && (!tasks || !value_visits || !value_visits_executed)))
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                (void)read_status(a);
+                uint32_t const levels = static_cast<uint32_t>(a->last_level_stats.size() / kStats);
+                *n = levels;
+                for (uint32_t d = 0; d < std::min(cap, levels); ++d)
+                {
+                    tasks[d] = a->last_level_stats[d * kStats + 0];
+                    value_visits[d] = a->last_level_stats[d * kStats + 1];
+                    value_visits_executed[d] = a->last_level_stats[d * kStats + 2];
+                }
             });
     }
 

@@ -29,6 +29,29 @@ struct alignas(16) dev_node
 
 int sm_count();
 
+// One build phase's time, kept like the reference's concurrent_timer (include/hibf/misc/timer.hpp): the seconds of
+// all intervals, the longest interval and the number of intervals.
+struct phase_timer
+{
+    double seconds{};
+    double max_seconds{};
+    uint64_t count{};
+    void add(double s)
+    {
+        seconds += s;
+        max_seconds = s > max_seconds ? s : max_seconds;
+        ++count;
+    }
+};
+enum : int
+{
+    timer_index_allocation,
+    timer_user_bin_io,
+    timer_merge_kmers,
+    timer_fill_ibf,
+    n_timers
+};
+
 } // namespace hibf_gb300
 
 struct hibf_gpu_hibf
@@ -54,6 +77,8 @@ struct hibf_gpu_hibf
     std::vector<uint8_t> track_occupancy;
     // every user bin's position in membership_for's traversal order (computed on first use, under `mu`)
     std::vector<uint64_t> trav_rank;
+    // the build's phase timers (zero unless built by hibf_gpu_hibf_build / _build_synthetic)
+    hibf_gb300::phase_timer timers[hibf_gb300::n_timers];
     cudaStream_t stream{};
     std::mutex mu;
 };

@@ -173,6 +173,15 @@ class hierarchical_interleaved_bloom_filter:
         N.call("hibf_gpu_hibf_digests", self._h, out.ctypes.data, int(threads))
         return out[:self.n_ibfs]
 
+    def build_timers(self) -> dict:
+        """The build's phase timers (hierarchical_interleaved_bloom_filter.hpp:283-290): per phase
+        (index_allocation, user_bin_io, merge_kmers, fill_ibf) its seconds, longest interval and interval count;
+        all zero for an HIBF that was loaded or created from tables."""
+        t = (N.Timer * len(N.TIMER_NAMES))()
+        N.call("hibf_gpu_hibf_build_timers", self._h, t)
+        return {n: {"seconds": t[i].seconds, "max_seconds": t[i].max_seconds, "count": int(t[i].count)}
+                for i, n in enumerate(N.TIMER_NAMES)}
+
     def emplace(self, k: int, values, bin: int) -> None:
         v = _u64(values)
         N.call("hibf_gpu_hibf_emplace", self._h, k, v.ctypes.data, v.size, int(bin))
@@ -286,6 +295,16 @@ class _agent_base:
         out = (ctypes.c_float * 16)()
         N.call("hibf_gpu_agent_level_ms", self._a, out, 16, ctypes.byref(n))
         return [float(out[i]) for i in range(min(n.value, 16))]
+
+    def level_work(self) -> list[dict]:
+        """Per level of the last batch under the level schedule: its tasks, value visits and executed value visits
+        (root first); [] for the queue."""
+        n = ctypes.c_uint32(0)
+        t, v, e = (np.zeros(64, np.uint64) for _ in range(3))
+        N.call("hibf_gpu_agent_level_work", self._a, t.ctypes.data, v.ctypes.data, e.ctypes.data, 64,
+               ctypes.byref(n))
+        return [dict(tasks=int(t[i]), value_visits=int(v[i]), value_visits_executed=int(e[i]))
+                for i in range(min(n.value, 64))]
 
     def last_timeline(self) -> list[float]:
         """ms from the last host batch's first device work: each value chunk's copy done, kernel start, kernel end,

@@ -239,6 +239,28 @@ void hibf_gpu_split_table_destroy(hibf_gpu_split_table * t);
 int hibf_gpu_hibf_build_synthetic(hibf_gpu_build_config const * cfg, char const * layout_text, uint64_t seed,
                                   uint64_t const * user_bin_offsets, hibf_gpu_split_table const * table,
                                   hibf_gpu_hibf ** out);
+/* The build's phase timers (hierarchical_interleaved_bloom_filter.hpp:283-290, each a concurrent_timer,
+ * include/hibf/misc/timer.hpp): the seconds of all intervals, the longest interval and the interval count of
+ *   [0] index_allocation: allocating and zeroing the bit stores (src/build/construct_ibf.cpp:49-57);
+ *   [1] user_bin_io: the input_fn calls, one interval per user bin (src/build/compute_kmers.cpp:27-31), and the
+ *       upload of the distinct values; no interval in a synthetic build, whose fill kernel generates the values;
+ *   [2] merge_kmers: the set work that stands in for the reference's parent merges (update_parent_kmers): distinct
+ *       sets, union sizes and the split-order replay, one interval each;
+ *   [3] fill_ibf: the device inserts into every IBF, one interval (src/build/insert_into_ibf.cpp:37-68).
+ * All zero for an HIBF that was loaded or created from tables: the reference's timers hold values only after a
+ * build.  The reference's layout_* timers time the layout computation, which stays with seqan::hibf. */
+typedef struct hibf_gpu_timer
+{
+    double seconds;     /* concurrent_timer::in_seconds()     */
+    double max_seconds; /* concurrent_timer::max_in_seconds() */
+    uint64_t count;     /* intervals added                    */
+} hibf_gpu_timer;
+#define HIBF_GPU_TIMER_INDEX_ALLOCATION 0
+#define HIBF_GPU_TIMER_USER_BIN_IO 1
+#define HIBF_GPU_TIMER_MERGE_KMERS 2
+#define HIBF_GPU_TIMER_FILL_IBF 3
+#define HIBF_GPU_TIMER_COUNT 4
+int hibf_gpu_hibf_build_timers(hibf_gpu_hibf const * h, hibf_gpu_timer * timers /* [HIBF_GPU_TIMER_COUNT] */);
 /* interleaved_bloom_filter(config&, max_bin_elements) (interleaved_bloom_filter.hpp:241, src/interleaved_bloom_filter.cpp:
  * 55-117): bin count = number_of_user_bins; bin size from max_bin_elements, or -- when 0 -- from the exact distinct
  * count of the user bin with the largest HyperLogLog estimate (sketch_bits), the first such bin on ties; then user
@@ -347,6 +369,11 @@ int hibf_gpu_agent_kernel_ms(hibf_gpu_agent * a, float * ms);
  * includes grouping its tasks by IBF).  *n receives the level count (0 for a batch run by the queue); at most `cap`
  * are written. */
 int hibf_gpu_agent_level_ms(hibf_gpu_agent * a, float * ms, uint32_t cap, uint32_t * n);
+/* Per level of the last level-scheduled batch: tasks, value visits and executed value visits (the early exit's
+ * saving per level; their sums are hibf_gpu_agent_last_work / _last_work_executed).  *n receives the level count (0
+ * for a batch run by the queue); at most `cap` entries of each array are written.  Synchronises the agent's stream. */
+int hibf_gpu_agent_level_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits,
+                              uint64_t * value_visits_executed, uint32_t cap, uint32_t * n);
 /* Number of chunks in which the agent's last host batch streamed its values (0: copied whole before the launch). */
 int hibf_gpu_agent_input_chunks(hibf_gpu_agent const * a, uint32_t * chunks);
 /* Timeline of the agent's last host batch (hibf_gpu_agent_query_batch), in ms from the call's first device work:
@@ -486,7 +513,9 @@ int hibf_gpu_server_submit(hibf_gpu_server * s, uint64_t const * values, uint64_
                            uint64_t n_queries, uint64_t const * thresholds, double arrival_s, int copy, uint64_t * id);
 /* Registers [ptr, ptr + bytes) as page-locked request memory: borrowed requests whose values lie inside a registered
  * range are copied to the device directly (no staging).  already_pinned == 0: the server page-locks the range
- * (cudaHostRegister) and unlocks it on unregister or destroy; != 0: the caller allocated it page-locked. */
+ * (cudaHostRegister) and unlocks it on unregister or destroy; != 0: the caller allocated it page-locked.  The device
+ * reads the range once on registration (synchronous): a page-locked page's first device read is several times slower
+ * than later ones, so requests from a registered range start warm. */
 int hibf_gpu_server_register_host(hibf_gpu_server * s, void const * ptr, uint64_t bytes, int already_pinned);
 int hibf_gpu_server_unregister_host(hibf_gpu_server * s, void const * ptr);
 /* Waits up to timeout_ms (< 0: forever); *status is the request's status; results valid until release. */

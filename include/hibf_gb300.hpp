@@ -333,6 +333,35 @@ struct config
     size_t threads{1};
 };
 
+// The read side of the reference's concurrent_timer (include/hibf/misc/timer.hpp): a build phase's seconds, its
+// longest interval and the interval count.
+class build_timer
+{
+public:
+    build_timer() = default;
+    explicit build_timer(hibf_gpu_timer const & t) : t_{t} {}
+    double in_seconds() const
+    {
+        return t_.seconds;
+    }
+    double max_in_seconds() const
+    {
+        return t_.max_seconds;
+    }
+    // as in the reference, only meaningful once an interval was added
+    double avg_in_seconds() const
+    {
+        return t_.count ? t_.seconds / static_cast<double>(t_.count) : 0.0;
+    }
+    uint64_t count() const
+    {
+        return t_.count;
+    }
+
+private:
+    hibf_gpu_timer t_{};
+};
+
 class hierarchical_interleaved_bloom_filter
 {
 public:
@@ -354,6 +383,10 @@ public:
     hierarchical_interleaved_bloom_filter & operator=(hierarchical_interleaved_bloom_filter const &) = delete;
     hierarchical_interleaved_bloom_filter(hierarchical_interleaved_bloom_filter && o) noexcept :
         number_of_user_bins{o.number_of_user_bins},
+        index_allocation_timer{o.index_allocation_timer},
+        user_bin_io_timer{o.user_bin_io_timer},
+        merge_kmers_timer{o.merge_kmers_timer},
+        fill_ibf_timer{o.fill_ibf_timer},
         h_{std::exchange(o.h_, nullptr)}
     {}
     ~hierarchical_interleaved_bloom_filter()
@@ -363,6 +396,13 @@ public:
     }
 
     size_t number_of_user_bins{};
+
+    // The build's phase timers (hierarchical_interleaved_bloom_filter.hpp:283-290); zero unless this object was
+    // built.  The layout_* timers of the reference time the layout computation, which seqan::hibf keeps.
+    build_timer index_allocation_timer{};
+    build_timer user_bin_io_timer{};
+    build_timer merge_kmers_timer{};
+    build_timer fill_ibf_timer{};
 
     class membership_agent_type
     {
@@ -535,6 +575,12 @@ private:
         uint64_t info[4];
         check(hibf_gpu_hibf_info(h_, info));
         number_of_user_bins = info[0];
+        hibf_gpu_timer t[HIBF_GPU_TIMER_COUNT];
+        check(hibf_gpu_hibf_build_timers(h_, t));
+        index_allocation_timer = build_timer{t[HIBF_GPU_TIMER_INDEX_ALLOCATION]};
+        user_bin_io_timer = build_timer{t[HIBF_GPU_TIMER_USER_BIN_IO]};
+        merge_kmers_timer = build_timer{t[HIBF_GPU_TIMER_MERGE_KMERS]};
+        fill_ibf_timer = build_timer{t[HIBF_GPU_TIMER_FILL_IBF]};
     }
 
     hibf_gpu_hibf * h_{};

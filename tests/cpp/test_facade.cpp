@@ -161,6 +161,11 @@ static void hibf_small(std::string const & dir)
     agent.sort_results();
     CHECK(result == (std::vector<uint64_t>{0, 1}));
     CHECK(hibf.number_of_user_bins == 2);
+    // the build's timers: two user bins read, one allocation, one fill
+    CHECK(hibf.user_bin_io_timer.count() == 3 && hibf.user_bin_io_timer.in_seconds() > 0.0);
+    CHECK(hibf.index_allocation_timer.count() == 1 && hibf.fill_ibf_timer.count() == 1);
+    CHECK(hibf.fill_ibf_timer.max_in_seconds() == hibf.fill_ibf_timer.in_seconds());
+    CHECK(hibf.merge_kmers_timer.avg_in_seconds() <= hibf.merge_kmers_timer.max_in_seconds());
     // copy_agents: counting {5, 5} at threshold 1 and {0, 0} at threshold 6
     auto counter = hibf.counting_agent<uint16_t>();
     CHECK(counter.bulk_count(query, 1) == (std::vector<uint16_t>{5, 5}));

@@ -108,6 +108,34 @@ def test_build_matches_reference_unit_expectations(gpu_lib):
         assert a.membership_for(np.arange(s + 5, s + 9), 4).tolist() == [ub]
 
 
+def test_build_timers(gpu_lib, tmp_path):
+    """The build's phase timers (hierarchical_interleaved_bloom_filter.hpp:283-290): an input_fn build reads every
+    user bin once (one user_bin_io interval each, plus the upload of the distinct values), sizes unions and replays
+    split orders (merge_kmers), allocates once and fills once; a synthetic build generates its values in the fill
+    kernel (no user_bin_io) and replays split orders only without a table; a loaded HIBF holds no timers."""
+    d = G.hibf_case("synth600")
+    seed = int(d["synthetic_seed"][0])
+    ubs = [S.user_bin_values(seed, d["ub_offsets"], u) for u in range(d["n_ub"])]
+
+    def check(t, counts):
+        assert {n: v["count"] for n, v in t.items()} == counts
+        for n, v in t.items():
+            assert v["seconds"] >= v["max_seconds"] >= 0.0, n
+            assert (v["seconds"] > 0.0) == (v["count"] > 0), n
+
+    H = hg.hierarchical_interleaved_bloom_filter(_cfg(d, lambda ub, it: it.push(ubs[ub])), d["layout_text"])
+    check(H.build_timers(), dict(index_allocation=1, user_bin_io=d["n_ub"] + 1, merge_kmers=3, fill_ibf=1))
+    cfg = _cfg(d)
+    check(B.build_synthetic(cfg, d["layout_text"], seed, d["ub_offsets"]).build_timers(),
+          dict(index_allocation=1, user_bin_io=0, merge_kmers=1, fill_ibf=1))
+    table = B.split_table.synthetic(cfg, d["layout_text"], seed, d["ub_offsets"])
+    check(B.build_synthetic(cfg, d["layout_text"], seed, d["ub_offsets"], table).build_timers(),
+          dict(index_allocation=1, user_bin_io=0, merge_kmers=0, fill_ibf=1))
+    H.save(tmp_path / "h.bin")
+    L = hg.hierarchical_interleaved_bloom_filter.load(tmp_path / "h.bin")
+    check(L.build_timers(), dict(index_allocation=0, user_bin_io=0, merge_kmers=0, fill_ibf=0))
+
+
 def _digests_by_path(t, digests):
     return {path: int(digests[k]) for path, (_b, _s, _r, k) in canonical(t).items()}
 

@@ -478,6 +478,17 @@ def test_level_schedule_gives_the_reference_results(gpu_lib, name):
         offs, ids, _ = a.query_batch(qv, qo, d["mem_t"])
         for i, (g, e) in enumerate(zip(_split(offs, ids), exp)):
             np.testing.assert_array_equal(g, e, err_msg=f"{ee} query {i}")
+        # per-level work adds up to the batch's; the roots visit every value once
+        lw = a.level_work()
+        if nq == 0:
+            assert lw == []
+        else:
+            tasks, visits = a.last_work()
+            assert len(lw) == H.info()["max_depth"] + 1
+            assert sum(x["tasks"] for x in lw) == tasks and sum(x["value_visits"] for x in lw) == visits
+            assert sum(x["value_visits_executed"] for x in lw) == a.last_work_executed()
+            assert lw[0]["tasks"] == nq and lw[0]["value_visits"] == int(qo[-1])
+            assert all(x["value_visits_executed"] <= x["value_visits"] for x in lw)
         offs, ids, cnts = a.query_batch(qv, qo, d["cnt_t"], mode=N.QUERY_COUNT, width=w)
         dense = np.zeros_like(d[f"count{w}"])
         for i in range(nq):
