@@ -330,6 +330,7 @@ def learned_scheduler(hibf, tuning, d_v, d_qo, d_thr, qo, nq, n, stream):
     kernel with its root tasks in query order, in order of length, and in order of the model's prediction."""
     import torch
 
+    from hibf_gb300 import _native as N
     from hibf_gb300.scheduler import cost_model
 
     a = hibf.membership_agent()
@@ -372,26 +373,39 @@ def learned_scheduler(hibf, tuning, d_v, d_qo, d_thr, qo, nq, n, stream):
     work = w_te.cpu().numpy().astype(np.float64)
     rho = lambda x: float(np.corrcoef(_ranks(x), _ranks(work))[0, 1])
     v, q, t = sub(first)
-    times, results = {}, {}
-    for name, order in (("query_order", None), ("length_order", o_len), ("learned_order", o_learned)):
-        a.set_order(order.data_ptr() if order is not None else None, n)
-        ks = []
-        for _ in range(7):
-            a.query_batch_device(v, q, n, t)
-            stream.synchronize()
-            ks.append(a.kernel_ms())
-        a.status()
-        times[name] = float(np.median(ks[2:]))
-        o, i, _ = a.fetch_results(n)
-        results[name] = (o, i)
-    a.set_order(None)
-    same = all(np.array_equal(results[k][0], results["query_order"][0]) and
-               np.array_equal(results[k][1], results["query_order"][1]) for k in results)
+    results = {}
+
+    def timed_orders(schedule):
+        a.tuning = dict(tuning, schedule=schedule)
+        times = {}
+        for name, order in (("query_order", None), ("length_order", o_len), ("learned_order", o_learned)):
+            a.set_order(order.data_ptr() if order is not None else None, n)
+            ks = []
+            for _ in range(7):
+                a.query_batch_device(v, q, n, t)
+                stream.synchronize()
+                ks.append(a.kernel_ms())
+            a.status()
+            times[name] = float(np.median(ks[2:]))
+            o, i, _ = a.fetch_results(n)
+            results[(schedule, name)] = (o, i)
+        a.set_order(None)
+        return times
+
+    times = timed_orders(tuning["schedule"])
+    # the work queue (the schedule of streamed host batches): its claim order decides which tasks run last
+    times_queue = timed_orders(N.SCHEDULE_QUEUE) if tuning["schedule"] != N.SCHEDULE_QUEUE else times
+    base = results[(tuning["schedule"], "query_order")]
+    same = all(np.array_equal(r[0], base[0]) and np.array_equal(r[1], base[1]) for r in results.values())
     return {"batch_queries": n, "train_queries": n, "train_steps": 500, "train_s": train_s, "train_mse": loss,
             "order_s": order_s, "spearman_learned": rho(pred.cpu().numpy().astype(np.float64)),
             "spearman_length": rho(np.diff(qo[first:first + n + 1]).astype(np.float64)),
             "kernel_ms": times, "gain_vs_query_order": times["query_order"] / times["learned_order"],
-            "gain_vs_length_order": times["length_order"] / times["learned_order"], "results_identical": same,
+            "gain_vs_length_order": times["length_order"] / times["learned_order"],
+            "work_queue": {"kernel_ms": times_queue,
+                           "gain_vs_query_order": times_queue["query_order"] / times_queue["learned_order"],
+                           "gain_vs_length_order": times_queue["length_order"] / times_queue["learned_order"]},
+            "results_identical": same,
             "model": "6 features -> 32 -> 32 -> 1 ReLU MLP, full-batch Adam on log(1 + executed visits), "
                      "hibf_gb300/csrc/cost_model.cu"}
 
@@ -611,6 +625,10 @@ def measure_hibf(args, wl, world, stream, full):
         "h2d_GBps_probe": h2d_probe(min(nv * 8, 4 << 30)),
         "wall_ms_per_call": [round(w * 1e3, 2) for w in wall],
         "values_copied_ms_per_call": [round(t[n_chunks - 1], 2) for t in timelines],
+        # calls whose value copy took over 1.5x the fastest call's: the host link, not the kernel, set their time
+        "slow_copy_calls": int(sum(t[n_chunks - 1] > 1.5 * min(u[n_chunks - 1] for u in timelines)
+                                   for t in timelines)),
+        "wall_ms_median": round(float(np.median(wall)) * 1e3, 2),
         "results_back_ms_per_call": [round(t[n_chunks + 2], 2) for t in timelines],
         "note": "ms from the call's first device work; values_copied = the last chunk's copy done",
     }
@@ -621,9 +639,13 @@ def measure_hibf(args, wl, world, stream, full):
         from hibf_gb300.serve import server
 
         pool_q = min(nq, 100_000)
-        pool_v = hv[:int(qo[pool_q])]
+        # the requests' values live in their own page-locked pool written by the host, as a server's receive buffers
+        # would be (not a view of the end-to-end buffer, which the device wrote)
+        pool_t = torch.empty(int(qo[pool_q]), dtype=torch.int64, pin_memory=True)
+        pool_v = pool_t.numpy().view(np.uint64)
+        pool_v[:] = hv[:pool_v.size]
 
-        def pool_copy_ms(mb=29):
+        def pool_copy_ms(src_t, mb=29):
             """Device time of plain copies of pool slices (CUDA events on a side stream): the link's own rate."""
             n = int(mb * (1 << 20) / 8)
             dst = torch.empty(n, dtype=torch.int64, device="cuda")
@@ -631,7 +653,7 @@ def measure_hibf(args, wl, world, stream, full):
             ms = []
             for rep in range(5):
                 a = (rep * 1_000_003) % (pool_v.size - n)
-                src = h_v[a:a + n]
+                src = src_t[a:a + n]
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 with torch.cuda.stream(side):
                     e0.record(side)
@@ -642,7 +664,7 @@ def measure_hibf(args, wl, world, stream, full):
                 time.sleep(0.02)
             return round(float(np.median(ms)), 4)
 
-        pool_copy_before = pool_copy_ms()
+        pool_copy_before = {"request_pool": pool_copy_ms(pool_t), "end_to_end_buffer": pool_copy_ms(h_v)}
         # 1e5 and 1e6 queries/s run for at least 10,000 requests (about 490 queries per request)
         for load, dur in ((1e4, 10.0), (1e5, 50.0), (1e6, 5.0)):
             srv = server(hibf, slots=4, max_batch_queries=65536, max_batch_values=1 << 27, admission_bytes=4 << 30)
@@ -656,8 +678,12 @@ def measure_hibf(args, wl, world, stream, full):
                 r["p99_note"] = f"{r['requests']} requests: the 99th percentile is near the maximum"
             serving.append(r)
             srv.close()
-        # plain copies from the request pool before the server read it (cold pages) and after the load points
-        serving[0]["pool_copy_29MB_ms"] = {"before": pool_copy_before, "after": pool_copy_ms()}
+        # plain copies of 29 MB slices before the load points (from the request pool and from the same range of the
+        # end-to-end buffer) and after them
+        serving[0]["pool_copy_29MB_ms"] = {"before": pool_copy_before,
+                                           "after": {"request_pool": pool_copy_ms(pool_t),
+                                                     "end_to_end_buffer": pool_copy_ms(h_v)}}
+        del pool_t
     learned = None
     if full and not args.no_learned and nq >= 2 * args.sched_queries:
         learned = learned_scheduler(hibf, agent.tuning, d_v, d_qo, d_thr, qo, nq, args.sched_queries, stream)
@@ -764,7 +790,9 @@ def run_ours(args, wl, rank, world, local):
             "index_bytes": m["index_bytes"], "queries_per_s": m["queries_per_s"], "plain": m["plain"],
             "batched_vs_plain": m["batched_vs_plain"], "bulk_count": m["bulk_count"], "build": m["build"],
             "autotune": m["autotune"], "learned_scheduler": m["learned_scheduler"],
-            "serving": serving, "p99_serve_latency_ms": serving[-1]["p99_ms"] if serving else None,
+            "serving": serving,
+            "p99_serve_latency_ms": ({f"{r['offered_qps']:.0e} queries/s offered": round(r["p99_ms"], 3)
+                                      for r in serving} if serving else None),
             "serving_config": "open-loop Poisson, request sizes log-uniform 1-4096 queries from the batch's first "
                               "100k queries, thresholds U(0.5,0.9)*len, 4 slots, 4 GiB admission cap",
             "c4": c4,
