@@ -454,11 +454,20 @@ def make_ref_build(R: Reference, name: str, scale: float):
     print(f"{out.name}: {len(T['bins'])} IBFs, {int(offs[-1])} values, {time.time() - t0:.0f}s")
 
 
+def make_simple_case(R: Reference):
+    # test/unit/hibf/hierarchical_interleaved_bloom_filter_test.cpp:47 simple_user_bins: 73 user bins holding only the
+    # value 5 (the reference computes the layout); queries that hit every user bin, some, or none
+    ubs = [[5]] * 73
+    v, o = csr(ubs)
+    q = csr([[5], [5, 6], [6], [5, 5, 5], [6, 7, 8, 5]])
+    hibf_case(R, "simple", ref_cfg(73), v, o, q, [1, 2, 1, 3, 2], [1, 1, 1, 2, 1], widths=(1, 2, 8))
+
+
 def main(argv):
     build_reference()
     R = Reference()
     which = set(argv) or {"ibf", "ibfcfg", "hll", "serial", "hibf", "hibfwide", "dups", "hashes", "empty", "sizing",
-                          "c1", "c3"}
+                          "simple", "c1", "c3"}
     if "ibf" in which:
         make_ibf_cases(R)
     if "serial" in which:
@@ -479,6 +488,8 @@ def main(argv):
         make_ibf_config(R)
     if "hibf" in which:
         make_hibf_cases(R)
+    if "simple" in which:
+        make_simple_case(R)
     if "c1" in which:
         make_c1(R)
     if "c3" in which:

@@ -7,7 +7,8 @@ import numpy as np
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 HIBF_CASES = ["snippet", "readme", "three_level", "uneven", "similar", "same", "synth64", "synth600", "synth_t128",
-              "synth_t256", "dups", "synth_h1", "synth_h4", "synth_h5", "empty_bins", "relaxed_fpr", "synth_t512"]
+              "synth_t256", "dups", "synth_h1", "synth_h4", "synth_h5", "empty_bins", "relaxed_fpr", "synth_t512",
+              "simple"]
 
 
 def ibf_cases():

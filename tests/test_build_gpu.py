@@ -73,7 +73,7 @@ def test_build_synthetic_matches_reference(gpu_lib, oracle, name):
         assert int(ca.bulk_count(v, 1)[ub]) >= v.size
 
 
-@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "same", "synth64",
+@pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "same", "simple", "synth64",
                                   "synth600", "synth_t128", "synth_t256"])
 def test_build_input_fn_matches_reference(gpu_lib, oracle, name):
     """hierarchical_interleaved_bloom_filter(config&, layout) through input_fn: every IBF's bit store equals the
