@@ -102,7 +102,8 @@ struct hibf_gpu_server
     // fetched, requests finished (seconds, now_s clock), queries, values, device time of its input copies and of
     // its query kernel (seconds, CUDA events)
     static constexpr size_t kBatchLogCap = 1u << 20;
-    std::vector<std::array<double, 10>> batch_log;
+    static constexpr int kBatchLogCols = 11;
+    std::vector<std::array<double, kBatchLogCols>> batch_log;
     // page-locked host ranges [begin, end) registered with the server, and whether the server pinned them
     struct host_range
     {
@@ -180,6 +181,7 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     ho[0] = 0;
     HG_CUDA(cudaEventRecord(sl.ev_in, sl.stream));
     uint64_t staged_from = 0; // start of the current run of staged requests
+    uint64_t staged_values = 0; // values copied through the slot's pinned buffer (requests outside registered ranges)
     auto flush_staged = [&](uint64_t to)
     {
         if (to > staged_from)
@@ -188,6 +190,8 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     };
     for (request * r : sl.reqs)
     {
+        if (!r->pinned)
+            staged_values += r->nv;
         if (r->pinned)
         {
             // page-locked caller memory: one DMA straight into the batch's input, no host copy
@@ -283,7 +287,8 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     S->t_split += t - t_fetched;
     if (S->batch_log.size() < hibf_gpu_server::kBatchLogCap)
         S->batch_log.push_back({t_oldest, t_start, t_launched, t_device_done, t_fetched, t, static_cast<double>(nq),
-                                static_cast<double>(sl.nv), copy_ms * 1e-3, kernel_ms * 1e-3});
+                                static_cast<double>(sl.nv), copy_ms * 1e-3, kernel_ms * 1e-3,
+                                static_cast<double>(staged_values)});
     return requeue;
 }
 
@@ -663,7 +668,8 @@ extern "C"
                 std::lock_guard<std::mutex> lk(S->mu);
                 *n = S->batch_log.size();
                 for (uint64_t i = 0; i < std::min<uint64_t>(cap, S->batch_log.size()); ++i)
-                    std::copy(S->batch_log[i].begin(), S->batch_log[i].end(), out + 10 * i);
+                    std::copy(S->batch_log[i].begin(), S->batch_log[i].end(),
+                              out + hibf_gpu_server::kBatchLogCols * i);
             });
     }
 

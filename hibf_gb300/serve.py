@@ -102,13 +102,14 @@ class server:
 
     def batch_log(self) -> np.ndarray:
         """Per batch: oldest arrival, slot start, launched, device done, fetched, finished (s), queries, values,
-        device time of the input copies and of the query kernel (s)."""
+        device time of the input copies and of the query kernel (s), values staged through the slot's pinned
+        buffer."""
         n = ctypes.c_uint64(0)
         N.call("hibf_gpu_server_batch_log", self._s, None, 0, ctypes.byref(n))
-        out = np.zeros(max(n.value, 1) * 10, np.float64)
+        out = np.zeros(max(n.value, 1) * 11, np.float64)
         N.call("hibf_gpu_server_batch_log", self._s, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n.value,
                ctypes.byref(n))
-        return out[:n.value * 10].reshape(n.value, 10)
+        return out[:n.value * 11].reshape(n.value, 11)
 
     def tail_phases(self, quantile: float = 0.99) -> dict:
         """Phase times (ms) of the batches whose oldest request waited longest (the top 1 - quantile share), beside
@@ -126,6 +127,7 @@ class server:
                 "median_batch": dict(zip(names, np.median(ph, axis=0).round(4).tolist())),
                 "tail_mean": dict(zip(names, tail.mean(axis=0).round(4).tolist())),
                 "tail_queries_mean": float(log[total >= cut, 6].mean()),
+                "tail_staged_share": float(log[total >= cut, 10].sum() / max(log[total >= cut, 7].sum(), 1.0)),
                 "median_queries": float(np.median(log[:, 6]))}
 
     def open_loop(self, pool_values, pool_offsets, offered_qps: float, duration_s: float = 1.0,

@@ -527,10 +527,11 @@ double hibf_gpu_server_now(void);
 /* Mean seconds per batch since creation: queueing of the batch's oldest request, staging + launch, device work,
  * result fetch, per-request split. */
 int hibf_gpu_server_phase_times(hibf_gpu_server * s, double out[5]);
-/* Per batch, in the order batches finished (at most 2^20 are kept): 10 doubles -- the arrival of its oldest request,
+/* Per batch, in the order batches finished (at most 2^20 are kept): 11 doubles -- the arrival of its oldest request,
  * the slot's start, the launch, device work done, results fetched, requests finished (seconds on the server's
- * clock, hibf_gpu_server_now), its queries and values, and the device time (s, CUDA events) of its input copies and
- * of its query kernel.  *n receives the batch count; at most `cap` are written. */
+ * clock, hibf_gpu_server_now), its queries and values, the device time (s, CUDA events) of its input copies and of
+ * its query kernel, and the values it staged through the slot's pinned buffer (requests outside a registered range).
+ * *n receives the batch count; at most `cap` are written. */
 int hibf_gpu_server_batch_log(hibf_gpu_server * s, double * out, uint64_t cap, uint64_t * n);
 int hibf_gpu_server_stats(hibf_gpu_server * s, uint64_t out[4]);
 /* Open-loop Poisson load from a pool of queries (host CSR): request sizes log-uniform in [1, max_request_queries],

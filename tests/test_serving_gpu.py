@@ -137,4 +137,25 @@ def test_pinned_borrowed_requests_match(gpu_lib):
         assert st == 0
         np.testing.assert_array_equal(offs, eo)
         np.testing.assert_array_equal(res, ei)
+    # the batch log: every value once, and only the copied requests' values staged through the slots' buffers
+    log = srv.batch_log()
+    assert log.shape[1] == 11 and int(log[:, 6].sum()) == sum(qo.size - 1 for _, qo, _ in reqs)
+    assert int(log[:, 7].sum()) == sum(v.size for v, _, _ in reqs)
+    assert int(log[:, 10].sum()) == sum(v.size for i, (v, _, _) in enumerate(reqs) if i % 2)
+    srv.close()
+
+
+def test_open_loop_reads_a_page_locked_pool_without_staging(gpu_lib):
+    """The open-loop driver registers a page-locked request pool, so its borrowed requests go to the device by DMA
+    from the pool: no value is staged through a slot's buffer."""
+    import torch
+
+    H, d = _hibf()
+    pool = torch.from_numpy(d["q_values"].view(np.int64)).pin_memory()
+    srv = server(H, slots=2, max_batch_queries=4096, max_batch_values=1 << 22, admission_bytes=1 << 30)
+    r = srv.open_loop(pool.numpy().view(np.uint64), d["q_offsets"], offered_qps=20000, duration_s=0.3,
+                      max_request_queries=64)
+    log = srv.batch_log()
+    assert r["requests"] > 0 and log.shape[0] > 0
+    assert int(log[:, 10].sum()) == 0
     srv.close()
