@@ -215,6 +215,7 @@ _SIGS = [
                                     ctypes.POINTER(u64p), ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_server_release", None, [vp, u64]),
     ("hibf_gpu_server_register_host", None, [vp, vp, u64, ci]),
+    ("hibf_gpu_server_set_zero_copy", None, [vp, ci]),
     ("hibf_gpu_server_unregister_host", None, [vp, vp]),
     ("hibf_gpu_server_now", ctypes.c_double, []),
     ("hibf_gpu_server_stats", None, [vp, u64p]),

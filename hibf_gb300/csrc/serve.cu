@@ -55,6 +55,7 @@ struct request
     std::atomic<bool> done{false}; // set by a slot thread after the results, read by waiters
     bool solo{false};   // run alone (after a batch overflowed)
     bool pinned{false}; // values are in page-locked host memory: copied to the device directly, not staged
+    uint64_t const * dev_values{}; // the device's address of `values` when its registered range is mapped, else null
     std::vector<uint64_t> res_off, res_ids;
 };
 
@@ -102,15 +103,18 @@ struct hibf_gpu_server
     // fetched, requests finished (seconds, now_s clock), queries, values, device time of its input copies and of
     // its query kernel (seconds, CUDA events)
     static constexpr size_t kBatchLogCap = 1u << 20;
-    static constexpr int kBatchLogCols = 11;
+    static constexpr int kBatchLogCols = 12;
     std::vector<std::array<double, kBatchLogCols>> batch_log;
     // page-locked host ranges [begin, end) registered with the server, and whether the server pinned them
     struct host_range
     {
         uintptr_t begin, end;
         bool pinned_here;
+        uint64_t const * dev; // the device's address of `begin` (mapped page-locked memory), else null
     };
     std::vector<host_range> host_ranges;
+    // a batch whose requests lie back to back in one mapped registered range is read in place by the kernel
+    std::atomic<bool> zero_copy{true};
 };
 
 namespace
@@ -182,6 +186,18 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     HG_CUDA(cudaEventRecord(sl.ev_in, sl.stream));
     uint64_t staged_from = 0; // start of the current run of staged requests
     uint64_t staged_values = 0; // values copied through the slot's pinned buffer (requests outside registered ranges)
+    // Zero copy: when the batch's requests lie back to back in one mapped page-locked range, the kernel reads their
+    // values there (over the host link, as it needs them) and no copy precedes the launch.  The batch's offsets are
+    // the same as for a compacted copy, relative to its first request's values.
+    bool zc = S->zero_copy.load() && !sl.reqs.empty();
+    for (size_t k = 0; zc && k < sl.reqs.size(); ++k)
+    {
+        request const * r = sl.reqs[k];
+        zc = r->pinned && r->dev_values &&
+             (k == 0 || (r->values == sl.reqs[k - 1]->values + sl.reqs[k - 1]->nv &&
+                         r->dev_values == sl.reqs[k - 1]->dev_values + sl.reqs[k - 1]->nv));
+    }
+    uint64_t const * const batch_values = zc ? sl.reqs.front()->dev_values : sl.d_values.as<uint64_t>();
     auto flush_staged = [&](uint64_t to)
     {
         if (to > staged_from)
@@ -191,8 +207,11 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     for (request * r : sl.reqs)
     {
         if (!r->pinned)
+        {
             staged_values += r->nv;
-        if (r->pinned)
+            std::memcpy(hv + v, r->values, r->nv * 8);
+        }
+        else if (!zc)
         {
             // page-locked caller memory: one DMA straight into the batch's input, no host copy
             flush_staged(v);
@@ -200,10 +219,6 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
                 HG_CUDA(cudaMemcpyAsync(sl.d_values.as<uint64_t>() + v, r->values, r->nv * 8, cudaMemcpyHostToDevice,
                                         sl.stream));
             staged_from = v + r->nv;
-        }
-        else
-        {
-            std::memcpy(hv + v, r->values, r->nv * 8);
         }
         for (uint64_t i = 0; i < r->nq; ++i)
         {
@@ -213,12 +228,13 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
         q += r->nq;
         v += r->nv;
     }
-    flush_staged(v);
+    if (!zc)
+        flush_staged(v);
     HG_CUDA(cudaMemcpyAsync(sl.d_qoff.p, ho, (nq + 1) * 8, cudaMemcpyHostToDevice, sl.stream));
     HG_CUDA(cudaMemcpyAsync(sl.d_thr.p, ht, std::max<uint64_t>(nq, 1) * 8, cudaMemcpyHostToDevice, sl.stream));
     void const * cnt = nullptr;
     HG_CUDA(cudaEventRecord(sl.ev_q, sl.stream));
-    int st = hibf_gpu_agent_query_batch_d(sl.agent, HIBF_GPU_QUERY_MEMBERSHIP, sl.d_values.as<uint64_t>(),
+    int st = hibf_gpu_agent_query_batch_d(sl.agent, HIBF_GPU_QUERY_MEMBERSHIP, batch_values,
                                           sl.d_qoff.as<uint64_t>(), nq, sl.d_thr.as<uint64_t>(), 2, &sl.d_roff,
                                           &sl.d_ids, &cnt);
     if (st != HIBF_GPU_OK)
@@ -288,7 +304,7 @@ std::vector<request *> run_batch(hibf_gpu_server * S, slot & sl)
     if (S->batch_log.size() < hibf_gpu_server::kBatchLogCap)
         S->batch_log.push_back({t_oldest, t_start, t_launched, t_device_done, t_fetched, t, static_cast<double>(nq),
                                 static_cast<double>(sl.nv), copy_ms * 1e-3, kernel_ms * 1e-3,
-                                static_cast<double>(staged_values)});
+                                static_cast<double>(staged_values), zc ? 1.0 : 0.0});
     return requeue;
 }
 
@@ -501,8 +517,28 @@ extern "C"
                     throw;
                 }
                 uintptr_t const b = reinterpret_cast<uintptr_t>(ptr);
+                // the device's address of the range, if it maps page-locked memory (zero-copy batches)
+                void * dev = nullptr;
+                if (cudaHostGetDevicePointer(&dev, const_cast<void *>(ptr), 0) != cudaSuccess)
+                {
+                    cudaGetLastError();
+                    dev = nullptr;
+                }
                 std::lock_guard<std::mutex> lk(S->mu);
-                S->host_ranges.push_back(hibf_gpu_server::host_range{b, b + bytes, !already_pinned});
+                S->host_ranges.push_back(
+                    hibf_gpu_server::host_range{b, b + bytes, !already_pinned, static_cast<uint64_t const *>(dev)});
+            });
+    }
+
+    int hibf_gpu_server_set_zero_copy(hibf_gpu_server * S, int on)
+    {
+        return guarded(
+            [&]
+            {
+                if (!S)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->zero_copy = on != 0;
             });
     }
 
@@ -578,7 +614,10 @@ extern "C"
                     std::lock_guard<std::mutex> lk(S->mu);
                     for (auto const & hr : S->host_ranges)
                         if (r->nv && b >= hr.begin && e <= hr.end)
+                        {
                             r->pinned = true;
+                            r->dev_values = hr.dev ? hr.dev + (b - hr.begin) / 8 : nullptr;
+                        }
                 }
                 r->t_arrival = arrival_s >= 0 ? arrival_s : now_s();
                 std::lock_guard<std::mutex> lk(S->mu);

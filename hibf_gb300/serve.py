@@ -54,6 +54,10 @@ class server:
         """Registers host memory for borrowed requests: their values are then copied to the device without staging."""
         N.call("hibf_gpu_server_register_host", self._s, ptr, nbytes, int(already_pinned))
 
+    def set_zero_copy(self, on: bool) -> None:
+        """Batches of back-to-back borrowed requests in one mapped registered range are read in place (default on)."""
+        N.call("hibf_gpu_server_set_zero_copy", self._s, int(on))
+
     def unregister_host(self, ptr: int) -> None:
         N.call("hibf_gpu_server_unregister_host", self._s, ptr)
 
@@ -103,13 +107,13 @@ class server:
     def batch_log(self) -> np.ndarray:
         """Per batch: oldest arrival, slot start, launched, device done, fetched, finished (s), queries, values,
         device time of the input copies and of the query kernel (s), values staged through the slot's pinned
-        buffer."""
+        buffer, 1 if the kernel read the values in place (zero copy)."""
         n = ctypes.c_uint64(0)
         N.call("hibf_gpu_server_batch_log", self._s, None, 0, ctypes.byref(n))
-        out = np.zeros(max(n.value, 1) * 11, np.float64)
+        out = np.zeros(max(n.value, 1) * 12, np.float64)
         N.call("hibf_gpu_server_batch_log", self._s, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n.value,
                ctypes.byref(n))
-        return out[:n.value * 11].reshape(n.value, 11)
+        return out[:n.value * 12].reshape(n.value, 12)
 
     def tail_phases(self, quantile: float = 0.99) -> dict:
         """Phase times (ms) of the batches whose oldest request waited longest (the top 1 - quantile share), beside
@@ -128,6 +132,7 @@ class server:
                 "tail_mean": dict(zip(names, tail.mean(axis=0).round(4).tolist())),
                 "tail_queries_mean": float(log[total >= cut, 6].mean()),
                 "tail_staged_share": float(log[total >= cut, 10].sum() / max(log[total >= cut, 7].sum(), 1.0)),
+                "zero_copy_batches_share": float(log[:, 11].mean()),
                 "median_queries": float(np.median(log[:, 6]))}
 
     def open_loop(self, pool_values, pool_offsets, offered_qps: float, duration_s: float = 1.0,

@@ -517,6 +517,10 @@ int hibf_gpu_server_submit(hibf_gpu_server * s, uint64_t const * values, uint64_
  * reads the range once on registration (synchronous): a page-locked page's first device read is several times slower
  * than later ones, so requests from a registered range start warm. */
 int hibf_gpu_server_register_host(hibf_gpu_server * s, void const * ptr, uint64_t bytes, int already_pinned);
+/* Zero copy (on by default): a batch whose borrowed requests lie back to back in one registered range that the
+ * device can address (mapped page-locked memory) is answered without copying its values: the kernel reads them in
+ * place over the host link as it needs them.  Other batches copy their values first.  Results are the same. */
+int hibf_gpu_server_set_zero_copy(hibf_gpu_server * s, int on);
 int hibf_gpu_server_unregister_host(hibf_gpu_server * s, void const * ptr);
 /* Waits up to timeout_ms (< 0: forever); *status is the request's status; results valid until release. */
 int hibf_gpu_server_wait(hibf_gpu_server * s, uint64_t id, double timeout_ms, int * status,
@@ -527,11 +531,12 @@ double hibf_gpu_server_now(void);
 /* Mean seconds per batch since creation: queueing of the batch's oldest request, staging + launch, device work,
  * result fetch, per-request split. */
 int hibf_gpu_server_phase_times(hibf_gpu_server * s, double out[5]);
-/* Per batch, in the order batches finished (at most 2^20 are kept): 11 doubles -- the arrival of its oldest request,
+/* Per batch, in the order batches finished (at most 2^20 are kept): 12 doubles -- the arrival of its oldest request,
  * the slot's start, the launch, device work done, results fetched, requests finished (seconds on the server's
  * clock, hibf_gpu_server_now), its queries and values, the device time (s, CUDA events) of its input copies and of
- * its query kernel, and the values it staged through the slot's pinned buffer (requests outside a registered range).
- * *n receives the batch count; at most `cap` are written. */
+ * its query kernel, the values it staged through the slot's pinned buffer (requests outside a registered range), and
+ * 1 if the kernel read its values in place (zero copy), else 0.  *n receives the batch count; at most `cap` are
+ * written. */
 int hibf_gpu_server_batch_log(hibf_gpu_server * s, double * out, uint64_t cap, uint64_t * n);
 int hibf_gpu_server_stats(hibf_gpu_server * s, uint64_t out[4]);
 /* Open-loop Poisson load from a pool of queries (host CSR): request sizes log-uniform in [1, max_request_queries],

@@ -139,10 +139,49 @@ def test_pinned_borrowed_requests_match(gpu_lib):
         np.testing.assert_array_equal(res, ei)
     # the batch log: every value once, and only the copied requests' values staged through the slots' buffers
     log = srv.batch_log()
-    assert log.shape[1] == 11 and int(log[:, 6].sum()) == sum(qo.size - 1 for _, qo, _ in reqs)
+    assert log.shape[1] == 12 and int(log[:, 6].sum()) == sum(qo.size - 1 for _, qo, _ in reqs)
     assert int(log[:, 7].sum()) == sum(v.size for v, _, _ in reqs)
     assert int(log[:, 10].sum()) == sum(v.size for i, (v, _, _) in enumerate(reqs) if i % 2)
     srv.close()
+
+
+def test_zero_copy_batches_match(gpu_lib):
+    """Back-to-back borrowed requests in one mapped page-locked range are answered without copying their values (the
+    kernel reads them in place); the same requests with zero copy off are copied first.  Every result equals the
+    query answered alone, both ways."""
+    import torch
+
+    H, d = _hibf()
+    qs = G.queries(d)
+    agent = H.membership_agent()
+    pool = torch.from_numpy(np.concatenate(qs).view(np.int64)).pin_memory()
+    starts = np.zeros(len(qs) + 1, np.int64)
+    np.cumsum([q.size for q in qs], out=starts[1:])
+    # consecutive slices of the pool, so that a batch of several of them is one contiguous run
+    reqs = []
+    k0 = 0
+    rng = np.random.default_rng(3)
+    while k0 < len(qs) - 1:
+        k1 = min(len(qs), k0 + int(rng.integers(1, 12)))
+        qo = (starts[k0:k1 + 1] - starts[k0]).astype(np.uint64)
+        thr = np.array([int(np.ceil(0.6 * q.size)) for q in qs[k0:k1]], np.uint64)
+        reqs.append((k0, k1, qo, thr))
+        k0 = k1
+    for zc in (True, False):
+        srv = server(H, slots=2, max_batch_queries=4096, max_batch_values=1 << 22, admission_bytes=1 << 30)
+        srv.set_zero_copy(zc)
+        srv.register_host(pool.data_ptr(), pool.numel() * 8, already_pinned=True)
+        ids = [srv.submit_borrowed(pool.data_ptr() + 8 * int(starts[a]), qo, thr) for a, b, qo, thr in reqs]
+        for rid, (a, b, qo, thr) in zip(ids, reqs):
+            st, offs, res, _ = srv.wait_result(rid, qo.size - 1)
+            assert st == 0
+            eo, ei, _ = agent.query_batch(pool.numpy()[starts[a]:starts[b]].view(np.uint64), qo, thr)
+            np.testing.assert_array_equal(offs, eo)
+            np.testing.assert_array_equal(res, ei)
+        log = srv.batch_log()
+        assert int(log[:, 10].sum()) == 0
+        assert (log[:, 11].sum() > 0) == zc
+        srv.close()
 
 
 def test_open_loop_reads_a_page_locked_pool_without_staging(gpu_lib):
