@@ -615,23 +615,44 @@ def measure_hibf(args, wl, world, stream, full):
     d2h = (nq + 1) * 8 + int(eo[-1]) * 8 + 8 * 8 + 16
     last = timelines[-1]
     n_chunks = len(last) - 3
+    in_place = ea.last_in_place()
+    e2e_level_ms = [round(x, 3) for x in ea.level_ms()]
     e2e_timeline = {
-        "chunks": n_chunks,
-        "median_ms": {"values_copied": float(np.median([t[n_chunks - 1] for t in timelines])),
+        "values": "read in place by the kernel over the host link" if in_place else f"copied in {n_chunks} chunks",
+        "median_ms": {("inputs_ready" if in_place else "values_copied"):
+                      float(np.median([t[n_chunks - 1] for t in timelines])),
                       "kernel_start": float(np.median([t[n_chunks] for t in timelines])),
                       "kernel_end": float(np.median([t[n_chunks + 1] for t in timelines])),
                       "results_back": float(np.median([t[n_chunks + 2] for t in timelines]))},
-        "h2d_GBps_in_call": nv * 8 / (float(np.median([t[n_chunks - 1] for t in timelines])) / 1e3) / 1e9,
-        "h2d_GBps_probe": h2d_probe(min(nv * 8, 4 << 30)),
         "wall_ms_per_call": [round(w * 1e3, 2) for w in wall],
-        "values_copied_ms_per_call": [round(t[n_chunks - 1], 2) for t in timelines],
-        # calls whose value copy took over 1.5x the fastest call's: the host link, not the kernel, set their time
-        "slow_copy_calls": int(sum(t[n_chunks - 1] > 1.5 * min(u[n_chunks - 1] for u in timelines)
-                                   for t in timelines)),
         "wall_ms_median": round(float(np.median(wall)) * 1e3, 2),
         "results_back_ms_per_call": [round(t[n_chunks + 2], 2) for t in timelines],
-        "note": "ms from the call's first device work; values_copied = the last chunk's copy done",
+        "level_ms": e2e_level_ms,
+        "note": "ms from the call's first device work; inputs_ready = offsets and thresholds on the device",
     }
+    # the same calls with the values copied first (streamed in chunks while the work queue runs)
+    ea.set_host_read(False)
+    ea.query_batch(hv, qo, thr)
+    wall_cp, timelines_cp = [], []
+    for _ in range(e2e_steps):
+        t0 = time.perf_counter()
+        co, ci, _ = ea.query_batch(hv, qo, thr)
+        wall_cp.append(time.perf_counter() - t0)
+        timelines_cp.append(ea.last_timeline())
+    parity["e2e_copied_equals_batch"] = bool(not ea.last_in_place() and np.array_equal(co, res_offs) and
+                                             np.array_equal(ci, res_ids))
+    nc = len(timelines_cp[-1]) - 3
+    e2e_copied = {"value": world * nv / (sum(wall_cp) / len(wall_cp)), "unit": "values/s",
+                  "ms_per_step": sum(wall_cp) / len(wall_cp) * 1e3,
+                  "wall_ms_median": round(float(np.median(wall_cp)) * 1e3, 2),
+                  "wall_ms_per_call": [round(w * 1e3, 2) for w in wall_cp],
+                  "chunks": nc,
+                  "values_copied_ms_per_call": [round(t[nc - 1], 2) for t in timelines_cp],
+                  # calls whose copy took over 1.5x the fastest call's: the host link, not the kernel, set their time
+                  "slow_copy_calls": int(sum(t[nc - 1] > 1.5 * min(u[nc - 1] for u in timelines_cp)
+                                             for t in timelines_cp)),
+                  "h2d_GBps_probe": h2d_probe(min(nv * 8, 4 << 30)),
+                  "call": "hibf_gpu_agent_query_batch after hibf_gpu_agent_set_host_read(0)"}
     del ea
 
     serving = []
@@ -721,7 +742,8 @@ def measure_hibf(args, wl, world, stream, full):
         "queries_per_s": world * nq / (ms / 1e3),
         "e2e": {"value": world * nv / e2e_s, "unit": "values/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
-                "call": "hibf_gpu_agent_query_batch (host buffers, pinned)", "timeline": e2e_timeline},
+                "call": "hibf_gpu_agent_query_batch (host buffers, page-locked: values read in place)",
+                "timeline": e2e_timeline, "copied_first": e2e_copied},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": peak_kind, "achieved_executed": achieved_executed,
                      "frac_executed": achieved_executed / hbm,

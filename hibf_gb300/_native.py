@@ -185,6 +185,8 @@ _SIGS = [
     ("hibf_gpu_agent_level_ms", None, [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_uint32,
                                        ctypes.POINTER(ctypes.c_uint32)]),
     ("hibf_gpu_agent_level_work", None, [vp, vp, vp, vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]),
+    ("hibf_gpu_agent_set_host_read", None, [vp, ci]),
+    ("hibf_gpu_agent_last_in_place", None, [vp, ctypes.POINTER(ci)]),
     ("hibf_gpu_agent_input_chunks", None, [vp, ctypes.POINTER(ctypes.c_uint32)]),
     ("hibf_gpu_agent_last_timeline", None, [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
                                             ctypes.POINTER(ctypes.c_uint32)]),

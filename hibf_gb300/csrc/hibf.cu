@@ -458,6 +458,8 @@ struct hibf_gpu_agent
     std::vector<cudaEvent_t> ev_lvl;
     uint32_t last_levels{};
     bool force_queue{}; // set for the duration of a streamed host batch
+    bool host_read{true}; // host batches in mapped page-locked memory are read in place (hibf_gpu_agent_set_host_read)
+    bool last_in_place{}; // the last host batch was read in place
     // host-call staging
     dbuf in_values, in_qoff, in_thr;
     // streamed host batches: value chunks copied on copy_stream while the kernel answers the arrived ones
@@ -890,11 +892,25 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
         if (qoff[q + 1] < qoff[q])
             fail(HIBF_GPU_ERR_INVALID_ARG, "query offsets must be non-decreasing");
     uint64_t const nv = nq ? qoff[nq] : 0;
-    a->in_values.ensure(nv * 8);
+    // In place: values in mapped page-locked memory are read by the kernel over the host link as it needs them, so
+    // no copy precedes (or paces) the launch; only the offsets and thresholds are copied.
+    uint64_t const * in_place = nullptr;
+    if (a->host_read && !plain && nv)
+    {
+        cudaPointerAttributes attr{};
+        void * dev = nullptr;
+        if (cudaPointerGetAttributes(&attr, values) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+            cudaHostGetDevicePointer(&dev, const_cast<uint64_t *>(values), 0) == cudaSuccess)
+            in_place = static_cast<uint64_t const *>(dev);
+        cudaGetLastError(); // pageable memory: the queries above fail, and the values are copied
+    }
+    a->last_in_place = in_place != nullptr;
+    if (!in_place)
+        a->in_values.ensure(nv * 8);
     a->in_qoff.ensure((nq + 1) * 8);
     a->in_thr.ensure(std::max<uint64_t>(nq, 1) * 8);
     std::vector<uint64_t> qb;
-    if (!plain && !a->order && nv * 8 >= kStreamMinBytes)
+    if (!in_place && !plain && !a->order && nv * 8 >= kStreamMinBytes)
         qb = stream_chunks(qoff, nq);
     bool const streamed = qb.size() > 2;
     a->last_chunks = streamed ? static_cast<uint32_t>(qb.size() - 1) : 0u;
@@ -988,20 +1004,19 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
     }
     else
     {
-        if (nv)
+        if (nv && !in_place)
             HG_CUDA(cudaMemcpyAsync(a->in_values.p, values, nv * 8, cudaMemcpyHostToDevice, a->stream));
         HG_CUDA(cudaEventRecord(a->tl_chunk[0], a->stream));
         a->tl_n = 1;
     }
+    uint64_t const * const d_values = in_place ? in_place : a->in_values.as<uint64_t>();
     for (int attempt = 0;; ++attempt)
     {
         ensure_capacity(a, std::max<uint64_t>(nq, 1), tasks, results);
         if (plain)
-            launch_plain(a, mode, a->in_values.as<uint64_t>(), qoff, a->in_qoff.as<uint64_t>(),
-                         a->in_thr.as<uint64_t>(), nq, width);
+            launch_plain(a, mode, d_values, qoff, a->in_qoff.as<uint64_t>(), a->in_thr.as<uint64_t>(), nq, width);
         else
-            launch_batch(a, mode, a->in_values.as<uint64_t>(), a->in_qoff.as<uint64_t>(), a->in_thr.as<uint64_t>(),
-                         nq, width);
+            launch_batch(a, mode, d_values, a->in_qoff.as<uint64_t>(), a->in_thr.as<uint64_t>(), nq, width);
         if (streamed && attempt == 0)
             HG_CUDA(cudaStreamWaitEvent(a->stream, a->ev_copied, 0)); // later work on the stream follows the copies
         int const st = read_status(a);
@@ -2362,6 +2377,28 @@ extern "C"
                 HG_CUDA(cudaEventSynchronize(a->ev_lvl[a->last_levels - 1]));
                 for (uint32_t d = 0; d < std::min(cap, a->last_levels); ++d)
                     HG_CUDA(cudaEventElapsedTime(ms + d, d ? a->ev_lvl[d - 1] : a->ev_k0, a->ev_lvl[d]));
+            });
+    }
+
+    int hibf_gpu_agent_set_host_read(hibf_gpu_agent * a, int in_place)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                a->host_read = in_place != 0;
+            });
+    }
+
+    int hibf_gpu_agent_last_in_place(hibf_gpu_agent const * a, int * in_place)
+    {
+        return guarded(
+            [&]
+            {
+                if (!a || !in_place)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *in_place = a->last_in_place ? 1 : 0;
             });
     }
 

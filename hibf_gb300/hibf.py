@@ -296,6 +296,16 @@ class _agent_base:
         N.call("hibf_gpu_agent_level_ms", self._a, out, 16, ctypes.byref(n))
         return [float(out[i]) for i in range(min(n.value, 16))]
 
+    def set_host_read(self, in_place: bool) -> None:
+        """Host batches in mapped page-locked memory are read in place by the kernel (the default) or copied first."""
+        N.call("hibf_gpu_agent_set_host_read", self._a, int(in_place))
+
+    def last_in_place(self) -> bool:
+        """Whether the last host batch was read in place."""
+        v = ctypes.c_int(0)
+        N.call("hibf_gpu_agent_last_in_place", self._a, ctypes.byref(v))
+        return bool(v.value)
+
     def level_work(self) -> list[dict]:
         """Per level of the last batch under the level schedule: its tasks, value visits and executed value visits
         (root first); [] for the queue."""

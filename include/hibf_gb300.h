@@ -374,6 +374,15 @@ int hibf_gpu_agent_level_ms(hibf_gpu_agent * a, float * ms, uint32_t cap, uint32
  * for a batch run by the queue); at most `cap` entries of each array are written.  Synchronises the agent's stream. */
 int hibf_gpu_agent_level_work(hibf_gpu_agent * a, uint64_t * tasks, uint64_t * value_visits,
                               uint64_t * value_visits_executed, uint32_t cap, uint32_t * n);
+/* In place (on by default): host batches (hibf_gpu_agent_query_batch) whose values lie in mapped page-locked memory
+ * (cudaHostAlloc, cudaHostRegister) are not copied: the kernel reads the values over the host link as it needs them,
+ * and the batch runs its configured schedule from the first root.  in_place == 0 copies them first (a batch of 64 MiB
+ * or more is then streamed in chunks and runs the work queue).  Pageable values are always copied.  Results are the
+ * same either way; on the 8,192-bin batch (8.1 GB of values) in place took 50.3 ms per call, every call, where the
+ * copy's rate varied with the host link (47-344 ms). */
+int hibf_gpu_agent_set_host_read(hibf_gpu_agent * a, int in_place);
+/* Whether the agent's last host batch was read in place (1) or copied (0). */
+int hibf_gpu_agent_last_in_place(hibf_gpu_agent const * a, int * in_place);
 /* Number of chunks in which the agent's last host batch streamed its values (0: copied whole before the launch). */
 int hibf_gpu_agent_input_chunks(hibf_gpu_agent const * a, uint32_t * chunks);
 /* Timeline of the agent's last host batch (hibf_gpu_agent_query_batch), in ms from the call's first device work:

@@ -535,6 +535,39 @@ def test_level_schedule_streamed_host_batch(gpu_lib, oracle):
     assert len(t) == a.input_chunks() + 3 and t[-1] >= t[-2] >= t[-3]
 
 
+def test_host_batch_read_in_place(gpu_lib, oracle):
+    """A large host batch in page-locked memory is read in place by the kernel by default (no copy, the configured
+    schedule from the first root): the oracle's results, membership and counts; pageable values, or page-locked ones
+    with in-place reads switched off, are copied (streamed)."""
+    import torch
+
+    d = G.hibf_case("synth600")
+    H = _gpu_hibf(d)
+    vals, qo, thr = _long_batch(d, 24000, np.random.default_rng(31))
+    pinned = torch.from_numpy(vals.view(np.int64)).pin_memory().numpy().view(np.uint64)
+    O = oracle.hibf(G.tables(d))
+    o_off, o_ids = O.membership_batch(vals, qo, thr, threads=8)
+    for schedule in (N.SCHEDULE_LEVELS, N.SCHEDULE_QUEUE):
+        a = H.membership_agent()
+        a.tuning = dict(a.tuning, schedule=schedule)
+        offs, ids, _ = a.query_batch(pinned, qo, thr)  # in place is the default
+        assert a.last_in_place() and a.input_chunks() == 0
+        np.testing.assert_array_equal(offs, o_off)
+        np.testing.assert_array_equal(ids, o_ids)
+        c = H.counting_agent(2)
+        c.set_host_read(True)
+        c_off, c_ids, c_cnt = c.query_batch(pinned, qo, thr, mode=N.QUERY_COUNT, width=2)
+        np.testing.assert_array_equal(c_ids, o_ids)
+        assert c.last_in_place()
+        offs, ids, _ = a.query_batch(vals, qo, thr)  # pageable: copied
+        assert not a.last_in_place()
+        np.testing.assert_array_equal(ids, o_ids)
+        a.set_host_read(False)  # page-locked but copied first: streamed in chunks
+        offs, ids, _ = a.query_batch(pinned, qo, thr)
+        assert not a.last_in_place() and a.input_chunks() > 2
+        np.testing.assert_array_equal(ids, o_ids)
+
+
 def test_autotune_on_a_throughput_batch_tries_the_level_schedule(gpu_lib, oracle):
     """A batch above block_queries runs the persistent kernel, so the search times the level schedule too; whichever
     it keeps, the results are the oracle's."""
