@@ -112,9 +112,12 @@ __device__ __forceinline__ void load_row_words(uint64_t const * p, uint64_t (&w)
 // must then be even).  Each lane hashes U values per pass and keeps their H row offsets; the row words of
 // GS = 4 * UM masks per lane are loaded together, so GS * H * W loads per lane are in flight.  K planes count up to
 // 2^K - 1 masks between flushes.
+//
+// stage (optional): every value read is also stored at stage[i], so that later reads of the same values (the lower
+// levels of an in-place host batch) come from device memory instead of the host link.
 template <int LPV, int H, int K, bool ATOMIC, int UM = 1, int W = 1, bool EF = false>
 __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const * __restrict__ vals, uint64_t n,
-                                           uint32_t * counts, int lane)
+                                           uint32_t * counts, int lane, uint64_t * __restrict__ stage = nullptr)
 {
     constexpr int G = 32 / LPV;
     constexpr int U = UM * (LPV >= 4 ? 1 : 4 / LPV);
@@ -144,6 +147,8 @@ __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const
         {
             uint64_t const idx = base + static_cast<uint64_t>(u * 32 + lane);
             uint64_t const v = idx < n ? __ldcg(vals + idx) : 0u;
+            if (stage && idx < n)
+                stage[idx] = v;
 #pragma unroll
             for (int i = 0; i < H; ++i)
                 off[u][i] = hash_row(v, c_hash_seeds[i], rp.hash_shift, rp.bin_size) * rp.row_words;
@@ -223,11 +228,13 @@ __device__ __forceinline__ void warp_count(row_params const & rp, uint64_t const
 
 // Rows wider than a warp (bin_words > 32): lanes stride over the words, set bits are added one by one.
 __device__ __forceinline__ void warp_count_wide(row_params const & rp, uint64_t const * __restrict__ vals, uint64_t n,
-                                                uint32_t * counts, int lane)
+                                                uint32_t * counts, int lane, uint64_t * __restrict__ stage = nullptr)
 {
     for (uint64_t i = 0; i < n; ++i)
     {
         uint64_t const v = __ldcg(vals + i);
+        if (stage && lane == 0)
+            stage[i] = v;
         uint64_t off[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k)
@@ -253,39 +260,39 @@ __device__ __forceinline__ void warp_count_wide(row_params const & rp, uint64_t 
 
 template <int H, bool ATOMIC, bool EF = false>
 __device__ __forceinline__ void warp_count_lpv(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
-                                               uint64_t n, uint32_t * counts, int lane)
+                                               uint64_t n, uint32_t * counts, int lane, uint64_t * stage = nullptr)
 {
     switch (lpv_log2)
     {
     case 0:
-        warp_count<1, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
+        warp_count<1, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane, stage);
         break;
     case 1:
-        warp_count<2, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
+        warp_count<2, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane, stage);
         break;
     case 2:
-        warp_count<4, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
+        warp_count<4, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane, stage);
         break;
     case 3:
-        warp_count<8, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
+        warp_count<8, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane, stage);
         break;
     case 4:
-        warp_count<16, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
+        warp_count<16, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane, stage);
         break;
     default:
-        warp_count<32, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane);
+        warp_count<32, H, 7, ATOMIC, 1, 1, EF>(rp, vals, n, counts, lane, stage);
     }
 }
 
 // Dispatch on lanes-per-value for a compile-time hash function count (rows wider than a warp use the generic loop).
 template <int H, bool ATOMIC>
 __device__ __forceinline__ void warp_count_h(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
-                                             uint64_t n, uint32_t * counts, int lane)
+                                             uint64_t n, uint32_t * counts, int lane, uint64_t * stage = nullptr)
 {
     if (rp.bin_words > 32)
-        warp_count_wide(rp, vals, n, counts, lane);
+        warp_count_wide(rp, vals, n, counts, lane, stage);
     else
-        warp_count_lpv<H, ATOMIC>(rp, lpv_log2, vals, n, counts, lane);
+        warp_count_lpv<H, ATOMIC>(rp, lpv_log2, vals, n, counts, lane, stage);
 }
 
 // Dispatch on the node's hash function count and lanes-per-value (log2).  K = 7 planes: flush every 124 masks per

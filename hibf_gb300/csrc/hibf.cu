@@ -460,6 +460,11 @@ struct hibf_gpu_agent
     bool force_queue{}; // set for the duration of a streamed host batch
     bool host_read{true}; // host batches in mapped page-locked memory are read in place (hibf_gpu_agent_set_host_read)
     bool last_in_place{}; // the last host batch was read in place
+    // set for the duration of an in-place host batch: where its roots stage the values they read (device) and how
+    // many of each query's values they staged
+    uint64_t * stage_values{};
+    uint32_t * stage_counts{};
+    dbuf staged;
     // host-call staging
     dbuf in_values, in_qoff, in_thr;
     // streamed host batches: value chunks copied on copy_stream while the kernel answers the arrived ones
@@ -557,6 +562,8 @@ query_params base_params(hibf_gpu_agent * a, uint64_t const * d_values, uint64_t
     p.arrive_first = a->arrive ? a->arrive_first.as<uint64_t>() : nullptr;
     p.arrive_chunks = a->arrive_chunks;
     p.arrive_limit_ns = a->arrive_limit_ns;
+    p.stage = nullptr;
+    p.staged = nullptr;
     return p;
 }
 
@@ -655,6 +662,9 @@ void launch_batch(hibf_gpu_agent * a, int mode, uint64_t const * d_values, uint6
         HG_CUDA(cudaEventRecordWithFlags(a->ev_k0, s, rec_flags));
         if (levels)
         {
+            // an in-place host batch: the roots stage the values they read, the lower levels read them from there
+            p.stage = a->stage_values;
+            p.staged = a->stage_counts;
             // one launch per level: the roots, then each level's appended tasks grouped by IBF
             uint64_t const stats_bytes = (h->max_depth + 1) * kStats * 8;
             if (!a->lvl_tasks.p || a->lvl_tasks.bytes < a->cap_tasks * 8 || !a->lvl_hist.p ||
@@ -905,8 +915,23 @@ void host_batch(hibf_gpu_agent * a, int mode, uint64_t const * values, uint64_t 
         cudaGetLastError(); // pageable memory: the queries above fail, and the values are copied
     }
     a->last_in_place = in_place != nullptr;
-    if (!in_place)
-        a->in_values.ensure(nv * 8);
+    a->in_values.ensure(nv * 8); // the copy's destination, or where an in-place batch's roots stage the values
+    if (in_place)
+        a->staged.ensure(std::max<uint64_t>(nq, 1) * 4);
+    struct stage_reset
+    {
+        hibf_gpu_agent * a;
+        ~stage_reset()
+        {
+            a->stage_values = nullptr;
+            a->stage_counts = nullptr;
+        }
+    } const stage_guard{a};
+    if (in_place)
+    {
+        a->stage_values = a->in_values.as<uint64_t>();
+        a->stage_counts = a->staged.as<uint32_t>();
+    }
     a->in_qoff.ensure((nq + 1) * 8);
     a->in_thr.ensure(std::max<uint64_t>(nq, 1) * 8);
     std::vector<uint64_t> qb;

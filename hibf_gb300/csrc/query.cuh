@@ -129,6 +129,11 @@ struct query_params
     uint32_t level;
     unsigned long long const * in_tasks;
     unsigned long long const * in_count;
+    // in-place host batches under the level schedule: `values` is the host's memory; root tasks store every value
+    // they read at stage[same position] and how many they read (from the query's first value) at staged[query], and
+    // the lower levels read that prefix from stage and only the rest from the host.  Null otherwise.
+    uint64_t * stage;
+    uint32_t * staged;
 };
 
 using query_kernel_t = void (*)(query_params);
@@ -347,29 +352,29 @@ __device__ inline int segment_state(query_params const & p, dev_node const & nd,
 // host offers them only for such hierarchies, and process_task refuses wider rows).
 template <int H, int V>
 __device__ __forceinline__ void count_variant(row_params const & rp, uint32_t lpv_log2, uint64_t const * vals,
-                                              uint64_t n, uint32_t * counts, int lane)
+                                              uint64_t n, uint32_t * counts, int lane, uint64_t * stage)
 {
     using Q = qvariant<V>;
     switch (lpv_log2)
     {
     case 0:
-        warp_count<1, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane);
+        warp_count<1, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane, stage);
         break;
     case 1:
         if constexpr (Q::W == 2)
-            warp_count<1, H, Q::K, false, Q::UM, 2>(rp, vals, n, counts, lane);
+            warp_count<1, H, Q::K, false, Q::UM, 2>(rp, vals, n, counts, lane, stage);
         else
-            warp_count<2, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane);
+            warp_count<2, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane, stage);
         break;
     case 2:
         if constexpr (Q::W == 2)
-            warp_count<2, H, Q::K, false, Q::UM, 2>(rp, vals, n, counts, lane);
+            warp_count<2, H, Q::K, false, Q::UM, 2>(rp, vals, n, counts, lane, stage);
         else
-            warp_count<4, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane);
+            warp_count<4, H, Q::K, false, Q::UM, 1>(rp, vals, n, counts, lane, stage);
         break;
     default:
         if constexpr (V == 0)
-            warp_count_h<H, false>(rp, lpv_log2, vals, n, counts, lane);
+            warp_count_h<H, false>(rp, lpv_log2, vals, n, counts, lane, stage);
     }
 }
 
@@ -528,6 +533,10 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
     // of the counting code for the stages and the rest: each call site inlines every row width's counting path, and a
     // hierarchy of mixed widths runs them all at once, so a second copy would double the instruction footprint.
     uint64_t done = 0;
+    // in-place host batch under the level schedule: a root stages what it reads; a lower level reads the staged prefix
+    // [0, staged) from device memory and the rest from the host
+    bool const stage_root = p.stage && depth == 0;
+    uint64_t const staged = p.stage && depth > 0 ? p.staged[q] : 0u;
     bool const adaptive = p.ee_stages == kEarlyExitAdaptive && n >= p.ee_min;
     unsigned int next = kNever;
     int state = segment_state(p, nd, counts, n, thr, lane, adaptive ? &next : nullptr);
@@ -556,8 +565,15 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
                 }
             }
         }
-        count_variant<H, V>(rp, nd.lpv_log2, p.values + b0 + done, stop - done, counts, lane);
-        done = stop;
+        // one call site: [done, stop) in at most two pieces, the staged prefix first
+        while (done < stop)
+        {
+            bool const from_stage = done < staged;
+            uint64_t const end = from_stage ? min(stop, staged) : stop;
+            count_variant<H, V>(rp, nd.lpv_log2, (from_stage ? p.stage : p.values) + b0 + done, end - done, counts,
+                                lane, stage_root ? p.stage + b0 + done : nullptr);
+            done = end;
+        }
         if (done < n)
         {
             __syncwarp();
@@ -565,6 +581,8 @@ __device__ void process_task(query_params const & p, unsigned long long task, ui
         }
     }
     __syncwarp();
+    if (stage_root && lane == 0)
+        p.staged[q] = static_cast<uint32_t>(done); // read by the next level's launch
     if (state == kHopeless)
     {
         if (lane == 0)
@@ -892,7 +910,7 @@ __global__ void __launch_bounds__(256, HIBF_QUERY_MIN_BLOCKS) k_query_blk(query_
         uint64_t const lo = min(n, static_cast<uint64_t>(warp) * per);
         uint64_t const hi = min(n, lo + per);
         if (hi > lo)
-            count_variant<H, 0>(rp, nd.lpv_log2, p.values + b0 + lo, hi - lo, counts, lane);
+            count_variant<H, 0>(rp, nd.lpv_log2, p.values + b0 + lo, hi - lo, counts, lane, nullptr);
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < ncount; i += blockDim.x)
         {
@@ -945,7 +963,7 @@ __global__ void __launch_bounds__(256) k_query_features(query_params p, uint32_t
             counts[i] = 0;
         __syncwarp();
         if (m)
-            count_variant<H, 0>(rp, nd.lpv_log2, p.values + b0, m, counts, lane);
+            count_variant<H, 0>(rp, nd.lpv_log2, p.values + b0, m, counts, lane, nullptr);
         __syncwarp();
         double const rate = n ? static_cast<double>(p.thr[q]) / static_cast<double>(n) : 0.0;
         unsigned long long const need = static_cast<unsigned long long>(ceil(rate * static_cast<double>(m)));
