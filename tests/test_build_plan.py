@@ -96,6 +96,15 @@ def _ub_values(d):
     return [S.user_bin_values(seed, d["ub_offsets"], u) for u in range(d["n_ub"])]
 
 
+def test_bin_size_in_bits_known_answers():
+    """include/hibf/build/bin_size_in_bits.hpp through the IBF sizing (test/unit/hibf/build/bin_size_in_bits_test.cpp
+    :11-19): 1,000 elements at fpr 0.05 with two hash functions take 7,903 bits; user bins without elements, 0."""
+    cfg = B.config(input_fn=lambda ub, it: None, number_of_user_bins=3, number_of_hash_functions=2, maximum_fpr=0.05)
+    assert B.ibf_plan(cfg, max_bin_elements=1000)[0] == 7903
+    cfg = B.config(input_fn=lambda ub, it: None, number_of_user_bins=3, number_of_hash_functions=1, maximum_fpr=0.05)
+    assert B.ibf_plan(cfg)[0] == 0  # every user bin empty: the largest holds no element
+
+
 @pytest.mark.parametrize("name", ["snippet", "readme", "three_level", "uneven", "similar", "same", "synth64",
                                   "synth600", "synth_t128", "synth_t256", "dups", "synth_h1", "synth_h4",
                                   "synth_h5", "empty_bins", "relaxed_fpr", "synth_t512"])
