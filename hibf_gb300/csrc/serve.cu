@@ -616,7 +616,10 @@ extern "C"
                         if (r->nv && b >= hr.begin && e <= hr.end)
                         {
                             r->pinned = true;
-                            r->dev_values = hr.dev ? hr.dev + (b - hr.begin) / 8 : nullptr;
+                            r->dev_values =
+                                hr.dev ? reinterpret_cast<uint64_t const *>(reinterpret_cast<char const *>(hr.dev) +
+                                                                            (b - hr.begin))
+                                       : nullptr;
                         }
                 }
                 r->t_arrival = arrival_s >= 0 ? arrival_s : now_s();
