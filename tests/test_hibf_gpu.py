@@ -458,8 +458,9 @@ def test_streamed_host_batch_with_empty_queries_and_zero_thresholds(gpu_lib):
 @pytest.mark.parametrize("name", G.HIBF_CASES)
 def test_level_schedule_gives_the_reference_results(gpu_lib, name):
     """HIBF_GPU_SCHEDULE_LEVELS (one launch per level, each level's tasks grouped by IBF): membership lists and
-    counts equal the reference's with the adaptive early exit and without one, in a permuted claim order, and from
-    a graph-captured batch replayed twice."""
+    counts equal the reference's with the adaptive early exit and without one, read in place from page-locked host
+    memory (roots staging the values for the lower levels), in a permuted claim order, and from a graph-captured batch
+    replayed twice."""
     import torch
 
     d = G.hibf_case(name)
@@ -496,6 +497,19 @@ def test_level_schedule_gives_the_reference_results(gpu_lib, name):
         np.testing.assert_array_equal(dense, d[f"count{w}"], err_msg=str(ee))
     if nq == 0:
         return
+    # the same batch read in place from page-locked memory (the roots stage the values for the lower levels)
+    if qv.size:
+        a.tuning = dict(a.tuning, early_exit_stages=N.EARLY_EXIT_ADAPTIVE, level_values_per_lane=0)
+        pinned = torch.from_numpy(qv.view(np.int64)).pin_memory().numpy().view(np.uint64)
+        offs, ids, _ = a.query_batch(pinned, qo, d["mem_t"])
+        assert a.last_in_place()
+        for i, (g, e) in enumerate(zip(_split(offs, ids), exp)):
+            np.testing.assert_array_equal(g, e, err_msg=f"in place query {i}")
+        offs, ids, cnts = a.query_batch(pinned, qo, d["cnt_t"], mode=N.QUERY_COUNT, width=w)
+        dense = np.zeros_like(d[f"count{w}"])
+        for i in range(nq):
+            dense[i, ids[offs[i]:offs[i + 1]].astype(np.int64)] = cnts[offs[i]:offs[i + 1]]
+        np.testing.assert_array_equal(dense, d[f"count{w}"], err_msg="in place counts")
     dv = torch.from_numpy(qv.view(np.int64)).cuda() if qv.size else torch.zeros(1, dtype=torch.int64, device="cuda")
     dq = torch.from_numpy(qo.view(np.int64)).cuda()
     dt = torch.from_numpy(d["mem_t"].astype(np.uint64).view(np.int64)).cuda()
