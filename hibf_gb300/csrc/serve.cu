@@ -504,8 +504,8 @@ extern "C"
             {
                 if (!S || !ptr || bytes == 0)
                     fail(HIBF_GPU_ERR_INVALID_ARG, "bad argument");
-                if (!already_pinned)
-                    HG_CUDA(cudaHostRegister(const_cast<void *>(ptr), bytes, cudaHostRegisterDefault));
+                if (!already_pinned) // mapped, so that zero-copy batches can read the range in place
+                    HG_CUDA(cudaHostRegister(const_cast<void *>(ptr), bytes, cudaHostRegisterMapped));
                 try
                 {
                     warm_host_range(ptr, bytes);

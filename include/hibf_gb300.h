@@ -521,8 +521,9 @@ int hibf_gpu_server_destroy(hibf_gpu_server * s);
 int hibf_gpu_server_submit(hibf_gpu_server * s, uint64_t const * values, uint64_t const * query_offsets,
                            uint64_t n_queries, uint64_t const * thresholds, double arrival_s, int copy, uint64_t * id);
 /* Registers [ptr, ptr + bytes) as page-locked request memory: borrowed requests whose values lie inside a registered
- * range are copied to the device directly (no staging).  already_pinned == 0: the server page-locks the range
- * (cudaHostRegister) and unlocks it on unregister or destroy; != 0: the caller allocated it page-locked.  The device
+ * range are read in place or copied to the device directly (no staging).  already_pinned == 0: the server page-locks
+ * and maps the range (cudaHostRegister, mapped) and unlocks it on unregister or destroy; != 0: the caller allocated it
+ * page-locked.  The device
  * reads the range once on registration (synchronous): a page-locked page's first device read is several times slower
  * than later ones, so requests from a registered range start warm. */
 int hibf_gpu_server_register_host(hibf_gpu_server * s, void const * ptr, uint64_t bytes, int already_pinned);

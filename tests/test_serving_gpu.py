@@ -147,8 +147,8 @@ def test_pinned_borrowed_requests_match(gpu_lib):
 
 def test_zero_copy_batches_match(gpu_lib):
     """Back-to-back borrowed requests in one mapped page-locked range are answered without copying their values (the
-    kernel reads them in place); the same requests with zero copy off are copied first.  Every result equals the
-    query answered alone, both ways."""
+    kernel reads them in place), in memory the caller page-locked and in pageable memory the server page-locks on
+    registration; with zero copy off they are copied first.  Every result equals the query answered alone."""
     import torch
 
     H, d = _hibf()
@@ -167,11 +167,13 @@ def test_zero_copy_batches_match(gpu_lib):
         thr = np.array([int(np.ceil(0.6 * q.size)) for q in qs[k0:k1]], np.uint64)
         reqs.append((k0, k1, qo, thr))
         k0 = k1
-    for zc in (True, False):
+    pageable = np.concatenate(qs).astype(np.uint64)  # page-locked by the server on registration
+    for zc, base, pinned in ((True, pool.data_ptr(), True), (False, pool.data_ptr(), True),
+                             (True, pageable.ctypes.data, False)):
         srv = server(H, slots=2, max_batch_queries=4096, max_batch_values=1 << 22, admission_bytes=1 << 30)
         srv.set_zero_copy(zc)
-        srv.register_host(pool.data_ptr(), pool.numel() * 8, already_pinned=True)
-        ids = [srv.submit_borrowed(pool.data_ptr() + 8 * int(starts[a]), qo, thr) for a, b, qo, thr in reqs]
+        srv.register_host(base, starts[-1] * 8, already_pinned=pinned)
+        ids = [srv.submit_borrowed(base + 8 * int(starts[a]), qo, thr) for a, b, qo, thr in reqs]
         for rid, (a, b, qo, thr) in zip(ids, reqs):
             st, offs, res, _ = srv.wait_result(rid, qo.size - 1)
             assert st == 0
@@ -181,6 +183,8 @@ def test_zero_copy_batches_match(gpu_lib):
         log = srv.batch_log()
         assert int(log[:, 10].sum()) == 0
         assert (log[:, 11].sum() > 0) == zc
+        if not pinned:
+            srv.unregister_host(base)
         srv.close()
 
 
