@@ -456,6 +456,28 @@ def test_streamed_host_batch_with_empty_queries_and_zero_thresholds(gpu_lib):
 
 
 @pytest.mark.parametrize("name", G.HIBF_CASES)
+def test_implied_visits_equal_the_oracles(gpu_lib, oracle, name):
+    """The work the roofline counts: the (query, IBF) tasks and value visits the reference's traversal implies, as the
+    kernel reports them (hibf_gpu_agent_last_work), equal the oracle's walk of the same queries (every IBF it counts,
+    times the query's length), under the work queue and the level schedule."""
+    d = G.hibf_case(name)
+    qv, qo = d["q_values"], d["q_offsets"]
+    nq = qo.size - 1
+    if nq == 0:
+        return
+    O = oracle.hibf(G.tables(d))
+    walks = O.query_batch(qv, qo, d["mem_t"], d["cnt_t"], threads=4)["visits"].astype(np.int64)
+    lengths = np.diff(qo).astype(np.int64)
+    H = _gpu_hibf(d)
+    a = H.membership_agent()
+    for schedule in (N.SCHEDULE_QUEUE, N.SCHEDULE_LEVELS):
+        a.tuning = dict(a.tuning, block_queries=0, schedule=schedule)
+        a.query_batch(qv, qo, d["mem_t"])
+        tasks, visits = a.last_work()
+        assert tasks == int(walks.sum()) and visits == int((walks * lengths).sum()), schedule
+
+
+@pytest.mark.parametrize("name", G.HIBF_CASES)
 def test_level_schedule_gives_the_reference_results(gpu_lib, name):
     """HIBF_GPU_SCHEDULE_LEVELS (one launch per level, each level's tasks grouped by IBF): membership lists and
     counts equal the reference's with the adaptive early exit and without one, read in place from page-locked host
