@@ -33,11 +33,11 @@ void set_last_error(std::string msg)
 // ---------------------------------------------------------------------------------------------------------------
 
 // emplace (src/interleaved_bloom_filter.cpp:119-140).  One thread per value; atomicOr makes concurrent inserts
-// order-independent.  With occupancy tracking, a value counts for its bin when one of its bits was newly set.
+// order-independent.  The old words are not needed (an IBF that tracks occupancy inserts through emplace_exact), so
+// the atomics return nothing and a warp never waits on them.
 __global__ void k_emplace(uint64_t * __restrict__ words, uint64_t bin_size, uint32_t row_words, uint32_t shift,
                           uint32_t h, uint64_t const * __restrict__ values, uint64_t const * __restrict__ bins,
-                          uint64_t n, uint64_t bin, uint64_t n_bins, unsigned long long * occupancy,
-                          int * bad_bin)
+                          uint64_t n, uint64_t bin, uint64_t n_bins, int * bad_bin)
 {
     uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
     for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
@@ -51,24 +51,20 @@ __global__ void k_emplace(uint64_t * __restrict__ words, uint64_t bin_size, uint
         }
         uint64_t const bit = 1ull << (b & 63u);
         uint64_t const wofs = b >> 6;
-        bool exists = true;
         for (uint32_t k = 0; k < h; ++k)
         {
             uint64_t const r = hash_row(v, c_hash_seeds[k], shift, bin_size);
-            unsigned long long * w = reinterpret_cast<unsigned long long *>(words + r * row_words + wofs);
-            unsigned long long const old = atomicOr(w, static_cast<unsigned long long>(bit));
-            exists = exists && (old & bit);
+            atomicOr(reinterpret_cast<unsigned long long *>(words + r * row_words + wofs),
+                     static_cast<unsigned long long>(bit));
         }
-        if (occupancy && !exists)
-            atomicAdd(occupancy + b, 1ull);
     }
 }
 
 // emplace of the synthetic single-level workload: value i of the launch is hg_ibf_bin_value of bin
-// first_bin + i / vpb, generated in place instead of read (same bits as k_emplace with those values).
+// first_bin + i / vpb, generated in place instead of read (same bits as k_emplace with those values; the atomics
+// return nothing).
 __global__ void k_synth_emplace(uint64_t * __restrict__ words, uint64_t bin_size, uint32_t row_words, uint32_t shift,
-                                uint32_t h, uint64_t seed, uint64_t vpb, uint64_t first_bin, uint64_t n,
-                                unsigned long long * occupancy)
+                                uint32_t h, uint64_t seed, uint64_t vpb, uint64_t first_bin, uint64_t n)
 {
     uint64_t const stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
     for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
@@ -77,16 +73,12 @@ __global__ void k_synth_emplace(uint64_t * __restrict__ words, uint64_t bin_size
         uint64_t const v = hg_ibf_bin_value(seed, vpb, b, i % vpb);
         uint64_t const bit = 1ull << (b & 63u);
         uint64_t const wofs = b >> 6;
-        bool exists = true;
         for (uint32_t k = 0; k < h; ++k)
         {
             uint64_t const r = hash_row(v, c_hash_seeds[k], shift, bin_size);
-            unsigned long long * w = reinterpret_cast<unsigned long long *>(words + r * row_words + wofs);
-            unsigned long long const old = atomicOr(w, static_cast<unsigned long long>(bit));
-            exists = exists && (old & bit);
+            atomicOr(reinterpret_cast<unsigned long long *>(words + r * row_words + wofs),
+                     static_cast<unsigned long long>(bit));
         }
-        if (occupancy && !exists)
-            atomicAdd(occupancy + b, 1ull);
     }
 }
 
@@ -539,8 +531,7 @@ void emplace_exact(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t const *
         HG_CUDA(cudaGetLastError());
         k_emplace<<<grid_for(c, block), block, 0, s>>>(f->store.as<uint64_t>(), f->bin_size,
                                                        static_cast<uint32_t>(f->row_words), f->shift, h, vals,
-                                                       SYNTH ? nullptr : bins, c, bin, f->bins, nullptr,
-                                                       f->flag.as<int>());
+                                                       SYNTH ? nullptr : bins, c, bin, f->bins, f->flag.as<int>());
         HG_CUDA(cudaGetLastError());
     }
     HG_CUDA(cudaStreamSynchronize(s)); // the scratch buffers are freed on return
@@ -560,7 +551,7 @@ void launch_emplace(hibf_gpu_ibf * f, uint64_t const * d_values, uint64_t const 
     k_emplace<<<grid_for(n, block), block, 0, s>>>(f->store.as<uint64_t>(), f->bin_size,
                                                    static_cast<uint32_t>(f->row_words), f->shift,
                                                    static_cast<uint32_t>(f->hash_funs), d_values, d_bins, n, bin,
-                                                   f->bins, nullptr, f->flag.as<int>());
+                                                   f->bins, f->flag.as<int>());
     HG_CUDA(cudaGetLastError());
 }
 
@@ -821,8 +812,7 @@ extern "C"
                 unsigned const block = 256;
                 k_synth_emplace<<<grid_for(n, block), block, 0, pick(f, stream)>>>(
                     f->store.as<uint64_t>(), f->bin_size, static_cast<uint32_t>(f->row_words), f->shift,
-                    static_cast<uint32_t>(f->hash_funs), seed, values_per_bin, first_bin, n,
-                    f->track_occupancy ? f->occupancy.as<unsigned long long>() : nullptr);
+                    static_cast<uint32_t>(f->hash_funs), seed, values_per_bin, first_bin, n);
                 HG_CUDA(cudaGetLastError());
             });
     }
