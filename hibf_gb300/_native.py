@@ -121,6 +121,7 @@ _SIGS = [
     ("hibf_gpu_ibf_upload_words", None, [vp, vp, u64]),
     ("hibf_gpu_ibf_download_words", None, [vp, vp, u64]),
     ("hibf_gpu_ibf_download_occupancy", None, [vp, vp, u64]),
+    ("hibf_gpu_ibf_track_occupancy", None, [vp, vp]),
     ("hibf_gpu_ibf_status", None, [vp]),
     ("hibf_gpu_hibf_create", None, [u64, u64, vp, vp, vp, vp, vp, ctypes.POINTER(vp)]),
     ("hibf_gpu_hibf_destroy", None, [vp]),

@@ -1160,6 +1160,17 @@ extern "C"
             });
     }
 
+    int hibf_gpu_ibf_track_occupancy(hibf_gpu_ibf const * f, int * out)
+    {
+        return guarded(
+            [&]
+            {
+                if (!f || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                *out = f->track_occupancy ? 1 : 0;
+            });
+    }
+
     int hibf_gpu_ibf_status(hibf_gpu_ibf * f)
     {
         if (!f)

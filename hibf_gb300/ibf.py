@@ -166,6 +166,12 @@ class interleaved_bloom_filter:
         N.call("hibf_gpu_ibf_upload_words", self._h, w.ctypes.data, w.size)
 
     @property
+    def track_occupancy(self) -> bool:
+        v = ctypes.c_int(0)
+        N.call("hibf_gpu_ibf_track_occupancy", self._h, ctypes.byref(v))
+        return bool(v.value)
+
+    @property
     def occupancy(self) -> np.ndarray:
         self.flush()
         out = np.zeros(self.bin_words * 64, np.uint64)

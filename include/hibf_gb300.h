@@ -124,6 +124,8 @@ int hibf_gpu_ibf_upload_words(hibf_gpu_ibf * ibf, uint64_t const * words, uint64
 int hibf_gpu_ibf_download_words(hibf_gpu_ibf * ibf, uint64_t * words, uint64_t n_words);
 /* occupancy vector (interleaved_bloom_filter.hpp:433-437): technical_bins counters. */
 int hibf_gpu_ibf_download_occupancy(hibf_gpu_ibf * ibf, uint64_t * out, uint64_t n);
+/* track_occupancy (interleaved_bloom_filter.hpp:457-458): 1 when emplace counts newly set bits, else 0. */
+int hibf_gpu_ibf_track_occupancy(hibf_gpu_ibf const * ibf, int * out);
 /* Status of the last asynchronous (_d) call on this filter. */
 int hibf_gpu_ibf_status(hibf_gpu_ibf * ibf);
 

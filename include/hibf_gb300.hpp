@@ -112,20 +112,97 @@ private:
     uint64_t bits_{};
 };
 
+// What config::input_fn receives: `it = value` inserts one value (insert_iterator.hpp:24-111).
+class insert_iterator
+{
+public:
+    explicit insert_iterator(hibf_gpu_sink * sink) : sink_{sink}
+    {}
+    insert_iterator & operator=(uint64_t value)
+    {
+        check(hibf_gpu_sink_push(sink_, &value, 1));
+        return *this;
+    }
+    insert_iterator & operator*()
+    {
+        return *this;
+    }
+    insert_iterator & operator++()
+    {
+        return *this;
+    }
+    insert_iterator & operator++(int)
+    {
+        return *this;
+    }
+    // Many values in one call.
+    void push(std::vector<uint64_t> const & values)
+    {
+        check(hibf_gpu_sink_push(sink_, values.data(), values.size()));
+    }
+
+private:
+    hibf_gpu_sink * sink_;
+};
+
+// The fields of seqan::hibf::config the device build uses (config.hpp:75-413).
+struct config
+{
+    std::function<void(size_t const, insert_iterator &&)> input_fn;
+    size_t number_of_user_bins{};
+    size_t number_of_hash_functions{2};
+    double maximum_fpr{0.05};
+    double relaxed_fpr{0.3};
+    size_t threads{1};
+    uint8_t sketch_bits{12};     // picks the largest user bin for interleaved_bloom_filter(config&)
+    bool track_occupancy{false}; // interleaved_bloom_filter(config&) only
+};
+
+namespace detail
+{
+// config::input_fn behind the C ABI's callback: the sink is the insert_iterator's target.
+inline void input_trampoline(void * user, uint64_t user_bin, hibf_gpu_sink * sink)
+{
+    auto & c = *static_cast<config *>(user);
+    c.input_fn(static_cast<size_t>(user_bin), insert_iterator{sink});
+}
+} // namespace detail
+
 class interleaved_bloom_filter
 {
 public:
     interleaved_bloom_filter(hibf_gb300::bin_count bins, hibf_gb300::bin_size size,
                              hibf_gb300::hash_function_count funs = {2},
-                             bool track_occupancy = false)
+                             bool track_occupancy_ = false)
     {
-        check(hibf_gpu_ibf_create(bins.value, size.value, funs.value, track_occupancy ? 1 : 0, &f_));
+        check(hibf_gpu_ibf_create(bins.value, size.value, funs.value, track_occupancy_ ? 1 : 0, &f_));
+        adopt();
+    }
+    // interleaved_bloom_filter(config&, size_t max_bin_elements) (interleaved_bloom_filter.hpp:241,
+    // src/interleaved_bloom_filter.cpp:81-117): one technical bin per user bin, the bin size from the exact distinct
+    // count of the largest user bin (picked by its HyperLogLog sketch unless max_bin_elements is given), then every
+    // user bin's values inserted on the device.
+    explicit interleaved_bloom_filter(config & configuration, size_t max_bin_elements = 0)
+    {
+        if (!configuration.input_fn)
+            throw std::invalid_argument{"[HIBF CONFIG ERROR] You did not set the required config::input_fn."};
+        hibf_gpu_build_config c{configuration.number_of_user_bins, configuration.number_of_hash_functions,
+                                configuration.maximum_fpr, configuration.relaxed_fpr, configuration.threads, 0};
+        check(hibf_gpu_ibf_build(&c, max_bin_elements, configuration.sketch_bits,
+                                 configuration.track_occupancy ? 1 : 0, &detail::input_trampoline, &configuration,
+                                 &f_));
+        adopt();
     }
     explicit interleaved_bloom_filter(hibf_gpu_ibf * adopted) : f_{adopted}
-    {}
+    {
+        adopt();
+    }
     interleaved_bloom_filter(interleaved_bloom_filter const &) = delete;
     interleaved_bloom_filter & operator=(interleaved_bloom_filter const &) = delete;
-    interleaved_bloom_filter(interleaved_bloom_filter && o) noexcept : f_{std::exchange(o.f_, nullptr)}
+    interleaved_bloom_filter(interleaved_bloom_filter && o) noexcept :
+        occupancy{std::move(o.occupancy)},
+        track_occupancy{o.track_occupancy},
+        f_{std::exchange(o.f_, nullptr)}
     {}
     ~interleaved_bloom_filter()
     {
@@ -133,9 +210,16 @@ public:
             hibf_gpu_ibf_destroy(f_);
     }
 
+    // The reference's public members (interleaved_bloom_filter.hpp:451-458): one counter per technical bin, non-zero
+    // only when the filter tracks occupancy.  This is a host copy of the device's counters, brought up to date by
+    // every modifier called through this object.
+    std::vector<size_t> occupancy{};
+    bool track_occupancy{false};
+
     void emplace(uint64_t value, bin_index bin)
     {
         check(hibf_gpu_ibf_emplace(f_, &value, 1, bin.value));
+        refresh_occupancy();
     }
     // Many values into one bin in one device call (the insert_iterator loop of the reference, batched).
     template <std::ranges::input_range values_t>
@@ -143,10 +227,12 @@ public:
     {
         auto const v = detail::to_vector(values);
         check(hibf_gpu_ibf_emplace(f_, v.data(), v.size(), bin.value));
+        refresh_occupancy();
     }
     void clear(bin_index bin)
     {
         check(hibf_gpu_ibf_clear(f_, bin.value));
+        refresh_occupancy();
     }
     template <std::ranges::forward_range bins_t>
         requires std::same_as<std::ranges::range_value_t<bins_t>, bin_index>
@@ -156,6 +242,7 @@ public:
         for (bin_index x : bins)
             b.push_back(x.value);
         check(hibf_gpu_ibf_clear_range(f_, b.data(), b.size()));
+        refresh_occupancy();
     }
     bool try_increase_bin_number_to(hibf_gb300::bin_count new_bins)
     {
@@ -166,6 +253,7 @@ public:
     void increase_bin_number_to(hibf_gb300::bin_count new_bins)
     {
         check(hibf_gpu_ibf_increase_bin_number_to(f_, new_bins.value));
+        load_occupancy(); // technical_bins may have grown
     }
 
     uint64_t bin_count() const
@@ -244,6 +332,9 @@ public:
             result_.resize(n);
             return result_;
         }
+        // Has no effect, as in the reference (interleaved_bloom_filter.hpp:712-720): the ids are already ascending.
+        void sort_results()
+        {}
 
     private:
         interleaved_bloom_filter const * ibf_;
@@ -279,58 +370,62 @@ public:
         return f_;
     }
 
+    // Equal shape, bits, occupancy and tracking flag (the reference's defaulted operator==,
+    // interleaved_bloom_filter.hpp:433).  The bit stores are compared through host copies.
+    bool operator==(interleaved_bloom_filter const & other) const
+    {
+        auto const a = info(), b = other.info();
+        if (a[0] != b[0] || a[1] != b[1] || a[2] != b[2] || track_occupancy != other.track_occupancy ||
+            occupancy != other.occupancy)
+            return false;
+        return words() == other.words();
+    }
+
 private:
+    std::vector<uint64_t> words() const
+    {
+        auto const i = info();
+        std::vector<uint64_t> w((i[0] + 63) / 64 * i[1]);
+        check(hibf_gpu_ibf_download_words(f_, w.data(), w.size()));
+        return w;
+    }
     std::vector<uint64_t> info() const
     {
         std::vector<uint64_t> out(5);
         check(hibf_gpu_ibf_info(f_, out.data()));
         return out;
     }
+    // Takes the new handle's occupancy; on failure releases the handle, since no destructor will run.
+    void adopt()
+    {
+        try
+        {
+            load_occupancy();
+        }
+        catch (...)
+        {
+            hibf_gpu_ibf_destroy(std::exchange(f_, nullptr));
+            throw;
+        }
+    }
+    // Sizes occupancy to the technical bins and reads the tracking flag and the counters.
+    void load_occupancy()
+    {
+        int tracks = 0;
+        check(hibf_gpu_ibf_track_occupancy(f_, &tracks));
+        track_occupancy = tracks != 0;
+        auto const i = info();
+        occupancy.assign(i[3] / i[1], 0u); // bit size / bin size = technical bins
+        refresh_occupancy();
+    }
+    void refresh_occupancy()
+    {
+        if (!track_occupancy)
+            return;
+        static_assert(sizeof(size_t) == sizeof(uint64_t));
+        check(hibf_gpu_ibf_download_occupancy(f_, reinterpret_cast<uint64_t *>(occupancy.data()), occupancy.size()));
+    }
     hibf_gpu_ibf * f_{};
-};
-
-// What config::input_fn receives: `it = value` inserts one value (insert_iterator.hpp:24-111).
-class insert_iterator
-{
-public:
-    explicit insert_iterator(hibf_gpu_sink * sink) : sink_{sink}
-    {}
-    insert_iterator & operator=(uint64_t value)
-    {
-        check(hibf_gpu_sink_push(sink_, &value, 1));
-        return *this;
-    }
-    insert_iterator & operator*()
-    {
-        return *this;
-    }
-    insert_iterator & operator++()
-    {
-        return *this;
-    }
-    insert_iterator & operator++(int)
-    {
-        return *this;
-    }
-    // Many values in one call.
-    void push(std::vector<uint64_t> const & values)
-    {
-        check(hibf_gpu_sink_push(sink_, values.data(), values.size()));
-    }
-
-private:
-    hibf_gpu_sink * sink_;
-};
-
-// The fields of seqan::hibf::config the device build uses (config.hpp:75-413).
-struct config
-{
-    std::function<void(size_t const, insert_iterator &&)> input_fn;
-    size_t number_of_user_bins{};
-    size_t number_of_hash_functions{2};
-    double maximum_fpr{0.05};
-    double relaxed_fpr{0.3};
-    size_t threads{1};
 };
 
 // The read side of the reference's concurrent_timer (include/hibf/misc/timer.hpp): a build phase's seconds, its
@@ -372,7 +467,7 @@ public:
             throw std::invalid_argument{"[HIBF CONFIG ERROR] You did not set the required config::input_fn."};
         hibf_gpu_build_config c{configuration.number_of_user_bins, configuration.number_of_hash_functions,
                                 configuration.maximum_fpr, configuration.relaxed_fpr, configuration.threads, 0};
-        check(hibf_gpu_hibf_build(&c, layout_text.c_str(), &trampoline, &configuration, &h_));
+        check(hibf_gpu_hibf_build(&c, layout_text.c_str(), &detail::input_trampoline, &configuration, &h_));
         load_tables();
     }
     explicit hierarchical_interleaved_bloom_filter(hibf_gpu_hibf * adopted) : h_{adopted}
@@ -564,12 +659,6 @@ public:
     }
 
 private:
-    static void trampoline(void * user, uint64_t user_bin, hibf_gpu_sink * sink)
-    {
-        auto & c = *static_cast<config *>(user);
-        c.input_fn(static_cast<size_t>(user_bin), insert_iterator{sink});
-    }
-
     void load_tables()
     {
         uint64_t info[4];

@@ -2,6 +2,7 @@
 // (test/unit/hibf/interleaved_bloom_filter_test.cpp, test/unit/hibf/hierarchical_interleaved_bloom_filter_test.cpp,
 // test/snippet/readme.cpp), with the expectations those tests state.  Usage: test_facade <dir with layout files>.
 // Exits 0 when every check holds.
+#include <algorithm>
 #include <cstdio>
 #include <fstream>
 #include <functional>
@@ -142,6 +143,81 @@ static void ibf_increase()
     })));
 }
 
+// interleaved_bloom_filter_test.cpp: construction_from_config, construction_from_config_with_max_bin_elements and
+// membership_for through the config constructor (user bins {1..10} and {0, 2, 3, 4, 5}, or {1..5})
+static void ibf_from_config()
+{
+    std::vector<std::vector<uint64_t>> hashes{{1, 2, 3, 4, 5, 6, 7, 8, 9, 10}, {0, 2, 3, 4, 5}};
+    h::config cfg{};
+    cfg.input_fn = [&](size_t const num, h::insert_iterator it)
+    {
+        for (uint64_t const v : hashes[num])
+            it = v;
+    };
+    cfg.number_of_user_bins = hashes.size();
+    h::interleaved_bloom_filter ibf{cfg};
+    CHECK(ibf.bin_count() == 2);
+    auto agent = ibf.containment_agent();
+    CHECK(agent.bulk_contains(2) == (std::vector<bool>{true, true}));
+    CHECK(agent.bulk_contains(8) == (std::vector<bool>{true, false}));
+    CHECK(agent.bulk_contains(0) == (std::vector<bool>{false, true}));
+
+    h::interleaved_bloom_filter default_num_elements{cfg, 0u};
+    h::interleaved_bloom_filter appropriate_num_elements{cfg, 10u};
+    h::interleaved_bloom_filter larger_num_elements{cfg, 20u};
+    CHECK(ibf == default_num_elements);
+    CHECK(ibf == appropriate_num_elements);
+    CHECK(!(ibf == larger_num_elements));
+    CHECK(!(appropriate_num_elements == larger_num_elements));
+
+    hashes[1] = {1, 2, 3, 4, 5};
+    h::interleaved_bloom_filter both{cfg};
+    auto m = both.membership_agent();
+    auto const & result = m.membership_for(std::vector<uint64_t>{1, 2, 3, 4, 5}, 2u);
+    CHECK(result == (std::vector<uint64_t>{0, 1}));
+    m.sort_results();
+    CHECK(result == (std::vector<uint64_t>{0, 1}));
+
+    h::config no_input{};
+    no_input.number_of_user_bins = 2;
+    CHECK((throws<std::function<void()>, std::invalid_argument>([&] { h::interleaved_bloom_filter f{no_input}; })));
+}
+
+// interleaved_bloom_filter_test.cpp: emplace (occupancy untracked: technical_bins zeros) and emplace_with_occupancy
+// (128 bins, bins 0-63 filled: their counters non-zero, the rest zero), clear resets a bin's counter
+static void ibf_occupancy()
+{
+    h::interleaved_bloom_filter plain{h::bin_count{64}, h::bin_size{1024}};
+    for (uint64_t b = 0; b < 64; ++b)
+        for (uint64_t v = 0; v < 64; ++v)
+            plain.emplace(v, h::bin_index{b});
+    CHECK(!plain.track_occupancy);
+    CHECK(plain.occupancy.size() == 64u);
+    CHECK(std::ranges::all_of(plain.occupancy, [](size_t const occ) { return occ == 0u; }));
+
+    h::interleaved_bloom_filter ibf{h::bin_count{128}, h::bin_size{512}, h::hash_function_count{2}, true};
+    CHECK(ibf.track_occupancy);
+    for (uint64_t b = 0; b < 64; ++b)
+        for (uint64_t v = 0; v < 64; ++v)
+            ibf.emplace(v, h::bin_index{b});
+    auto agent = ibf.containment_agent();
+    std::vector<bool> expected(128);
+    std::fill(expected.begin(), expected.begin() + 64, true);
+    for (uint64_t v = 0; v < 64; ++v)
+        CHECK(agent.bulk_contains(v) == expected);
+    CHECK(ibf.occupancy.size() == 128u);
+    for (uint64_t b = 0; b < 64; ++b)
+        CHECK(ibf.occupancy[b] != 0u);
+    for (uint64_t b = 64; b < 128; ++b)
+        CHECK(ibf.occupancy[b] == 0u);
+    ibf.clear(h::bin_index{5});
+    CHECK(ibf.occupancy[5] == 0u && ibf.occupancy[6] != 0u);
+    ibf.increase_bin_number_to(h::bin_count{200});
+    CHECK(ibf.occupancy.size() == 256u && ibf.occupancy[6] != 0u && ibf.occupancy[199] == 0u);
+    h::interleaved_bloom_filter moved{std::move(ibf)};
+    CHECK(moved.track_occupancy && moved.occupancy.size() == 256u);
+}
+
 // hierarchical_interleaved_bloom_filter_test.cpp small example and test/snippet/readme.cpp, with the layouts the
 // reference computes for them.
 static void hibf_small(std::string const & dir)
@@ -256,6 +332,8 @@ int main(int argc, char ** argv)
     ibf_clear();
     ibf_membership();
     ibf_increase();
+    ibf_from_config();
+    ibf_occupancy();
     hibf_small(dir);
     hibf_readme(dir);
     hibf_batch(dir);

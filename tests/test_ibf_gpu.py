@@ -136,6 +136,7 @@ def test_occupancy_in_insertion_order(gpu_lib, oracle, binned):
     bins, size = 70, 64
     ibf = _ibf(bins, size, 3, True)
     O = oracle.ibf(bins, size, 3, True)
+    assert ibf.track_occupancy and not _ibf(bins, size, 3, False).track_occupancy
     for n in (5, 1000, 3_000_000):
         v = rng.integers(0, 1 << 62, n, dtype=np.uint64)
         if binned:
