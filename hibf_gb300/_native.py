@@ -135,6 +135,7 @@ _SIGS = [
     ("hibf_gpu_ibf_build", None, [ctypes.POINTER(BuildConfig), u64, ctypes.c_uint32, ci, INPUT_FN, vp,
                                   ctypes.POINTER(vp)]),
     ("hibf_gpu_hibf_set_prev", None, [vp, vp, vp]),
+    ("hibf_gpu_hibf_get_prev", None, [vp, vp, vp]),
     ("hibf_gpu_ibf_save", None, [vp, ctypes.c_char_p]),
     ("hibf_gpu_ibf_load", None, [ctypes.c_char_p, ctypes.POINTER(vp)]),
     ("hibf_gpu_hibf_save", None, [vp, ctypes.c_char_p]),

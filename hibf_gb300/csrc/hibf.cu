@@ -1792,6 +1792,21 @@ extern "C"
             });
     }
 
+    int hibf_gpu_hibf_get_prev(hibf_gpu_hibf const * h, uint64_t * prev_ibf, uint64_t * prev_bin)
+    {
+        return guarded(
+            [&]
+            {
+                if (!h)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(const_cast<hibf_gpu_hibf *>(h)->mu); // against a concurrent set_prev
+                if (prev_ibf)
+                    std::copy(h->prev_ibf.begin(), h->prev_ibf.end(), prev_ibf);
+                if (prev_bin)
+                    std::copy(h->prev_bin.begin(), h->prev_bin.end(), prev_bin);
+            });
+    }
+
     int hibf_gpu_hibf_save(hibf_gpu_hibf * h, char const * path)
     {
         return guarded(

@@ -137,6 +137,14 @@ class hierarchical_interleaved_bloom_filter:
         pi, pb = _u64(prev_ibf), _u64(prev_bin)
         N.call("hibf_gpu_hibf_set_prev", self._h, pi.ctypes.data, pb.ctypes.data)
 
+    @property
+    def prev_ibf_id(self) -> np.ndarray:
+        """prev_ibf_id as an (n_ibfs, 2) array of (parent IBF, parent bin) rows."""
+        n = len(self.next_ibf_id)
+        pi, pb = np.zeros(n, np.uint64), np.zeros(n, np.uint64)
+        N.call("hibf_gpu_hibf_get_prev", self._h, pi.ctypes.data, pb.ctypes.data)
+        return np.stack([pi, pb], axis=1)
+
     def __del__(self):
         if getattr(self, "_h", None):
             try:

@@ -164,6 +164,8 @@ int hibf_gpu_hibf_upload_words(hibf_gpu_hibf * h, uint64_t ibf, uint64_t const *
  * hierarchies give every merged bin's child its parent and the root (0, 0); the build leaves the reference's
  * convention ((0, 0) also for favourite children); set it to carry a host-built HIBF's table through serialisation. */
 int hibf_gpu_hibf_set_prev(hibf_gpu_hibf * h, uint64_t const * prev_ibf, uint64_t const * prev_bin);
+/* The same table read back: n_ibfs entries each; either pointer may be NULL. */
+int hibf_gpu_hibf_get_prev(hibf_gpu_hibf const * h, uint64_t * prev_ibf, uint64_t * prev_bin);
 /* Serialisation in the reference's byte layout (cereal binary archive encoding of the serialize functions of
  * interleaved_bloom_filter.hpp:471-485 with bit_vector.hpp:885-925, and hierarchical_interleaved_bloom_filter.hpp:
  * 267-277): save streams the device stores to `path`, load reads one into new device stores.  Invalid or

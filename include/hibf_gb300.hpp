@@ -12,6 +12,8 @@
 #pragma once
 
 #include <algorithm>
+#include <compare>
+#include <cstddef>
 #include <cstdint>
 #include <exception>
 #include <functional>
@@ -39,6 +41,13 @@ inline void check(int status)
         throw std::invalid_argument{msg};
     throw std::runtime_error{msg};
 }
+
+// Sentinels of ibf_bin_to_user_bin_id (hierarchical_interleaved_bloom_filter.hpp:32-40).
+namespace bin_kind
+{
+static constexpr uint64_t merged{HIBF_GPU_BIN_MERGED};
+static constexpr uint64_t deleted{HIBF_GPU_BIN_DELETED};
+} // namespace bin_kind
 
 struct bin_count
 {
@@ -468,16 +477,19 @@ public:
         hibf_gpu_build_config c{configuration.number_of_user_bins, configuration.number_of_hash_functions,
                                 configuration.maximum_fpr, configuration.relaxed_fpr, configuration.threads, 0};
         check(hibf_gpu_hibf_build(&c, layout_text.c_str(), &detail::input_trampoline, &configuration, &h_));
-        load_tables();
+        adopt();
     }
     explicit hierarchical_interleaved_bloom_filter(hibf_gpu_hibf * adopted) : h_{adopted}
     {
-        load_tables();
+        adopt();
     }
     hierarchical_interleaved_bloom_filter(hierarchical_interleaved_bloom_filter const &) = delete;
     hierarchical_interleaved_bloom_filter & operator=(hierarchical_interleaved_bloom_filter const &) = delete;
     hierarchical_interleaved_bloom_filter(hierarchical_interleaved_bloom_filter && o) noexcept :
         number_of_user_bins{o.number_of_user_bins},
+        next_ibf_id{std::move(o.next_ibf_id)},
+        prev_ibf_id{std::move(o.prev_ibf_id)},
+        ibf_bin_to_user_bin_id{std::move(o.ibf_bin_to_user_bin_id)},
         index_allocation_timer{o.index_allocation_timer},
         user_bin_io_timer{o.user_bin_io_timer},
         merge_kmers_timer{o.merge_kmers_timer},
@@ -491,6 +503,20 @@ public:
     }
 
     size_t number_of_user_bins{};
+
+    // The tables (hierarchical_interleaved_bloom_filter.hpp:208-238, 296-301), host copies read at construction:
+    // per IBF and technical bin the child IBF (the IBF itself for a leaf bin) and the user bin (bin_kind::merged or
+    // bin_kind::deleted), and per IBF its parent IBF and bin.  The IBFs themselves stay on the device (their shapes:
+    // hibf_gpu_hibf_ibf_info).
+    struct previous_ibf_id_pair
+    {
+        size_t ibf_idx{};
+        size_t bin_idx{};
+        friend constexpr auto operator<=>(previous_ibf_id_pair const &, previous_ibf_id_pair const &) = default;
+    };
+    std::vector<std::vector<uint64_t>> next_ibf_id;
+    std::vector<previous_ibf_id_pair> prev_ibf_id;
+    std::vector<std::vector<uint64_t>> ibf_bin_to_user_bin_id{};
 
     // The build's phase timers (hierarchical_interleaved_bloom_filter.hpp:283-290); zero unless this object was
     // built.  The layout_* timers of the reference time the layout computation, which seqan::hibf keeps.
@@ -658,12 +684,73 @@ public:
         return h_;
     }
 
+    // Equal user bin count, tables, IBF shapes and bits (the reference's defaulted operator==,
+    // hierarchical_interleaved_bloom_filter.hpp:252, 312; its timers always compare equal).  The bit stores are
+    // compared IBF by IBF through host copies; the occupancy counters of the IBFs are not compared.
+    bool operator==(hierarchical_interleaved_bloom_filter const & other) const
+    {
+        if (number_of_user_bins != other.number_of_user_bins || next_ibf_id != other.next_ibf_id ||
+            prev_ibf_id != other.prev_ibf_id || ibf_bin_to_user_bin_id != other.ibf_bin_to_user_bin_id)
+            return false;
+        std::vector<uint64_t> wa, wb;
+        for (uint64_t k = 0; k < next_ibf_id.size(); ++k)
+        {
+            uint64_t a[5], b[5];
+            check(hibf_gpu_hibf_ibf_info(h_, k, a));
+            check(hibf_gpu_hibf_ibf_info(other.h_, k, b));
+            if (!std::equal(a, a + 4, b)) // bins, technical bins, bin size, hash functions
+                return false;
+            wa.resize(a[1] / 64 * a[2]);
+            wb.resize(wa.size());
+            check(hibf_gpu_hibf_download_words(h_, k, wa.data(), wa.size()));
+            check(hibf_gpu_hibf_download_words(other.h_, k, wb.data(), wb.size()));
+            if (wa != wb)
+                return false;
+        }
+        return true;
+    }
+
 private:
+    // Reads the new handle's tables; on failure releases the handle, since no destructor will run.
+    void adopt()
+    {
+        try
+        {
+            load_tables();
+        }
+        catch (...)
+        {
+            hibf_gpu_hibf_destroy(std::exchange(h_, nullptr));
+            throw;
+        }
+    }
+
     void load_tables()
     {
         uint64_t info[4];
         check(hibf_gpu_hibf_info(h_, info));
         number_of_user_bins = info[0];
+        uint64_t const n_ibfs = info[1];
+        std::vector<uint64_t> bins(n_ibfs), prev_ibf(n_ibfs), prev_bin(n_ibfs);
+        check(hibf_gpu_hibf_get_tables(h_, bins.data(), nullptr, nullptr, nullptr, nullptr));
+        uint64_t total = 0;
+        for (uint64_t const b : bins)
+            total += b;
+        std::vector<uint64_t> next(total), user_bin(total);
+        check(hibf_gpu_hibf_get_tables(h_, nullptr, nullptr, nullptr, next.data(), user_bin.data()));
+        check(hibf_gpu_hibf_get_prev(h_, prev_ibf.data(), prev_bin.data()));
+        next_ibf_id.assign(n_ibfs, {});
+        ibf_bin_to_user_bin_id.assign(n_ibfs, {});
+        prev_ibf_id.assign(n_ibfs, {});
+        for (uint64_t k = 0, at = 0; k < n_ibfs; at += bins[k], ++k)
+        {
+            auto const first = next.begin() + static_cast<std::ptrdiff_t>(at);
+            auto const last = first + static_cast<std::ptrdiff_t>(bins[k]);
+            next_ibf_id[k].assign(first, last);
+            ibf_bin_to_user_bin_id[k].assign(user_bin.begin() + (first - next.begin()),
+                                             user_bin.begin() + (last - next.begin()));
+            prev_ibf_id[k] = previous_ibf_id_pair{prev_ibf[k], prev_bin[k]};
+        }
         hibf_gpu_timer t[HIBF_GPU_TIMER_COUNT];
         check(hibf_gpu_hibf_build_timers(h_, t));
         index_allocation_timer = build_timer{t[HIBF_GPU_TIMER_INDEX_ALLOCATION]};

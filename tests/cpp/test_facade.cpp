@@ -220,6 +220,43 @@ static void ibf_occupancy()
 
 // hierarchical_interleaved_bloom_filter_test.cpp small example and test/snippet/readme.cpp, with the layouts the
 // reference computes for them.
+// The tables' conventions (hierarchical_interleaved_bloom_filter.hpp:208-238): a merged bin names its child IBF, whose
+// parent entry is that bin (or (0, 0), as the reference's build leaves it for some children); any other bin names
+// its own IBF and a user bin (or bin_kind::deleted); every user bin appears.
+static void check_tables(h::hierarchical_interleaved_bloom_filter const & hibf)
+{
+    size_t const n = hibf.next_ibf_id.size();
+    CHECK(n >= 1 && hibf.ibf_bin_to_user_bin_id.size() == n && hibf.prev_ibf_id.size() == n);
+    std::vector<bool> seen(hibf.number_of_user_bins);
+    for (size_t k = 0; k < n; ++k)
+    {
+        CHECK(hibf.next_ibf_id[k].size() == hibf.ibf_bin_to_user_bin_id[k].size());
+        for (size_t b = 0; b < hibf.next_ibf_id[k].size(); ++b)
+        {
+            uint64_t const ub = hibf.ibf_bin_to_user_bin_id[k][b];
+            uint64_t const next = hibf.next_ibf_id[k][b];
+            if (ub == h::bin_kind::merged)
+            {
+                CHECK(next != k && next < n);
+                if (next < n)
+                {
+                    auto const p = hibf.prev_ibf_id[next];
+                    using pair = h::hierarchical_interleaved_bloom_filter::previous_ibf_id_pair;
+                    CHECK((p == pair{k, b}) || (p == pair{0, 0}));
+                }
+            }
+            else
+            {
+                CHECK(next == k);
+                CHECK(ub == h::bin_kind::deleted || ub < hibf.number_of_user_bins);
+                if (ub < hibf.number_of_user_bins)
+                    seen[ub] = true;
+            }
+        }
+    }
+    CHECK(std::ranges::all_of(seen, [](bool x) { return x; }));
+}
+
 static void hibf_small(std::string const & dir)
 {
     std::vector<std::vector<uint64_t>> hashes{{1, 2, 3, 4, 5, 6, 7, 8, 9, 10}, {1, 2, 3, 4, 5}};
@@ -237,6 +274,7 @@ static void hibf_small(std::string const & dir)
     agent.sort_results();
     CHECK(result == (std::vector<uint64_t>{0, 1}));
     CHECK(hibf.number_of_user_bins == 2);
+    check_tables(hibf);
     // the build's timers: two user bins read, one allocation, one fill
     CHECK(hibf.user_bin_io_timer.count() == 3 && hibf.user_bin_io_timer.in_seconds() > 0.0);
     CHECK(hibf.index_allocation_timer.count() == 1 && hibf.fill_ibf_timer.count() == 1);
@@ -270,6 +308,16 @@ static void hibf_readme(std::string const & dir)
     auto loaded = h::hierarchical_interleaved_bloom_filter::load(dir + "/readme.hibf");
     auto agent2 = loaded.membership_agent();
     CHECK(agent2.membership_for(std::vector<uint64_t>{3, 9, 12, 14}, 2) == (std::vector<uint64_t>{2, 0}));
+    check_tables(hibf);
+    CHECK(loaded == hibf);
+    CHECK(loaded.next_ibf_id == hibf.next_ibf_id && loaded.prev_ibf_id == hibf.prev_ibf_id);
+    // same layout and tables, other bits: not equal
+    hashes[2] = {3, 9, 12};
+    h::hierarchical_interleaved_bloom_filter other{config, read_file(dir + "/layout_readme.txt")};
+    CHECK(other.ibf_bin_to_user_bin_id == hibf.ibf_bin_to_user_bin_id);
+    CHECK(!(other == hibf));
+    h::hierarchical_interleaved_bloom_filter moved{std::move(other)};
+    CHECK(moved.next_ibf_id == hibf.next_ibf_id && moved.number_of_user_bins == 3);
 }
 
 // The batched calls (no counterpart in the reference) give, per query, what the one-query agents give.

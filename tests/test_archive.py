@@ -71,6 +71,7 @@ def test_device_hibf_archive_round_trip(gpu_lib, tmp_path, name):
     H = hg.hierarchical_interleaved_bloom_filter.load(src)
     H.save(tmp_path / "h.bin")
     assert (tmp_path / "h.bin").read_bytes() == src.read_bytes()
+    np.testing.assert_array_equal(H.prev_ibf_id, np.array(A.hibf(src.read_bytes())["prev"], np.uint64))
     g = G.hibf_case(name)
     offs, ids, _ = H.membership_agent().query_batch(g["q_values"], g["q_offsets"], g["mem_t"])
     for i, e in enumerate(G.mem_lists(g, "mem_sorted")):
