@@ -140,7 +140,7 @@ class hierarchical_interleaved_bloom_filter:
     @property
     def prev_ibf_id(self) -> np.ndarray:
         """prev_ibf_id as an (n_ibfs, 2) array of (parent IBF, parent bin) rows."""
-        n = len(self.next_ibf_id)
+        n = int(self.bins.size)
         pi, pb = np.zeros(n, np.uint64), np.zeros(n, np.uint64)
         N.call("hibf_gpu_hibf_get_prev", self._h, pi.ctypes.data, pb.ctypes.data)
         return np.stack([pi, pb], axis=1)
