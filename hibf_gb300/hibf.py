@@ -246,25 +246,32 @@ class _agent_base:
     def status(self) -> None:
         N.call("hibf_gpu_agent_status", self._a)
 
-    def query_batch(self, values, query_offsets, thresholds, mode=N.QUERY_MEMBERSHIP, width=2):
-        """All queries in one persistent launch.  Returns (offsets, ids, counts) as numpy copies; ids ascending per
-        query; counts (mode COUNT) are the non-zero entries of each dense counting vector.  Batches of at least 64 MiB
-        of values are copied to the device in chunks while the kernel answers the chunks already copied
-        (input_chunks() reports how many)."""
+    def query_batch(self, values, query_offsets, thresholds, mode=N.QUERY_MEMBERSHIP, width=2, copy=True):
+        """All queries in one persistent launch.  Returns (offsets, ids, counts); ids ascending per query; counts
+        (mode COUNT) are the non-zero entries of each dense counting vector.  Values in page-locked memory are read
+        in place by the kernel; batches of at least 64 MiB of pageable values are copied in chunks while the kernel
+        answers the chunks already copied (input_chunks() reports how many).  The arrays are copies, or with
+        copy=False views of the agent's page-locked result buffers, valid until the agent's next call (as the
+        reference's agents hand out their own result buffers)."""
         v, qo = _u64(values), _u64(query_offsets)
         nq = qo.size - 1
         t = _u64(thresholds)
         ro, ri, rc = N.u64p(), N.u64p(), ctypes.c_void_p()
         N.call("hibf_gpu_agent_query_batch", self._a, mode, v.ctypes.data if v.size else None, qo.ctypes.data, nq,
                t.ctypes.data if nq else None, width, ctypes.byref(ro), ctypes.byref(ri), ctypes.byref(rc))
-        offs = np.ctypeslib.as_array(ro, shape=(nq + 1,)).copy()
+        offs = np.ctypeslib.as_array(ro, shape=(nq + 1,))
         nr = int(offs[-1])
-        ids = np.ctypeslib.as_array(ri, shape=(nr,)).copy() if nr else np.zeros(0, np.uint64)
+        ids = np.ctypeslib.as_array(ri, shape=(nr,)) if nr else np.zeros(0, np.uint64)
         cnts = None
         if mode == N.QUERY_COUNT:
-            cnts = np.zeros(nr, _DT[width])
             if nr:
-                ctypes.memmove(cnts.ctypes.data, rc.value, nr * width)
+                ct = np.ctypeslib.as_ctypes_type(_DT[width])
+                cnts = np.ctypeslib.as_array(ctypes.cast(rc, ctypes.POINTER(ct)), shape=(nr,))
+            else:
+                cnts = np.zeros(0, _DT[width])
+        if copy:
+            offs, ids = offs.copy(), ids.copy()
+            cnts = None if cnts is None else cnts.copy()
         return offs, ids, cnts
 
     def query_batch_device(self, d_values: int, d_query_offsets: int, n_queries: int, d_thresholds: int,
@@ -428,8 +435,9 @@ class counting_agent_type(_agent_base):
         ctypes.memmove(out.ctypes.data, p.value, out.nbytes)
         return out
 
-    def query_batch(self, values, query_offsets, thresholds, mode=N.QUERY_COUNT, width=None):
-        return super().query_batch(values, query_offsets, thresholds, mode, self.width if width is None else width)
+    def query_batch(self, values, query_offsets, thresholds, mode=N.QUERY_COUNT, width=None, copy=True):
+        return super().query_batch(values, query_offsets, thresholds, mode, self.width if width is None else width,
+                                   copy)
 
 
 def stream_plan(query_offsets) -> np.ndarray:

@@ -595,6 +595,14 @@ def test_host_batch_read_in_place(gpu_lib, oracle):
         c_off, c_ids, c_cnt = c.query_batch(pinned, qo, thr, mode=N.QUERY_COUNT, width=2)
         np.testing.assert_array_equal(c_ids, o_ids)
         assert c.last_in_place()
+        # results as views of the agents' page-locked buffers: the same arrays
+        v_off, v_ids, _ = a.query_batch(pinned, qo, thr, copy=False)
+        np.testing.assert_array_equal(v_off, o_off)
+        np.testing.assert_array_equal(v_ids, o_ids)
+        w_off, w_ids, w_cnt = c.query_batch(pinned, qo, thr, mode=N.QUERY_COUNT, width=2, copy=False)
+        assert w_cnt.dtype == np.uint16 and not w_cnt.flags.owndata
+        np.testing.assert_array_equal(w_ids, c_ids)
+        np.testing.assert_array_equal(w_cnt, c_cnt)
         offs, ids, _ = a.query_batch(vals, qo, thr)  # pageable: copied
         assert not a.last_in_place()
         np.testing.assert_array_equal(ids, o_ids)
