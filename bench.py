@@ -7,7 +7,8 @@ values; layout from the reference's DP), h=2, fpr 0.05, tmax 64; one step = memb
 ceil(0.7 * length).  Inputs (8 GB of query values) and the index (13.4 GB) are both larger than L2.  The index is
 the reference's filter: split user bins are chunked in the reference's hash-set order (committed split table), and
 every IBF is compared with the reference's own build of the same workload (tests/golden/ref_c3_1.npz).  A sub-record
-measures the 65,536-user-bin workload the same way (--no-c4 skips it).
+measures the 65,536-user-bin workload the same way (--no-c4 skips it), another the single-level 1,024-bin IBF
+(bulk_count + bulk_contains over 2^24 values, --workload ibf1024; --no-c2 skips it).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload hibf8192|...]
 
@@ -67,6 +68,7 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-c4", action="store_true", help="skip the 65,536-user-bin sub-record")
+    ap.add_argument("--no-c2", action="store_true", help="skip the single-level 1,024-bin IBF sub-record")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel schedule")
     ap.add_argument("--tuning", type=str, default="",
                     help="fixed kernel schedule 'values_per_lane,fetch_bytes,counter_bits[,adaptive_step,ee_min"
@@ -798,6 +800,18 @@ def run_ours(args, wl, rank, world, local):
                                  "e2e", "roofline", "cpu_baseline", "plain", "batched_vs_plain", "bulk_count",
                                  "build", "autotune", "clocks")}
         m["parity"].update({"c4_" + k: v for k, v in m4["parity"].items()})
+        del m4
+        gc.collect()
+        torch.cuda.empty_cache()
+    c2 = None
+    if wl.name == "hibf8192" and not args.no_c2 and args.scale == 1.0 and not args.queries:
+        r2 = run_ibf_ours(args, rank, world, local, own_pg=False)
+        if r2 is not None:
+            c2 = {k: r2[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "config", "kernels", "build",
+                                     "e2e", "gpu_launches", "roofline", "cpu_baseline", "clocks")}
+            m["parity"].update({"c2_" + k: v for k, v in r2["parity"].items()})
+        gc.collect()
+        torch.cuda.empty_cache()
     out = None
     if rank == 0:
         serving = m["serving"]
@@ -819,6 +833,7 @@ def run_ours(args, wl, rank, world, local):
             "serving_config": "open-loop Poisson, request sizes log-uniform 1-4096 queries from the batch's first "
                               "100k queries, thresholds U(0.5,0.9)*len, 4 slots, 4 GiB admission cap",
             "c4": c4,
+            "c2": c2,
             "parity": parity,
         }
     if world > 1:
@@ -945,13 +960,15 @@ def build_ibf1024(w, stream):
     return ibf, b0.elapsed_time(b1)
 
 
-def run_ibf_ours(args, rank, world, local):
+def run_ibf_ours(args, rank, world, local, own_pg=True):
+    """The single-level IBF workload; own_pg=False when it runs as a sub-record inside run_ours (whose process
+    group it then uses)."""
     import torch
 
     from hibf_gb300 import _native as N
 
     torch.cuda.set_device(local)
-    if world > 1:
+    if world > 1 and own_pg:
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
@@ -1085,7 +1102,7 @@ def run_ibf_ours(args, rank, world, local):
                          "algorithmic_bytes_per_value": {"bulk_count": rows + 8, "bulk_contains": rows + 8 + bw * 8}},
             "cpu_baseline": cpu, "clocks": clk, "parity": parity,
         }
-    if world > 1:
+    if world > 1 and own_pg:
         torch.distributed.destroy_process_group()
     return out
 
