@@ -140,11 +140,15 @@ def peaks():
 
 
 def traffic_per_value_visit(workload="hibf8192"):
-    """DRAM bytes per executed (value, IBF) visit of the query kernel from the committed ncu summary, if present."""
+    """DRAM bytes per executed (value, IBF) visit of the query kernel (per query value of a step for the single-level
+    IBF) from the committed ncu summary, if present."""
     p = ROOT / "profiles" / "traffic.txt"
     if not p.exists():
         return None
-    key = "k_query_bytes_per_value_visit" + ("" if workload == "hibf8192" else "_" + workload) + "="
+    if workload == "ibf1024":
+        key = "k_bulk_bytes_per_value_ibf1024="
+    else:
+        key = "k_query_bytes_per_value_visit" + ("" if workload == "hibf8192" else "_" + workload) + "="
     for line in p.read_text().splitlines():
         if line.startswith(key):
             return float(line.split("=", 1)[1])
@@ -1052,6 +1056,7 @@ def run_ibf_ours(args, rank, world, local, own_pg=True):
         count_bytes = nq * (rows + 8)
         contains_bytes = nq * (rows + 8 + bw * 8)
         achieved = (count_bytes + contains_bytes) / (ms / 1e3) / 1e9
+        tb = traffic_per_value_visit("ibf1024")
         parity = {"counts_equal_contains_column_sums": counts_equal_contains, "e2e_equals_device": e2e_equal}
         cpu = None
         if not args.no_cpu:
@@ -1098,7 +1103,10 @@ def run_ibf_ours(args, rank, world, local, own_pg=True):
                     "call": "hibf_gpu_ibf_bulk_count + hibf_gpu_ibf_bulk_contains (pinned host buffers)"},
             "gpu_launches": 4 * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "peak_kind": peak_kind, "traffic": None,
+                         "peak_kind": peak_kind,
+                         # both kernels of a step, from the committed ncu capture scaled by the values
+                         "traffic": None if tb is None else tb * nq,
+                         "dram_bytes_per_value": tb,
                          "algorithmic_bytes_per_value": {"bulk_count": rows + 8, "bulk_contains": rows + 8 + bw * 8}},
             "cpu_baseline": cpu, "clocks": clk, "parity": parity,
         }
