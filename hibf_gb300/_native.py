@@ -227,6 +227,7 @@ _SIGS = [
     ("hibf_gpu_server_batch_log", None, [vp, ctypes.POINTER(ctypes.c_double), u64, u64p]),
     ("hibf_gpu_server_open_loop", None, [vp, vp, vp, u64, ctypes.c_double, ctypes.c_double, u64, ctypes.c_double,
                                          ctypes.c_double, u64, ctypes.POINTER(ctypes.c_double)]),
+    ("hibf_gpu_server_open_loop_detail", None, [vp, vp]),
     ("hibf_gpu_probe_random_reads", None, [u64, u64, ctypes.POINTER(ctypes.c_double)]),
     ("hibf_gpu_synth_user_bin_offsets", None, [u64, ci, ctypes.c_double, ctypes.c_double, u64, u64, u64, vp]),
     ("hibf_gpu_synth_query_offsets", None, [u64, ci, u64, u64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,

@@ -115,6 +115,9 @@ struct hibf_gpu_server
     std::vector<host_range> host_ranges;
     // a batch whose requests lie back to back in one mapped registered range is read in place by the kernel
     std::atomic<bool> zero_copy{true};
+    // the last open-loop run's load generator: the largest and the 99.9th-percentile lateness of a submission behind
+    // its scheduled arrival, the submissions more than 1 ms late, and p99 / p99.9 latency from the actual submission
+    double open_loop_detail[5]{};
 };
 
 namespace
@@ -817,19 +820,23 @@ extern "C"
                     }
                 }
                 std::vector<uint64_t> ids(plans.size(), 0);
+                std::vector<double> late(plans.size(), 0.0); // submission behind the scheduled arrival
                 double const t0 = now_s() + 0.01;
                 for (size_t i = 0; i < plans.size(); ++i)
                 {
                     double const ta = t0 + plans[i].t;
-                    while (now_s() < ta)
-                        ;
+                    double tn = now_s();
+                    while (tn < ta)
+                        tn = now_s();
+                    late[i] = tn - ta;
                     int const st = hibf_gpu_server_submit(S, vals[i], offs[i].data(), plans[i].nq, thrs[i].data(), ta,
                                                           0, &ids[i]);
                     if (st != HIBF_GPU_OK)
                         fail(st, "submit failed");
                 }
-                std::vector<double> lat;
+                std::vector<double> lat, lat_sub;
                 lat.reserve(plans.size());
+                lat_sub.reserve(plans.size());
                 uint64_t nqs = 0, rej = 0;
                 double t_end = t0;
                 for (size_t i = 0; i < plans.size(); ++i)
@@ -842,6 +849,7 @@ extern "C"
                     if (st == HIBF_GPU_OK)
                     {
                         lat.push_back(l);
+                        lat_sub.push_back(l - late[i]);
                         nqs += plans[i].nq;
                         t_end = std::max(t_end, t0 + plans[i].t + l);
                     }
@@ -850,13 +858,26 @@ extern "C"
                     hibf_gpu_server_release(S, ids[i]);
                 }
                 std::sort(lat.begin(), lat.end());
-                auto pct = [&](double p) -> double
+                std::sort(lat_sub.begin(), lat_sub.end());
+                auto pct_of = [](std::vector<double> const & v, double p) -> double
                 {
-                    if (lat.empty())
+                    if (v.empty())
                         return 0.0;
-                    size_t const k = std::min(lat.size() - 1, static_cast<size_t>(std::ceil(p * lat.size())) - 1);
-                    return lat[k];
+                    size_t const k = std::min(v.size() - 1, static_cast<size_t>(std::ceil(p * v.size())) - 1);
+                    return v[k];
                 };
+                auto pct = [&](double p) { return pct_of(lat, p); };
+                std::vector<double> late_sorted = late;
+                std::sort(late_sorted.begin(), late_sorted.end());
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    S->open_loop_detail[0] = late_sorted.empty() ? 0.0 : late_sorted.back();
+                    S->open_loop_detail[1] = pct_of(late_sorted, 0.999);
+                    S->open_loop_detail[2] = static_cast<double>(
+                        std::count_if(late.begin(), late.end(), [](double x) { return x > 1e-3; }));
+                    S->open_loop_detail[3] = pct_of(lat_sub, 0.99);
+                    S->open_loop_detail[4] = pct_of(lat_sub, 0.999);
+                }
                 uint64_t st4[4];
                 hibf_gpu_server_stats(S, st4);
                 out[0] = static_cast<double>(nqs) / std::max(1e-9, t_end - t0);
@@ -867,6 +888,18 @@ extern "C"
                 out[5] = static_cast<double>(nqs);
                 out[6] = static_cast<double>(rej);
                 out[7] = st4[0] ? static_cast<double>(st4[1]) / static_cast<double>(st4[0]) : 0.0;
+            });
+    }
+
+    int hibf_gpu_server_open_loop_detail(hibf_gpu_server * S, double out[5])
+    {
+        return guarded(
+            [&]
+            {
+                if (!S || !out)
+                    fail(HIBF_GPU_ERR_INVALID_ARG, "null argument");
+                std::lock_guard<std::mutex> lk(S->mu);
+                std::copy(S->open_loop_detail, S->open_loop_detail + 5, out);
             });
     }
 

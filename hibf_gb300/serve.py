@@ -141,6 +141,12 @@ class server:
         out = (ctypes.c_double * 8)()
         N.call("hibf_gpu_server_open_loop", self._s, v.ctypes.data, qo.ctypes.data, qo.size - 1, offered_qps,
                duration_s, max_request_queries, thr_lo, thr_hi, seed, out)
+        det = (ctypes.c_double * 5)()
+        N.call("hibf_gpu_server_open_loop_detail", self._s, det)
         return dict(offered_qps=offered_qps, achieved_qps=out[0], p50_ms=out[1] * 1e3, p99_ms=out[2] * 1e3,
                     p999_ms=out[3] * 1e3, requests=int(out[4]), queries=int(out[5]), rejected=int(out[6]),
-                    mean_batch_queries=out[7], duration_s=duration_s)
+                    mean_batch_queries=out[7], duration_s=duration_s,
+                    # the load generator: how late it submitted, and latency counted from the actual submission
+                    generator_late_max_ms=det[0] * 1e3, generator_late_p999_ms=det[1] * 1e3,
+                    generator_late_over_1ms=int(det[2]), p99_from_submit_ms=det[3] * 1e3,
+                    p999_from_submit_ms=det[4] * 1e3)

@@ -560,6 +560,10 @@ int hibf_gpu_server_open_loop(hibf_gpu_server * s, uint64_t const * pool_values,
                               uint64_t pool_queries, double offered_qps, double duration_s,
                               uint64_t max_request_queries, double thr_lo, double thr_hi, uint64_t seed,
                               double out[8]);
+/* The last open-loop run's load generator (seconds): the largest and the 99.9th-percentile lateness of a submission
+ * behind its scheduled arrival, the number of submissions more than 1 ms late, and the p99 and p99.9 latency measured
+ * from the actual submission (the open-loop figures above count from the scheduled arrival). */
+int hibf_gpu_server_open_loop_detail(hibf_gpu_server * s, double out[5]);
 
 
 /* ============================================================================================================ */

@@ -89,6 +89,11 @@ def test_open_loop_driver(gpu_lib):
     r = srv.open_loop(d["q_values"], d["q_offsets"], offered_qps=20000, duration_s=0.3, max_request_queries=64)
     assert r["requests"] > 0 and r["rejected"] == 0
     assert 0 < r["p50_ms"] <= r["p99_ms"] <= r["p999_ms"]
+    # the load generator's lateness, and latency from the actual submission, which the lateness can only shorten
+    assert 0 <= r["generator_late_p999_ms"] <= r["generator_late_max_ms"]
+    assert 0 <= r["generator_late_over_1ms"] <= r["requests"]
+    assert 0 < r["p99_from_submit_ms"] <= r["p99_ms"] + 1e-6
+    assert r["p99_from_submit_ms"] <= r["p999_from_submit_ms"] <= r["p999_ms"] + 1e-6
     srv.close()
 
 
