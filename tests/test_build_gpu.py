@@ -149,7 +149,7 @@ def _same_index_as_reference(H, ref):
 
 
 def test_c1_matches_reference(gpu_lib):
-    """The 64-user-bin workload (BASELINE config 1), built from the reference's layout both through input_fn and
+    """The 64-user-bin workload (h = 2, fpr 0.05, tmax 64; user bins of 1e3-1e5 values), built from the reference's layout both through input_fn and
     from the generator: every IBF holds the reference's bits, and all 10,000 queries answer as the reference did --
     membership_for + sort_results at t = 125 and counting_agent<uint16_t>::bulk_count at t = 125, compared per query
     by length and digest (hierarchical_interleaved_bloom_filter.hpp:424-439, 549-566)."""

@@ -177,7 +177,7 @@ def test_hibf_unit_expectations(oracle):
 
 
 def test_c1_oracle_answers_like_the_reference(oracle):
-    """The 64-user-bin workload (BASELINE config 1): the oracle's HIBF with the reference's tables, filled in the
+    """The 64-user-bin workload (h = 2, fpr 0.05, tmax 64; user bins of 1e3-1e5 values): the oracle's HIBF with the reference's tables, filled in the
     builder's insertion order, holds the reference's bits in every IBF, and answers all 10,000 queries
     (membership_for + sort_results at t = 125, counting_agent<uint16_t>::bulk_count at t = 125) with the
     reference's per-query lengths and digests (hierarchical_interleaved_bloom_filter.hpp:424-439, 549-566)."""
