@@ -191,7 +191,7 @@ public:
     // src/interleaved_bloom_filter.cpp:81-117): one technical bin per user bin, the bin size from the exact distinct
     // count of the largest user bin (picked by its HyperLogLog sketch unless max_bin_elements is given), then every
     // user bin's values inserted on the device.
-    explicit interleaved_bloom_filter(config & configuration, size_t max_bin_elements = 0)
+    interleaved_bloom_filter(config & configuration, size_t max_bin_elements = 0)
     {
         if (!configuration.input_fn)
             throw std::invalid_argument{"[HIBF CONFIG ERROR] You did not set the required config::input_fn."};
