@@ -142,6 +142,31 @@ def test_invalid_thresholds(gpu_lib):
         a.query_batch([1, 2], [0, 2], [0], mode=N.QUERY_COUNT)
 
 
+def test_large_batch_checks_every_slice(gpu_lib):
+    """A large batch's host checks run in slices on several threads: a decreasing offset or a bad threshold in the
+    last slice is still an invalid argument, and a valid batch of the same size answers."""
+    H = _gpu_hibf(G.hibf_case("snippet"))
+    a = H.membership_agent()
+    nq = 300_000
+    qo = np.zeros(nq + 1, np.uint64)  # every query empty
+    thr = np.ones(nq, np.uint64)
+    offs, ids, _ = a.query_batch(np.zeros(0, np.uint64), qo, thr)
+    assert offs.size == nq + 1 and ids.size == 0
+    bad = qo.copy()
+    bad[-2] = 5  # qoff[nq - 1] > qoff[nq]
+    with pytest.raises(hg.InvalidArgument, match="non-decreasing"):
+        a.query_batch(np.zeros(5, np.uint64), bad, thr)
+    t = thr.copy()
+    t[-1] = 70000
+    with pytest.raises(hg.InvalidArgument, match="uint16"):
+        a.query_batch(np.zeros(0, np.uint64), qo, t)
+    t[-1] = 0
+    with pytest.raises(hg.InvalidArgument, match="> 0"):
+        a.query_batch(np.zeros(0, np.uint64), qo, t, mode=N.QUERY_COUNT)
+    offs, ids, _ = a.query_batch(np.zeros(0, np.uint64), qo, thr)  # the agent still answers
+    assert offs.size == nq + 1 and ids.size == 0
+
+
 def test_work_counters(gpu_lib):
     d = G.hibf_case("synth600")
     H = _gpu_hibf(d)
