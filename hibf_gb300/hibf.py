@@ -153,6 +153,23 @@ class hierarchical_interleaved_bloom_filter:
                 pass
             self._h = None
 
+    def __eq__(self, other) -> bool:
+        """Equal user bin count, tables, IBF shapes and bits (the reference's defaulted operator==,
+        hierarchical_interleaved_bloom_filter.hpp:252, 312; its timers always compare equal).  The stores are compared
+        IBF by IBF through host copies; the IBFs' occupancy counters are not compared."""
+        if not isinstance(other, hierarchical_interleaved_bloom_filter):
+            return NotImplemented
+        if self.number_of_user_bins != other.number_of_user_bins or self.n_ibfs != other.n_ibfs:
+            return False
+        for x, y in ((self.bins, other.bins), (self.bin_size, other.bin_size), (self.hash_funs, other.hash_funs),
+                     (self.next_ibf_id, other.next_ibf_id), (self.ibf_bin_to_user_bin_id, other.ibf_bin_to_user_bin_id),
+                     (self.prev_ibf_id, other.prev_ibf_id)):
+            if not np.array_equal(np.asarray(x, np.uint64), np.asarray(y, np.uint64)):
+                return False
+        return all(np.array_equal(self.words(k), other.words(k)) for k in range(self.n_ibfs))
+
+    __hash__ = None  # mutable, compared by content
+
     # -- structure --------------------------------------------------------------------------------------------
     @property
     def n_ibfs(self) -> int:

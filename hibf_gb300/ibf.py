@@ -89,6 +89,17 @@ class interleaved_bloom_filter:
                 pass
             self._h = None
 
+    def __eq__(self, other) -> bool:
+        """Equal shape, tracking flag, occupancy and bits (the reference's defaulted operator==,
+        interleaved_bloom_filter.hpp:433); the stores are compared through host copies."""
+        if not isinstance(other, interleaved_bloom_filter):
+            return NotImplemented
+        a, b = self._info(), other._info()
+        return (a[:3] == b[:3] and self.track_occupancy == other.track_occupancy and
+                np.array_equal(self.occupancy, other.occupancy) and np.array_equal(self.words(), other.words()))
+
+    __hash__ = None  # mutable, compared by content
+
     # -- properties ------------------------------------------------------------------------------------------
     def _info(self):
         out = (ctypes.c_uint64 * 5)()

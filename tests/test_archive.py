@@ -57,8 +57,11 @@ def test_device_ibf_archive_round_trip(gpu_lib, tmp_path):
     loaded = hg.interleaved_bloom_filter.load(G.GOLDEN / "serial_ibf.bin")
     np.testing.assert_array_equal(loaded.words(), ibf.words())
     np.testing.assert_array_equal(loaded.occupancy[:130], ibf.occupancy[:130])
+    assert loaded == ibf  # the reference's operator==: shape, occupancy, bits
     loaded.save(tmp_path / "b.bin")
     assert (tmp_path / "b.bin").read_bytes() == ref
+    loaded.clear(hg.bin_index(0))
+    assert not loaded == ibf
 
 
 @pytest.mark.gpu
@@ -72,6 +75,7 @@ def test_device_hibf_archive_round_trip(gpu_lib, tmp_path, name):
     H.save(tmp_path / "h.bin")
     assert (tmp_path / "h.bin").read_bytes() == src.read_bytes()
     np.testing.assert_array_equal(H.prev_ibf_id, np.array(A.hibf(src.read_bytes())["prev"], np.uint64))
+    assert hg.hierarchical_interleaved_bloom_filter.load(tmp_path / "h.bin") == H
     g = G.hibf_case(name)
     offs, ids, _ = H.membership_agent().query_batch(g["q_values"], g["q_offsets"], g["mem_t"])
     for i, e in enumerate(G.mem_lists(g, "mem_sorted")):
